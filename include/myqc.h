@@ -1,0 +1,174 @@
+/*
+ * myqc.h -- C ABI of libmyqc, the GB300 (sm_103a) engine behind the myQC
+ * drop-in executables int2e, scf, ao2mo and mp2.
+ *
+ * Every entry point is extern "C", takes plain pointers and sizes, and
+ * returns an int status (MQ_OK == 0).  Host arrays follow the reference's
+ * Fortran conventions: column-major, 0-based in Fortran terms, owned by the
+ * caller and read or written only during the call.  Device memory and the
+ * CUDA stream belong to the opaque context.  A context is single-threaded
+ * (one caller thread at a time), like the reference's programs.
+ *
+ * Each declaration names the reference routine it replaces (file:line in
+ * jhthorpe/myQC).  A Fortran host binds them through iso_c_binding; the
+ * interface block is in INTEGRATION.md.
+ */
+#ifndef MYQC_H
+#define MYQC_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define MQ_OK 0
+#define MQ_EINVAL 1     /* bad argument, unsupported basis, size limits */
+#define MQ_ENOMEM 2     /* device allocation failed */
+#define MQ_ECUDA 3      /* CUDA runtime / launch error */
+#define MQ_ETIMEOUT 4   /* a bounded device wait gave up */
+#define MQ_ENOCONV 5    /* SCF or eigensolver did not converge */
+#define MQ_ESTATE 6     /* call order violated (e.g. no system set) */
+
+/* Boys-function / pi mode passed to mq_set_system */
+#define MQ_MODE_REFERENCE 0 /* reference parity: Ftab Taylor table, the
+                               reference's float-valued pi and its regimes */
+#define MQ_MODE_TIGHT 1     /* accurate FP64 Boys (~1e-15) and true pi */
+
+typedef struct mq_ctx mq_ctx;
+
+/* Create / destroy a context on CUDA device `device`.  The reference has one
+ * process per stage; a context plays that role (src/myQC/myQC.f90:29-105). */
+int mq_init(mq_ctx **ctx, int device);
+int mq_free(mq_ctx *ctx);
+
+/* Copy the last error message (NUL-terminated, truncated to len). */
+int mq_last_error(const mq_ctx *ctx, char *buf, int len);
+
+/* Library version string, e.g. "myqc-gb300 0.1 sm_103a". */
+const char *mq_version(void);
+
+/* Define the molecule and basis.  Replaces getenv (src/myQC/env.f90:16-74)
+ * plus buildBasis (src/myQC/basis.f90:23-226) plus the Ftab read
+ * (src/integrals/int2e.f90:160-163):
+ *   Z[nnuc]           nuclear charges (atoms(0:nnuc-1))
+ *   xyz[nnuc*3]       bohr, Fortran xyz(0:nnuc-1,0:2), column-major
+ *   bas, set, basinfo, setinfo   the flat arrays buildBasis returns
+ *   ftab[121*23]      Ft(0:120,0:22) column-major; required in
+ *                     MQ_MODE_REFERENCE, may be NULL in MQ_MODE_TIGHT
+ * Contracted s and p functions only (the reference rejects d:
+ * basis.f90:170-174).  Uploads shells, primitive pairs and the Boys table. */
+int mq_set_system(mq_ctx *ctx, int nnuc, const int *Z, const double *xyz, const double *bas, const double *set,
+                  const int *basinfo, const int *setinfo, const double *ftab, int mode);
+
+/* Number of AOs (basinfo(1)) of the current system. */
+int mq_norb(const mq_ctx *ctx, int *norb);
+
+/* Contracted-quartet Schwarz threshold for the integral kernels
+ * (0 = off, the reference's behaviour; 1e-12 for direct SCF at scale). */
+int mq_set_schwarz(mq_ctx *ctx, double threshold);
+
+/* One-electron integrals S and H = T + V, n x n column-major host arrays.
+ * Replaces proc1e (src/integrals/int1e.f90:132-280). */
+int mq_int1e(mq_ctx *ctx, double *S, double *H);
+
+/* Full two-electron integral array XX(i,j,g,h) at i+n*(j+n*(g+n*h)), all 8
+ * permutations filled, into a host buffer of n^4 doubles.  Replaces proc2e +
+ * fillsym (src/integrals/int2e.f90:78-351,540-613).  Also leaves the array
+ * resident on the device for mq_fock / mq_ao2mo_iajb. */
+int mq_eri_full(mq_ctx *ctx, double *XX);
+
+/* As mq_eri_full but keeps the array on the device only (no host copy). */
+int mq_eri_store(mq_ctx *ctx);
+
+/* Upload an existing XX (n^4 doubles, the int2e file payload) to the device,
+ * e.g. when a drop-in scf reads the reference's XX file. */
+int mq_eri_upload(mq_ctx *ctx, const double *XX);
+
+/* Fock two-electron part from the device-resident XX.
+ * RHF (Db == NULL, Gb == NULL): G = sum_kl D_kl[(ij|kl) - 1/4(ik|jl) - 1/4(il|jk)]
+ *   replaces RHFI2G (src/I2G/RHFI2G.f90:80-90);
+ * UHF: Ga = J[Da+Db] - K[Da], Gb = J[Da+Db] - K[Db]
+ *   replaces UHFI2G (src/I2G/UHFI2G.f90:80-93).
+ * All matrices n x n column-major host arrays. */
+int mq_fock(mq_ctx *ctx, const double *Da, const double *Db, double *Ga, double *Gb);
+
+/* Direct Fock build: integrals recomputed and digested in one kernel, no
+ * stored XX (the (H2O)64-scale path).  Same meaning as mq_fock. */
+int mq_fock_direct(mq_ctx *ctx, const double *Da, const double *Db, double *Ga, double *Gb);
+
+/* SCF options (zero-initialise, then set what you need). */
+typedef struct mq_scf_opts {
+  int uhf;          /* 0 RHF, 1 UHF (options(3), src/parser/parser.f90:25) */
+  int nalpha;       /* nelcA */
+  int nbeta;        /* nelcB */
+  int max_iter;     /* 0 -> 500 RHF / 300 UHF (src/scf/scf.f90:172,337) */
+  double conv;      /* density threshold; 0 -> 1e-7 (options(8)=7) */
+  int conv_rms;     /* 0: max|D_new-D_old| (the reference, scf.f90:1227-1258);
+                       1: RMS of D_new-D_old */
+  int diis;         /* 0: plain Roothaan like the reference; >0: DIIS subspace */
+  int direct;       /* 0: digest the device-resident XX; 1: direct Fock build */
+  int guess;        /* 0: core Hamiltonian (scf.f90:410-512); 1: use C_in;
+                       2: use D_in (density guess, e.g. the learned guess) */
+  const double *C_in;   /* guess orbitals, n x n (x2 for UHF) */
+  const double *D_in;   /* guess density, n x n (x2 for UHF: alpha, beta) */
+} mq_scf_opts;
+
+/* Converged SCF.  Replaces the scf executable's iteration loop
+ * (src/scf/scf.f90:61-404, RHFiter :720-904, UHFiter :909-1117) including the
+ * dens and RHFI2G/UHFI2G child processes it spawns each iteration.
+ *   S, H     n x n host arrays (Suv, Huv)
+ *   C        out, n x n (RHF) or 2 x n x n (UHF alpha then beta), C^T S C = 1
+ *   eps      out, n (RHF) or 2n (UHF), ascending
+ *   D        out (may be NULL), the last input density(ies) n x n (x2)
+ *   energy   out, total SCF energy of the last iteration's input density,
+ *            as the reference prints it (scf.f90:900)
+ *   iters    out, iterations taken
+ *   history  out (may be NULL), 2*max_iter doubles: (E_k, maxdiff_k) */
+int mq_scf(mq_ctx *ctx, const double *S, const double *H, const mq_scf_opts *opts, double *C, double *eps,
+           double *D, double *energy, int *iters, double *history);
+
+/* Precision of the four-index transform */
+#define MQ_PREC_FP64 0      /* plain FP64 GEMMs */
+#define MQ_PREC_SPLIT_BF16 1 /* hi+lo BF16 operands on tcgen05 tensor cores,
+                                FP32 accumulation */
+
+/* (ia|jb) block, Om(i,a,j,b) with i fastest (ao2mo.f90:465-602 and the
+ * idx1..idx4_trans quarter transforms :1306-1439).  Ci: n x no1, Ca: n x nv1,
+ * Cj: n x no2, Cb: n x nv2 column-major (leading dimension n).  out is a host
+ * buffer of no1*nv1*no2*nv2 doubles, or NULL to keep it on the device for
+ * mq_mp2_energy. */
+int mq_ao2mo_iajb(mq_ctx *ctx, const double *Ci, int no1, const double *Ca, int nv1, const double *Cj, int no2,
+                  const double *Cb, int nv2, int precision, double *out);
+
+/* RHF MP2 from the device-resident (ia|jb) of the last mq_ao2mo_iajb call:
+ * e_out[0] = E(AA) = sum_{i<j,a<b}[(ia|jb)-(ib|ja)]^2/D,
+ * e_out[1] = E(AB) = sum_{ijab}(ia|jb)^2/D, e_out[2] = E(MBPT2) = 2*E(AA)+E(AB)
+ * (src/mp2/mp2.f90:79-144).  eig: n orbital energies. */
+int mq_mp2_rhf(mq_ctx *ctx, const double *eig, int nocc, int nvir, double *e_out);
+
+/* UHF MP2 (src/mp2/mp2.f90:154-232 with ao2mo.f90:614-904): CA, CB n x n,
+ * eA, eB n.  e_out = {E(AA), E(BB), E(AB), E(MBPT2)}. */
+int mq_mp2_uhf(mq_ctx *ctx, const double *CA, const double *CB, const double *eA, const double *eB, int noA,
+               int noB, int precision, double *e_out);
+
+/* Batched symmetric eigensolver (FP64 Jacobi): `batch` matrices of order n,
+ * A (n*n each, column-major, overwritten) -> eigenvalues w (ascending, n each)
+ * and eigenvectors V (n*n each).  Replaces DSYEV/DSYGV's eigen step
+ * (src/scf/scf.f90:692,848). */
+int mq_syev_batched(mq_ctx *ctx, int n, int batch, double *A, double *w, double *V);
+
+/* Generalized problem F C = S C eps (DSYGV itype 1, 'V', 'L',
+ * src/scf/scf.f90:478,848) for one n x n pair of host matrices. */
+int mq_sygv(mq_ctx *ctx, int n, const double *F, const double *S, double *w, double *C);
+
+/* Profiling counters of the last call (device milliseconds by stage and the
+ * number of kernel launches).  keys: "eri", "fock", "diag", "ao2mo", "mp2",
+ * "launches", "quartets", "prim_quartets".  Returns MQ_EINVAL on unknown key. */
+int mq_stat(const mq_ctx *ctx, const char *key, double *value);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MYQC_H */

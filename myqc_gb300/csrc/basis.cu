@@ -1,0 +1,229 @@
+// basis.cu -- contracted shells and primitive-pair tables from the
+// reference's flat basis arrays (src/myQC/basis.f90:23-226 layout), plus the
+// accurate Boys table used in MQ_MODE_TIGHT.
+#include <algorithm>
+#include <cmath>
+#include <map>
+
+#include "internal.h"
+
+namespace mq {
+
+static double gto_norm(int l, double a, double pi) {
+  // primitive normalisation, the formula of gtoD (src/integrals/auxilary.f90:704-726)
+  if (l == 0) return std::pow(2.0 * a / pi, 3.0 / 4.0);
+  return std::pow(128.0 * std::pow(a, 5.0) / std::pow(pi, 3.0), 1.0 / 4.0);
+}
+
+int build_shells(mq_ctx *c, int nnuc, const int *Z, const double *xyz, const double *bas, const double *set,
+                 const int *basinfo, const int *setinfo) {
+  if (nnuc <= 0 || !Z || !xyz || !bas || !set || !basinfo || !setinfo) return set_err(c, MQ_EINVAL, "null system array");
+  const int ops = basinfo[0], norb = basinfo[1];
+  const int nset = setinfo[0], setl = setinfo[1];
+  if (norb <= 0 || nset <= 0 || setl != 3 + ops) return set_err(c, MQ_EINVAL, "inconsistent basinfo/setinfo");
+  c->nnuc = nnuc;
+  c->Z.assign(Z, Z + nnuc);
+  c->xyz.resize(3 * (size_t)nnuc);
+  for (int a = 0; a < nnuc; ++a)
+    for (int k = 0; k < 3; ++k) c->xyz[3 * a + k] = xyz[a + (size_t)nnuc * k];  // xyz(0:nnuc-1,0:2)
+  const double pi = c->mode == MQ_MODE_REFERENCE ? PI_REF : PI_TRUE;
+
+  // per AO: the sets that carry it and its coefficient in each
+  std::vector<std::vector<std::pair<int, double>>> ao_sets(norb);
+  std::vector<int> set_lmax(nset), set_ctr(nset);
+  for (int s = 0; s < nset; ++s) {
+    const int *si = setinfo + 1 + s * setl;  // si[1]=#AO, si[2]=lmax, si[3]=centre, si[4..]=AOs
+    set_lmax[s] = si[2];
+    set_ctr[s] = si[3];
+    for (int k = 0; k < si[1]; ++k) {
+      int o = si[4 + k];
+      if (o < 0 || o >= norb) return set_err(c, MQ_EINVAL, "setinfo AO index out of range");
+      ao_sets[o].push_back({s, bas[s * ops + k]});
+    }
+  }
+  // group AOs that share atom and primitive sets into shells
+  std::map<std::pair<int, std::vector<int>>, std::vector<int>> groups;
+  std::vector<std::pair<int, std::vector<int>>> order;
+  for (int o = 0; o < norb; ++o) {
+    const int *bi = basinfo + 2 + 5 * o;  // [n, l, ori, nprim, centre]
+    if (bi[1] > 1) return set_err(c, MQ_EINVAL, "only s and p functions are supported");
+    std::vector<int> key;
+    for (auto &pr : ao_sets[o]) key.push_back(pr.first);
+    std::sort(key.begin(), key.end());
+    if (key.empty() || (int)key.size() > KMAX) return set_err(c, MQ_EINVAL, "AO with 0 or too many primitives");
+    auto k = std::make_pair(bi[4], key);
+    if (!groups.count(k)) order.push_back(k);
+    groups[k].push_back(o);
+  }
+  c->shells.clear();
+  for (auto &k : order) {
+    std::vector<int> &aos = groups[k];
+    std::vector<int> s_aos, p_aos[3];
+    for (int o : aos) {
+      const int *bi = basinfo + 2 + 5 * o;
+      if (bi[1] == 0) s_aos.push_back(o);
+      else if (bi[2] >= 0 && bi[2] <= 2) p_aos[bi[2]].push_back(o);
+      else return set_err(c, MQ_EINVAL, "bad p orientation");
+    }
+    size_t np = p_aos[0].size();
+    if (p_aos[1].size() != np || p_aos[2].size() != np || np > 1)
+      return set_err(c, MQ_EINVAL, "p functions must come as one x,y,z triple per primitive set group");
+    size_t nsh = std::max(s_aos.size(), np);
+    for (size_t t = 0; t < nsh; ++t) {
+      HostShell sh{};
+      sh.atom = k.first;
+      sh.has_s = t < s_aos.size();
+      sh.has_p = t < np;
+      sh.type = sh.has_p ? 1 : 0;
+      sh.nprim = (int)k.second.size();
+      sh.qlmax = 0;
+      int so = sh.has_s ? s_aos[t] : -1, px = sh.has_p ? p_aos[0][t] : -1;
+      for (int i = 0; i < sh.nprim; ++i) {
+        int s = k.second[i];
+        sh.alpha[i] = set[s];
+        sh.qlmax = std::max(sh.qlmax, set_lmax[s]);
+        auto coef_of = [&](int o) {
+          double v = 0.0;
+          if (o >= 0)
+            for (auto &pr : ao_sets[o])
+              if (pr.first == s) v = pr.second;
+          return v;
+        };
+        double csv = coef_of(so), cpv = coef_of(px);
+        sh.cs[i] = sh.has_s ? csv * gto_norm(0, set[s], pi) : 0.0;
+        sh.cp[i] = sh.has_p ? cpv * gto_norm(1, set[s], pi) : 0.0;
+      }
+      // AO indices: s, px, py, pz must be consecutive (the reference orders a
+      // section's functions that way, basis.f90:182-192)
+      if (sh.has_p && sh.has_s && (p_aos[0][t] != so + 1 || p_aos[1][t] != so + 2 || p_aos[2][t] != so + 3))
+        return set_err(c, MQ_EINVAL, "sp shell AOs are not consecutive");
+      if (sh.has_p && (p_aos[1][t] != px + 1 || p_aos[2][t] != px + 2))
+        return set_err(c, MQ_EINVAL, "p AOs are not consecutive");
+      if (!sh.has_s) return set_err(c, MQ_EINVAL, "p functions without an s function on the same primitive sets");
+      sh.ao0 = so;
+      c->shells.push_back(sh);
+    }
+  }
+  c->nshell = (int)c->shells.size();
+  c->nao = norb;
+  return MQ_OK;
+}
+
+void free_pairs(mq_ctx *c) {
+  for (void *p : c->pair_allocs) cudaFree(p);
+  c->pair_allocs.clear();
+  c->pt = PairTable{};
+}
+
+template <class T>
+static int upload(mq_ctx *c, T *&dst, const std::vector<T> &src) {
+  dst = nullptr;
+  size_t bytes = std::max<size_t>(1, src.size()) * sizeof(T);
+  cudaError_t e = cudaMalloc((void **)&dst, bytes);
+  if (e != cudaSuccess) return set_err(c, MQ_ENOMEM, "cudaMalloc pair table");
+  c->pair_allocs.push_back(dst);
+  if (!src.empty()) MQ_CUDA(c, cudaMemcpy(dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice));
+  return MQ_OK;
+}
+
+int build_pairs(mq_ctx *c) {
+  free_pairs(c);
+  const int ns = c->nshell;
+  std::vector<std::pair<int, int>> pl[3];
+  for (int a = 0; a < ns; ++a)
+    for (int b = 0; b <= a; ++b) {
+      int A = a, B = b;
+      const HostShell &sa = c->shells[a], &sb = c->shells[b];
+      if (sb.type > sa.type) std::swap(A, B);
+      pl[sa.type + sb.type].push_back({A, B});
+    }
+  std::vector<int> shA, shB, off, aoA, aoB;
+  std::vector<double> p, inv2p, beta, Px, Py, Pz, PAx, PAy, PAz, PBx, PBy, PBz, K, c4;
+  int idx = 0;
+  for (int cl = 0; cl < 3; ++cl) {
+    c->pt.class_off[cl] = idx;
+    for (auto &ab : pl[cl]) {
+      const HostShell &A = c->shells[ab.first], &B = c->shells[ab.second];
+      const double *xa = &c->xyz[3 * A.atom], *xb = &c->xyz[3 * B.atom];
+      double AB2 = 0;
+      for (int k = 0; k < 3; ++k) AB2 += (xa[k] - xb[k]) * (xa[k] - xb[k]);
+      shA.push_back(ab.first);
+      shB.push_back(ab.second);
+      aoA.push_back(A.ao0);
+      aoB.push_back(B.ao0);
+      off.push_back((int)p.size());
+      for (int i = 0; i < A.nprim; ++i)
+        for (int j = 0; j < B.nprim; ++j) {
+          double a = A.alpha[i], b = B.alpha[j], pp = a + b;
+          double Kab = std::exp(-a * b * AB2 / pp);
+          // a primitive pair whose EIJ is below 1e-14 fails the reference's
+          // screen EIJ*EGH < 1e-14 (int2e.f90:257; int1e.f90:238) for any
+          // partner, since EGH <= 1
+          if (Kab < 1.0e-14) continue;
+          double P[3], PA[3], PB[3];
+          for (int k = 0; k < 3; ++k) {
+            P[k] = (a * xa[k] + b * xb[k]) / pp;
+            PA[k] = P[k] - xa[k];
+            PB[k] = P[k] - xb[k];
+          }
+          p.push_back(pp);
+          inv2p.push_back(1.0 / (2.0 * pp));
+          beta.push_back(b);
+          Px.push_back(P[0]); Py.push_back(P[1]); Pz.push_back(P[2]);
+          PAx.push_back(PA[0]); PAy.push_back(PA[1]); PAz.push_back(PA[2]);
+          PBx.push_back(PB[0]); PBy.push_back(PB[1]); PBz.push_back(PB[2]);
+          K.push_back(Kab);
+          double ca[2] = {A.cs[i], A.cp[i]}, cb[2] = {B.cs[j], B.cp[j]};
+          for (int la = 0; la < 2; ++la)
+            for (int lb = 0; lb < 2; ++lb) c4.push_back(Kab * ca[la] * cb[lb]);
+        }
+      ++idx;
+    }
+  }
+  c->pt.class_off[3] = idx;
+  off.push_back((int)p.size());
+  c->pt.npairs = idx;
+  c->pt.npp = (int)p.size();
+  PairTable &t = c->pt;
+  MQ_TRY(upload(c, t.shA, shA));
+  MQ_TRY(upload(c, t.shB, shB));
+  MQ_TRY(upload(c, t.pp_off, off));
+  MQ_TRY(upload(c, t.aoA, aoA));
+  MQ_TRY(upload(c, t.aoB, aoB));
+  std::vector<double> ones(idx, 1.0e300);
+  MQ_TRY(upload(c, t.schwarz, ones));
+  MQ_TRY(upload(c, t.p, p));
+  MQ_TRY(upload(c, t.inv2p, inv2p));
+  MQ_TRY(upload(c, t.beta, beta));
+  MQ_TRY(upload(c, t.Px, Px)); MQ_TRY(upload(c, t.Py, Py)); MQ_TRY(upload(c, t.Pz, Pz));
+  MQ_TRY(upload(c, t.PAx, PAx)); MQ_TRY(upload(c, t.PAy, PAy)); MQ_TRY(upload(c, t.PAz, PAz));
+  MQ_TRY(upload(c, t.PBx, PBx)); MQ_TRY(upload(c, t.PBy, PBy)); MQ_TRY(upload(c, t.PBz, PBz));
+  MQ_TRY(upload(c, t.K, K));
+  MQ_TRY(upload(c, t.c4, c4));
+  c->pair_class_count = {(int)pl[0].size(), (int)pl[1].size(), (int)pl[2].size()};
+  return MQ_OK;
+}
+
+// F_m(T) for T = 0.0, 0.1, ..., 36.0 and m = 0..12 by the power series
+//   F_m(T) = e^-T sum_k (2T)^k / ((2m+1)(2m+3)...(2m+2k+1))
+// at m = 12 in long double, then downward recursion F_m = (2T F_{m+1} + e^-T)/(2m+1).
+void tight_boys_table(std::vector<double> &tab) {
+  tab.assign((size_t)TIGHT_NT * TIGHT_NM, 0.0);
+  for (int it = 0; it < TIGHT_NT; ++it) {
+    long double T = it / 10.0L;
+    const int m = TIGHT_NM - 1;
+    long double term = 1.0L / (2 * m + 1), sum = term;
+    for (int k = 1; k < 2000; ++k) {
+      term *= 2.0L * T / (2 * m + 2 * k + 1);
+      sum += term;
+      if (term < 1e-22L * sum) break;
+    }
+    long double e = expl(-T);
+    long double F[TIGHT_NM];
+    F[m] = e * sum;
+    for (int j = m - 1; j >= 0; --j) F[j] = (2.0L * T * F[j + 1] + e) / (2.0L * j + 1.0L);
+    for (int j = 0; j < TIGHT_NM; ++j) tab[(size_t)it * TIGHT_NM + j] = (double)F[j];
+  }
+}
+
+}  // namespace mq

@@ -1,0 +1,436 @@
+// capi.cu -- the extern "C" entry points of libmyqc (include/myqc.h).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "internal.h"
+
+namespace mq {
+
+int set_err(mq_ctx *c, int code, const std::string &msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+int cuda_check(mq_ctx *c, cudaError_t e, const char *what) {
+  char b[512];
+  snprintf(b, sizeof b, "%s: %s", what, cudaGetErrorString(e));
+  return set_err(c, e == cudaErrorMemoryAllocation ? MQ_ENOMEM : MQ_ECUDA, b);
+}
+
+void *buf(mq_ctx *c, const char *name, size_t bytes) {
+  DeviceBuf &b = c->bufs[name];
+  if (b.bytes >= bytes && b.ptr) return b.ptr;
+  if (b.ptr) {
+    cudaStreamSynchronize(c->stream);
+    cudaFree(b.ptr);
+    b.ptr = nullptr;
+    b.bytes = 0;
+  }
+  void *p = nullptr;
+  const size_t want = std::max<size_t>(bytes, 256);
+  if (cudaMalloc(&p, want) != cudaSuccess) {
+    cudaGetLastError();
+    set_err(c, MQ_ENOMEM, std::string("device allocation failed: ") + name);
+    return nullptr;
+  }
+  b.ptr = p;
+  b.bytes = want;
+  return p;
+}
+
+static int need_system(mq_ctx *c) {
+  if (!c) return MQ_EINVAL;
+  if (!c->have_system) return set_err(c, MQ_ESTATE, "no system: call mq_set_system first");
+  return MQ_OK;
+}
+
+// device copy of a host matrix into buffer `name`
+static double *to_dev(mq_ctx *c, const char *name, const double *h, size_t count) {
+  double *d = (double *)buf(c, name, count * sizeof(double));
+  if (!d) return nullptr;
+  if (cudaMemcpyAsync(d, h, count * sizeof(double), cudaMemcpyHostToDevice, c->stream) != cudaSuccess) {
+    set_err(c, MQ_ECUDA, "host to device copy failed");
+    return nullptr;
+  }
+  return d;
+}
+
+static int ensure_xx(mq_ctx *c) {
+  const size_t n = c->nao, n4 = n * n * n * n;
+  if (c->d_XX && c->XX_elems == n4) return MQ_OK;
+  if (c->d_XX) cudaFree(c->d_XX);
+  c->d_XX = nullptr;
+  c->XX_elems = 0;
+  if (cudaMalloc((void **)&c->d_XX, n4 * sizeof(double)) != cudaSuccess) {
+    cudaGetLastError();
+    return set_err(c, MQ_ENOMEM, "cannot allocate the n^4 integral array on the device");
+  }
+  c->XX_elems = n4;
+  return MQ_OK;
+}
+
+}  // namespace mq
+
+using namespace mq;
+
+extern "C" {
+
+const char *mq_version(void) { return "myqc-gb300 0.1 sm_103a"; }
+
+int mq_init(mq_ctx **ctx, int device) {
+  if (!ctx) return MQ_EINVAL;
+  *ctx = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return MQ_ECUDA;
+  }
+  if (device < 0 || device >= ndev) return MQ_EINVAL;
+  if (cudaSetDevice(device) != cudaSuccess) return MQ_ECUDA;
+  mq_ctx *c = new mq_ctx();
+  c->device = device;
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete c;
+    return MQ_ECUDA;
+  }
+  *ctx = c;
+  return MQ_OK;
+}
+
+int mq_free(mq_ctx *c) {
+  if (!c) return MQ_OK;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  free_pairs(c);
+  for (auto &kv : c->bufs)
+    if (kv.second.ptr) cudaFree(kv.second.ptr);
+  if (c->d_XX) cudaFree(c->d_XX);
+  if (c->d_boys) cudaFree(c->d_boys);
+  if (c->d_nuc) cudaFree(c->d_nuc);
+  if (c->cublas) cublas_destroy(c->cublas);
+  cudaStreamDestroy(c->stream);
+  delete c;
+  return MQ_OK;
+}
+
+int mq_last_error(const mq_ctx *c, char *out, int len) {
+  if (!out || len <= 0) return MQ_EINVAL;
+  const char *m = c ? c->err.c_str() : "no context";
+  strncpy(out, m, len - 1);
+  out[len - 1] = 0;
+  return MQ_OK;
+}
+
+int mq_set_system(mq_ctx *c, int nnuc, const int *Z, const double *xyz, const double *bas, const double *set,
+                  const int *basinfo, const int *setinfo, const double *ftab, int mode) {
+  if (!c) return MQ_EINVAL;
+  if (mode != MQ_MODE_REFERENCE && mode != MQ_MODE_TIGHT) return set_err(c, MQ_EINVAL, "bad mode");
+  if (mode == MQ_MODE_REFERENCE && !ftab) return set_err(c, MQ_EINVAL, "reference mode needs the Ftab table");
+  cudaSetDevice(c->device);
+  c->have_system = 0;
+  c->mode = mode;
+  MQ_TRY(build_shells(c, nnuc, Z, xyz, bas, set, basinfo, setinfo));
+  MQ_TRY(build_pairs(c));
+  // Boys table (+ its grid values Tk/10, as the reference computes them)
+  std::vector<double> tab;
+  if (mode == MQ_MODE_REFERENCE) {
+    tab.assign(ftab, ftab + FTAB_NT * FTAB_NM);
+    for (int k = 0; k < FTAB_NT; ++k) tab.push_back(k / 10.0);
+  } else {
+    tight_boys_table(tab);
+    for (int k = 0; k < TIGHT_NT; ++k) tab.push_back(k / 10.0);
+  }
+  if (c->d_boys) cudaFree(c->d_boys);
+  c->d_boys = nullptr;
+  MQ_CUDA(c, cudaMalloc((void **)&c->d_boys, tab.size() * sizeof(double)));
+  MQ_CUDA(c, cudaMemcpy(c->d_boys, tab.data(), tab.size() * sizeof(double), cudaMemcpyHostToDevice));
+  std::vector<double> nuc(4 * (size_t)nnuc);
+  for (int a = 0; a < nnuc; ++a) {
+    for (int k = 0; k < 3; ++k) nuc[4 * a + k] = c->xyz[3 * a + k];
+    nuc[4 * a + 3] = Z[a];
+  }
+  if (c->d_nuc) cudaFree(c->d_nuc);
+  c->d_nuc = nullptr;
+  MQ_CUDA(c, cudaMalloc((void **)&c->d_nuc, nuc.size() * sizeof(double)));
+  MQ_CUDA(c, cudaMemcpy(c->d_nuc, nuc.data(), nuc.size() * sizeof(double), cudaMemcpyHostToDevice));
+  // integrals of a previous system are stale
+  if (c->d_XX) cudaFree(c->d_XX);
+  c->d_XX = nullptr;
+  c->XX_elems = 0;
+  c->have_system = 1;
+  if (c->schwarz_thr > 0) MQ_TRY(eri_schwarz(c));
+  return MQ_OK;
+}
+
+int mq_norb(const mq_ctx *c, int *norb) {
+  if (!c || !norb) return MQ_EINVAL;
+  if (!c->have_system) return MQ_ESTATE;
+  *norb = c->nao;
+  return MQ_OK;
+}
+
+int mq_set_schwarz(mq_ctx *c, double threshold) {
+  if (!c || threshold < 0) return MQ_EINVAL;
+  c->schwarz_thr = threshold;
+  if (c->have_system && threshold > 0) return eri_schwarz(c);
+  return MQ_OK;
+}
+
+int mq_int1e(mq_ctx *c, double *S, double *H) {
+  MQ_TRY(need_system(c));
+  if (!S || !H) return set_err(c, MQ_EINVAL, "null output");
+  cudaSetDevice(c->device);
+  const size_t n2 = (size_t)c->nao * c->nao;
+  double *d = (double *)buf(c, "int1e_out", 2 * n2 * sizeof(double));
+  if (!d) return MQ_ENOMEM;
+  MQ_TRY(int1e_device(c, d, d + n2));
+  MQ_CUDA(c, cudaMemcpyAsync(S, d, n2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  MQ_CUDA(c, cudaMemcpyAsync(H, d + n2, n2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  MQ_CUDA(c, cudaStreamSynchronize(c->stream));
+  return MQ_OK;
+}
+
+int mq_eri_store(mq_ctx *c) {
+  MQ_TRY(need_system(c));
+  cudaSetDevice(c->device);
+  MQ_TRY(ensure_xx(c));
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventRecord(e0, c->stream);
+  int rc = eri_full_device(c, c->d_XX);
+  cudaEventRecord(e1, c->stream);
+  cudaEventSynchronize(e1);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e0, e1);
+  c->stats.ms_eri = ms;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return rc;
+}
+
+int mq_eri_full(mq_ctx *c, double *XX) {
+  if (!XX) return set_err(c, MQ_EINVAL, "null output");
+  MQ_TRY(mq_eri_store(c));
+  MQ_CUDA(c, cudaMemcpyAsync(XX, c->d_XX, c->XX_elems * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  MQ_CUDA(c, cudaStreamSynchronize(c->stream));
+  return MQ_OK;
+}
+
+int mq_eri_upload(mq_ctx *c, const double *XX) {
+  MQ_TRY(need_system(c));
+  if (!XX) return set_err(c, MQ_EINVAL, "null input");
+  cudaSetDevice(c->device);
+  MQ_TRY(ensure_xx(c));
+  MQ_CUDA(c, cudaMemcpyAsync(c->d_XX, XX, c->XX_elems * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  MQ_CUDA(c, cudaStreamSynchronize(c->stream));
+  return MQ_OK;
+}
+
+static int fock_common(mq_ctx *c, const double *Da, const double *Db, double *Ga, double *Gb, bool direct) {
+  MQ_TRY(need_system(c));
+  if (!Da || !Ga || (Db && !Gb)) return set_err(c, MQ_EINVAL, "null matrix");
+  cudaSetDevice(c->device);
+  const size_t n2 = (size_t)c->nao * c->nao;
+  const int ns = Db ? 2 : 1;
+  double *dD = to_dev(c, "fock_in", Da, n2 * ns);
+  if (!dD) return MQ_ENOMEM;
+  if (Db) MQ_CUDA(c, cudaMemcpyAsync(dD + n2, Db, n2 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  double *dG = (double *)buf(c, "fock_out", n2 * (ns + 3) * sizeof(double));
+  if (!dG) return MQ_ENOMEM;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventRecord(e0, c->stream);
+  int rc;
+  if (direct) {
+    double *J = dG + n2 * ns, *Ka = J + n2, *Kb = Db ? Ka + n2 : nullptr;
+    rc = fock_direct_device(c, dD, Db ? dD + n2 : nullptr, J, Ka, Kb);
+    if (rc == MQ_OK) rc = direct_combine(c, J, Ka, Kb, dG, Db ? dG + n2 : nullptr);
+  } else {
+    rc = fock_stored_device(c, dD, Db ? dD + n2 : nullptr, dG, Db ? dG + n2 : nullptr);
+  }
+  cudaEventRecord(e1, c->stream);
+  cudaEventSynchronize(e1);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e0, e1);
+  c->stats.ms_fock = ms;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc != MQ_OK) return rc;
+  MQ_CUDA(c, cudaMemcpyAsync(Ga, dG, n2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  if (Db) MQ_CUDA(c, cudaMemcpyAsync(Gb, dG + n2, n2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  MQ_CUDA(c, cudaStreamSynchronize(c->stream));
+  return MQ_OK;
+}
+
+int mq_fock(mq_ctx *c, const double *Da, const double *Db, double *Ga, double *Gb) {
+  return fock_common(c, Da, Db, Ga, Gb, false);
+}
+
+int mq_fock_direct(mq_ctx *c, const double *Da, const double *Db, double *Ga, double *Gb) {
+  return fock_common(c, Da, Db, Ga, Gb, true);
+}
+
+int mq_scf(mq_ctx *c, const double *S, const double *H, const mq_scf_opts *o, double *C, double *eps, double *D,
+           double *energy, int *iters, double *history) {
+  MQ_TRY(need_system(c));
+  if (!S || !H || !o || !C || !eps || !energy || !iters) return set_err(c, MQ_EINVAL, "null argument");
+  cudaSetDevice(c->device);
+  return scf_device(c, S, H, o, C, eps, D, energy, iters, history);
+}
+
+int mq_ao2mo_iajb(mq_ctx *c, const double *Ci, int no1, const double *Ca, int nv1, const double *Cj, int no2,
+                  const double *Cb, int nv2, int precision, double *out) {
+  MQ_TRY(need_system(c));
+  if (!Ci || !Ca || !Cj || !Cb || no1 < 0 || nv1 < 0 || no2 < 0 || nv2 < 0)
+    return set_err(c, MQ_EINVAL, "bad ao2mo arguments");
+  if (precision != MQ_PREC_FP64 && precision != MQ_PREC_SPLIT_BF16) return set_err(c, MQ_EINVAL, "bad precision");
+  cudaSetDevice(c->device);
+  const size_t n = c->nao;
+  // pack all four coefficient blocks into one buffer
+  double *dCc = (double *)buf(c, "ao2mo_C", n * (size_t)(no1 + nv1 + no2 + nv2) * sizeof(double));
+  if (!dCc) return MQ_ENOMEM;
+  double *dCi = dCc, *dCa = dCi + n * no1, *dCj = dCa + n * nv1, *dCb = dCj + n * no2;
+  MQ_CUDA(c, cudaMemcpyAsync(dCi, Ci, n * no1 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  MQ_CUDA(c, cudaMemcpyAsync(dCa, Ca, n * nv1 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  MQ_CUDA(c, cudaMemcpyAsync(dCj, Cj, n * no2 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  MQ_CUDA(c, cudaMemcpyAsync(dCb, Cb, n * nv2 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  const size_t cnt = (size_t)no1 * nv1 * no2 * nv2;
+  if (c->iajb_elems < cnt) {
+    if (c->d_iajb) cudaFree(c->d_iajb);
+    c->d_iajb = nullptr;
+    c->iajb_elems = 0;
+    MQ_CUDA(c, cudaMalloc((void **)&c->d_iajb, std::max<size_t>(cnt, 1) * sizeof(double)));
+    c->iajb_elems = cnt;
+  }
+  c->iajb_dims[0] = no1;
+  c->iajb_dims[1] = nv1;
+  c->iajb_dims[2] = no2;
+  c->iajb_dims[3] = nv2;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventRecord(e0, c->stream);
+  int rc = ao2mo_device(c, dCi, no1, dCa, nv1, dCj, no2, dCb, nv2, precision, c->d_iajb);
+  cudaEventRecord(e1, c->stream);
+  cudaEventSynchronize(e1);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e0, e1);
+  c->stats.ms_ao2mo = ms;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc != MQ_OK) return rc;
+  if (out) {
+    MQ_CUDA(c, cudaMemcpyAsync(out, c->d_iajb, cnt * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    MQ_CUDA(c, cudaStreamSynchronize(c->stream));
+  }
+  return MQ_OK;
+}
+
+int mq_mp2_rhf(mq_ctx *c, const double *eig, int nocc, int nvir, double *e_out) {
+  MQ_TRY(need_system(c));
+  if (!eig || !e_out) return set_err(c, MQ_EINVAL, "null argument");
+  if (c->iajb_dims[0] != nocc || c->iajb_dims[1] != nvir || c->iajb_dims[2] != nocc || c->iajb_dims[3] != nvir)
+    return set_err(c, MQ_ESTATE, "the device (ia|jb) block does not match nocc/nvir");
+  cudaSetDevice(c->device);
+  double *de = to_dev(c, "mp2_eig", eig, (size_t)nocc + nvir);
+  if (!de) return MQ_ENOMEM;
+  return mp2_rhf_device(c, c->d_iajb, de, nocc, nvir, e_out);
+}
+
+int mq_mp2_uhf(mq_ctx *c, const double *CA, const double *CB, const double *eA, const double *eB, int noA, int noB,
+               int precision, double *e_out) {
+  MQ_TRY(need_system(c));
+  if (!CA || !CB || !eA || !eB || !e_out) return set_err(c, MQ_EINVAL, "null argument");
+  const int n = c->nao, nvA = n - noA, nvB = n - noB;
+  if (noA < 0 || noB < 0 || nvA < 0 || nvB < 0) return set_err(c, MQ_EINVAL, "bad occupation");
+  double *de = to_dev(c, "mp2_eig", eA, (size_t)2 * n);
+  if (!de) return MQ_ENOMEM;
+  MQ_CUDA(c, cudaMemcpyAsync(de + n, eB, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  double s[2], out[3];
+  // alpha-alpha, beta-beta, alpha-beta blocks as slow_ao2mo_MP2_UHF builds them (ao2mo.f90:614-904)
+  const double *Cs[3][2] = {{CA, CA}, {CB, CB}, {CA, CB}};
+  const int no[3][2] = {{noA, noA}, {noB, noB}, {noA, noB}};
+  for (int blk = 0; blk < 3; ++blk) {
+    const double *C1 = Cs[blk][0], *C2 = Cs[blk][1];
+    const int o1 = no[blk][0], o2 = no[blk][1], v1 = n - o1, v2 = n - o2;
+    MQ_TRY(mq_ao2mo_iajb(c, C1, o1, C1 + (size_t)n * o1, v1, C2, o2, C2 + (size_t)n * o2, v2, precision, nullptr));
+    const double *e1 = blk == 1 ? de + n : de, *e2 = blk == 0 ? de : de + n;
+    // mp2_pair_sums takes eo = e[0:no], ev = e[no:] for each side
+    MQ_TRY(mp2_pair_sums(c, c->d_iajb, o1, v1, o2, v2, e1, e2, blk < 2, s));
+    out[blk] = blk < 2 ? s[1] : s[0];
+  }
+  e_out[0] = out[0];
+  e_out[1] = out[1];
+  e_out[2] = out[2];
+  e_out[3] = out[0] + out[1] + out[2];
+  return MQ_OK;
+}
+
+int mq_syev_batched(mq_ctx *c, int n, int batch, double *A, double *w, double *V) {
+  if (!c || !A || !w || !V || n <= 0 || batch <= 0) return MQ_EINVAL;
+  cudaSetDevice(c->device);
+  const size_t n2 = (size_t)n * n;
+  double *dA = to_dev(c, "syev_A", A, n2 * batch);
+  double *dV = (double *)buf(c, "syev_V", (n2 + n) * batch * sizeof(double));
+  if (!dA || !dV) return MQ_ENOMEM;
+  double *dw = dV + n2 * batch;
+  MQ_TRY(syev_batched_device(c, n, batch, dA, dw, dV));
+  MQ_CUDA(c, cudaMemcpyAsync(V, dV, n2 * batch * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  MQ_CUDA(c, cudaMemcpyAsync(w, dw, (size_t)n * batch * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  MQ_CUDA(c, cudaStreamSynchronize(c->stream));
+  return MQ_OK;
+}
+
+int mq_sygv(mq_ctx *c, int n, const double *F, const double *S, double *w, double *C) {
+  if (!c || !F || !S || !w || !C || n <= 0) return MQ_EINVAL;
+  cudaSetDevice(c->device);
+  const size_t n2 = (size_t)n * n;
+  // S = U s U^T, X = U s^-1/2 U^T, F' = X^T F X = V w V^T, C = X V
+  std::vector<double> hs(n), U(n2), X(n2, 0.0), T(n2), Fp(n2, 0.0), V(n2);
+  std::vector<double> Sc(S, S + n2);
+  MQ_TRY(mq_syev_batched(c, n, 1, Sc.data(), hs.data(), U.data()));
+  if (hs[0] <= 0) return set_err(c, MQ_EINVAL, "S not positive definite");
+  double *d = (double *)buf(c, "sygv", 4 * n2 * sizeof(double));
+  if (!d) return MQ_ENOMEM;
+  double *dU = d, *dX = d + n2, *dT = d + 2 * n2, *dF = d + 3 * n2;
+  for (size_t i = 0; i < n2; ++i) T[i] = U[i] / std::sqrt(hs[i / n]);
+  MQ_CUDA(c, cudaMemcpyAsync(dU, U.data(), n2 * 8, cudaMemcpyHostToDevice, c->stream));
+  MQ_CUDA(c, cudaMemcpyAsync(dT, T.data(), n2 * 8, cudaMemcpyHostToDevice, c->stream));
+  MQ_TRY(gemm(c, 'N', 'T', n, n, n, 1.0, dT, n, dU, n, 0.0, dX, n));
+  MQ_CUDA(c, cudaMemcpyAsync(dF, F, n2 * 8, cudaMemcpyHostToDevice, c->stream));
+  MQ_TRY(gemm(c, 'T', 'N', n, n, n, 1.0, dX, n, dF, n, 0.0, dT, n));
+  MQ_TRY(gemm(c, 'N', 'N', n, n, n, 1.0, dT, n, dX, n, 0.0, dU, n));
+  MQ_CUDA(c, cudaMemcpyAsync(Fp.data(), dU, n2 * 8, cudaMemcpyDeviceToHost, c->stream));
+  MQ_CUDA(c, cudaMemcpyAsync(X.data(), dX, n2 * 8, cudaMemcpyDeviceToHost, c->stream));
+  MQ_CUDA(c, cudaStreamSynchronize(c->stream));
+  MQ_TRY(mq_syev_batched(c, n, 1, Fp.data(), w, V.data()));
+  MQ_CUDA(c, cudaMemcpyAsync(dT, V.data(), n2 * 8, cudaMemcpyHostToDevice, c->stream));
+  MQ_CUDA(c, cudaMemcpyAsync(dX, X.data(), n2 * 8, cudaMemcpyHostToDevice, c->stream));
+  MQ_TRY(gemm(c, 'N', 'N', n, n, n, 1.0, dX, n, dT, n, 0.0, dF, n));
+  MQ_CUDA(c, cudaMemcpyAsync(C, dF, n2 * 8, cudaMemcpyDeviceToHost, c->stream));
+  MQ_CUDA(c, cudaStreamSynchronize(c->stream));
+  return MQ_OK;
+}
+
+int mq_stat(const mq_ctx *c, const char *key, double *value) {
+  if (!c || !key || !value) return MQ_EINVAL;
+  const Stats &s = c->stats;
+  if (!strcmp(key, "eri")) *value = s.ms_eri;
+  else if (!strcmp(key, "fock")) *value = s.ms_fock;
+  else if (!strcmp(key, "diag")) *value = s.ms_diag;
+  else if (!strcmp(key, "ao2mo")) *value = s.ms_ao2mo;
+  else if (!strcmp(key, "mp2")) *value = s.ms_mp2;
+  else if (!strcmp(key, "launches")) *value = s.launches;
+  else if (!strcmp(key, "quartets")) *value = s.quartets;
+  else if (!strcmp(key, "prim_quartets")) *value = s.prim_quartets;
+  else return MQ_EINVAL;
+  return MQ_OK;
+}
+
+}  // extern "C"

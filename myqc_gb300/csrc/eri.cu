@@ -1,0 +1,492 @@
+// eri.cu -- FP64 two-electron repulsion integrals over contracted s/sp shell
+// quartets (McMurchie-Davidson), with three epilogues:
+//   EPI_XX      scatter each unique integral to its 8 places in the full
+//               XX(i,j,g,h) array (replaces proc2e + fillsym,
+//               src/integrals/int2e.f90:78-351,540-613);
+//   EPI_SCHWARZ sqrt(max |(ab|ab)|) per shell pair (Schwarz bounds);
+//   EPI_FOCK    digest each unique integral straight into J and K (direct SCF;
+//               the reference digests the stored XX in RHFI2G/UHFI2G).
+//
+// Integral formula (the reference's clmnew, int2e.f90:618-726):
+//   (ab|cd) = sum_prim  2 pi^5/2 / (p q sqrt(p+q)) *
+//             sum_{tuv} E^{ab}_{tuv} sum_{t'u'v'} (-1)^{t'+u'+v'} E^{cd}_{t'u'v'}
+//             R_{t+t',u+u',v+v'}(alpha = pq/(p+q), PQ)
+// with E the Hermite expansion coefficients (auxilary.f90:349-536), R the
+// Hermite Coulomb integrals (RNLMj, auxilary.f90:22-80) built on the Boys
+// values of boys.cuh, contraction coefficients times the primitive norms of
+// gtoD (auxilary.f90:704-726), and the reference's primitive screen
+// EIJ*EGH < 1e-14 (int2e.f90:257).
+//
+// Work decomposition: one thread per contracted shell quartet.  Shell pairs
+// are kept in three classes (s,s), (sp,s), (sp,sp); a kernel instance serves
+// one (bra class, ket class) combination, so every thread of a launch runs the
+// same fully unrolled register code.  Quartets with more than 16 integrals
+// ((sp sp|sp s): 64, (sp sp|sp sp): 256) are split over 4 or 16 threads by
+// bra function; the split index is constant per warp (warp w serves split
+// w % nsplit for 32 consecutive quartets), so no lane diverges.
+#include <algorithm>
+
+#include "boys.cuh"
+#include "internal.h"
+
+namespace mq {
+
+enum { EPI_XX = 0, EPI_SCHWARZ = 1, EPI_FOCK = 2 };
+
+struct EriArgs {
+  PairTable t;
+  const double *boys;
+  int mode;
+  int n;
+  int pOff, nP, qOff, nQ;
+  int tri;       // bra and ket pairs from the same class: P >= Q
+  int diag;      // Schwarz: quartet (P,P) only
+  long long nq;  // quartets in this launch
+  double thr;    // Schwarz threshold (0: off)
+  double *XX;
+  unsigned long long *sch;  // Schwarz output (bit pattern of a positive double)
+  const double *Da, *Db;
+  double *J, *Ka, *Kb;
+  int uhf;
+  unsigned long long *counters;  // [0] quartets computed, [1] primitive quartets
+};
+
+__host__ __device__ constexpr int fl(int f, int axis) { return f == axis + 1 ? 1 : 0; }  // f: 0 s, 1 px, 2 py, 3 pz
+__host__ __device__ constexpr int fang(int f) { return f > 0 ? 1 : 0; }
+__host__ __device__ constexpr int nfun(int L) { return L ? 4 : 1; }
+
+// Is Hermite index (t,u,v) used by some bra pair (a,b) with a in [A0,A1), b in [B0,B1)?
+__host__ __device__ constexpr bool bra_needs(int A0, int A1, int B0, int B1, int t, int u, int v) {
+  for (int a = A0; a < A1; ++a)
+    for (int b = B0; b < B1; ++b)
+      if (t <= fl(a, 0) + fl(b, 0) && u <= fl(a, 1) + fl(b, 1) && v <= fl(a, 2) + fl(b, 2)) return true;
+  return false;
+}
+
+// Hermite R_{tuv} (t+u+v <= L) from F_j already scaled by the prefactor.
+template <int L>
+__device__ __forceinline__ void hermite_R(const double (&F)[L + 1], double m2a, double X, double Y, double Z,
+                                          double (&R)[L + 1][L + 1][L + 1]) {
+  double Rj[L + 1][L + 1][L + 1][L + 1];
+  double pw = 1.0;
+#pragma unroll
+  for (int j = 0; j <= L; ++j) {
+    Rj[j][0][0][0] = pw * F[j];
+    pw *= m2a;
+  }
+#pragma unroll
+  for (int j = L - 1; j >= 0; --j) {
+#pragma unroll
+    for (int t = 0; t <= L; ++t)
+#pragma unroll
+      for (int u = 0; u <= L; ++u)
+#pragma unroll
+        for (int v = 0; v <= L; ++v) {
+          if (t + u + v == 0 || t + u + v > L - j) continue;
+          double r;
+          if (t > 0) {
+            r = X * Rj[j + 1][t - 1][u][v];
+            if (t > 1) r += (t - 1) * Rj[j + 1][t - 2][u][v];
+          } else if (u > 0) {
+            r = Y * Rj[j + 1][t][u - 1][v];
+            if (u > 1) r += (u - 1) * Rj[j + 1][t][u - 2][v];
+          } else {
+            r = Z * Rj[j + 1][t][u][v - 1];
+            if (v > 1) r += (v - 1) * Rj[j + 1][t][u][v - 2];
+          }
+          Rj[j][t][u][v] = r;
+        }
+  }
+#pragma unroll
+  for (int t = 0; t <= L; ++t)
+#pragma unroll
+    for (int u = 0; u <= L; ++u)
+#pragma unroll
+      for (int v = 0; v <= L; ++v)
+        if (t + u + v <= L) R[t][u][v] = Rj[0][t][u][v];
+}
+
+// Per-axis Hermite coefficients of a primitive pair for l_a, l_b in {0,1}:
+// e[la][lb][t], t <= la+lb (sign folded in for the ket when sgn = -1).
+__device__ __forceinline__ void pair_E(double PA, double PB, double i2p, double sgn, double (&e)[2][2][3]) {
+  e[0][0][0] = 1.0;
+  e[1][0][0] = PA;
+  e[1][0][1] = sgn * i2p;
+  e[0][1][0] = PB;
+  e[0][1][1] = sgn * i2p;
+  e[1][1][0] = PA * PB + i2p;
+  e[1][1][1] = sgn * (PA + PB) * i2p;
+  e[1][1][2] = i2p * i2p;
+}
+
+template <int LA, int LB, int LC, int LD, int A0, int A1, int B0, int B1, int EPI>
+__device__ __forceinline__ void quartet(const EriArgs &g, int P, int Q) {
+  constexpr int NC = nfun(LC), ND = nfun(LD);
+  constexpr int LAB = LA + LB, LT = LA + LB + LC + LD;
+  constexpr int QREF = 3 * LT;  // the reference's Boys order for s/sp sets
+  const PairTable &t = g.t;
+  double acc[A1 - A0][B1 - B0][NC][ND];
+#pragma unroll
+  for (int a = 0; a < A1 - A0; ++a)
+#pragma unroll
+    for (int b = 0; b < B1 - B0; ++b)
+#pragma unroll
+      for (int c = 0; c < NC; ++c)
+#pragma unroll
+        for (int d = 0; d < ND; ++d) acc[a][b][c][d] = 0.0;
+
+  const int p0 = t.pp_off[P], p1 = t.pp_off[P + 1];
+  const int q0 = t.pp_off[Q], q1 = t.pp_off[Q + 1];
+  const bool parity = g.mode == MQ_MODE_REFERENCE;
+  const double pref0 = parity ? 2.0 * 17.493419544621675 : 2.0 * 17.493418327624862;  // 2 pi^2.5
+  unsigned nprim = 0;
+  for (int ip = p0; ip < p1; ++ip) {
+    const double p = t.p[ip], i2p = t.inv2p[ip], Kab = t.K[ip];
+    const double Px = t.Px[ip], Py = t.Py[ip], Pz = t.Pz[ip];
+    double ex[2][2][3], ey[2][2][3], ez[2][2][3];
+    pair_E(t.PAx[ip], t.PBx[ip], i2p, 1.0, ex);
+    pair_E(t.PAy[ip], t.PBy[ip], i2p, 1.0, ey);
+    pair_E(t.PAz[ip], t.PBz[ip], i2p, 1.0, ez);
+    double cab[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) cab[k] = t.c4[4 * ip + k];
+    // bra products E^{ab}_{tuv} * c_a c_b K_ab
+    double eb[A1 - A0][B1 - B0][3][3][3];
+#pragma unroll
+    for (int a = A0; a < A1; ++a)
+#pragma unroll
+      for (int b = B0; b < B1; ++b)
+#pragma unroll
+        for (int x = 0; x <= fl(a, 0) + fl(b, 0); ++x)
+#pragma unroll
+          for (int y = 0; y <= fl(a, 1) + fl(b, 1); ++y)
+#pragma unroll
+            for (int z = 0; z <= fl(a, 2) + fl(b, 2); ++z)
+              eb[a - A0][b - B0][x][y][z] = ex[fl(a, 0)][fl(b, 0)][x] * ey[fl(a, 1)][fl(b, 1)][y] *
+                                            ez[fl(a, 2)][fl(b, 2)][z] * cab[2 * fang(a) + fang(b)];
+    for (int iq = q0; iq < q1; ++iq) {
+      const double Kcd = t.K[iq];
+      if (Kab * Kcd < 1.0e-14) continue;  // int2e.f90:257
+      ++nprim;
+      const double q = t.p[iq], i2q = t.inv2p[iq];
+      const double X = Px - t.Px[iq], Y = Py - t.Py[iq], Z = Pz - t.Pz[iq];
+      const double s = p + q;
+      const double rs = rsqrt(s);
+      const double ipq = 4.0 * i2p * i2q;  // 1/(pq)
+      const double alpha = (p * q) * (rs * rs);
+      const double T = alpha * (X * X + Y * Y + Z * Z);
+      const double pref = pref0 * rs * ipq;
+      double F[LT + 1];
+      boys<QREF, LT>(g.mode, T, g.boys, F);
+#pragma unroll
+      for (int j = 0; j <= LT; ++j) F[j] *= pref;
+      double R[LT + 1][LT + 1][LT + 1];
+      hermite_R<LT>(F, -2.0 * alpha, X, Y, Z, R);
+      double fx[2][2][3], fy[2][2][3], fz[2][2][3];
+      pair_E(t.PAx[iq], t.PBx[iq], i2q, -1.0, fx);
+      pair_E(t.PAy[iq], t.PBy[iq], i2q, -1.0, fy);
+      pair_E(t.PAz[iq], t.PBz[iq], i2q, -1.0, fz);
+      double ccd[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) ccd[k] = t.c4[4 * iq + k];
+#pragma unroll
+      for (int c = 0; c < NC; ++c)
+#pragma unroll
+        for (int d = 0; d < ND; ++d) {
+          const double cf = ccd[2 * fang(c) + fang(d)];
+          double W[LAB + 1][LAB + 1][LAB + 1];
+#pragma unroll
+          for (int x = 0; x <= LAB; ++x)
+#pragma unroll
+            for (int y = 0; y <= LAB; ++y)
+#pragma unroll
+              for (int z = 0; z <= LAB; ++z) {
+                if (x + y + z > LAB || !bra_needs(A0, A1, B0, B1, x, y, z)) continue;
+                double w = 0.0;
+#pragma unroll
+                for (int xx = 0; xx <= fl(c, 0) + fl(d, 0); ++xx)
+#pragma unroll
+                  for (int yy = 0; yy <= fl(c, 1) + fl(d, 1); ++yy)
+#pragma unroll
+                    for (int zz = 0; zz <= fl(c, 2) + fl(d, 2); ++zz)
+                      w += (fx[fl(c, 0)][fl(d, 0)][xx] * fy[fl(c, 1)][fl(d, 1)][yy] * fz[fl(c, 2)][fl(d, 2)][zz]) *
+                           R[x + xx][y + yy][z + zz];
+                W[x][y][z] = w * cf;
+              }
+#pragma unroll
+          for (int a = A0; a < A1; ++a)
+#pragma unroll
+            for (int b = B0; b < B1; ++b) {
+              double v = 0.0;
+#pragma unroll
+              for (int x = 0; x <= fl(a, 0) + fl(b, 0); ++x)
+#pragma unroll
+                for (int y = 0; y <= fl(a, 1) + fl(b, 1); ++y)
+#pragma unroll
+                  for (int z = 0; z <= fl(a, 2) + fl(b, 2); ++z) v += eb[a - A0][b - B0][x][y][z] * W[x][y][z];
+              acc[a - A0][b - B0][c][d] += v;
+            }
+        }
+    }
+  }
+
+  // ---------------- epilogues ----------------
+  const int A = t.shA[P], B = t.shB[P], C = t.shA[Q], D = t.shB[Q];
+  const int i0 = t.aoA[P], j0 = t.aoB[P], k0 = t.aoA[Q], l0 = t.aoB[Q];
+  if (EPI == EPI_SCHWARZ) {
+    double m = 0.0;
+#pragma unroll
+    for (int a = A0; a < A1; ++a)
+#pragma unroll
+      for (int b = B0; b < B1; ++b)
+        if (a < NC && b < ND) m = fmax(m, fabs(acc[a - A0][b - B0][a][b]));
+    atomicMax(g.sch + P, (unsigned long long)__double_as_longlong(sqrt(m)));
+    return;
+  }
+  if (g.counters && A0 == 0 && B0 == 0) {
+    atomicAdd(g.counters, 1ull);
+    atomicAdd(g.counters + 1, (unsigned long long)nprim);
+  }
+  const size_t n = (size_t)g.n;
+#pragma unroll
+  for (int a = A0; a < A1; ++a)
+#pragma unroll
+    for (int b = B0; b < B1; ++b)
+#pragma unroll
+      for (int c = 0; c < NC; ++c)
+#pragma unroll
+        for (int d = 0; d < ND; ++d) {
+          const int i = i0 + a, j = j0 + b, k = k0 + c, l = l0 + d;
+          if (A == B && i < j) continue;
+          if (C == D && k < l) continue;
+          if (P == Q && (size_t)i * n + j < (size_t)k * n + l) continue;
+          const double x = acc[a - A0][b - B0][c][d];
+          if (EPI == EPI_XX) {
+            double *XX = g.XX;
+            const size_t ij = (size_t)i + n * j, ji = (size_t)j + n * i, kl = (size_t)k + n * l,
+                         lk = (size_t)l + n * k, n2 = n * n;
+            XX[ij + n2 * kl] = x;
+            XX[ji + n2 * kl] = x;
+            XX[ij + n2 * lk] = x;
+            XX[ji + n2 * lk] = x;
+            XX[kl + n2 * ij] = x;
+            XX[lk + n2 * ij] = x;
+            XX[kl + n2 * ji] = x;
+            XX[lk + n2 * ji] = x;
+          } else {  // EPI_FOCK: half-sums, symmetrised afterwards
+            double deg = 1.0;
+            if (i == j) deg *= 0.5;
+            if (k == l) deg *= 0.5;
+            if (i == k && j == l) deg *= 0.5;
+            const double x2 = 2.0 * deg * x, x4 = 2.0 * x2;
+            const double *Da = g.Da;
+            if (!g.uhf) {
+              atomicAdd(g.J + i + n * j, x4 * Da[k + n * l]);
+              atomicAdd(g.J + k + n * l, x4 * Da[i + n * j]);
+              atomicAdd(g.Ka + i + n * k, x2 * Da[j + n * l]);
+              atomicAdd(g.Ka + j + n * k, x2 * Da[i + n * l]);
+              atomicAdd(g.Ka + i + n * l, x2 * Da[j + n * k]);
+              atomicAdd(g.Ka + j + n * l, x2 * Da[i + n * k]);
+            } else {
+              const double *Db = g.Db;
+              atomicAdd(g.J + i + n * j, x4 * (Da[k + n * l] + Db[k + n * l]));
+              atomicAdd(g.J + k + n * l, x4 * (Da[i + n * j] + Db[i + n * j]));
+              atomicAdd(g.Ka + i + n * k, x2 * Da[j + n * l]);
+              atomicAdd(g.Ka + j + n * k, x2 * Da[i + n * l]);
+              atomicAdd(g.Ka + i + n * l, x2 * Da[j + n * k]);
+              atomicAdd(g.Ka + j + n * l, x2 * Da[i + n * k]);
+              atomicAdd(g.Kb + i + n * k, x2 * Db[j + n * l]);
+              atomicAdd(g.Kb + j + n * k, x2 * Db[i + n * l]);
+              atomicAdd(g.Kb + i + n * l, x2 * Db[j + n * k]);
+              atomicAdd(g.Kb + j + n * l, x2 * Db[i + n * k]);
+            }
+          }
+        }
+}
+
+// decode (P, Q) of quartet index q in the launch; returns false past the end
+__device__ __forceinline__ bool decode(const EriArgs &g, long long q, int &P, int &Q) {
+  if (q >= g.nq) return false;
+  if (g.diag) {
+    P = Q = g.pOff + (int)q;
+    return true;
+  }
+  if (g.tri) {
+    long long r = (long long)((sqrt(8.0 * (double)q + 1.0) - 1.0) * 0.5);
+    while (r * (r + 1) / 2 > q) --r;
+    while ((r + 1) * (r + 2) / 2 <= q) ++r;
+    P = g.pOff + (int)r;
+    Q = g.qOff + (int)(q - r * (r + 1) / 2);
+  } else {
+    P = g.pOff + (int)(q / g.nQ);
+    Q = g.qOff + (int)(q % g.nQ);
+  }
+  if (g.thr > 0.0 && g.t.schwarz[P] * g.t.schwarz[Q] < g.thr) return false;
+  return true;
+}
+
+template <int LA, int LB, int LC, int LD, int EPI>
+__global__ void __launch_bounds__(128) eri_kernel(EriArgs g) {
+  constexpr int NA = nfun(LA), NB = nfun(LB);
+  constexpr int NOUT = NA * NB * nfun(LC) * nfun(LD);
+  constexpr int NSPLIT = NOUT <= 16 ? 1 : (NOUT <= 64 ? 4 : 16);
+  const long long gtid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long warp = gtid >> 5;
+  const int lane = threadIdx.x & 31;
+  const int split = (int)(warp % NSPLIT);
+  const long long q = (warp / NSPLIT) * 32 + lane;
+  int P, Q;
+  if (!decode(g, q, P, Q)) return;
+  if (NSPLIT == 1) {
+    quartet<LA, LB, LC, LD, 0, NA, 0, NB, EPI>(g, P, Q);
+  } else if (NSPLIT == 4) {
+    switch (split) {
+      case 0: quartet<LA, LB, LC, LD, 0, 1, 0, NB, EPI>(g, P, Q); break;
+      case 1: quartet<LA, LB, LC, LD, 1, 2, 0, NB, EPI>(g, P, Q); break;
+      case 2: quartet<LA, LB, LC, LD, 2, 3, 0, NB, EPI>(g, P, Q); break;
+      default: quartet<LA, LB, LC, LD, 3, 4, 0, NB, EPI>(g, P, Q); break;
+    }
+  } else {
+#define MQ_SPLIT16(s) \
+  case s: quartet<LA, LB, LC, LD, (s) / 4, (s) / 4 + 1, (s) % 4, (s) % 4 + 1, EPI>(g, P, Q); break;
+    switch (split) {
+      MQ_SPLIT16(0) MQ_SPLIT16(1) MQ_SPLIT16(2) MQ_SPLIT16(3) MQ_SPLIT16(4) MQ_SPLIT16(5) MQ_SPLIT16(6)
+      MQ_SPLIT16(7) MQ_SPLIT16(8) MQ_SPLIT16(9) MQ_SPLIT16(10) MQ_SPLIT16(11) MQ_SPLIT16(12) MQ_SPLIT16(13)
+      MQ_SPLIT16(14) default: quartet<LA, LB, LC, LD, 3, 4, 3, 4, EPI>(g, P, Q); break;
+    }
+#undef MQ_SPLIT16
+  }
+}
+
+static int nsplit_of(int cP, int cQ) {
+  int nout = (cP == 0 ? 1 : cP == 1 ? 4 : 16) * (cQ == 0 ? 1 : cQ == 1 ? 4 : 16);
+  return nout <= 16 ? 1 : (nout <= 64 ? 4 : 16);
+}
+
+template <int EPI>
+static int launch_class(mq_ctx *c, EriArgs g, int cP, int cQ) {
+  const int nsplit = nsplit_of(cP, cQ);
+  const long long warps = (g.nq + 31) / 32 * nsplit;
+  const long long threads = warps * 32;
+  const int block = 128;
+  const long long grid = (threads + block - 1) / block;
+  if (grid == 0) return MQ_OK;
+  if (grid > 2147483647LL) return set_err(c, MQ_EINVAL, "integral launch too large");
+  dim3 gd((unsigned)grid);
+#define MQ_LAUNCH(a, b, cc, d) eri_kernel<a, b, cc, d, EPI><<<gd, block, 0, c->stream>>>(g)
+  if (cP == 0 && cQ == 0) MQ_LAUNCH(0, 0, 0, 0);
+  else if (cP == 1 && cQ == 0) MQ_LAUNCH(1, 0, 0, 0);
+  else if (cP == 1 && cQ == 1) MQ_LAUNCH(1, 0, 1, 0);
+  else if (cP == 2 && cQ == 0) MQ_LAUNCH(1, 1, 0, 0);
+  else if (cP == 2 && cQ == 1) MQ_LAUNCH(1, 1, 1, 0);
+  else MQ_LAUNCH(1, 1, 1, 1);
+#undef MQ_LAUNCH
+  c->stats.launches += 1;
+  MQ_CUDA(c, cudaGetLastError());
+  return MQ_OK;
+}
+
+static EriArgs base_args(mq_ctx *c) {
+  EriArgs g{};
+  g.t = c->pt;
+  g.boys = c->d_boys;
+  g.mode = c->mode;
+  g.n = c->nao;
+  return g;
+}
+
+// all unique (bra class >= ket class) combinations
+template <int EPI>
+static int run_all(mq_ctx *c, EriArgs g) {
+  const int *off = c->pt.class_off;
+  for (int cP = 0; cP < 3; ++cP)
+    for (int cQ = 0; cQ <= cP; ++cQ) {
+      const int nP = off[cP + 1] - off[cP], nQ = off[cQ + 1] - off[cQ];
+      if (nP == 0 || nQ == 0) continue;
+      EriArgs h = g;
+      h.pOff = off[cP];
+      h.nP = nP;
+      h.qOff = off[cQ];
+      h.nQ = nQ;
+      h.tri = cP == cQ;
+      h.diag = 0;
+      h.nq = h.tri ? (long long)nP * (nP + 1) / 2 : (long long)nP * nQ;
+      MQ_TRY(launch_class<EPI>(c, h, cP, cQ));
+    }
+  return MQ_OK;
+}
+
+int eri_schwarz(mq_ctx *c) {
+  EriArgs g = base_args(c);
+  g.sch = (unsigned long long *)c->pt.schwarz;
+  MQ_CUDA(c, cudaMemsetAsync(c->pt.schwarz, 0, sizeof(double) * std::max(1, c->pt.npairs), c->stream));
+  const int *off = c->pt.class_off;
+  for (int cl = 0; cl < 3; ++cl) {
+    const int np = off[cl + 1] - off[cl];
+    if (!np) continue;
+    EriArgs h = g;
+    h.pOff = h.qOff = off[cl];
+    h.nP = h.nQ = np;
+    h.diag = 1;
+    h.nq = np;
+    MQ_TRY(launch_class<EPI_SCHWARZ>(c, h, cl, cl));
+  }
+  return MQ_OK;
+}
+
+int eri_full_device(mq_ctx *c, double *d_XX) {
+  const size_t n = (size_t)c->nao;
+  MQ_CUDA(c, cudaMemsetAsync(d_XX, 0, n * n * n * n * sizeof(double), c->stream));
+  EriArgs g = base_args(c);
+  g.XX = d_XX;
+  g.thr = c->schwarz_thr;
+  if (g.thr > 0) MQ_TRY(eri_schwarz(c));
+  unsigned long long *cnt = (unsigned long long *)buf(c, "eri_counters", 2 * sizeof(unsigned long long));
+  if (!cnt) return MQ_ENOMEM;
+  MQ_CUDA(c, cudaMemsetAsync(cnt, 0, 2 * sizeof(unsigned long long), c->stream));
+  g.counters = cnt;
+  MQ_TRY(run_all<EPI_XX>(c, g));
+  unsigned long long h[2];
+  MQ_CUDA(c, cudaMemcpyAsync(h, cnt, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+  MQ_CUDA(c, cudaStreamSynchronize(c->stream));
+  c->stats.quartets = (double)h[0];
+  c->stats.prim_quartets = (double)h[1];
+  return MQ_OK;
+}
+
+int fock_direct_device(mq_ctx *c, const double *d_Da, const double *d_Db, double *d_J, double *d_Ka, double *d_Kb) {
+  const size_t n = (size_t)c->nao;
+  MQ_CUDA(c, cudaMemsetAsync(d_J, 0, n * n * sizeof(double), c->stream));
+  MQ_CUDA(c, cudaMemsetAsync(d_Ka, 0, n * n * sizeof(double), c->stream));
+  if (d_Kb) MQ_CUDA(c, cudaMemsetAsync(d_Kb, 0, n * n * sizeof(double), c->stream));
+  EriArgs g = base_args(c);
+  g.thr = c->schwarz_thr;
+  g.Da = d_Da;
+  g.Db = d_Db;
+  g.J = d_J;
+  g.Ka = d_Ka;
+  g.Kb = d_Kb;
+  g.uhf = d_Db != nullptr;
+  return run_all<EPI_FOCK>(c, g);
+}
+
+// G = (J + J^T)/2 - f (K + K^T)/2: the direct kernel accumulates each unique
+// integral into one of the two mirror elements only
+__global__ void direct_combine_kernel(const double *J, const double *K, double f, int n, double *G) {
+  const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (size_t)n * n) return;
+  const size_t r = idx % n, col = idx / n, t = col + (size_t)n * r;
+  G[idx] = 0.5 * (J[idx] + J[t]) - f * 0.5 * (K[idx] + K[t]);
+}
+
+int direct_combine(mq_ctx *c, const double *J, const double *Ka, const double *Kb, double *Ga, double *Gb) {
+  const int n = c->nao;
+  const unsigned grid = (unsigned)(((size_t)n * n + 255) / 256);
+  direct_combine_kernel<<<grid, 256, 0, c->stream>>>(J, Ka, Kb ? 1.0 : 0.5, n, Ga);
+  if (Kb) direct_combine_kernel<<<grid, 256, 0, c->stream>>>(J, Kb, 1.0, n, Gb);
+  c->stats.launches += Kb ? 2 : 1;
+  MQ_CUDA(c, cudaGetLastError());
+  return MQ_OK;
+}
+
+}  // namespace mq

@@ -1,0 +1,190 @@
+// int1e.cu -- overlap S and core Hamiltonian H = T + V over contracted s/sp
+// shell pairs, FP64.  Restates proc1e (src/integrals/int1e.f90:132-280):
+// overlap :321-386, kinetic :391-474, coulomb (nuclear attraction) :479-582,
+// with the same Hermite coefficients, Boys regimes (Boys order 3*(la+lb)) and
+// primitive screen EIJ < 1e-14 (applied when the pair table is built).
+#include "boys.cuh"
+#include "internal.h"
+
+namespace mq {
+
+struct Int1eArgs {
+  PairTable t;
+  const double *boys;
+  const double *nuc;  // nnuc x 4 (x, y, z, Z)
+  int nnuc, n, mode;
+  int pOff, np;
+  double *S, *H;
+};
+
+// Hermite coefficients E^{ij}_t of one axis for i <= 1, j <= 3 (kinetic needs
+// j = l_b + 2), by the standard recursion the reference's lrec/rrec memoise.
+__device__ __forceinline__ void axis_E(double PA, double PB, double i2p, double (&E)[2][4][5]) {
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+      for (int t = 0; t < 5; ++t) E[i][j][t] = 0.0;
+  E[0][0][0] = 1.0;
+  E[1][0][0] = PA;
+  E[1][0][1] = i2p;
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+#pragma unroll
+      for (int t = 0; t <= i + j + 1; ++t) {
+        double v = PB * E[i][j][t];
+        if (t > 0) v += i2p * E[i][j][t - 1];
+        if (t + 1 <= i + j) v += (t + 1) * E[i][j][t + 1];
+        E[i][j + 1][t] = v;
+      }
+}
+
+template <int LA, int LB>
+__global__ void __launch_bounds__(128) int1e_kernel(Int1eArgs g) {
+  constexpr int NA = LA ? 4 : 1, NB = LB ? 4 : 1, L = LA + LB, QREF = 3 * L;
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= g.np) return;
+  const int P = g.pOff + idx;
+  const PairTable &t = g.t;
+  const bool parity = g.mode == MQ_MODE_REFERENCE;
+  const double pi = parity ? PI_REF : PI_TRUE;
+  double s[NA][NB], h[NA][NB];
+#pragma unroll
+  for (int a = 0; a < NA; ++a)
+#pragma unroll
+    for (int b = 0; b < NB; ++b) s[a][b] = h[a][b] = 0.0;
+  for (int ip = t.pp_off[P]; ip < t.pp_off[P + 1]; ++ip) {
+    const double p = t.p[ip], i2p = t.inv2p[ip];
+    const double Px = t.Px[ip], Py = t.Py[ip], Pz = t.Pz[ip];
+    double Ex[2][4][5], Ey[2][4][5], Ez[2][4][5];
+    axis_E(t.PAx[ip], t.PBx[ip], i2p, Ex);
+    axis_E(t.PAy[ip], t.PBy[ip], i2p, Ey);
+    axis_E(t.PAz[ip], t.PBz[ip], i2p, Ez);
+    const double bb = t.beta[ip];  // exponent of B (the kinetic term needs it)
+    const double pp32 = pow(pi / p, 1.5);
+    double c[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) c[k] = t.c4[4 * ip + k];
+    // nuclear attraction: R^{(0)}_{tuv}(p, P - C) for all nuclei
+    double V[L + 1][L + 1][L + 1];
+#pragma unroll
+    for (int x = 0; x <= L; ++x)
+#pragma unroll
+      for (int y = 0; y <= L; ++y)
+#pragma unroll
+        for (int z = 0; z <= L; ++z) V[x][y][z] = 0.0;
+    for (int cn = 0; cn < g.nnuc; ++cn) {
+      const double X = Px - g.nuc[4 * cn], Y = Py - g.nuc[4 * cn + 1], Z = Pz - g.nuc[4 * cn + 2];
+      const double T = p * (X * X + Y * Y + Z * Z);
+      double F[L + 1];
+      boys<QREF, L>(g.mode, T, g.boys, F);
+      const double w = -g.nuc[4 * cn + 3] * 2.0 * pi / p;
+      // R recursion (auxilary.f90:22-80) with alpha = p
+      double Rj[L + 1][L + 1][L + 1][L + 1];
+      double pw = 1.0;
+#pragma unroll
+      for (int j = 0; j <= L; ++j) {
+        Rj[j][0][0][0] = pw * F[j] * w;
+        pw *= -2.0 * p;
+      }
+#pragma unroll
+      for (int j = L - 1; j >= 0; --j)
+#pragma unroll
+        for (int x = 0; x <= L; ++x)
+#pragma unroll
+          for (int y = 0; y <= L; ++y)
+#pragma unroll
+            for (int z = 0; z <= L; ++z) {
+              if (x + y + z == 0 || x + y + z > L - j) continue;
+              double r;
+              if (x > 0) {
+                r = X * Rj[j + 1][x - 1][y][z];
+                if (x > 1) r += (x - 1) * Rj[j + 1][x - 2][y][z];
+              } else if (y > 0) {
+                r = Y * Rj[j + 1][x][y - 1][z];
+                if (y > 1) r += (y - 1) * Rj[j + 1][x][y - 2][z];
+              } else {
+                r = Z * Rj[j + 1][x][y][z - 1];
+                if (z > 1) r += (z - 1) * Rj[j + 1][x][y][z - 2];
+              }
+              Rj[j][x][y][z] = r;
+            }
+#pragma unroll
+      for (int x = 0; x <= L; ++x)
+#pragma unroll
+        for (int y = 0; y <= L; ++y)
+#pragma unroll
+          for (int z = 0; z <= L; ++z)
+            if (x + y + z <= L) V[x][y][z] += Rj[0][x][y][z];
+    }
+#pragma unroll
+    for (int a = 0; a < NA; ++a)
+#pragma unroll
+      for (int b = 0; b < NB; ++b) {
+        const int ax = a == 1, ay = a == 2, az = a == 3, bx = b == 1, by = b == 2, bz = b == 3;
+        const double cf = c[2 * (a > 0) + (b > 0)];
+        const double sx = Ex[ax][bx][0], sy = Ey[ay][by][0], sz = Ez[az][bz][0];
+        s[a][b] += cf * pp32 * sx * sy * sz;
+        // kinetic: -1/2 sum_axis [nb(nb-1) E(na,nb-2) - 2b(2nb+1) E(na,nb) + 4b^2 E(na,nb+2)] * others
+        auto kin = [&](const double (&E)[2][4][5], int na, int nb) {
+          double v = -2.0 * bb * (2 * nb + 1) * E[na][nb][0] + 4.0 * bb * bb * E[na][nb + 2][0];
+          if (nb >= 2) v += nb * (nb - 1) * E[na][nb - 2][0];
+          return v;
+        };
+        const double tk = kin(Ex, ax, bx) * sy * sz + kin(Ey, ay, by) * sx * sz + kin(Ez, az, bz) * sx * sy;
+        double v = 0.0;
+#pragma unroll
+        for (int x = 0; x <= ax + bx; ++x)
+#pragma unroll
+          for (int y = 0; y <= ay + by; ++y)
+#pragma unroll
+            for (int z = 0; z <= az + bz; ++z) v += Ex[ax][bx][x] * Ey[ay][by][y] * Ez[az][bz][z] * V[x][y][z];
+        h[a][b] += cf * (-0.5 * pp32 * tk + v);
+      }
+  }
+  const int A = t.shA[P], B = t.shB[P], i0 = t.aoA[P], j0 = t.aoB[P];
+  const size_t n = g.n;
+#pragma unroll
+  for (int a = 0; a < NA; ++a)
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+      const int i = i0 + a, j = j0 + b;
+      if (A == B && i < j) continue;
+      g.S[i + n * j] = s[a][b];
+      g.S[j + n * i] = s[a][b];
+      g.H[i + n * j] = h[a][b];
+      g.H[j + n * i] = h[a][b];
+    }
+}
+
+int int1e_device(mq_ctx *c, double *d_S, double *d_H) {
+  const size_t n = c->nao;
+  MQ_CUDA(c, cudaMemsetAsync(d_S, 0, n * n * sizeof(double), c->stream));
+  MQ_CUDA(c, cudaMemsetAsync(d_H, 0, n * n * sizeof(double), c->stream));
+  Int1eArgs g{};
+  g.t = c->pt;
+  g.boys = c->d_boys;
+  g.nuc = c->d_nuc;
+  g.nnuc = c->nnuc;
+  g.n = c->nao;
+  g.mode = c->mode;
+  g.S = d_S;
+  g.H = d_H;
+  for (int cl = 0; cl < 3; ++cl) {
+    g.pOff = c->pt.class_off[cl];
+    g.np = c->pt.class_off[cl + 1] - g.pOff;
+    if (!g.np) continue;
+    dim3 grid((g.np + 127) / 128);
+    if (cl == 0) int1e_kernel<0, 0><<<grid, 128, 0, c->stream>>>(g);
+    else if (cl == 1) int1e_kernel<1, 0><<<grid, 128, 0, c->stream>>>(g);
+    else int1e_kernel<1, 1><<<grid, 128, 0, c->stream>>>(g);
+    c->stats.launches += 1;
+    MQ_CUDA(c, cudaGetLastError());
+  }
+  return MQ_OK;
+}
+
+}  // namespace mq

@@ -1,0 +1,154 @@
+// internal.h -- shared declarations of libmyqc (not part of the C ABI).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/myqc.h"
+
+namespace mq {
+
+constexpr int KMAX = 6;            // primitives per contracted shell (mybasis "max sets")
+constexpr int FTAB_NT = 121;       // Ftab rows: T = 0.0 .. 12.0 step 0.1
+constexpr int FTAB_NM = 23;        // Ftab columns: m = 0 .. 22
+constexpr int TIGHT_NT = 361;      // own table rows: T = 0.0 .. 36.0 step 0.1
+constexpr int TIGHT_NM = 13;       // m = 0 .. 12 (order <= 4 plus 8 Taylor terms)
+constexpr double PI_REF = (double)3.1415926535897931f;  // the reference's pi
+constexpr double PI_TRUE = 3.14159265358979323846;
+
+// A contracted shell: s (1 function), or sp (4 functions: s, px, py, pz that
+// share exponents).  A p-only shell is an sp shell whose s coefficients are 0.
+struct HostShell {
+  int atom;
+  int type;      // 0: s, 1: sp
+  int qlmax;     // lmax of the reference's primitive sets (Boys order, parity)
+  int ao0;       // AO index of the first function
+  int has_s, has_p;
+  int nprim;
+  double alpha[KMAX];
+  double cs[KMAX];  // s coefficient x gtoD(0, alpha)
+  double cp[KMAX];  // p coefficient x gtoD(1, alpha)
+};
+
+// Device view of the shell-pair / primitive-pair tables (structure of arrays).
+struct PairTable {
+  int npairs;            // shell pairs in class order
+  int class_off[4];      // pair index ranges per class: [0]=ss, [1]=(sp,s), [2]=(sp,sp), [3]=end
+  int *shA, *shB;        // shells of each pair (type(A) >= type(B))
+  int *pp_off;           // primitive-pair offset, npairs+1
+  int *aoA, *aoB;        // first AO of A and B
+  double *schwarz;       // sqrt(max |(ab|ab)|) per pair
+  // primitive pairs
+  int npp;
+  double *p, *inv2p, *beta, *Px, *Py, *Pz, *PAx, *PAy, *PAz, *PBx, *PBy, *PBz, *K, *c4;  // c4: 4 per pp
+};
+
+struct DeviceBuf {
+  void *ptr = nullptr;
+  size_t bytes = 0;
+};
+
+struct Stats {
+  double ms_eri = 0, ms_fock = 0, ms_diag = 0, ms_ao2mo = 0, ms_mp2 = 0;
+  double launches = 0, quartets = 0, prim_quartets = 0;
+};
+
+}  // namespace mq
+
+struct mq_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  void *cublas = nullptr;
+  std::string err;
+  // system
+  int have_system = 0;
+  int mode = MQ_MODE_REFERENCE;
+  int nnuc = 0, nao = 0, nshell = 0;
+  double schwarz_thr = 0.0;
+  std::vector<int> Z;
+  std::vector<double> xyz;  // nnuc x 3, row-major (atom, xyz)
+  std::vector<mq::HostShell> shells;
+  std::vector<int> pair_class_count;
+  // device data
+  double *d_boys = nullptr;  // Ftab (parity) or own table (tight)
+  double *d_nuc = nullptr;   // nnuc x 4: x, y, z, Z
+  mq::PairTable pt{};
+  std::vector<void *> pair_allocs;
+  double *d_XX = nullptr;    // n^4 full integral array
+  size_t XX_elems = 0;
+  double *d_iajb = nullptr;  // last (ia|jb) block
+  size_t iajb_elems = 0;
+  int iajb_dims[4] = {0, 0, 0, 0};
+  // named device work buffers: each grows on demand and is reused across calls
+  std::map<std::string, mq::DeviceBuf> bufs;
+  mq::Stats stats;
+};
+
+namespace mq {
+// error helpers
+int set_err(mq_ctx *c, int code, const std::string &msg);
+int cuda_check(mq_ctx *c, cudaError_t e, const char *what);
+// device buffer `name` of at least `bytes` (contents undefined after growth);
+// nullptr on failure with the error set
+void *buf(mq_ctx *c, const char *name, size_t bytes);
+
+// basis.cu
+int build_shells(mq_ctx *c, int nnuc, const int *Z, const double *xyz, const double *bas, const double *set,
+                 const int *basinfo, const int *setinfo);
+int build_pairs(mq_ctx *c);
+void free_pairs(mq_ctx *c);
+void tight_boys_table(std::vector<double> &tab);  // TIGHT_NT x TIGHT_NM, row-major [T][m]
+
+// eri.cu
+int eri_full_device(mq_ctx *c, double *d_XX);
+int eri_schwarz(mq_ctx *c);
+int fock_direct_device(mq_ctx *c, const double *d_Da, const double *d_Db, double *d_J, double *d_Ka, double *d_Kb);
+// G = sym(J) - f sym(K) from the direct kernel's half-sums (f = 1/2 RHF, 1 UHF)
+int direct_combine(mq_ctx *c, const double *J, const double *Ka, const double *Kb, double *Ga, double *Gb);
+
+// int1e.cu
+int int1e_device(mq_ctx *c, double *d_S, double *d_H);
+
+// fock.cu
+int fock_stored_device(mq_ctx *c, const double *d_Da, const double *d_Db, double *d_Ga, double *d_Gb);
+
+// linalg.cu
+int syev_batched_device(mq_ctx *c, int n, int batch, double *d_A, double *d_w, double *d_V);
+int gemm(mq_ctx *c, char ta, char tb, int m, int n, int k, double alpha, const double *A, int lda, const double *B,
+         int ldb, double beta, double *C, int ldc);
+int gemm_strided_batched(mq_ctx *c, char ta, char tb, int m, int n, int k, double alpha, const double *A, int lda,
+                         long long sA, const double *B, int ldb, long long sB, double beta, double *C, int ldc,
+                         long long sC, int batch);
+int density_device(mq_ctx *c, int n, int nocc, const double *d_C, double factor, double *d_D);
+void cublas_destroy(void *handle);
+
+// ao2mo.cu
+int ao2mo_device(mq_ctx *c, const double *d_Ci, int no1, const double *d_Ca, int nv1, const double *d_Cj, int no2,
+                 const double *d_Cb, int nv2, int precision, double *d_out);
+int mp2_rhf_device(mq_ctx *c, const double *d_iajb, const double *d_eig, int nocc, int nvir, double *e_out);
+// sums[0] = sum_{ijab} x^2/D, sums[1] = sum_{i<j,a<b} (x_iajb - x_ibja)^2/D (same_spin only);
+// d_e1/d_e2: orbital energies of the (i,a) and (j,b) spins, occupied first
+int mp2_pair_sums(mq_ctx *c, const double *d_Om, int no1, int nv1, int no2, int nv2, const double *d_e1,
+                  const double *d_e2, int same_spin, double *sums);
+// ao2mo_split.cu: hi+lo BF16 tensor-core transform (tcgen05)
+int ao2mo_split_device(mq_ctx *c, const double *d_Ci, int no1, const double *d_Ca, int nv1, const double *d_Cj,
+                       int no2, const double *d_Cb, int nv2, double *d_out);
+
+// scf.cu
+int scf_device(mq_ctx *c, const double *S, const double *H, const mq_scf_opts *o, double *C, double *eps, double *D,
+               double *energy, int *iters, double *history);
+}  // namespace mq
+
+#define MQ_CUDA(c, call)                                   \
+  do {                                                     \
+    cudaError_t _e = (call);                               \
+    if (_e != cudaSuccess) return mq::cuda_check(c, _e, #call); \
+  } while (0)
+
+#define MQ_TRY(call)         \
+  do {                       \
+    int _rc = (call);        \
+    if (_rc != MQ_OK) return _rc; \
+  } while (0)

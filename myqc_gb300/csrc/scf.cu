@@ -1,0 +1,336 @@
+// scf.cu -- RHF/UHF SCF on the device.
+//
+// Restates the scf executable's loop (src/scf/scf.f90: RHF :61-216,
+// UHF :221-404, initRHF/initUHF :410-622, RHFiter :720-904, UHFiter
+// :909-1117, checkConv :1157-1267) with the dens and RHFI2G/UHFI2G child
+// processes folded in.  Iteration k takes the input density D_k (from the
+// orbitals of iteration k-1; D_0 from the core-Hamiltonian guess), forms
+// G[D_k], F = H + G and E_k = 1/2 sum D_k (F + H) + E_nuc, solves F C = S C e,
+// builds D_{k+1}, and for k > 0 stops when max|D_{k+1} - D_k| < threshold --
+// the reference's rule; the reported energy is E_k, as scf.f90:900 prints it.
+// Optional DIIS (a method addition with the same fixed point) extrapolates F
+// from the last m Fock matrices with commutator errors F D S - S D F.
+//
+// The generalized problem is solved as C = X C' with X = S^-1/2 and
+// X^T F X C' = C' e (Jacobi), which gives the C^T S C = 1 normalisation and
+// ascending eigenvalues that DSYGV(1,'V','L') returns.
+#include <cmath>
+#include <vector>
+
+#include "internal.h"
+
+namespace mq {
+
+__global__ void add_kernel(const double *a, const double *b, double *c, size_t n) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) c[i] = a[i] + b[i];
+}
+
+// out[0] += 1/2 sum D (F + H), out[1] = max |Dn - Do| (single block, fixed order)
+__global__ void energy_diff_kernel(const double *D, const double *F, const double *H, const double *Dn,
+                                   const double *Do, size_t n2, double *out, int slot) {
+  __shared__ double se[1024], sd[1024];
+  double e = 0.0, d = 0.0;
+  for (size_t i = threadIdx.x; i < n2; i += blockDim.x) {
+    e += D[i] * (F[i] + H[i]);
+    if (Dn) d = fmax(d, fabs(Dn[i] - Do[i]));
+  }
+  se[threadIdx.x] = e;
+  sd[threadIdx.x] = d;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      se[threadIdx.x] += se[threadIdx.x + s];
+      sd[threadIdx.x] = fmax(sd[threadIdx.x], sd[threadIdx.x + s]);
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    out[2 * slot] = 0.5 * se[0];
+    out[2 * slot + 1] = sd[0];
+  }
+}
+
+// max |Dn - Do| and RMS over all spin blocks -> out[0], out[1]
+__global__ void diff_kernel(const double *Dn, const double *Do, size_t n2, double *out) {
+  __shared__ double sm[1024], ss[1024];
+  double m = 0.0, s2 = 0.0;
+  for (size_t i = threadIdx.x; i < n2; i += blockDim.x) {
+    const double d = Dn[i] - Do[i];
+    m = fmax(m, fabs(d));
+    s2 += d * d;
+  }
+  sm[threadIdx.x] = m;
+  ss[threadIdx.x] = s2;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      sm[threadIdx.x] = fmax(sm[threadIdx.x], sm[threadIdx.x + s]);
+      ss[threadIdx.x] += ss[threadIdx.x + s];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    out[0] = sm[0];
+    out[1] = sqrt(ss[0] / (double)n2);
+  }
+}
+
+// X = U diag(s^-1/2) U^T: scale columns of U into W = U diag(s^-1/2)
+__global__ void scale_cols_kernel(const double *U, const double *s, double *W, int n, double power) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (size_t)n * n) return;
+  const int col = (int)(i / n);
+  W[i] = U[i] * pow(s[col], power);
+}
+
+// e = A - A^T  (commutator F D S - S D F for symmetric F, D, S)
+__global__ void antisym_kernel(const double *A, double *E, int n) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (size_t)n * n) return;
+  const int r = (int)(i % n), c = (int)(i / n);
+  E[i] = A[i] - A[c + (size_t)n * r];
+}
+
+// B[row, j] = <E_row, E_j> for j < m (one block per j)
+__global__ void dots_kernel(const double *E, size_t n2, int row, int m, size_t stride, double *B) {
+  __shared__ double sh[256];
+  const int j = blockIdx.x;
+  if (j >= m) return;
+  double s = 0.0;
+  for (size_t i = threadIdx.x; i < n2; i += blockDim.x) s += E[stride * row + i] * E[stride * j + i];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int k = blockDim.x / 2; k > 0; k >>= 1) {
+    if (threadIdx.x < k) sh[threadIdx.x] += sh[threadIdx.x + k];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) B[j] = sh[0];
+}
+
+__global__ void lincomb_kernel(const double *F, size_t stride, const double *coef, int m, double *out, size_t n2) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n2) return;
+  double s = 0.0;
+  for (int k = 0; k < m; ++k) s += coef[k] * F[stride * k + i];
+  out[i] = s;
+}
+
+// solve the DIIS system [B -1; -1 0][c; l] = [0; -1] (m <= 16) by Gaussian elimination
+static bool diis_solve(const std::vector<double> &B, int m, std::vector<double> &cvec) {
+  const int N = m + 1;
+  std::vector<double> A((size_t)N * N, 0.0), b(N, 0.0);
+  double scale = 0;
+  for (int i = 0; i < m; ++i) scale = std::max(scale, std::fabs(B[(size_t)i * m + i]));
+  if (scale <= 0) return false;
+  for (int i = 0; i < m; ++i)
+    for (int j = 0; j < m; ++j) A[(size_t)i * N + j] = B[(size_t)i * m + j] / scale;
+  for (int i = 0; i < m; ++i) A[(size_t)i * N + m] = A[(size_t)m * N + i] = -1.0;
+  b[m] = -1.0;
+  for (int k = 0; k < N; ++k) {
+    int piv = k;
+    for (int i = k + 1; i < N; ++i)
+      if (std::fabs(A[(size_t)i * N + k]) > std::fabs(A[(size_t)piv * N + k])) piv = i;
+    if (std::fabs(A[(size_t)piv * N + k]) < 1e-300) return false;
+    if (piv != k) {
+      for (int j = 0; j < N; ++j) std::swap(A[(size_t)k * N + j], A[(size_t)piv * N + j]);
+      std::swap(b[k], b[piv]);
+    }
+    for (int i = k + 1; i < N; ++i) {
+      const double f = A[(size_t)i * N + k] / A[(size_t)k * N + k];
+      for (int j = k; j < N; ++j) A[(size_t)i * N + j] -= f * A[(size_t)k * N + j];
+      b[i] -= f * b[k];
+    }
+  }
+  std::vector<double> x(N);
+  for (int i = N - 1; i >= 0; --i) {
+    double s = b[i];
+    for (int j = i + 1; j < N; ++j) s -= A[(size_t)i * N + j] * x[j];
+    x[i] = s / A[(size_t)i * N + i];
+  }
+  cvec.assign(x.begin(), x.begin() + m);
+  return true;
+}
+
+static double nuclear_repulsion(const mq_ctx *c) {
+  // getEnr, src/scf/scf.f90:1122-1152
+  double E = 0.0;
+  for (int a = 0; a < c->nnuc; ++a)
+    for (int b = 0; b < a; ++b) {
+      double r2 = 0;
+      for (int k = 0; k < 3; ++k) {
+        const double d = c->xyz[3 * a + k] - c->xyz[3 * b + k];
+        r2 += d * d;
+      }
+      E += c->Z[a] * c->Z[b] / std::sqrt(r2);
+    }
+  return E;
+}
+
+static unsigned blocks(size_t n, int tb = 256) { return (unsigned)((n + tb - 1) / tb); }
+
+int scf_device(mq_ctx *c, const double *S, const double *H, const mq_scf_opts *o, double *C, double *eps, double *D,
+               double *energy, int *iters, double *history) {
+  const int n = c->nao;
+  const size_t n2 = (size_t)n * n;
+  const bool uhf = o->uhf != 0;
+  const int ns = uhf ? 2 : 1;
+  const int max_iter = o->max_iter > 0 ? o->max_iter : (uhf ? 300 : 500);
+  const double thr = o->conv > 0 ? o->conv : 1e-7;
+  const int ndiis = std::min(o->diis, 16);
+  const int nocc[2] = {uhf ? o->nalpha : (o->nalpha + o->nbeta) / 2, o->nbeta};
+  const double occf = uhf ? 1.0 : 2.0;
+  if (!uhf && o->nalpha != o->nbeta) return set_err(c, MQ_EINVAL, "RHF needs nalpha == nbeta");
+  if (nocc[0] > n || nocc[1] > n || nocc[0] < 0 || nocc[1] < 0) return set_err(c, MQ_EINVAL, "bad occupation");
+  if (!o->direct && !c->d_XX) return set_err(c, MQ_ESTATE, "no stored integrals for a conventional SCF");
+
+  // device workspace
+  const size_t nmat = 8 + 6 * ns + (size_t)2 * ndiis * ns;
+  double *w = (double *)buf(c, "scf_work", sizeof(double) * (n2 * nmat + 256 + n * ns));
+  if (!w) return MQ_ENOMEM;
+  double *dS = w, *dH = dS + n2, *dX = dH + n2, *dT1 = dX + n2, *dT2 = dT1 + n2, *dT3 = dT2 + n2;
+  double *dU = dT3 + n2, *dW = dU + n2;
+  double *dD = dW + n2;            // ns input densities
+  double *dDn = dD + n2 * ns;      // ns new densities
+  double *dG = dDn + n2 * ns;      // ns
+  double *dF = dG + n2 * ns;       // ns
+  double *dC = dF + n2 * ns;       // ns
+  double *dFp = dC + n2 * ns;      // ns (orthogonal-basis Fock / eigvec scratch)
+  double *dFh = dFp + n2 * ns;     // DIIS Fock history ns * ndiis
+  double *dEh = dFh + n2 * ns * ndiis;  // DIIS error history
+  double *dScal = dEh + n2 * ns * ndiis;  // 256 scalars
+  double *dEps = dScal + 256;           // n * ns
+  MQ_CUDA(c, cudaMemcpyAsync(dS, S, n2 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  MQ_CUDA(c, cudaMemcpyAsync(dH, H, n2 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+
+  // X = S^-1/2
+  MQ_CUDA(c, cudaMemcpyAsync(dT1, dS, n2 * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+  MQ_TRY(syev_batched_device(c, n, 1, dT1, dEps, dU));
+  std::vector<double> sev(n);
+  MQ_CUDA(c, cudaMemcpyAsync(sev.data(), dEps, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  MQ_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (sev[0] <= 0.0) return set_err(c, MQ_EINVAL, "overlap matrix is not positive definite");
+  scale_cols_kernel<<<blocks(n2), 256, 0, c->stream>>>(dU, dEps, dW, n, -0.5);
+  MQ_TRY(gemm(c, 'N', 'T', n, n, n, 1.0, dW, n, dU, n, 0.0, dX, n));
+
+  // solve F C = S C e for ns Fock matrices in dF -> dC, dEps
+  auto diagonalize = [&](const double *Fm) -> int {
+    for (int s = 0; s < ns; ++s) {
+      MQ_TRY(gemm(c, 'T', 'N', n, n, n, 1.0, dX, n, Fm + n2 * s, n, 0.0, dT1, n));
+      MQ_TRY(gemm(c, 'N', 'N', n, n, n, 1.0, dT1, n, dX, n, 0.0, dFp + n2 * s, n));
+    }
+    // eigenvectors into dU (and dW, which follows it, for the beta block)
+    MQ_TRY(syev_batched_device(c, n, ns, dFp, dEps, dU));
+    return MQ_OK;
+  };
+  auto orbitals_to_density = [&]() -> int {
+    for (int s = 0; s < ns; ++s) {
+      MQ_TRY(gemm(c, 'N', 'N', n, n, n, 1.0, dX, n, dU + n2 * s, n, 0.0, dC + n2 * s, n));
+      MQ_TRY(density_device(c, n, nocc[s], dC + n2 * s, occf, dDn + n2 * s));
+    }
+    return MQ_OK;
+  };
+
+  // initial density
+  if (o->guess == 2 && o->D_in) {
+    MQ_CUDA(c, cudaMemcpyAsync(dD, o->D_in, n2 * ns * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  } else {
+    if (o->guess == 1 && o->C_in) {
+      MQ_CUDA(c, cudaMemcpyAsync(dC, o->C_in, n2 * ns * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    } else {  // core Hamiltonian (initRHF / initUHF): same orbitals for both spins
+      for (int s = 0; s < ns; ++s)
+        MQ_CUDA(c, cudaMemcpyAsync(dF + n2 * s, dH, n2 * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+      MQ_TRY(diagonalize(dF));
+      for (int s = 0; s < ns; ++s)
+        MQ_TRY(gemm(c, 'N', 'N', n, n, n, 1.0, dX, n, dU + n2 * s, n, 0.0, dC + n2 * s, n));
+    }
+    for (int s = 0; s < ns; ++s) MQ_TRY(density_device(c, n, nocc[s], dC + n2 * s, occf, dD + n2 * s));
+  }
+
+  const double enuc = nuclear_repulsion(c);
+  std::vector<double> Bm((size_t)ndiis * ndiis * 4, 0.0);
+  int nh = 0, head = 0;
+  double E = 0.0;
+  bool conv = false;
+  int it = 0;
+  std::vector<double> hist;
+  for (; it < max_iter && !conv; ++it) {
+    // G[D_k]
+    if (o->direct) {
+      double *J = dT1, *Ka = dT2, *Kb = uhf ? dT3 : nullptr;
+      MQ_TRY(fock_direct_device(c, dD, uhf ? dD + n2 : nullptr, J, Ka, Kb));
+      MQ_TRY(direct_combine(c, J, Ka, Kb, dG, uhf ? dG + n2 : nullptr));
+    } else {
+      MQ_TRY(fock_stored_device(c, dD, uhf ? dD + n2 : nullptr, dG, uhf ? dG + n2 : nullptr));
+    }
+    for (int s = 0; s < ns; ++s) add_kernel<<<blocks(n2), 256, 0, c->stream>>>(dH, dG + n2 * s, dF + n2 * s, n2);
+    for (int s = 0; s < ns; ++s)
+      energy_diff_kernel<<<1, 1024, 0, c->stream>>>(dD + n2 * s, dF + n2 * s, dH, nullptr, nullptr, n2, dScal, s);
+    const double *Fdiag = dF;
+    if (ndiis > 0) {
+      // commutator errors e_s = F D S - S D F, stored with F in ring slot `head`
+      for (int s = 0; s < ns; ++s) {
+        double *Fs = dFh + n2 * ((size_t)ns * head + s), *Es = dEh + n2 * ((size_t)ns * head + s);
+        MQ_CUDA(c, cudaMemcpyAsync(Fs, dF + n2 * s, n2 * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+        MQ_TRY(gemm(c, 'N', 'N', n, n, n, 1.0, dF + n2 * s, n, dD + n2 * s, n, 0.0, dT1, n));
+        MQ_TRY(gemm(c, 'N', 'N', n, n, n, 1.0, dT1, n, dS, n, 0.0, dT2, n));
+        antisym_kernel<<<blocks(n2), 256, 0, c->stream>>>(dT2, Es, n);
+      }
+      nh = std::min(nh + 1, ndiis);
+      // new row of B: sum over spins of <e_head, e_j>
+      for (int j = 0; j < ndiis; ++j) Bm[(size_t)head * ndiis + j] = Bm[(size_t)j * ndiis + head] = 0.0;
+      std::vector<double> row(ndiis, 0.0);
+      for (int s = 0; s < ns; ++s) {
+        dots_kernel<<<ndiis, 256, 0, c->stream>>>(dEh + n2 * s, n2, head, nh, n2 * ns, dScal + 16 + 16 * s);
+      }
+      std::vector<double> hrow(32);
+      MQ_CUDA(c, cudaMemcpyAsync(hrow.data(), dScal + 16, 32 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+      MQ_CUDA(c, cudaStreamSynchronize(c->stream));
+      for (int j = 0; j < nh; ++j) {
+        double v = hrow[j] + (uhf ? hrow[16 + j] : 0.0);
+        Bm[(size_t)head * ndiis + j] = Bm[(size_t)j * ndiis + head] = v;
+      }
+      if (nh >= 2) {
+        std::vector<double> Bs((size_t)nh * nh), cv;
+        for (int i = 0; i < nh; ++i)
+          for (int j = 0; j < nh; ++j) Bs[(size_t)i * nh + j] = Bm[(size_t)i * ndiis + j];
+        if (diis_solve(Bs, nh, cv)) {
+          MQ_CUDA(c, cudaMemcpyAsync(dScal + 64, cv.data(), nh * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+          // extrapolated Fock matrices into dG (free once F = H + G is formed)
+          for (int s = 0; s < ns; ++s)
+            lincomb_kernel<<<blocks(n2), 256, 0, c->stream>>>(dFh + n2 * s, n2 * ns, dScal + 64, nh, dG + n2 * s,
+                                                              n2);
+          Fdiag = dG;
+        }
+      }
+      head = (head + 1) % ndiis;
+    }
+    MQ_TRY(diagonalize(Fdiag));
+    MQ_TRY(orbitals_to_density());
+    diff_kernel<<<1, 1024, 0, c->stream>>>(dDn, dD, n2 * ns, dScal + 8);
+    double hs[10];
+    MQ_CUDA(c, cudaMemcpyAsync(hs, dScal, 10 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    MQ_CUDA(c, cudaStreamSynchronize(c->stream));
+    E = hs[0] + (uhf ? hs[2] : 0.0) + enuc;
+    const double diff = o->conv_rms ? hs[9] : hs[8];
+    hist.push_back(E);
+    hist.push_back(it > 0 ? diff : NAN);
+    if (it > 0) conv = diff < thr;
+    if (!conv) {
+      // D_{k+1} becomes the next input density
+      MQ_CUDA(c, cudaMemcpyAsync(dD, dDn, n2 * ns * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+    }
+  }
+  // outputs: orbitals and eigenvalues of the last diagonalisation, D_k of the last iteration
+  MQ_CUDA(c, cudaMemcpyAsync(C, dC, n2 * ns * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  MQ_CUDA(c, cudaMemcpyAsync(eps, dEps, (size_t)n * ns * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  if (D) MQ_CUDA(c, cudaMemcpyAsync(D, dD, n2 * ns * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  MQ_CUDA(c, cudaStreamSynchronize(c->stream));
+  *energy = E;
+  *iters = it;
+  if (history)
+    for (size_t k = 0; k < hist.size(); ++k) history[k] = hist[k];
+  return conv ? MQ_OK : set_err(c, MQ_ENOCONV, "SCF did not converge");
+}
+
+}  // namespace mq

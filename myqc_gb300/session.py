@@ -1,0 +1,213 @@
+"""Python host over the C ABI: one ``Context`` per GPU, mirroring the stages of
+the reference's executables (int1e, int2e, scf with dens + RHFI2G/UHFI2G,
+ao2mo, mp2) as method calls on device-resident data."""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib
+from ._lib import MODE_REFERENCE, MODE_TIGHT, PREC_FP64, PREC_SPLIT_BF16, MyQCError, f64, ptr
+from .formats import BasisArrays, System
+
+
+@dataclass
+class SCFResult:
+    energy: float
+    eig: np.ndarray      # (n,) RHF or (2, n) UHF
+    C: np.ndarray        # (n, n) RHF or (2, n, n) UHF, column-major orbitals
+    D: np.ndarray        # last input density (total for RHF; alpha, beta for UHF)
+    iterations: int
+    history: np.ndarray  # (iterations, 2): energy, max|dD|
+
+
+class Context:
+    def __init__(self, device: int = 0):
+        self.L = _lib.lib()
+        h = ctypes.c_void_p()
+        rc = self.L.mq_init(ctypes.byref(h), device)
+        if rc != 0:
+            raise MyQCError(rc, "mq_init failed (no CUDA device?)")
+        self.h = h
+        self.n = 0
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.mq_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, rc: int):
+        if rc != 0:
+            buf = ctypes.create_string_buffer(512)
+            self.L.mq_last_error(self.h, buf, 512)
+            raise MyQCError(rc, buf.value.decode())
+
+    # ---------------------------------------------------------------- setup
+    def set_system(self, sysm: System, basis: BasisArrays, ftab: np.ndarray | None = None,
+                   mode: int = MODE_REFERENCE):
+        Z = np.ascontiguousarray(sysm.atoms, dtype=np.int32)
+        xyz = f64(np.asarray(sysm.xyz).reshape(-1, 3))  # Fortran xyz(0:nnuc-1,0:2)
+        self._keep = (Z, xyz, np.ascontiguousarray(basis.bas, dtype=np.float64),
+                      np.ascontiguousarray(basis.set, dtype=np.float64),
+                      np.ascontiguousarray(basis.basinfo, dtype=np.int32),
+                      np.ascontiguousarray(basis.setinfo, dtype=np.int32),
+                      None if ftab is None else np.ascontiguousarray(ftab, dtype=np.float64))
+        k = self._keep
+        self._check(self.L.mq_set_system(self.h, len(Z), ptr(k[0]), ptr(k[1]), ptr(k[2]), ptr(k[3]), ptr(k[4]),
+                                         ptr(k[5]), ptr(k[6]), mode))
+        n = ctypes.c_int()
+        self._check(self.L.mq_norb(self.h, ctypes.byref(n)))
+        self.n = n.value
+        self.sys = sysm
+
+    def set_schwarz(self, thr: float):
+        self._check(self.L.mq_set_schwarz(self.h, thr))
+
+    # ---------------------------------------------------------------- integrals
+    def int1e(self):
+        n = self.n
+        S = np.zeros((n, n), order="F")
+        H = np.zeros((n, n), order="F")
+        self._check(self.L.mq_int1e(self.h, ptr(S), ptr(H)))
+        return S, H
+
+    def eri_full(self) -> np.ndarray:
+        n = self.n
+        XX = np.zeros((n, n, n, n), order="F")
+        self._check(self.L.mq_eri_full(self.h, ptr(XX)))
+        return XX
+
+    def eri_store(self):
+        self._check(self.L.mq_eri_store(self.h))
+
+    def eri_upload(self, XX: np.ndarray):
+        X = f64(XX)
+        self._check(self.L.mq_eri_upload(self.h, ptr(X)))
+
+    def fock(self, Da, Db=None, direct: bool = False):
+        n = self.n
+        Da_, Db_ = f64(Da), (None if Db is None else f64(Db))
+        Ga = np.zeros((n, n), order="F")
+        Gb = None if Db is None else np.zeros((n, n), order="F")
+        fn = self.L.mq_fock_direct if direct else self.L.mq_fock
+        self._check(fn(self.h, ptr(Da_), ptr(Db_), ptr(Ga), ptr(Gb)))
+        return Ga if Db is None else (Ga, Gb)
+
+    # ---------------------------------------------------------------- SCF
+    def scf(self, S, H, nalpha: int, nbeta: int, uhf: bool = False, conv: float = 1e-7, conv_rms: bool = False,
+            diis: int = 0, direct: bool = False, max_iter: int = 0, D_guess=None, C_guess=None) -> SCFResult:
+        n, ns = self.n, 2 if uhf else 1
+        o = _lib.ScfOpts()
+        o.uhf, o.nalpha, o.nbeta, o.max_iter = int(uhf), nalpha, nbeta, max_iter
+        o.conv, o.conv_rms, o.diis, o.direct = conv, int(conv_rms), diis, int(direct)
+        keep = []
+        if D_guess is not None:
+            Dg = f64(np.asarray(D_guess).reshape(ns, n, n).transpose(1, 2, 0))  # (n, n, ns) F-order = ns blocks
+            keep.append(Dg)
+            o.guess, o.D_in = 2, Dg.ctypes.data
+        elif C_guess is not None:
+            Cg = f64(np.asarray(C_guess).reshape(ns, n, n).transpose(1, 2, 0))
+            keep.append(Cg)
+            o.guess, o.C_in = 1, Cg.ctypes.data
+        S_, H_ = f64(S), f64(H)
+        C = np.zeros((n, n, ns), order="F")
+        eps = np.zeros((n, ns), order="F")
+        D = np.zeros((n, n, ns), order="F")
+        E = ctypes.c_double()
+        it = ctypes.c_int()
+        cap = max_iter if max_iter > 0 else (300 if uhf else 500)
+        hist = np.zeros(2 * cap)
+        self._check(self.L.mq_scf(self.h, ptr(S_), ptr(H_), ctypes.byref(o), ptr(C), ptr(eps), ptr(D),
+                                  ctypes.byref(E), ctypes.byref(it), ptr(hist)))
+        k = it.value
+        if uhf:
+            return SCFResult(E.value, eps.T.copy(), np.moveaxis(C, 2, 0).copy(), np.moveaxis(D, 2, 0).copy(), k,
+                             hist[: 2 * k].reshape(k, 2))
+        return SCFResult(E.value, eps[:, 0].copy(), C[:, :, 0].copy(order="F"), D[:, :, 0].copy(order="F"), k,
+                         hist[: 2 * k].reshape(k, 2))
+
+    # ---------------------------------------------------------------- post-HF
+    def ao2mo_iajb(self, Ci, Ca, Cj, Cb, precision: int = PREC_FP64, copy_out: bool = True):
+        Ci, Ca, Cj, Cb = f64(Ci), f64(Ca), f64(Cj), f64(Cb)
+        dims = (Ci.shape[1], Ca.shape[1], Cj.shape[1], Cb.shape[1])
+        out = np.zeros(dims, order="F") if copy_out else None
+        self._check(self.L.mq_ao2mo_iajb(self.h, ptr(Ci), dims[0], ptr(Ca), dims[1], ptr(Cj), dims[2], ptr(Cb),
+                                         dims[3], precision, ptr(out)))
+        return out
+
+    def mp2_rhf(self, eig, nocc: int, precision: int = PREC_FP64, C=None) -> dict:
+        if C is not None:
+            self.ao2mo_iajb(C[:, :nocc], C[:, nocc:], C[:, :nocc], C[:, nocc:], precision, copy_out=False)
+        e = np.zeros(3)
+        eg = np.ascontiguousarray(eig, dtype=np.float64)
+        self._check(self.L.mq_mp2_rhf(self.h, ptr(eg), nocc, self.n - nocc, ptr(e)))
+        return {"E_AA": e[0], "E_AB": e[1], "E_MP2": e[2]}
+
+    def mp2_uhf(self, CA, CB, eA, eB, noA: int, noB: int, precision: int = PREC_FP64) -> dict:
+        e = np.zeros(4)
+        CA_, CB_ = f64(CA), f64(CB)
+        eA_, eB_ = np.ascontiguousarray(eA, dtype=np.float64), np.ascontiguousarray(eB, dtype=np.float64)
+        self._check(self.L.mq_mp2_uhf(self.h, ptr(CA_), ptr(CB_), ptr(eA_), ptr(eB_), noA, noB, precision, ptr(e)))
+        return {"E_AA": e[0], "E_BB": e[1], "E_AB": e[2], "E_MP2": e[3]}
+
+    # ---------------------------------------------------------------- linear algebra
+    def syev_batched(self, A: np.ndarray):
+        A = np.asarray(A, dtype=np.float64)
+        batch, n = A.shape[0], A.shape[1]
+        Ab = np.ascontiguousarray(np.stack([np.asfortranarray(a).reshape(-1, order="F") for a in A]))
+        w = np.zeros((batch, n))
+        V = np.zeros((batch, n * n))
+        self._check(self.L.mq_syev_batched(self.h, n, batch, ptr(Ab), ptr(w), ptr(V)))
+        return w, np.stack([v.reshape(n, n, order="F") for v in V])
+
+    def sygv(self, F, S):
+        n = F.shape[0]
+        F_, S_ = f64(F), f64(S)
+        w = np.zeros(n)
+        C = np.zeros((n, n), order="F")
+        self._check(self.L.mq_sygv(self.h, n, ptr(F_), ptr(S_), ptr(w), ptr(C)))
+        return w, C
+
+    def stat(self, key: str) -> float:
+        v = ctypes.c_double()
+        self._check(self.L.mq_stat(self.h, key.encode(), ctypes.byref(v)))
+        return v.value
+
+
+def run_job(sysm: System, basis: BasisArrays, ftab=None, mode: int = MODE_REFERENCE, conv: float | None = None,
+            diis: int = 0, precision: int = PREC_FP64, ctx: Context | None = None, mp2: bool | None = None):
+    """parse -> int1e -> int2e -> scf [-> ao2mo -> mp2] on the GPU (the myQC.f90 stage order)."""
+    own = ctx is None
+    ctx = ctx or Context()
+    try:
+        ctx.set_system(sysm, basis, ftab, mode)
+        S, H = ctx.int1e()
+        ctx.eri_store()
+        lim = conv if conv is not None else 10.0 ** (-min(sysm.options[8], 12))
+        res = ctx.scf(S, H, sysm.nelcA, sysm.nelcB, uhf=sysm.uhf, conv=lim, diis=diis)
+        out = {"S": S, "H": H, "scf": res}
+        do_mp2 = (sysm.options[1] == 1) if mp2 is None else mp2
+        if do_mp2:
+            if sysm.uhf:
+                out["mp2"] = ctx.mp2_uhf(res.C[0], res.C[1], res.eig[0], res.eig[1], sysm.nelcA, sysm.nelcB,
+                                         precision)
+            else:
+                out["mp2"] = ctx.mp2_rhf(res.eig, sysm.nelcA, precision, C=res.C)
+        return out
+    finally:
+        if own:
+            ctx.close()
