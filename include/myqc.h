@@ -163,9 +163,12 @@ int mq_syev_batched(mq_ctx *ctx, int n, int batch, double *A, double *w, double 
  * src/scf/scf.f90:478,848) for one n x n pair of host matrices. */
 int mq_sygv(mq_ctx *ctx, int n, const double *F, const double *S, double *w, double *C);
 
-/* Profiling counters of the last call (device milliseconds by stage and the
- * number of kernel launches).  keys: "eri", "fock", "diag", "ao2mo", "mp2",
- * "launches", "quartets", "prim_quartets".  Returns MQ_EINVAL on unknown key. */
+/* Profiling counters.  Device milliseconds (CUDA events on the context's
+ * stream) of the last call of each stage: "eri", "ao2mo", "mp2", "scf" (whole
+ * SCF), "fock" and "diag" (summed over the last SCF's iterations);
+ * "fock_calls", "scf_iters"; cumulative launch counts "launches" (this
+ * library's kernels) and "lib_launches" (cuBLAS calls); "quartets" and
+ * "prim_quartets" of the last integral pass.  MQ_EINVAL on an unknown key. */
 int mq_stat(const mq_ctx *ctx, const char *key, double *value);
 
 #ifdef __cplusplus

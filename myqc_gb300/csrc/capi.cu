@@ -426,6 +426,10 @@ int mq_stat(const mq_ctx *c, const char *key, double *value) {
   else if (!strcmp(key, "diag")) *value = s.ms_diag;
   else if (!strcmp(key, "ao2mo")) *value = s.ms_ao2mo;
   else if (!strcmp(key, "mp2")) *value = s.ms_mp2;
+  else if (!strcmp(key, "scf")) *value = s.ms_scf;
+  else if (!strcmp(key, "fock_calls")) *value = s.fock_calls;
+  else if (!strcmp(key, "scf_iters")) *value = s.scf_iters;
+  else if (!strcmp(key, "lib_launches")) *value = s.lib_launches;
   else if (!strcmp(key, "launches")) *value = s.launches;
   else if (!strcmp(key, "quartets")) *value = s.quartets;
   else if (!strcmp(key, "prim_quartets")) *value = s.prim_quartets;

@@ -50,9 +50,42 @@ struct DeviceBuf {
   size_t bytes = 0;
 };
 
+// Device time (CUDA events on the context's stream) of the last call of each
+// stage; the SCF accumulates over its iterations.
 struct Stats {
-  double ms_eri = 0, ms_fock = 0, ms_diag = 0, ms_ao2mo = 0, ms_mp2 = 0;
-  double launches = 0, quartets = 0, prim_quartets = 0;
+  double ms_eri = 0, ms_fock = 0, ms_diag = 0, ms_ao2mo = 0, ms_mp2 = 0, ms_scf = 0;
+  double fock_calls = 0, diag_calls = 0, scf_iters = 0;
+  double launches = 0, lib_launches = 0, quartets = 0, prim_quartets = 0;
+};
+
+// Event pair on the context's stream that adds its elapsed time to a counter
+// at the next synchronisation point.
+struct StageTimer {
+  cudaEvent_t a = nullptr, b = nullptr;
+  double total = 0;
+  bool pending = false;
+  void start(cudaStream_t s) {
+    if (!a) {
+      cudaEventCreate(&a);
+      cudaEventCreate(&b);
+    }
+    cudaEventRecord(a, s);
+  }
+  void stop(cudaStream_t s) {
+    cudaEventRecord(b, s);
+    pending = true;
+  }
+  void collect() {  // call after the stream has been synchronised
+    if (!pending) return;
+    float ms = 0;
+    cudaEventElapsedTime(&ms, a, b);
+    total += ms;
+    pending = false;
+  }
+  ~StageTimer() {
+    if (a) cudaEventDestroy(a);
+    if (b) cudaEventDestroy(b);
+  }
 };
 
 }  // namespace mq
@@ -115,7 +148,11 @@ int int1e_device(mq_ctx *c, double *d_S, double *d_H);
 int fock_stored_device(mq_ctx *c, const double *d_Da, const double *d_Db, double *d_Ga, double *d_Gb);
 
 // linalg.cu
+constexpr int JAC_SMEM_MAX = 110;  // largest order whose A and V (2 n^2 doubles) fit in shared memory
 int syev_batched_device(mq_ctx *c, int n, int batch, double *d_A, double *d_w, double *d_V);
+// one matrix of order n > JAC_SMEM_MAX on all SMs; d_V0 (optional) are start
+// vectors and d_A must then already be V0^T A V0
+int syev_large_device(mq_ctx *c, int n, double *d_A, const double *d_V0, double *d_w, double *d_V);
 int gemm(mq_ctx *c, char ta, char tb, int m, int n, int k, double alpha, const double *A, int lda, const double *B,
          int ldb, double beta, double *C, int ldc);
 int gemm_strided_batched(mq_ctx *c, char ta, char tb, int m, int n, int k, double alpha, const double *A, int lda,

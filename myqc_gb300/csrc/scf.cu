@@ -213,14 +213,29 @@ int scf_device(mq_ctx *c, const double *S, const double *H, const mq_scf_opts *o
   scale_cols_kernel<<<blocks(n2), 256, 0, c->stream>>>(dU, dEps, dW, n, -0.5);
   MQ_TRY(gemm(c, 'N', 'T', n, n, n, 1.0, dW, n, dU, n, 0.0, dX, n));
 
-  // solve F C = S C e for ns Fock matrices in dF -> dC, dEps
+  // solve F C = S C e for ns Fock matrices in dF -> dC, dEps.  Eigenvectors
+  // (orthogonal basis) go to dU (and dW, which follows it, for beta).  Large
+  // orders start the Jacobi sweeps from the previous iteration's vectors:
+  // A0 = U^T F' U is nearly diagonal once the SCF settles, so few sweeps remain.
+  bool have_prev = false;
   auto diagonalize = [&](const double *Fm) -> int {
     for (int s = 0; s < ns; ++s) {
       MQ_TRY(gemm(c, 'T', 'N', n, n, n, 1.0, dX, n, Fm + n2 * s, n, 0.0, dT1, n));
       MQ_TRY(gemm(c, 'N', 'N', n, n, n, 1.0, dT1, n, dX, n, 0.0, dFp + n2 * s, n));
     }
-    // eigenvectors into dU (and dW, which follows it, for the beta block)
-    MQ_TRY(syev_batched_device(c, n, ns, dFp, dEps, dU));
+    if (n <= JAC_SMEM_MAX) {
+      MQ_TRY(syev_batched_device(c, n, ns, dFp, dEps, dU));
+    } else {
+      for (int s = 0; s < ns; ++s) {
+        double *A = dFp + n2 * s, *U = dU + n2 * s;
+        if (have_prev) {
+          MQ_TRY(gemm(c, 'T', 'N', n, n, n, 1.0, U, n, A, n, 0.0, dT1, n));
+          MQ_TRY(gemm(c, 'N', 'N', n, n, n, 1.0, dT1, n, U, n, 0.0, A, n));
+        }
+        MQ_TRY(syev_large_device(c, n, A, have_prev ? U : nullptr, dEps + (size_t)n * s, U));
+      }
+      have_prev = true;
+    }
     return MQ_OK;
   };
   auto orbitals_to_density = [&]() -> int {
@@ -248,6 +263,8 @@ int scf_device(mq_ctx *c, const double *S, const double *H, const mq_scf_opts *o
   }
 
   const double enuc = nuclear_repulsion(c);
+  StageTimer t_fock, t_diag, t_all;
+  t_all.start(c->stream);
   std::vector<double> Bm((size_t)ndiis * ndiis * 4, 0.0);
   int nh = 0, head = 0;
   double E = 0.0;
@@ -256,6 +273,7 @@ int scf_device(mq_ctx *c, const double *S, const double *H, const mq_scf_opts *o
   std::vector<double> hist;
   for (; it < max_iter && !conv; ++it) {
     // G[D_k]
+    t_fock.start(c->stream);
     if (o->direct) {
       double *J = dT1, *Ka = dT2, *Kb = uhf ? dT3 : nullptr;
       MQ_TRY(fock_direct_device(c, dD, uhf ? dD + n2 : nullptr, J, Ka, Kb));
@@ -263,6 +281,7 @@ int scf_device(mq_ctx *c, const double *S, const double *H, const mq_scf_opts *o
     } else {
       MQ_TRY(fock_stored_device(c, dD, uhf ? dD + n2 : nullptr, dG, uhf ? dG + n2 : nullptr));
     }
+    t_fock.stop(c->stream);
     for (int s = 0; s < ns; ++s) add_kernel<<<blocks(n2), 256, 0, c->stream>>>(dH, dG + n2 * s, dF + n2 * s, n2);
     for (int s = 0; s < ns; ++s)
       energy_diff_kernel<<<1, 1024, 0, c->stream>>>(dD + n2 * s, dF + n2 * s, dH, nullptr, nullptr, n2, dScal, s);
@@ -305,12 +324,17 @@ int scf_device(mq_ctx *c, const double *S, const double *H, const mq_scf_opts *o
       }
       head = (head + 1) % ndiis;
     }
+    t_diag.start(c->stream);
     MQ_TRY(diagonalize(Fdiag));
+    t_diag.stop(c->stream);
     MQ_TRY(orbitals_to_density());
     diff_kernel<<<1, 1024, 0, c->stream>>>(dDn, dD, n2 * ns, dScal + 8);
+    c->stats.launches += 2 + 2 * ns;
     double hs[10];
     MQ_CUDA(c, cudaMemcpyAsync(hs, dScal, 10 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     MQ_CUDA(c, cudaStreamSynchronize(c->stream));
+    t_fock.collect();
+    t_diag.collect();
     E = hs[0] + (uhf ? hs[2] : 0.0) + enuc;
     const double diff = o->conv_rms ? hs[9] : hs[8];
     hist.push_back(E);
@@ -325,7 +349,15 @@ int scf_device(mq_ctx *c, const double *S, const double *H, const mq_scf_opts *o
   MQ_CUDA(c, cudaMemcpyAsync(C, dC, n2 * ns * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   MQ_CUDA(c, cudaMemcpyAsync(eps, dEps, (size_t)n * ns * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   if (D) MQ_CUDA(c, cudaMemcpyAsync(D, dD, n2 * ns * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  t_all.stop(c->stream);
   MQ_CUDA(c, cudaStreamSynchronize(c->stream));
+  t_all.collect();
+  c->stats.ms_scf = t_all.total;
+  c->stats.ms_fock = t_fock.total;
+  c->stats.ms_diag = t_diag.total;
+  c->stats.fock_calls = it;
+  c->stats.diag_calls = it;
+  c->stats.scf_iters = it;
   *energy = E;
   *iters = it;
   if (history)

@@ -143,7 +143,8 @@ def parse_zmat_text(text: str) -> System:
 
 def system_from_geometry(symbols, xyz_angstrom, charge=0, multiplicity=1, uhf=False, calc_mp2=True) -> System:
     """Build a System the way parse would for a CARTESIAN ZMAT in Angstrom."""
-    lines = ["CARTESIAN"] + [f"{s} {x!r} {y!r} {z!r}" for s, (x, y, z) in zip(symbols, xyz_angstrom)]
+    lines = ["CARTESIAN"] + [f"{s} {float(x)!r} {float(y)!r} {float(z)!r}"
+                             for s, (x, y, z) in zip(symbols, xyz_angstrom)]
     lines += ["END", "", f"CALC= {'MP2' if calc_mp2 else 'SCF'}", "BASIS= STO-3G", f"CHARGE= {charge}",
               f"MULTI= {multiplicity}", f"REF= {'UHF' if uhf else 'RHF'}"]
     return parse_zmat_text("\n".join(lines) + "\n")

@@ -109,7 +109,8 @@ class Context:
 
     # ---------------------------------------------------------------- SCF
     def scf(self, S, H, nalpha: int, nbeta: int, uhf: bool = False, conv: float = 1e-7, conv_rms: bool = False,
-            diis: int = 0, direct: bool = False, max_iter: int = 0, D_guess=None, C_guess=None) -> SCFResult:
+            diis: int = 0, direct: bool = False, max_iter: int = 0, D_guess=None, C_guess=None,
+            raise_on_noconv: bool = True) -> SCFResult:
         n, ns = self.n, 2 if uhf else 1
         o = _lib.ScfOpts()
         o.uhf, o.nalpha, o.nbeta, o.max_iter = int(uhf), nalpha, nbeta, max_iter
@@ -131,8 +132,10 @@ class Context:
         it = ctypes.c_int()
         cap = max_iter if max_iter > 0 else (300 if uhf else 500)
         hist = np.zeros(2 * cap)
-        self._check(self.L.mq_scf(self.h, ptr(S_), ptr(H_), ctypes.byref(o), ptr(C), ptr(eps), ptr(D),
-                                  ctypes.byref(E), ctypes.byref(it), ptr(hist)))
+        rc = self.L.mq_scf(self.h, ptr(S_), ptr(H_), ctypes.byref(o), ptr(C), ptr(eps), ptr(D), ctypes.byref(E),
+                           ctypes.byref(it), ptr(hist))
+        if not (rc == _lib.MQ_ENOCONV and not raise_on_noconv):
+            self._check(rc)
         k = it.value
         if uhf:
             return SCFResult(E.value, eps.T.copy(), np.moveaxis(C, 2, 0).copy(), np.moveaxis(D, 2, 0).copy(), k,
