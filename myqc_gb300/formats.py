@@ -155,7 +155,7 @@ def write_env(sysm: System, folder: str = ".") -> None:
     import os
     with open(os.path.join(folder, "nucpos"), "w") as f:
         for z, (x, y, w) in zip(sysm.atoms, sysm.xyz):
-            f.write(f" {z:11d} {x!r:>25} {y!r:>25} {w!r:>25}\n")
+            f.write(f" {int(z):11d} {float(x)!r:>25} {float(y)!r:>25} {float(w)!r:>25}\n")
     with open(os.path.join(folder, "envdat"), "w") as f:
         f.write(f" {len(sysm.atoms):11d}\n {sysm.nelcA:11d} {sysm.nelcB:11d}\n {len(sysm.options):11d}\n")
         f.write(" " + " ".join(f"{o:20d}" for o in sysm.options) + "\n\n")

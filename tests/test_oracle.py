@@ -1,0 +1,87 @@
+"""The oracle against the reference's own known answers (no GPU).
+
+* myQC's MOLDEN orbital energies (examples/Be, O/singlet, NO) -- parity pins;
+* Ftab, a known-answer table: decoded values equal the exact Boys function
+  except for the four corrupted entries the reference ships;
+* CFOUR energies beside the examples -- loose sanity pins (true pi, exact
+  Boys, renormalised contractions in CFOUR);
+* the tight oracle's Boys function against scipy's confluent hypergeometric.
+"""
+import json
+
+import numpy as np
+import pytest
+
+import oracle as O
+from conftest import golden
+
+PINS = json.load(open(golden("reference_pins.json")))
+
+
+def _run(name, ftab, basis_text, mode=0, conv_exp=None):
+    return O.run_job(open(golden("zmat", name + ".ZMAT")).read(), basis_text, ftab, mode, conv_exp)
+
+
+@pytest.mark.parametrize("name,tol", [("Be", 1e-8), ("O_singlet", 1e-8), ("NO", 1e-7)])
+def test_molden_orbital_energies(ftab, basis_text, name, tol):
+    r = _run(name, ftab, basis_text)
+    p = PINS["molden"][name]
+    eig = r["scf"].eig
+    if p["beta"]:
+        assert np.max(np.abs(eig[0] - p["alpha"])) < tol
+        assert np.max(np.abs(eig[1] - p["beta"])) < tol
+    else:
+        assert np.max(np.abs(eig - p["alpha"])) < tol
+
+
+def test_ftab_known_answers(ftab):
+    sp = pytest.importorskip("scipy.special")
+    T = np.arange(121) / 10.0
+    exact = np.array([[sp.hyp1f1(m + 0.5, m + 1.5, -t) / (2 * m + 1) for t in T] for m in range(23)]).T
+    err = np.abs(ftab.reshape(23, 121).T - exact)
+    bad = sorted((round(T[i], 1), m) for i, m in zip(*np.nonzero(err > 1e-8)))
+    assert bad == [(3.6, 2), (7.4, 11), (8.4, 7), (9.4, 0)]
+    # every other entry carries the table's ~10 printed digits (worst 5.7e-10 at T=1.6, m=0)
+    assert np.max(np.where(err > 1e-8, 0, err)) < 1e-9
+
+
+def test_tight_boys(ftab):
+    sp = pytest.importorskip("scipy.special")
+    for T in (0.0, 1e-3, 0.7, 5.55, 11.9, 12.0, 25.0, 35.9, 36.1, 80.0):
+        F = O.boys(T, 12, ftab, mode=1)
+        ex = np.array([sp.hyp1f1(m + 0.5, m + 1.5, -T) / (2 * m + 1) for m in range(13)])
+        assert np.max(np.abs(F - ex) / ex) < 5e-14
+
+
+@pytest.mark.parametrize("name,tol_scf,tol_mp2", [("CO2", 1e-4, 2e-6), ("HeH", 1e-6, None), ("OH", 2e-5, None)])
+def test_cfour_sanity(ftab, basis_text, name, tol_scf, tol_mp2):
+    r = _run(name, ftab, basis_text, conv_exp=10)
+    c = PINS["cfour"][name]
+    assert abs(r["scf"].energy - c["E_SCF"]) < tol_scf
+    if tol_mp2:
+        assert abs(r["mp2"]["E_MP2"] - c["E2(TOT)"]) < tol_mp2
+
+
+def test_xx_symmetry_and_conventions(ftab, basis_text):
+    """XX carries all 8 permutations; G from RHFI2G's formula equals J - K/2."""
+    r = _run("HF", ftab, basis_text, conv_exp=8)
+    XX = r["XX"]
+    for perm in [(1, 0, 2, 3), (0, 1, 3, 2), (2, 3, 0, 1), (3, 2, 1, 0)]:
+        assert np.array_equal(XX, XX.transpose(perm))
+    D = r["scf"].D
+    J = np.einsum("ijkl,kl->ij", XX, D)
+    K = np.einsum("ikjl,kl->ij", XX, D)
+    assert np.allclose(O.fock_rhf(XX, D), J - 0.5 * K, atol=1e-12)
+
+
+def test_mp2_sum_identity(ftab, basis_text):
+    """E(MBPT2) = 2 E(AA) + E(AB) equals the closed-shell formula."""
+    r = _run("CO2", ftab, basis_text, conv_exp=9)
+    res, XX, no = r["scf"], r["XX"], r["mol"].nelcA
+    C, e = res.C, res.eig
+    Om = O.ao2mo(XX, C[:, :no], C[:, no:], C[:, :no], C[:, no:])
+    ref = np.einsum("ua,vb,lc,sd,uvls->abcd", C[:, :no], C[:, no:], C[:, :no], C[:, no:], XX)
+    assert np.allclose(Om, ref, atol=1e-12)
+    D = e[:no, None, None, None] - e[None, no:, None, None] + e[None, None, :no, None] - e[None, None, None, no:]
+    E = np.sum(Om * (2 * Om - Om.transpose(0, 3, 2, 1)) / D)
+    assert abs(E - r["mp2"]["E_MP2"]) < 1e-12
