@@ -1,0 +1,60 @@
+"""Split hi+lo BF16 tensor-core transform (tcgen05) against the FP64 path.
+
+(ia|jb) from the split path carries ~2^-16 relative operand rounding; the MP2
+energy error it causes must stay below 1 uEh (the precision target), and the
+transform itself within 5e-4 of the largest |(ia|jb)|."""
+import numpy as np
+import pytest
+
+from conftest import golden
+from myqc_gb300 import MODE_TIGHT, PREC_FP64, PREC_SPLIT_BF16, formats, molecules
+
+pytestmark = pytest.mark.gpu
+
+
+def _systems(basis_text):
+    out = []
+    for name in ("CO2", "HF", "NO"):
+        s = formats.parse_zmat_text(open(golden("zmat", name + ".ZMAT")).read())
+        out.append((name, s))
+    for nm in (2, 4):
+        out.append((f"(H2O){nm}", molecules.water_cluster_system(nm, (27.0 * nm) ** (1 / 3) + 1.0, 7)))
+    return out
+
+
+@pytest.mark.parametrize("idx", range(5))
+def test_split_transform_matches_fp64(ctx, basis_text, idx):
+    name, sysm = _systems(basis_text)[idx]
+    basis = formats.parse_mybasis_text(basis_text, sysm.atoms)
+    ctx.set_system(sysm, basis, None, MODE_TIGHT)
+    S, H = ctx.int1e()
+    ctx.eri_store()
+    res = ctx.scf(S, H, sysm.nelcA, sysm.nelcB, uhf=sysm.uhf, conv=1e-10, diis=8)
+    C = res.C[0] if sysm.uhf else res.C
+    no = sysm.nelcA
+    blocks = (C[:, :no], C[:, no:], C[:, :no], C[:, no:])
+    ref = ctx.ao2mo_iajb(*blocks, PREC_FP64)
+    got = ctx.ao2mo_iajb(*blocks, PREC_SPLIT_BF16)
+    scale = np.max(np.abs(ref))
+    assert np.max(np.abs(got - ref)) < 5e-4 * scale
+    if sysm.uhf:
+        e64 = ctx.mp2_uhf(res.C[0], res.C[1], res.eig[0], res.eig[1], sysm.nelcA, sysm.nelcB, PREC_FP64)
+        e16 = ctx.mp2_uhf(res.C[0], res.C[1], res.eig[0], res.eig[1], sysm.nelcA, sysm.nelcB, PREC_SPLIT_BF16)
+    else:
+        e64 = ctx.mp2_rhf(res.eig, no, PREC_FP64, C=C)
+        e16 = ctx.mp2_rhf(res.eig, no, PREC_SPLIT_BF16, C=C)
+    assert abs(e16["E_MP2"] - e64["E_MP2"]) < 1e-6, (name, e16, e64)
+
+
+def test_split_rectangular_blocks(ctx, basis_text):
+    """Unequal occupied / virtual blocks and odd sizes (K padding, partial tiles)."""
+    sysm = formats.parse_zmat_text(open(golden("zmat", "CO.ZMAT")).read())
+    basis = formats.parse_mybasis_text(basis_text, sysm.atoms)
+    ctx.set_system(sysm, basis, None, MODE_TIGHT)
+    ctx.eri_store()
+    n = ctx.n
+    rng = np.random.default_rng(5)
+    Ci, Ca, Cj, Cb = (rng.standard_normal((n, k)) * 0.3 for k in (3, 7, 5, 2))
+    ref = ctx.ao2mo_iajb(Ci, Ca, Cj, Cb, PREC_FP64)
+    got = ctx.ao2mo_iajb(Ci, Ca, Cj, Cb, PREC_SPLIT_BF16)
+    assert np.max(np.abs(got - ref)) < 5e-4 * np.max(np.abs(ref))
