@@ -27,12 +27,14 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 
 #include "internal.h"
 
 namespace mq {
 
 typedef __nv_bfloat16 bf16;
+typedef unsigned short h16;  // storage of one 16-bit operand (BF16 or FP16 bits)
 
 constexpr int UM = 128;         // MMA M (rows per tile)
 constexpr int UK = 64;          // K elements per stage (one 128-byte swizzle row)
@@ -137,17 +139,28 @@ struct GemmArgs {
   int M, N, K, batch;       // logical sizes (K is the padded K)
   int ntile;                // N rounded up to a multiple of 16
   int tmem_cols;            // power of two >= ntile
-  int out_f64;              // 1: FP64 output; 0: split BF16 output
+  int fp16;                 // operand format: 1 FP16, 0 BF16
+  int out_f64;              // 1: FP64 output; 0: split 16-bit output
+  float out_scale;          // exact power of two applied to the accumulator
   long long mdiv, s_m0, s_m1, s_n, s_b;  // out index = (m%mdiv)*s_m0 + (m/mdiv)*s_m1 + n*s_n + batch*s_b
   double *out;
-  bf16 *out_hi, *out_lo;
+  h16 *out_hi, *out_lo;
   int *err;
 };
 
-// split one FP32 value into two BF16 numbers
-__device__ __forceinline__ void split2(float x, bf16 &h, bf16 &l) {
-  h = __float2bfloat16_rn(x);
-  l = __float2bfloat16_rn(x - __bfloat162float(h));
+// split one FP32 value into two 16-bit numbers (hi + lo ~ x)
+__device__ __forceinline__ void split2(float x, int fp16, h16 &h, h16 &l) {
+  if (fp16) {
+    const __half a = __float2half_rn(x);
+    const __half b = __float2half_rn(x - __half2float(a));
+    h = __half_as_ushort(a);
+    l = __half_as_ushort(b);
+  } else {
+    const bf16 a = __float2bfloat16_rn(x);
+    const bf16 b = __float2bfloat16_rn(x - __bfloat162float(a));
+    h = __bfloat16_as_ushort(a);
+    l = __bfloat16_as_ushort(b);
+  }
 }
 
 template <int STAGES>
@@ -227,7 +240,9 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) split_gemm_kernel(const __gri
   } else if (warp == 1) {
     // ---------------- MMA issuer
     if (lane == 0) {
-      const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(ntile >> 3) << 17) |
+      // D = F32; A, B = BF16 (format 1) or F16 (format 0); both K-major
+      const uint32_t fmt = g.fp16 ? 0u : 1u;
+      const uint32_t idesc = (1u << 4) | (fmt << 7) | (fmt << 10) | ((uint32_t)(ntile >> 3) << 17) |
                              ((uint32_t)(UM >> 4) << 24);
       int s = 0;
       uint32_t ph = 0, acc_ph = 1;
@@ -287,10 +302,10 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) split_gemm_kernel(const __gri
           if (n >= g.N) break;
           const long long o = base + (long long)n * g.s_n;
           if (g.out_f64) {
-            g.out[o] = (double)v[i];
+            g.out[o] = (double)(v[i] * g.out_scale);
           } else {
-            bf16 h, l;
-            split2(v[i], h, l);
+            h16 h, l;
+            split2(v[i] * g.out_scale, g.fp16, h, l);
             g.out_hi[o] = h;
             g.out_lo[o] = l;
           }
@@ -322,18 +337,60 @@ __device__ __forceinline__ float f64_to_f32_bits(double x) {
   return __uint_as_float((hi & 0x80000000u) | ((unsigned)e << 23) | m);
 }
 
-// out[r*Kp + k] = split(in[k + ld*r]) for k < kvalid, 0 for kvalid <= k < Kp
+// out[r*Kp + k] = split(scale * in[k + ld*r]) for k < kvalid, 0 for kvalid <= k < Kp
 __global__ void split_rows_kernel(const double *__restrict__ in, long long rows, int kvalid, long long ld, int Kp,
-                                  bf16 *__restrict__ hi, bf16 *__restrict__ lo) {
+                                  float scale, int fp16, h16 *__restrict__ hi, h16 *__restrict__ lo) {
   const long long tot = rows * Kp;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < tot; i += (long long)gridDim.x * blockDim.x) {
     const long long r = i / Kp;
     const int k = (int)(i - r * Kp);
-    bf16 h = __float2bfloat16_rn(0.0f), l = h;
-    if (k < kvalid) split2(f64_to_f32_bits(__ldcs(in + k + ld * r)), h, l);
+    h16 h = 0, l = 0;  // +0 in both formats
+    if (k < kvalid) split2(f64_to_f32_bits(__ldcs(in + k + ld * r)) * scale, fp16, h, l);
     hi[i] = h;
     lo[i] = l;
   }
+}
+
+// per column of an n x cols block: max |c| and the 1-norm; out[2] = {max|c|, max_col ||c||_1}
+__global__ void col_norms_kernel(const double *__restrict__ C, int n, int cols, double *__restrict__ out) {
+  __shared__ double smax[256], snorm[256];
+  double mx = 0.0, nm = 0.0;
+  for (int col = threadIdx.x; col < cols; col += blockDim.x) {
+    double s = 0.0;
+    for (int r = 0; r < n; ++r) {
+      const double v = fabs(C[r + (size_t)n * col]);
+      s += v;
+      mx = fmax(mx, v);
+    }
+    nm = fmax(nm, s);
+  }
+  smax[threadIdx.x] = mx;
+  snorm[threadIdx.x] = nm;
+  __syncthreads();
+  for (int k = blockDim.x / 2; k > 0; k >>= 1) {
+    if (threadIdx.x < k) {
+      smax[threadIdx.x] = fmax(smax[threadIdx.x], smax[threadIdx.x + k]);
+      snorm[threadIdx.x] = fmax(snorm[threadIdx.x], snorm[threadIdx.x + k]);
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    out[0] = smax[0];
+    out[1] = snorm[0];
+  }
+}
+
+__global__ void max_kernel(const double *__restrict__ x, int n, double *__restrict__ out) {
+  __shared__ double s[256];
+  double m = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) m = fmax(m, fabs(x[i]));
+  s[threadIdx.x] = m;
+  __syncthreads();
+  for (int k = blockDim.x / 2; k > 0; k >>= 1) {
+    if (threadIdx.x < k) s[threadIdx.x] = fmax(s[threadIdx.x], s[threadIdx.x + k]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[0] = s[0];
 }
 
 // ------------------------------------------------------------------ host side
@@ -350,41 +407,27 @@ static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   return fn;
 }
 
-// rank-3 map of a K-major BF16 operand [batch][rows][Kp] (Kp % 8 == 0), box (64, box_rows, 1)
-static int make_map(mq_ctx *c, CUtensorMap *m, const bf16 *ptr, int Kp, long long rows, long long batch,
+// rank-3 map of a K-major 16-bit operand [batch][rows][Kp] (Kp % 8 == 0), box (64, box_rows, 1)
+static int make_map(mq_ctx *c, CUtensorMap *m, const h16 *ptr, int fp16, int Kp, long long rows, long long batch,
                     long long batch_stride_elems, int box_rows) {
   auto fn = encode_fn();
   if (!fn) return set_err(c, MQ_ECUDA, "cuTensorMapEncodeTiled unavailable");
+  if (batch == 1) batch_stride_elems = rows * Kp;  // unused, but must be a valid stride
   if (Kp % 8 || ((uintptr_t)ptr & 15) || (batch_stride_elems * 2) % 16)
     return set_err(c, MQ_EINVAL, "TMA operand not 16-byte aligned");
-  if (batch == 1) batch_stride_elems = rows * Kp;  // unused, but must be a valid stride
   cuuint64_t dims[3] = {(cuuint64_t)Kp, (cuuint64_t)rows, (cuuint64_t)batch};
   cuuint64_t strides[2] = {(cuuint64_t)Kp * 2, (cuuint64_t)batch_stride_elems * 2};
   cuuint32_t box[3] = {(cuuint32_t)UK, (cuuint32_t)box_rows, 1};
   cuuint32_t estr[3] = {1, 1, 1};
-  CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, (void *)ptr, dims, strides, box, estr,
-                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-  if (r != CUDA_SUCCESS) return set_err(c, MQ_ECUDA, "cuTensorMapEncodeTiled failed");
-  return MQ_OK;
-}
-
-static int make_map2(mq_ctx *c, CUtensorMap *m, const bf16 *ptr, int Kp, long long rows, int box_rows) {
-  auto fn = encode_fn();
-  if (!fn) return set_err(c, MQ_ECUDA, "cuTensorMapEncodeTiled unavailable");
-  cuuint64_t dims[2] = {(cuuint64_t)Kp, (cuuint64_t)rows};
-  cuuint64_t strides[1] = {(cuuint64_t)Kp * 2};
-  cuuint32_t box[2] = {(cuuint32_t)UK, (cuuint32_t)box_rows};
-  cuuint32_t estr[2] = {1, 1};
-  CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void *)ptr, dims, strides, box, estr,
-                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  CUresult r = fn(m, fp16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, (void *)ptr, dims,
+                  strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return set_err(c, MQ_ECUDA, "cuTensorMapEncodeTiled failed");
   return MQ_OK;
 }
 
 struct SplitOperand {
-  bf16 *hi, *lo;
+  h16 *hi, *lo;
 };
 
 // D = A B^T over split operands; A: [batch][M][Kp], B: [N][Kp] (shared by all batches)
@@ -392,12 +435,13 @@ static int split_gemm(mq_ctx *c, SplitOperand A, long long M, int batch, long lo
                       int N, int Kp, GemmArgs g) {
   if (N <= 0 || M <= 0 || batch <= 0) return MQ_OK;
   if (N > 256) return set_err(c, MQ_EINVAL, "split GEMM: N > 256");
+  if (M > 2147483647LL) return set_err(c, MQ_EINVAL, "split GEMM: M too large");
   CUtensorMap mAh, mAl, mBh, mBl;
   const int ntile = (N + 15) / 16 * 16;
-  MQ_TRY(make_map(c, &mAh, A.hi, Kp, M, batch, a_batch_stride, UM));
-  MQ_TRY(make_map(c, &mAl, A.lo, Kp, M, batch, a_batch_stride, UM));
-  MQ_TRY(make_map2(c, &mBh, B.hi, Kp, N, ntile));
-  MQ_TRY(make_map2(c, &mBl, B.lo, Kp, N, ntile));
+  MQ_TRY(make_map(c, &mAh, A.hi, g.fp16, Kp, M, batch, a_batch_stride, UM));
+  MQ_TRY(make_map(c, &mAl, A.lo, g.fp16, Kp, M, batch, a_batch_stride, UM));
+  MQ_TRY(make_map(c, &mBh, B.hi, g.fp16, Kp, N, 1, 0, ntile));
+  MQ_TRY(make_map(c, &mBl, B.lo, g.fp16, Kp, N, 1, 0, ntile));
   g.M = (int)M;
   g.N = N;
   g.K = Kp;
@@ -422,47 +466,83 @@ static int split_gemm(mq_ctx *c, SplitOperand A, long long M, int batch, long lo
   return MQ_OK;
 }
 
-static int split_rows(mq_ctx *c, const double *in, long long rows, int kvalid, long long ld, int Kp, SplitOperand o) {
+static int split_rows(mq_ctx *c, const double *in, long long rows, int kvalid, long long ld, int Kp, float scale,
+                      int fp16, SplitOperand o) {
   const long long tot = rows * Kp;
   const int tb = 256;
-  const long long blocks = std::min<long long>((tot + tb - 1) / tb, 1 << 20);
-  split_rows_kernel<<<(unsigned)blocks, tb, 0, c->stream>>>(in, rows, kvalid, ld, Kp, o.hi, o.lo);
+  const long long blocks = std::max<long long>(1, std::min<long long>((tot + tb - 1) / tb, 1 << 20));
+  split_rows_kernel<<<(unsigned)blocks, tb, 0, c->stream>>>(in, rows, kvalid, ld, Kp, scale, fp16, o.hi, o.lo);
   c->stats.launches += 1;
   MQ_CUDA(c, cudaGetLastError());
   return MQ_OK;
 }
 
+// power of two s with bound * s <= 2^14 (FP16 operands keep their hi and lo
+// parts inside the normal range with room for the FP32 sums)
+static double pow2_scale(double bound) {
+  if (!(bound > 0)) return 1.0;
+  return std::ldexp(1.0, 14 - (int)std::ceil(std::log2(bound)));
+}
+
 int ao2mo_split_device(mq_ctx *c, const double *Ci, int no1, const double *Ca, int nv1, const double *Cj, int no2,
-                       const double *Cb, int nv2, double *d_out) {
+                       const double *Cb, int nv2, double *d_out, int fp16) {
   const long long n = c->nao;
   const int Kp = (int)((n + 7) / 8 * 8);
   if (no1 > 256 || nv1 > 256 || no2 > 256 || nv2 > 256)
     return set_err(c, MQ_EINVAL, "split transform: orbital blocks above 256 are not supported");
   const long long n2 = n * n, n3 = n2 * n;
-  // buffers (BF16 elements)
+  // buffers (16-bit elements)
   const size_t eX = (size_t)n3 * Kp, e1 = (size_t)nv2 * n2 * Kp, e2 = (size_t)no2 * nv2 * n * Kp,
                e3 = (size_t)nv1 * no2 * nv2 * Kp, eC = (size_t)(no1 + nv1 + no2 + nv2) * Kp;
-  bf16 *bx = (bf16 *)buf(c, "split_xx", 2 * eX * sizeof(bf16));
-  bf16 *b1 = (bf16 *)buf(c, "split_y1", 2 * std::max(e1, e3) * sizeof(bf16));
-  bf16 *b2 = (bf16 *)buf(c, "split_y2", 2 * e2 * sizeof(bf16));
-  bf16 *bc = (bf16 *)buf(c, "split_c", 2 * eC * sizeof(bf16));
+  h16 *bx = (h16 *)buf(c, "split_xx", 2 * eX * sizeof(h16));
+  h16 *b1 = (h16 *)buf(c, "split_y1", 2 * std::max(e1, e3) * sizeof(h16));
+  h16 *b2 = (h16 *)buf(c, "split_y2", 2 * e2 * sizeof(h16));
+  h16 *bc = (h16 *)buf(c, "split_c", 2 * eC * sizeof(h16));
   int *err = (int *)buf(c, "split_err", 64);
-  if (!bx || !b1 || !b2 || !bc || !err) return MQ_ENOMEM;
+  double *nrm = (double *)buf(c, "split_norms", 16 * sizeof(double));
+  if (!bx || !b1 || !b2 || !bc || !err || !nrm) return MQ_ENOMEM;
   MQ_CUDA(c, cudaMemsetAsync(err, 0, sizeof(int), c->stream));
+  // scale factors from rigorous bounds (FP16 only; BF16 has the FP32 range):
+  // |XX| <= max_P (sqrt max (ab|ab))^2 (Schwarz), |Y_k| <= |Y_{k-1}| * max column 1-norm of C_k
+  double sX = 1, sI = 1, sA = 1, sJ = 1, sB = 1, s1 = 1, s2 = 1, s3 = 1;
+  if (fp16) {
+    MQ_TRY(eri_schwarz(c));
+    max_kernel<<<1, 256, 0, c->stream>>>(c->pt.schwarz, c->pt.npairs, nrm);
+    col_norms_kernel<<<1, 256, 0, c->stream>>>(Ci, (int)n, no1, nrm + 2);
+    col_norms_kernel<<<1, 256, 0, c->stream>>>(Ca, (int)n, nv1, nrm + 4);
+    col_norms_kernel<<<1, 256, 0, c->stream>>>(Cj, (int)n, no2, nrm + 6);
+    col_norms_kernel<<<1, 256, 0, c->stream>>>(Cb, (int)n, nv2, nrm + 8);
+    c->stats.launches += 5;
+    double h[10];
+    MQ_CUDA(c, cudaMemcpyAsync(h, nrm, sizeof h, cudaMemcpyDeviceToHost, c->stream));
+    MQ_CUDA(c, cudaStreamSynchronize(c->stream));
+    const double bX = h[0] * h[0];
+    sX = pow2_scale(bX);
+    sI = pow2_scale(h[2]);
+    sA = pow2_scale(h[4]);
+    sJ = pow2_scale(h[6]);
+    sB = pow2_scale(h[8]);
+    const double b1 = bX * h[9], b2 = b1 * h[7], b3 = b2 * h[5];
+    s1 = pow2_scale(b1);
+    s2 = pow2_scale(b2);
+    s3 = pow2_scale(b3);
+  }
   SplitOperand X{bx, bx + eX}, Y1{b1, b1 + e1}, Y2{b2, b2 + e2}, Y3{b1, b1 + e3};  // Y3 reuses Y1's space
   SplitOperand Bi{bc, bc + eC}, Ba{Bi.hi + (size_t)no1 * Kp, Bi.lo + (size_t)no1 * Kp};
   SplitOperand Bj{Ba.hi + (size_t)nv1 * Kp, Ba.lo + (size_t)nv1 * Kp}, Bb{Bj.hi + (size_t)no2 * Kp, Bj.lo + (size_t)no2 * Kp};
   // coefficient blocks: column p of C (n contiguous) becomes row p of B (K-major)
-  MQ_TRY(split_rows(c, Ci, no1, (int)n, n, Kp, Bi));
-  MQ_TRY(split_rows(c, Ca, nv1, (int)n, n, Kp, Ba));
-  MQ_TRY(split_rows(c, Cj, no2, (int)n, n, Kp, Bj));
-  MQ_TRY(split_rows(c, Cb, nv2, (int)n, n, Kp, Bb));
+  MQ_TRY(split_rows(c, Ci, no1, (int)n, n, Kp, (float)sI, fp16, Bi));
+  MQ_TRY(split_rows(c, Ca, nv1, (int)n, n, Kp, (float)sA, fp16, Ba));
+  MQ_TRY(split_rows(c, Cj, no2, (int)n, n, Kp, (float)sJ, fp16, Bj));
+  MQ_TRY(split_rows(c, Cb, nv2, (int)n, n, Kp, (float)sB, fp16, Bb));
   // XX(d,l,u,v) at d + n*((l,u,v)): rows (l,u,v) with K = d
-  MQ_TRY(split_rows(c, c->d_XX, n3, (int)n, n, Kp, X));
+  MQ_TRY(split_rows(c, c->d_XX, n3, (int)n, n, Kp, (float)sX, fp16, X));
   GemmArgs g{};
   g.err = err;
+  g.fp16 = fp16;
   // 1: Y1[b][(u,v)][l] = sum_d XX(d,l,u,v) Cb(d,b);   row m = l + n*(u + n*v)
   g.out_f64 = 0;
+  g.out_scale = (float)(s1 / (sX * sB));
   g.out_hi = Y1.hi;
   g.out_lo = Y1.lo;
   g.mdiv = n;
@@ -472,6 +552,7 @@ int ao2mo_split_device(mq_ctx *c, const double *Ci, int no1, const double *Ca, i
   g.s_b = 0;
   MQ_TRY(split_gemm(c, X, n3, 1, 0, Bb, nv2, Kp, g));
   // 2: batch b; rows m = u + n*v, K = l -> Y2[j,b][v][u]
+  g.out_scale = (float)(s2 / (s1 * sJ));
   g.out_hi = Y2.hi;
   g.out_lo = Y2.lo;
   g.mdiv = n;
@@ -481,6 +562,7 @@ int ao2mo_split_device(mq_ctx *c, const double *Ci, int no1, const double *Ca, i
   g.s_b = (long long)no2 * n * Kp;
   MQ_TRY(split_gemm(c, Y1, n2, nv2, n2 * Kp, Bj, no2, Kp, g));
   // 3: batch (j + no2*b); rows v, K = u -> Y3[a + nv1*(j + no2*b)][v]
+  g.out_scale = (float)(s3 / (s2 * sA));
   g.out_hi = Y3.hi;
   g.out_lo = Y3.lo;
   g.mdiv = 1ll << 62;
@@ -491,6 +573,7 @@ int ao2mo_split_device(mq_ctx *c, const double *Ci, int no1, const double *Ca, i
   MQ_TRY(split_gemm(c, Y2, n, no2 * nv2, n * Kp, Ba, nv1, Kp, g));
   // 4: rows (a, j, b), K = v -> Om(i, a, j, b) = D[m][i] at i + no1*m
   g.out_f64 = 1;
+  g.out_scale = (float)(1.0 / (s3 * sI));
   g.out = d_out;
   g.mdiv = 1ll << 62;
   g.s_m0 = no1;
