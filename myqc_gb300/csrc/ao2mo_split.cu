@@ -463,7 +463,7 @@ static int split_gemm(mq_ctx *c, SplitOperand A, long long M, int batch, long lo
   kern<<<grid, GEMM_THREADS, smem, c->stream>>>(mAh, mAl, mBh, mBl, g);
   c->stats.launches += 1;
   MQ_CUDA(c, cudaGetLastError());
-  return MQ_OK;
+  return sync_check(c, "split_gemm");
 }
 
 static int split_rows(mq_ctx *c, const double *in, long long rows, int kvalid, long long ld, int Kp, float scale,
@@ -474,7 +474,7 @@ static int split_rows(mq_ctx *c, const double *in, long long rows, int kvalid, l
   split_rows_kernel<<<(unsigned)blocks, tb, 0, c->stream>>>(in, rows, kvalid, ld, Kp, scale, fp16, o.hi, o.lo);
   c->stats.launches += 1;
   MQ_CUDA(c, cudaGetLastError());
-  return MQ_OK;
+  return sync_check(c, "split_rows");
 }
 
 // power of two s with bound * s <= 2^14 (FP16 operands keep their hi and lo
@@ -507,12 +507,14 @@ int ao2mo_split_device(mq_ctx *c, const double *Ci, int no1, const double *Ca, i
   double sX = 1, sI = 1, sA = 1, sJ = 1, sB = 1, s1 = 1, s2 = 1, s3 = 1;
   if (fp16) {
     MQ_TRY(eri_schwarz(c));
+    MQ_TRY(sync_check(c, "schwarz"));
     max_kernel<<<1, 256, 0, c->stream>>>(c->pt.schwarz, c->pt.npairs, nrm);
     col_norms_kernel<<<1, 256, 0, c->stream>>>(Ci, (int)n, no1, nrm + 2);
     col_norms_kernel<<<1, 256, 0, c->stream>>>(Ca, (int)n, nv1, nrm + 4);
     col_norms_kernel<<<1, 256, 0, c->stream>>>(Cj, (int)n, no2, nrm + 6);
     col_norms_kernel<<<1, 256, 0, c->stream>>>(Cb, (int)n, nv2, nrm + 8);
     c->stats.launches += 5;
+    MQ_TRY(sync_check(c, "norms"));
     double h[10];
     MQ_CUDA(c, cudaMemcpyAsync(h, nrm, sizeof h, cudaMemcpyDeviceToHost, c->stream));
     MQ_CUDA(c, cudaStreamSynchronize(c->stream));

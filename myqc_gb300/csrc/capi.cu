@@ -42,6 +42,23 @@ void *buf(mq_ctx *c, const char *name, size_t bytes) {
   return p;
 }
 
+int sync_check(mq_ctx *c, const char *label) {
+  static int on = -1;
+  if (on < 0) {
+    const char *e = getenv("MYQC_SYNC_CHECK");
+    on = e && e[0] == '1';
+  }
+  if (!on) return MQ_OK;
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    char b[512];
+    snprintf(b, sizeof b, "stage %s: %s", label, cudaGetErrorString(e));
+    return set_err(c, MQ_ECUDA, b);
+  }
+  return MQ_OK;
+}
+
 static int need_system(mq_ctx *c) {
   if (!c) return MQ_EINVAL;
   if (!c->have_system) return set_err(c, MQ_ESTATE, "no system: call mq_set_system first");

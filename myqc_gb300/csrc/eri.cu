@@ -383,7 +383,7 @@ static int launch_class(mq_ctx *c, EriArgs g, int cP, int cQ) {
 #undef MQ_LAUNCH
   c->stats.launches += 1;
   MQ_CUDA(c, cudaGetLastError());
-  return MQ_OK;
+  return sync_check(c, EPI == EPI_SCHWARZ ? "eri_schwarz" : (EPI == EPI_XX ? "eri_xx" : "eri_fock"));
 }
 
 static EriArgs base_args(mq_ctx *c) {

@@ -126,6 +126,9 @@ int cuda_check(mq_ctx *c, cudaError_t e, const char *what);
 // device buffer `name` of at least `bytes` (contents undefined after growth);
 // nullptr on failure with the error set
 void *buf(mq_ctx *c, const char *name, size_t bytes);
+// With MYQC_SYNC_CHECK=1 in the environment: synchronise the stream and report
+// the first failing stage by `label` (a diagnostic; off by default).
+int sync_check(mq_ctx *c, const char *label);
 
 // basis.cu
 int build_shells(mq_ctx *c, int nnuc, const int *Z, const double *xyz, const double *bas, const double *set,
