@@ -122,8 +122,10 @@ __device__ __forceinline__ void umma_commit(uint64_t *bar) {
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
+// warp-collective (.sync.aligned): every lane of the warp must arrive converged
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
   uint32_t r[16];
+  __syncwarp();
   asm volatile(
       "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
       : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
@@ -197,6 +199,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) split_gemm_kernel(const __gri
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 1) {
+    __syncwarp();
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(tmem_slot)),
                  "r"(g.tmem_cols)
                  : "memory");
@@ -286,7 +289,11 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) split_gemm_kernel(const __gri
     uint32_t acc_ph = 0;
     for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
       const int mt = (int)(t % mtiles), bt = (int)(t / mtiles);
-      if (!mbar_wait(acc_full, acc_ph, g.err)) break;
+      // one lane polls, the warp reconverges before the aligned TMEM loads
+      int ok = 0;
+      if (lane == 0) ok = mbar_wait(acc_full, acc_ph, g.err);
+      ok = __shfl_sync(0xffffffffu, ok, 0);
+      if (!ok) break;
       acc_ph ^= 1;
       tc_fence_after();
       const long long m = (long long)mt * UM + row;
@@ -319,6 +326,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) split_gemm_kernel(const __gri
   tc_fence_before();
   __syncthreads();
   if (warp == 1) {
+    __syncwarp();
     tc_fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(g.tmem_cols) : "memory");
   }
