@@ -5,7 +5,7 @@ ao2mo, mp2) on the (H2O)_32 RHF/STO-3G precision workload.
 One step = one complete solve of the molecule: one-electron integrals, the
 full two-electron integral array on the device, DIIS-accelerated FP64 SCF to a
 1e-10 RMS density change, then the (ia|jb) transform and the MP2 pair sum
-(split hi+lo BF16 tensor-core transform when built, else FP64).  The plain
+(split hi+mid+lo BF16 tensor-core transform, else FP64).  The plain
 FP64 path (core-Hamiltonian Roothaan iterations like the reference, FP64
 transform) is timed beside it.
 
@@ -100,13 +100,13 @@ def solve(ctx, sysm, basis, fast: bool, set_system: bool):
     FP64 transform.  Both start from the core Hamiltonian and use DIIS(8)
     (plain Roothaan iterations, the reference's scheme, oscillate without
     converging on this cluster)."""
-    from myqc_gb300 import MODE_TIGHT, PREC_FP64, PREC_SPLIT_FP16
+    from myqc_gb300 import MODE_TIGHT, PREC_FP64, PREC_SPLIT_BF16X3
     if set_system:
         ctx.set_system(sysm, basis, None, MODE_TIGHT)
     S, H = ctx.int1e()
     ctx.eri_store()
     res = ctx.scf(S, H, sysm.nelcA, sysm.nelcB, conv=1e-10, conv_rms=True, diis=8, max_iter=200)
-    prec = PREC_SPLIT_FP16 if fast and split_available(ctx) else PREC_FP64
+    prec = PREC_SPLIT_BF16X3 if fast and split_available(ctx) else PREC_FP64
     mp2 = ctx.mp2_rhf(res.eig, sysm.nelcA, prec, C=res.C)
     return res, mp2, prec
 
@@ -117,11 +117,11 @@ _split_ok = None
 def split_available(ctx) -> bool:
     global _split_ok
     if _split_ok is None:
-        from myqc_gb300 import PREC_SPLIT_FP16, MyQCError
+        from myqc_gb300 import PREC_SPLIT_BF16X3, MyQCError
         try:
             n = ctx.n
             C = np.eye(n)[:, :4]
-            ctx.ao2mo_iajb(C[:, :2], C[:, 2:], C[:, :2], C[:, 2:], PREC_SPLIT_FP16, copy_out=False)
+            ctx.ao2mo_iajb(C[:, :2], C[:, 2:], C[:, :2], C[:, 2:], PREC_SPLIT_BF16X3, copy_out=False)
             _split_ok = True
         except MyQCError:
             _split_ok = False
@@ -236,12 +236,12 @@ def run_ours(args):
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f64" if prec == 0 else "f64+fp16x2",
+        "dtype": "f64" if prec == 0 else "f64+bf16x3",
         "data": "synthetic: seeded (H2O)32 cluster, rigid monomers, PCG64 seed %d" % args.seed,
         "config": {"workload": WORKLOAD, "molecule": "(H2O)32", "n_basis": n, "n_occ": sysm.nelcA,
                    "n_vir": n - sysm.nelcA, "box_angstrom": BOX, "seed": args.seed, "basis": "STO-3G",
                    "boys": "tight FP64 table", "scf": "DIIS(8), conv 1e-10 RMS dD",
-                   "mp2_precision": "split hi+lo fp16 (tcgen05), fp32 accumulate" if prec else "fp64",
+                   "mp2_precision": "split hi+mid+lo bf16 (tcgen05), fp32 accumulate" if prec else "fp64",
                    "l2": "inputs larger than L2: the 20 GB integral array is rebuilt and streamed every step",
                    "parallelism": f"replicas x{world}"},
         "e2e": {"value": world * 1000.0 / ms_e2e, "unit": "solves/s", "h2d_bytes_per_step": int(h2d),

@@ -131,11 +131,11 @@ int mq_scf(mq_ctx *ctx, const double *S, const double *H, const mq_scf_opts *opt
 
 /* Precision of the four-index transform */
 #define MQ_PREC_FP64 0      /* plain FP64 GEMMs */
-#define MQ_PREC_SPLIT_BF16 1 /* hi+lo BF16 operands on tcgen05 tensor cores,
-                                FP32 accumulation (~16-bit operands) */
-#define MQ_PREC_SPLIT_FP16 2 /* hi+lo FP16 operands (~22-bit), exact power-of-two
-                                scaling from Schwarz and column-norm bounds,
-                                FP32 accumulation */
+#define MQ_PREC_SPLIT_BF16 1   /* hi+lo BF16 operands on tcgen05 tensor cores,
+                                  3 MMAs per K step, FP32 accumulation
+                                  (~16-bit operands) */
+#define MQ_PREC_SPLIT_BF16X3 2 /* hi+mid+lo BF16 operands, 6 MMAs per K step,
+                                  FP32 accumulation (~24-bit operands) */
 
 /* (ia|jb) block, Om(i,a,j,b) with i fastest (ao2mo.f90:465-602 and the
  * idx1..idx4_trans quarter transforms :1306-1439).  Ci: n x no1, Ca: n x nv1,

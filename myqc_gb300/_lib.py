@@ -18,7 +18,7 @@ HEADER = os.path.join(HERE, "..", "include", "myqc.h")
 
 MQ_OK, MQ_EINVAL, MQ_ENOMEM, MQ_ECUDA, MQ_ETIMEOUT, MQ_ENOCONV, MQ_ESTATE = range(7)
 MODE_REFERENCE, MODE_TIGHT = 0, 1
-PREC_FP64, PREC_SPLIT_BF16, PREC_SPLIT_FP16 = 0, 1, 2
+PREC_FP64, PREC_SPLIT_BF16, PREC_SPLIT_BF16X3 = 0, 1, 2
 _NAMES = {0: "MQ_OK", 1: "MQ_EINVAL", 2: "MQ_ENOMEM", 3: "MQ_ECUDA", 4: "MQ_ETIMEOUT", 5: "MQ_ENOCONV",
           6: "MQ_ESTATE"}
 

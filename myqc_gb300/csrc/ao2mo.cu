@@ -25,7 +25,7 @@ int ao2mo_device(mq_ctx *c, const double *Ci, int no1, const double *Ca, int nv1
   if (!c->d_XX) return set_err(c, MQ_ESTATE, "no integrals on the device");
   if (no1 == 0 || nv1 == 0 || no2 == 0 || nv2 == 0) return MQ_OK;  // empty block (e.g. no beta electrons)
   if (precision != MQ_PREC_FP64)
-    return ao2mo_split_device(c, Ci, no1, Ca, nv1, Cj, no2, Cb, nv2, d_out, precision == MQ_PREC_SPLIT_FP16);
+    return ao2mo_split_device(c, Ci, no1, Ca, nv1, Cj, no2, Cb, nv2, d_out, precision == MQ_PREC_SPLIT_BF16X3 ? 3 : 2);
   const size_t y1 = (size_t)(n * n * n) * nv2, y2 = (size_t)(n * n) * no2 * nv2, y3 = (size_t)n * nv1 * no2 * nv2;
   double *Y1 = (double *)buf(c, "ao2mo_y1", sizeof(double) * std::max(y1, y3));
   double *Y2 = (double *)buf(c, "ao2mo_y2", sizeof(double) * y2);

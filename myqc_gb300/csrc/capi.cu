@@ -306,7 +306,7 @@ int mq_ao2mo_iajb(mq_ctx *c, const double *Ci, int no1, const double *Ca, int nv
   MQ_TRY(need_system(c));
   if (!Ci || !Ca || !Cj || !Cb || no1 < 0 || nv1 < 0 || no2 < 0 || nv2 < 0)
     return set_err(c, MQ_EINVAL, "bad ao2mo arguments");
-  if (precision < MQ_PREC_FP64 || precision > MQ_PREC_SPLIT_FP16) return set_err(c, MQ_EINVAL, "bad precision");
+  if (precision < MQ_PREC_FP64 || precision > MQ_PREC_SPLIT_BF16X3) return set_err(c, MQ_EINVAL, "bad precision");
   cudaSetDevice(c->device);
   const size_t n = c->nao;
   // pack all four coefficient blocks into one buffer

@@ -172,9 +172,9 @@ int mp2_rhf_device(mq_ctx *c, const double *d_iajb, const double *d_eig, int noc
 // d_e1/d_e2: orbital energies of the (i,a) and (j,b) spins, occupied first
 int mp2_pair_sums(mq_ctx *c, const double *d_Om, int no1, int nv1, int no2, int nv2, const double *d_e1,
                   const double *d_e2, int same_spin, double *sums);
-// ao2mo_split.cu: hi+lo 16-bit tensor-core transform (tcgen05); fp16 = 1 FP16 operands, 0 BF16
+// ao2mo_split.cu: split-BF16 tensor-core transform (tcgen05) with 2 or 3 operand planes
 int ao2mo_split_device(mq_ctx *c, const double *d_Ci, int no1, const double *d_Ca, int nv1, const double *d_Cj,
-                       int no2, const double *d_Cb, int nv2, double *d_out, int fp16);
+                       int no2, const double *d_Cb, int nv2, double *d_out, int planes);
 
 // scf.cu
 int scf_device(mq_ctx *c, const double *S, const double *H, const mq_scf_opts *o, double *C, double *eps, double *D,

@@ -1,6 +1,6 @@
-"""Smallest split-transform case (CO2, FP16 hi+lo) with per-stage stream checks.
+"""Smallest split-transform case (CO2) with per-stage stream checks.
 
-    MYQC_SYNC_CHECK=1 python tests/diag_split_case.py [fp16|bf16]
+    MYQC_SYNC_CHECK=1 python tests/diag_split_case.py [bf16|bf16x3]
 
 Prints the failing stage, if any.  A diagnostic, not collected by pytest."""
 import os
@@ -9,11 +9,11 @@ import sys
 sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
 import numpy as np  # noqa: E402
 
-from myqc_gb300 import MODE_TIGHT, PREC_FP64, PREC_SPLIT_BF16, PREC_SPLIT_FP16, formats  # noqa: E402
+from myqc_gb300 import MODE_TIGHT, PREC_FP64, PREC_SPLIT_BF16, PREC_SPLIT_BF16X3, formats  # noqa: E402
 from myqc_gb300.session import Context  # noqa: E402
 
 g = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-prec = PREC_SPLIT_BF16 if len(sys.argv) > 1 and sys.argv[1] == "bf16" else PREC_SPLIT_FP16
+prec = PREC_SPLIT_BF16X3 if len(sys.argv) > 1 and sys.argv[1] == "bf16x3" else PREC_SPLIT_BF16
 s = formats.parse_zmat_text(open(os.path.join(g, "zmat", "CO2.ZMAT")).read())
 b = formats.parse_mybasis_text(open(os.path.join(g, "mybasis")).read(), s.atoms)
 ctx = Context(0)

@@ -1,33 +1,33 @@
-"""Split hi+lo BF16 tensor-core transform (tcgen05) against the FP64 path.
+"""Split-BF16 tensor-core transform (tcgen05) against the FP64 path.
 
-(ia|jb) from the split path carries ~2^-16 relative operand rounding; the MP2
-energy error it causes must stay below 1 uEh (the precision target), and the
-transform itself within 5e-4 of the largest |(ia|jb)|."""
+hi+lo BF16 operands (~16-bit) leave a few uEh in the MP2 energy because the
+transform's sums cancel strongly; hi+mid+lo operands (~24-bit) meet the 1 uEh
+target.  Each mode is checked to its own bound, on the transform (relative to
+the largest |(ia|jb)|) and on E(MBPT2)."""
 import numpy as np
 import pytest
 
 from conftest import golden
-from myqc_gb300 import MODE_TIGHT, PREC_FP64, PREC_SPLIT_BF16, PREC_SPLIT_FP16, formats, molecules
+from myqc_gb300 import MODE_TIGHT, PREC_FP64, PREC_SPLIT_BF16, PREC_SPLIT_BF16X3, formats, molecules
 
 pytestmark = pytest.mark.gpu
 
+MODES = [(PREC_SPLIT_BF16, 5e-4, 5e-6), (PREC_SPLIT_BF16X3, 1e-6, 1e-7)]
 
-def _systems(basis_text):
+
+def _systems():
     out = []
     for name in ("CO2", "HF", "NO"):
-        s = formats.parse_zmat_text(open(golden("zmat", name + ".ZMAT")).read())
-        out.append((name, s))
+        out.append((name, formats.parse_zmat_text(open(golden("zmat", name + ".ZMAT")).read())))
     for nm in (2, 4):
         out.append((f"(H2O){nm}", molecules.water_cluster_system(nm, (27.0 * nm) ** (1 / 3) + 1.0, 7)))
     return out
 
 
-@pytest.mark.parametrize("prec,tol_rel,tol_mp2", [(PREC_SPLIT_FP16, 2e-5, 1e-6), (PREC_SPLIT_BF16, 5e-4, 5e-6)])
+@pytest.mark.parametrize("prec,tol_rel,tol_mp2", MODES)
 @pytest.mark.parametrize("idx", range(5))
 def test_split_transform_matches_fp64(ctx, basis_text, idx, prec, tol_rel, tol_mp2):
-    """FP16 hi+lo (22-bit operands) meets the 1 uEh MP2 target; BF16 hi+lo
-    (16-bit operands) is kept as an option and checked to its own bound."""
-    name, sysm = _systems(basis_text)[idx]
+    name, sysm = _systems()[idx]
     basis = formats.parse_mybasis_text(basis_text, sysm.atoms)
     ctx.set_system(sysm, basis, None, MODE_TIGHT)
     S, H = ctx.int1e()
@@ -38,8 +38,7 @@ def test_split_transform_matches_fp64(ctx, basis_text, idx, prec, tol_rel, tol_m
     blocks = (C[:, :no], C[:, no:], C[:, :no], C[:, no:])
     ref = ctx.ao2mo_iajb(*blocks, PREC_FP64)
     got = ctx.ao2mo_iajb(*blocks, prec)
-    scale = np.max(np.abs(ref))
-    assert np.max(np.abs(got - ref)) < tol_rel * scale
+    assert np.max(np.abs(got - ref)) < tol_rel * np.max(np.abs(ref))
     if sysm.uhf:
         e64 = ctx.mp2_uhf(res.C[0], res.C[1], res.eig[0], res.eig[1], sysm.nelcA, sysm.nelcB, PREC_FP64)
         e16 = ctx.mp2_uhf(res.C[0], res.C[1], res.eig[0], res.eig[1], sysm.nelcA, sysm.nelcB, prec)
@@ -59,6 +58,6 @@ def test_split_rectangular_blocks(ctx, basis_text):
     rng = np.random.default_rng(5)
     Ci, Ca, Cj, Cb = (rng.standard_normal((n, k)) * 0.3 for k in (3, 7, 5, 2))
     ref = ctx.ao2mo_iajb(Ci, Ca, Cj, Cb, PREC_FP64)
-    for prec, tol in ((PREC_SPLIT_BF16, 5e-4), (PREC_SPLIT_FP16, 2e-5)):
+    for prec, tol, _ in MODES:
         got = ctx.ao2mo_iajb(Ci, Ca, Cj, Cb, prec)
         assert np.max(np.abs(got - ref)) < tol * np.max(np.abs(ref))
