@@ -2,13 +2,12 @@
 // BF16 operands and FP32 accumulation (the precision option of the four-index
 // transform that src/ao2mo/ao2mo.f90:1306-1439 does in FP64).
 //
-// Each FP64/FP32 operand x is stored as P BF16 planes (x ~ hi + lo, or
-// hi + mid + lo), each plane the BF16 rounding of what the previous ones left;
-// the products of plane pairs above the FP32 accumulator's resolution are
-// accumulated (3 MMAs per K step for P = 2, 6 for P = 3).
+// Each operand row is scaled by a power of two and cut into S integer slices
+// that BF16 holds exactly (S = 2: hi+lo, S = 3: hi+mid+lo); slice products
+// are accumulated exactly in FP32 TMEM (see "kernels" below).
 //
 // One GEMM kernel serves all four quarter transforms:
-//     D[m][n] = sum_k A[m][k] * B[n][k]      (A, B K-major BF16 planes)
+//     D[m][n] = sum_k A[m][k] * B[n][k]      (A, B K-major BF16 slices)
 // TMA (cp.async.bulk.tensor, 128-byte swizzle) stages 128 x 64 A tiles and
 // N x 64 B tiles through a ring of shared-memory stages; one thread issues
 // tcgen05.mma (M = 128, K = 16, N = the whole output width) into a TMEM
@@ -136,61 +135,68 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
 }
 
 // ------------------------------------------------------------------ kernels
-// An operand is stored as P BF16 planes (P = 2: hi, lo; P = 3: hi, mid, lo),
-// x ~ sum of planes.  The products accumulated per K step are all plane pairs
-// whose combined weight is above the FP32 accumulator's resolution:
-//   P = 2: hh, hl, lh          (~16-bit operands)
-//   P = 3: hh, hm, mh, hl, mm, lh   (~24-bit operands)
-template <int P>
-struct PlaneProducts;
+// Operands are cut into S exact BF16 slices with one power-of-two scale per
+// row (per row of A over K, per row of B over K):
+//     x = 2^(e - 8S + 1) * (s0 * 2^(8(S-1)) + ... + s_{S-1}),   s_k integers, |s_k| <= 128
+// Each slice is an integer that BF16 holds exactly, so a slice product is an
+// integer below 2^14 and, for one output element and one slice pair, every
+// partial sum over K is an integer too.  Products are grouped by level
+// L = k + l (L < S) into S TMEM accumulators; with at most 3 pairs per level
+// and K <= 340, every partial sum stays below 2^24 and the FP32 accumulation
+// is exact in any order and rounding mode.  Only the slicing itself rounds
+// (to nearest, unbiased), at 2^-8S of the row maximum.  Levels >= S (pairs
+// of weight below 2^-8S) are not formed.
+//   S = 2: levels {00}, {01,10}                 3 MMAs per K step (~16-bit)
+//   S = 3: levels {00}, {01,10}, {02,11,20}     6 MMAs per K step (~24-bit)
+constexpr int SLICE_KMAX = 340;  // 3 * 340 * 128^2 < 2^24
+
+template <int S>
+struct Levels;
 template <>
-struct PlaneProducts<2> {
+struct Levels<2> {
   static constexpr int n = 3;
   __device__ static constexpr int a(int i) { return i == 2 ? 1 : 0; }
   __device__ static constexpr int b(int i) { return i == 1 ? 1 : 0; }
+  __device__ static constexpr int lev(int i) { return i == 0 ? 0 : 1; }
 };
 template <>
-struct PlaneProducts<3> {
+struct Levels<3> {
   static constexpr int n = 6;
-  __device__ static constexpr int a(int i) { return i == 0 ? 0 : i == 1 ? 0 : i == 2 ? 1 : i == 3 ? 0 : i == 4 ? 1 : 2; }
+  __device__ static constexpr int a(int i) { return i < 2 ? 0 : i == 2 ? 1 : i == 3 ? 0 : i == 4 ? 1 : 2; }
   __device__ static constexpr int b(int i) { return i == 0 ? 0 : i == 1 ? 1 : i == 2 ? 0 : i == 3 ? 2 : i == 4 ? 1 : 0; }
+  __device__ static constexpr int lev(int i) { return i == 0 ? 0 : i < 3 ? 1 : 2; }
 };
 
 struct GemmArgs {
   int M, N, K, batch;       // logical sizes (K is the padded K)
   int ntile;                // N rounded up to a multiple of 16
-  int tmem_cols;            // power of two >= ntile
-  int out_f64;              // 1: FP64 output; 0: split BF16 output (P planes)
+  int tmem_cols;            // power of two >= S * ntile
+  int out_f64;              // 1: FP64 output; 0: FP32 output
   long long mdiv, s_m0, s_m1, s_n, s_b;  // out index = (m%mdiv)*s_m0 + (m/mdiv)*s_m1 + n*s_n + batch*s_b
-  long long out_plane;      // elements between output planes
-  double *out;
-  bf16 *out16;
+  const int *eA;            // row exponents of A, [batch][M]
+  const int *eB;            // row exponents of B, [N]
+  double *out64;
+  float *out32;
   int *err;
 };
-
-// x ~ p[0] + p[1] (+ p[2]) in BF16, each part the rounding of the remainder
-template <int P>
-__device__ __forceinline__ void split_planes(float x, bf16 (&p)[P]) {
-#pragma unroll
-  for (int k = 0; k < P; ++k) {
-    p[k] = __float2bfloat16_rn(x);
-    x = x - __bfloat162float(p[k]);
-  }
-}
 
 struct Maps {
   CUtensorMap a[3];
   CUtensorMap b[3];
 };
 
-template <int P, int STAGES>
-__global__ void __launch_bounds__(GEMM_THREADS, 1) split_gemm_kernel(const __grid_constant__ Maps maps, GemmArgs g) {
+__device__ __forceinline__ float pow2f(int e) {  // 2^e for e in the FP32 normal range, 0 below
+  return e < -126 ? 0.0f : __int_as_float((min(e, 127) + 127) << 23);
+}
+
+template <int S, int STAGES>
+__global__ void __launch_bounds__(GEMM_THREADS, 1) slice_gemm_kernel(const __grid_constant__ Maps maps, GemmArgs g) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   // 1024-byte aligned base for the swizzled tiles
   uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   const int ntile = g.ntile;
   const uint32_t a_bytes = UM * UK * 2, b_bytes = (uint32_t)ntile * UK * 2;
-  const uint32_t stage_bytes = P * (a_bytes + b_bytes);
+  const uint32_t stage_bytes = S * (a_bytes + b_bytes);
   uint64_t *full = (uint64_t *)(smem + STAGES * stage_bytes);
   uint64_t *empty = full + STAGES;
   uint64_t *acc_full = empty + STAGES;
@@ -237,9 +243,9 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) split_gemm_kernel(const __gri
           uint8_t *st = smem + s * stage_bytes;
           mbar_expect_tx(full + s, stage_bytes);
 #pragma unroll
-          for (int pl = 0; pl < P; ++pl) {
+          for (int pl = 0; pl < S; ++pl) {
             tma_load_3d(st + pl * a_bytes, &maps.a[pl], full + s, kc * UK, mt * UM, bt);
-            tma_load_3d(st + P * a_bytes + pl * b_bytes, &maps.b[pl], full + s, kc * UK, 0, 0);
+            tma_load_3d(st + S * a_bytes + pl * b_bytes, &maps.b[pl], full + s, kc * UK, 0, 0);
           }
           armed |= 1u << s;
           armed_par = (armed_par & ~(1u << s)) | ((ph ^ 1u) << s);  // the consumer waits on parity ph^1
@@ -279,10 +285,13 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) split_gemm_kernel(const __gri
           for (int kk = 0; kk < UK / 16; ++kk) {
             const uint32_t off = kk * 32;  // 16 BF16 = 32 bytes along the swizzled row
 #pragma unroll
-            for (int pr = 0; pr < PlaneProducts<P>::n; ++pr) {
-              const uint64_t ad = sdesc(base + PlaneProducts<P>::a(pr) * a_bytes + off);
-              const uint64_t bd = sdesc(base + P * a_bytes + PlaneProducts<P>::b(pr) * b_bytes + off);
-              umma(tmem, ad, bd, idesc, (kc | kk | pr) != 0);
+            for (int pr = 0; pr < Levels<S>::n; ++pr) {
+              const int L = Levels<S>::lev(pr);
+              const uint64_t ad = sdesc(base + Levels<S>::a(pr) * a_bytes + off);
+              const uint64_t bd = sdesc(base + S * a_bytes + Levels<S>::b(pr) * b_bytes + off);
+              // the first product of each level in a tile overwrites its accumulator
+              const bool first = kc == 0 && kk == 0 && (pr == 0 || Levels<S>::lev(pr - 1) != L);
+              umma(tmem + (uint32_t)(L * ntile), ad, bd, idesc, first ? 0u : 1u);
             }
           }
           umma_commit(empty + s);  // stage free once these MMAs have read it
@@ -314,23 +323,24 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) split_gemm_kernel(const __gri
       const long long m = (long long)mt * UM + row;
       const bool live = m < g.M;
       const long long base = live ? (m % g.mdiv) * g.s_m0 + (m / g.mdiv) * g.s_m1 + (long long)bt * g.s_b : 0;
+      const int ea = live ? g.eA[(long long)bt * g.M + m] : 0;
       for (int c0 = 0; c0 < ntile; c0 += 16) {
-        float v[16];
-        tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c0, v);
+        float v[S][16];
+#pragma unroll
+        for (int L = 0; L < S; ++L) tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(L * ntile + c0), v[L]);
         if (!live) continue;
 #pragma unroll
         for (int i = 0; i < 16; ++i) {
           const int n = c0 + i;
           if (n >= g.N) break;
-          const long long o = base + (long long)n * g.s_n;
-          if (g.out_f64) {
-            g.out[o] = (double)v[i];
-          } else {
-            bf16 p[P];
-            split_planes<P>(v[i], p);
+          // exact integer levels combined once, rounding to nearest
+          float x = v[S - 1][i];
 #pragma unroll
-            for (int k = 0; k < P; ++k) g.out16[o + k * g.out_plane] = p[k];
-          }
+          for (int L = S - 2; L >= 0; --L) x = fmaf(x, 0.00390625f, v[L][i]);
+          x *= pow2f(ea + g.eB[n] - 14);
+          const long long o = base + (long long)n * g.s_n;
+          if (g.out_f64) g.out64[o] = (double)x;
+          else g.out32[o] = x;
         }
       }
       tc_fence_before();
@@ -347,31 +357,79 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) split_gemm_kernel(const __gri
   }
 }
 
-// FP64 -> FP32 without FP64 arithmetic: exponent rebias and the top 23 mantissa
-// bits with integer operations (values below the FP32 normal range become 0).
-__device__ __forceinline__ float f64_to_f32_bits(double x) {
+// Row exponent and fixed-point digits with integer operations only.
+// A value |x| < 2^e becomes q = round(x * 2^(8S-1-e)), |q| < 2^(8S-1), split in
+// balanced base-256 digits s_0 .. s_{S-1} (|s_0| <= 128, others in [-128, 127]).
+__device__ __forceinline__ int exp_field(double x) {
+  return (int)((unsigned long long)__double_as_longlong(x) >> 52) & 0x7ff;
+}
+__device__ __forceinline__ int exp_field(float x) { return (__float_as_int(x) >> 23) & 0xff; }
+// value = mant * 2^(ex) with mant the full integer significand (implicit bit set)
+__device__ __forceinline__ void decompose(double x, long long &mant, int &ex) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-  const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
-  const int e = (int)((hi >> 20) & 0x7ff) - 1023 + 127;
-  if (e <= 0) return 0.0f;
-  if (e >= 255) return __uint_as_float((hi & 0x80000000u) | 0x7f800000u);
-  const unsigned m = ((hi & 0xfffffu) << 3) | (lo >> 29);
-  return __uint_as_float((hi & 0x80000000u) | ((unsigned)e << 23) | m);
+  const int E = (int)(b >> 52) & 0x7ff;
+  if (E == 0) {  // zero (subnormals are far below any slice)
+    mant = 0;
+    ex = 0;
+    return;
+  }
+  mant = (long long)((b & 0xfffffffffffffull) | 0x10000000000000ull);
+  if (b >> 63) mant = -mant;
+  ex = E - 1075;
+}
+__device__ __forceinline__ void decompose(float x, long long &mant, int &ex) {
+  const unsigned b = (unsigned)__float_as_int(x);
+  const int E = (int)(b >> 23) & 0xff;
+  if (E == 0) {
+    mant = 0;
+    ex = 0;
+    return;
+  }
+  mant = (long long)((b & 0x7fffffu) | 0x800000u);
+  if (b >> 31) mant = -mant;
+  ex = E - 150;
 }
 
-// plane k of out holds part k of in[k' + ld*r] at r*Kp + k' (zero for kvalid <= k' < Kp)
-template <int P>
-__global__ void split_rows_kernel(const double *__restrict__ in, long long rows, int kvalid, long long ld, int Kp,
-                                  long long plane, bf16 *__restrict__ out) {
-  const long long tot = rows * Kp;
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < tot; i += (long long)gridDim.x * blockDim.x) {
-    const long long r = i / Kp;
-    const int k = (int)(i - r * Kp);
-    const float x = k < kvalid ? f64_to_f32_bits(__ldcs(in + k + ld * r)) : 0.0f;
-    bf16 p[P];
-    split_planes<P>(x, p);
+// one warp per row: r-th row at in + r*ld (kvalid values), slices to planes of
+// `plane` elements at out + r*Kp, row exponent to e[r]
+template <int S, class T>
+__global__ void slice_rows_kernel(const T *__restrict__ in, long long rows, int kvalid, long long ld, int Kp,
+                                  long long plane, bf16 *__restrict__ out, int *__restrict__ e) {
+  const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
+  const int lane = threadIdx.x & 31;
+  for (long long r = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); r < rows; r += warps) {
+    const T *x = in + r * ld;
+    int emax = 0;
+    for (int k = lane; k < kvalid; k += 32) emax = max(emax, exp_field(x[k]));
 #pragma unroll
-    for (int q = 0; q < P; ++q) out[i + q * plane] = p[q];
+    for (int o = 16; o > 0; o >>= 1) emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o));
+    // |x| < 2^erow with erow = unbiased exponent of the largest element + 1
+    const int erow = emax == 0 ? -200 : emax - (sizeof(T) == 8 ? 1022 : 126);
+    if (lane == 0) e[r] = erow;
+    for (int k = lane; k < Kp; k += 32) {
+      long long q = 0;
+      if (k < kvalid) {
+        long long mant;
+        int ex;
+        decompose(x[k], mant, ex);
+        // q = round(mant * 2^(ex + 8S - 1 - erow)); the shift is negative for every nonzero x
+        const int sh = -(ex + 8 * S - 1 - erow);
+        if (mant != 0 && sh < 62) {
+          const long long half = sh > 0 ? (1ll << (sh - 1)) : 0;
+          q = sh > 0 ? ((mant + half) >> sh) : (mant << -sh);
+        }
+      }
+      float dig[S];
+#pragma unroll
+      for (int d = S - 1; d > 0; --d) {
+        const long long hi = (q + 128) >> 8;  // balanced digit: q = hi*256 + lo, lo in [-128, 127]
+        dig[d] = (float)(q - hi * 256);
+        q = hi;
+      }
+      dig[0] = (float)q;
+#pragma unroll
+      for (int d = 0; d < S; ++d) out[d * plane + r * Kp + k] = __float2bfloat16_rn(dig[d]);
+    }
   }
 }
 
@@ -408,21 +466,22 @@ static int make_map(mq_ctx *c, CUtensorMap *m, const bf16 *ptr, int Kp, long lon
   return MQ_OK;
 }
 
-// a split operand: P planes of `plane` elements each, starting at `base`
-struct SplitOperand {
+// a sliced operand: S planes of `plane` elements from `base`, row exponents `e`
+struct Sliced {
   bf16 *base;
   long long plane;
+  int *e;
 };
 
-template <int P>
-static int split_gemm(mq_ctx *c, SplitOperand A, long long M, int batch, long long a_batch_stride, SplitOperand B,
-                      int N, int Kp, GemmArgs g) {
+template <int S>
+static int slice_gemm(mq_ctx *c, Sliced A, long long M, int batch, long long a_batch_stride, Sliced B, int N, int Kp,
+                      GemmArgs g) {
   if (N <= 0 || M <= 0 || batch <= 0) return MQ_OK;
   if (N > 256) return set_err(c, MQ_EINVAL, "split GEMM: N > 256");
   if (M > 2147483647LL) return set_err(c, MQ_EINVAL, "split GEMM: M too large");
   Maps maps;
   const int ntile = (N + 15) / 16 * 16;
-  for (int p = 0; p < P; ++p) {
+  for (int p = 0; p < S; ++p) {
     MQ_TRY(make_map(c, &maps.a[p], A.base + p * A.plane, Kp, M, batch, a_batch_stride, UM));
     MQ_TRY(make_map(c, &maps.b[p], B.base + p * B.plane, Kp, N, 1, 0, ntile));
   }
@@ -431,105 +490,116 @@ static int split_gemm(mq_ctx *c, SplitOperand A, long long M, int batch, long lo
   g.K = Kp;
   g.batch = batch;
   g.ntile = ntile;
+  g.eA = A.e;
+  g.eB = B.e;
   int cols = 32;
-  while (cols < ntile) cols <<= 1;
+  while (cols < S * ntile) cols <<= 1;
+  if (cols > 512) return set_err(c, MQ_EINVAL, "split GEMM: accumulators exceed TMEM");
   g.tmem_cols = cols;
-  const size_t stage = (size_t)P * ((size_t)UM * UK * 2 + (size_t)ntile * UK * 2);
+  const size_t stage = (size_t)S * ((size_t)UM * UK * 2 + (size_t)ntile * UK * 2);
   const size_t limit = 227 * 1024 - 1024 - 256;
-  const int stages = limit >= 4 * stage ? 4 : (limit >= 3 * stage ? 3 : 2);
   if (limit < 2 * stage) return set_err(c, MQ_EINVAL, "split GEMM: shared memory");
+  const int stages = limit >= 4 * stage ? 4 : (limit >= 3 * stage ? 3 : 2);
   const size_t smem = stages * stage + 1024 + 256;
   int sms = 148;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
   const long long tiles = (M + UM - 1) / UM * batch;
   const int grid = (int)std::min<long long>(tiles, sms);
-  auto kern = stages == 4 ? split_gemm_kernel<P, 4> : (stages == 3 ? split_gemm_kernel<P, 3> : split_gemm_kernel<P, 2>);
+  auto kern = stages == 4 ? slice_gemm_kernel<S, 4> : (stages == 3 ? slice_gemm_kernel<S, 3> : slice_gemm_kernel<S, 2>);
   MQ_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   kern<<<grid, GEMM_THREADS, smem, c->stream>>>(maps, g);
   c->stats.launches += 1;
   MQ_CUDA(c, cudaGetLastError());
-  return sync_check(c, "split_gemm");
+  return sync_check(c, "slice_gemm");
 }
 
-template <int P>
-static int split_rows(mq_ctx *c, const double *in, long long rows, int kvalid, long long ld, int Kp, SplitOperand o) {
-  const long long tot = rows * Kp;
+template <int S, class T>
+static int slice_rows(mq_ctx *c, const T *in, long long rows, int kvalid, long long ld, int Kp, Sliced o) {
   const int tb = 256;
-  const long long blocks = std::max<long long>(1, std::min<long long>((tot + tb - 1) / tb, 1 << 20));
-  split_rows_kernel<P><<<(unsigned)blocks, tb, 0, c->stream>>>(in, rows, kvalid, ld, Kp, o.plane, o.base);
+  const long long blocks = std::max<long long>(1, std::min<long long>((rows + 7) / 8, 1 << 20));
+  slice_rows_kernel<S, T><<<(unsigned)blocks, tb, 0, c->stream>>>(in, rows, kvalid, ld, Kp, o.plane, o.base, o.e);
   c->stats.launches += 1;
   MQ_CUDA(c, cudaGetLastError());
-  return sync_check(c, "split_rows");
+  return sync_check(c, "slice_rows");
 }
 
-template <int P>
-static int ao2mo_split_planes(mq_ctx *c, const double *Ci, int no1, const double *Ca, int nv1, const double *Cj,
-                              int no2, const double *Cb, int nv2, double *d_out) {
+template <int S>
+static int ao2mo_slices(mq_ctx *c, const double *Ci, int no1, const double *Ca, int nv1, const double *Cj, int no2,
+                        const double *Cb, int nv2, double *d_out) {
   const long long n = c->nao;
   const int Kp = (int)((n + 7) / 8 * 8);
   if (no1 > 256 || nv1 > 256 || no2 > 256 || nv2 > 256)
     return set_err(c, MQ_EINVAL, "split transform: orbital blocks above 256 are not supported");
+  if (Kp > SLICE_KMAX) return set_err(c, MQ_EINVAL, "split transform: more than 340 basis functions");
   const long long n2 = n * n, n3 = n2 * n;
-  // plane sizes (BF16 elements)
-  const long long eX = n3 * Kp, e1 = (long long)nv2 * n2 * Kp, e2 = (long long)no2 * nv2 * n * Kp,
-                  e3 = (long long)nv1 * no2 * nv2 * Kp;
-  const long long eC[4] = {(long long)no1 * Kp, (long long)nv1 * Kp, (long long)no2 * Kp, (long long)nv2 * Kp};
-  bf16 *bx = (bf16 *)buf(c, "split_xx", P * eX * sizeof(bf16));
-  bf16 *b1 = (bf16 *)buf(c, "split_y1", P * std::max(e1, e3) * sizeof(bf16));
-  bf16 *b2 = (bf16 *)buf(c, "split_y2", P * e2 * sizeof(bf16));
-  bf16 *bc = (bf16 *)buf(c, "split_c", P * (eC[0] + eC[1] + eC[2] + eC[3]) * sizeof(bf16));
+  // A operand rows per step, and the FP32 intermediates [rows][Kp]
+  const long long rX = n3, r1 = (long long)nv2 * n2, r2 = (long long)no2 * nv2 * n, r3 = (long long)nv1 * no2 * nv2;
+  const long long rB = (long long)no1 + nv1 + no2 + nv2;
+  const long long rmax = std::max(std::max(rX, r1), std::max(r2, r3));
+  bf16 *pa = (bf16 *)buf(c, "slice_a", S * rmax * Kp * sizeof(bf16));
+  int *ea = (int *)buf(c, "slice_ea", rmax * sizeof(int));
+  bf16 *pb = (bf16 *)buf(c, "slice_b", S * rB * Kp * sizeof(bf16));
+  int *eb = (int *)buf(c, "slice_eb", rB * sizeof(int));
+  float *y1 = (float *)buf(c, "slice_y1", std::max(r1, r3) * Kp * sizeof(float));
+  float *y2 = (float *)buf(c, "slice_y2", r2 * Kp * sizeof(float));
   int *err = (int *)buf(c, "split_err", 64);
-  if (!bx || !b1 || !b2 || !bc || !err) return MQ_ENOMEM;
+  if (!pa || !ea || !pb || !eb || !y1 || !y2 || !err) return MQ_ENOMEM;
   MQ_CUDA(c, cudaMemsetAsync(err, 0, sizeof(int), c->stream));
-  SplitOperand X{bx, eX}, Y1{b1, e1}, Y2{b2, e2}, Y3{b1, e3};  // Y3 reuses Y1's space
-  SplitOperand Bi{bc, eC[0]}, Ba{bc + P * eC[0], eC[1]}, Bj{Ba.base + P * eC[1], eC[2]},
-      Bb{Bj.base + P * eC[2], eC[3]};
+  // the padding columns Kp > n of the intermediates stay zero
+  MQ_CUDA(c, cudaMemsetAsync(y1, 0, std::max(r1, r3) * Kp * sizeof(float), c->stream));
+  MQ_CUDA(c, cudaMemsetAsync(y2, 0, r2 * Kp * sizeof(float), c->stream));
   // coefficient blocks: column p of C (n contiguous) becomes row p of B (K-major)
-  MQ_TRY(split_rows<P>(c, Ci, no1, (int)n, n, Kp, Bi));
-  MQ_TRY(split_rows<P>(c, Ca, nv1, (int)n, n, Kp, Ba));
-  MQ_TRY(split_rows<P>(c, Cj, no2, (int)n, n, Kp, Bj));
-  MQ_TRY(split_rows<P>(c, Cb, nv2, (int)n, n, Kp, Bb));
-  // XX(d,l,u,v) at d + n*((l,u,v)): rows (l,u,v) with K = d
-  MQ_TRY(split_rows<P>(c, c->d_XX, n3, (int)n, n, Kp, X));
+  const long long plB = rB * Kp;
+  Sliced Bi{pb, plB, eb}, Ba{pb + (long long)no1 * Kp, plB, eb + no1};
+  Sliced Bj{Ba.base + (long long)nv1 * Kp, plB, Ba.e + nv1}, Bb{Bj.base + (long long)no2 * Kp, plB, Bj.e + no2};
+  MQ_TRY(slice_rows<S>(c, Ci, no1, (int)n, n, Kp, Bi));
+  MQ_TRY(slice_rows<S>(c, Ca, nv1, (int)n, n, Kp, Ba));
+  MQ_TRY(slice_rows<S>(c, Cj, no2, (int)n, n, Kp, Bj));
+  MQ_TRY(slice_rows<S>(c, Cb, nv2, (int)n, n, Kp, Bb));
   GemmArgs g{};
   g.err = err;
-  // 1: Y1[b][(u,v)][l] = sum_d XX(d,l,u,v) Cb(d,b);   row m = l + n*(u + n*v)
+  // 1: XX(d,l,u,v) at d + n*((l,u,v)): rows (l,u,v), K = d -> Y1[b][(u,v)][l]
+  Sliced A{pa, rX * Kp, ea};
+  MQ_TRY(slice_rows<S>(c, c->d_XX, rX, (int)n, n, Kp, A));
   g.out_f64 = 0;
-  g.out16 = Y1.base;
-  g.out_plane = Y1.plane;
+  g.out32 = y1;
   g.mdiv = n;
   g.s_m0 = 1;
   g.s_m1 = Kp;
   g.s_n = n2 * Kp;
   g.s_b = 0;
-  MQ_TRY(split_gemm<P>(c, X, n3, 1, 0, Bb, nv2, Kp, g));
+  MQ_TRY(slice_gemm<S>(c, A, rX, 1, 0, Bb, nv2, Kp, g));
   // 2: batch b; rows m = u + n*v, K = l -> Y2[j,b][v][u]
-  g.out16 = Y2.base;
-  g.out_plane = Y2.plane;
+  A = Sliced{pa, r1 * Kp, ea};
+  MQ_TRY(slice_rows<S>(c, y1, r1, (int)n, Kp, Kp, A));
+  g.out32 = y2;
   g.mdiv = n;
   g.s_m0 = 1;
   g.s_m1 = Kp;
   g.s_n = n * Kp;
   g.s_b = (long long)no2 * n * Kp;
-  MQ_TRY(split_gemm<P>(c, Y1, n2, nv2, n2 * Kp, Bj, no2, Kp, g));
+  MQ_TRY(slice_gemm<S>(c, A, n2, nv2, n2 * Kp, Bj, no2, Kp, g));
   // 3: batch (j + no2*b); rows v, K = u -> Y3[a + nv1*(j + no2*b)][v]
-  g.out16 = Y3.base;
-  g.out_plane = Y3.plane;
+  A = Sliced{pa, r2 * Kp, ea};
+  MQ_TRY(slice_rows<S>(c, y2, r2, (int)n, Kp, Kp, A));
+  g.out32 = y1;  // Y1 is dead
   g.mdiv = 1ll << 62;
   g.s_m0 = 1;
   g.s_m1 = 0;
   g.s_n = Kp;
   g.s_b = (long long)nv1 * Kp;
-  MQ_TRY(split_gemm<P>(c, Y2, n, no2 * nv2, n * Kp, Ba, nv1, Kp, g));
+  MQ_TRY(slice_gemm<S>(c, A, n, no2 * nv2, n * Kp, Ba, nv1, Kp, g));
   // 4: rows (a, j, b), K = v -> Om(i, a, j, b) = D[m][i] at i + no1*m
+  A = Sliced{pa, r3 * Kp, ea};
+  MQ_TRY(slice_rows<S>(c, y1, r3, (int)n, Kp, Kp, A));
   g.out_f64 = 1;
-  g.out = d_out;
+  g.out64 = d_out;
   g.mdiv = 1ll << 62;
   g.s_m0 = no1;
   g.s_m1 = 0;
   g.s_n = 1;
   g.s_b = 0;
-  MQ_TRY(split_gemm<P>(c, Y3, (long long)nv1 * no2 * nv2, 1, 0, Bi, no1, Kp, g));
+  MQ_TRY(slice_gemm<S>(c, A, r3, 1, 0, Bi, no1, Kp, g));
   int h = 0;
   MQ_CUDA(c, cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   MQ_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -539,8 +609,8 @@ static int ao2mo_split_planes(mq_ctx *c, const double *Ci, int no1, const double
 
 int ao2mo_split_device(mq_ctx *c, const double *Ci, int no1, const double *Ca, int nv1, const double *Cj, int no2,
                        const double *Cb, int nv2, double *d_out, int planes) {
-  if (planes == 3) return ao2mo_split_planes<3>(c, Ci, no1, Ca, nv1, Cj, no2, Cb, nv2, d_out);
-  return ao2mo_split_planes<2>(c, Ci, no1, Ca, nv1, Cj, no2, Cb, nv2, d_out);
+  if (planes == 3) return ao2mo_slices<3>(c, Ci, no1, Ca, nv1, Cj, no2, Cb, nv2, d_out);
+  return ao2mo_slices<2>(c, Ci, no1, Ca, nv1, Cj, no2, Cb, nv2, d_out);
 }
 
 }  // namespace mq
