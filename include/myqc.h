@@ -94,6 +94,26 @@ int mq_eri_upload(mq_ctx *ctx, const double *XX);
  * All matrices n x n column-major host arrays. */
 int mq_fock(mq_ctx *ctx, const double *Da, const double *Db, double *Ga, double *Gb);
 
+/* Allocation-free RHF Fock build.  No counterpart in the reference: it exists
+ * for callers that cannot allocate device memory themselves (device arrays
+ * owned by an OpenACC / OpenMP-offload runtime or a preallocated pool, code
+ * that must not call cudaMalloc while it runs).  All pointers are device
+ * pointers the caller owns: d_XX (n^4 doubles, the XX layout), d_D (n x n
+ * total density), d_G (n x n output, G = J - K/2 as mq_fock computes it).
+ * No context is needed and nothing is allocated or freed: the kernels'
+ * scratch is a fixed 16 MiB array inside the library, held by every GPU that
+ * loads it until the process exits, which limits n to 2 n^2 <= 2097152
+ * doubles (n <= 1024); larger n returns MQ_EINVAL.  The work is queued on
+ * `stream` (NULL: the default stream) and the call returns without waiting;
+ * G is ready once that stream reaches this point.  All calls share the one
+ * scratch array, so calls that overlap on the GPU (other streams, other host
+ * threads) race; serialise them.  The first call on each device looks up the
+ * array's device address (cudaGetSymbolAddress, with that device current);
+ * make that first call before any stream capture.  msg (may be NULL) receives
+ * a message on failure. */
+int mq_fock_rhf_noalloc(int n, const double *d_XX, const double *d_D, double *d_G, void *stream, char *msg,
+                        int msglen);
+
 /* Direct Fock build: integrals recomputed and digested in one kernel, no
  * stored XX (the (H2O)64-scale path).  Same meaning as mq_fock. */
 int mq_fock_direct(mq_ctx *ctx, const double *Da, const double *Db, double *Ga, double *Gb);

@@ -69,6 +69,7 @@ def lib(path: str | None = None):
     L.mq_eri_upload.argtypes = [vp, dp]
     L.mq_fock.argtypes = [vp, dp, dp, dp, dp]
     L.mq_fock_direct.argtypes = [vp, dp, dp, dp, dp]
+    L.mq_fock_rhf_noalloc.argtypes = [c_int, vp, vp, vp, vp, ctypes.c_char_p, c_int]
     L.mq_scf.argtypes = [vp, dp, dp, ctypes.POINTER(ScfOpts), dp, dp, dp, ctypes.POINTER(c_double), ip, dp]
     L.mq_ao2mo_iajb.argtypes = [vp, dp, c_int, dp, c_int, dp, c_int, dp, c_int, c_int, dp]
     L.mq_mp2_rhf.argtypes = [vp, dp, c_int, c_int, dp]

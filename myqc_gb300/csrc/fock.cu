@@ -11,6 +11,10 @@
 // column i of K.  A CTA owns one i and a chunk of j: J_ij is complete inside
 // the CTA, and the chunk's partial K column goes to a scratch slice; a second
 // kernel sums the slices in a fixed order.  No atomics, deterministic.
+#include <algorithm>
+#include <cstring>
+#include <mutex>
+
 #include "internal.h"
 
 namespace mq {
@@ -110,4 +114,71 @@ int fock_stored_device(mq_ctx *c, const double *d_Da, const double *d_Db, double
   return MQ_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Allocation-free RHF Fock build (mq_fock_rhf_noalloc).
+//
+// For callers that may not allocate device memory themselves -- a Fortran or
+// C host whose device arrays are owned by an OpenACC / OpenMP-offload runtime
+// or by a preallocated pool, or code that must not call cudaMalloc while it
+// runs -- the same two kernels as fock_stored_device run on caller-owned
+// device buffers, with their scratch (J and the per-chunk K columns) in the
+// fixed array below instead of a context buffer.  The array is part of the
+// loaded library: every GPU that loads libmyqc holds its 16 MiB until the
+// process exits.  Host code cannot use the array's name as a device address;
+// the first call on each device looks the address up with
+// cudaGetSymbolAddress (with that device current) and keeps it.
+constexpr size_t NOALLOC_SCRATCH_DOUBLES = (size_t)2 << 20;  // 16 MiB
+static __device__ __align__(256) double g_fock_noalloc_scratch[NOALLOC_SCRATCH_DOUBLES];
+constexpr int NOALLOC_MAX_DEVICES = 64;
+static double *g_fock_noalloc_addr[NOALLOC_MAX_DEVICES];
+static std::mutex g_fock_noalloc_mu;
+
+static int noalloc_fail(char *msg, int len, int code, const char *what) {
+  if (msg && len > 0) {
+    strncpy(msg, what, len - 1);
+    msg[len - 1] = 0;
+  }
+  return code;
+}
+
 }  // namespace mq
+
+extern "C" int mq_fock_rhf_noalloc(int n, const double *d_XX, const double *d_D, double *d_G, void *stream,
+                                   char *msg, int msglen) {
+  using namespace mq;
+  if (n <= 0 || !d_XX || !d_D || !d_G) return noalloc_fail(msg, msglen, MQ_EINVAL, "null pointer or n <= 0");
+  if (n > 4 * FOCK_THREADS) return noalloc_fail(msg, msglen, MQ_EINVAL, "n > 1024 is not supported");
+  const size_t n2 = (size_t)n * n;
+  // J plus at least one K slice must fit the fixed scratch: 2 n^2 <= 2 Mi doubles
+  if (2 * n2 > NOALLOC_SCRATCH_DOUBLES)
+    return noalloc_fail(msg, msglen, MQ_EINVAL, "scratch too small: 2 n^2 must not exceed 2097152 doubles");
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= NOALLOC_MAX_DEVICES)
+    return noalloc_fail(msg, msglen, MQ_ECUDA, "cudaGetDevice failed");
+  double *scr = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_fock_noalloc_mu);
+    if (!g_fock_noalloc_addr[dev]) {
+      void *p = nullptr;
+      cudaError_t e = cudaGetSymbolAddress(&p, g_fock_noalloc_scratch);
+      if (e != cudaSuccess || !p) return noalloc_fail(msg, msglen, MQ_ECUDA, cudaGetErrorString(e));
+      g_fock_noalloc_addr[dev] = (double *)p;
+    }
+    scr = g_fock_noalloc_addr[dev];
+  }
+  int sms = 148;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int nmax = (int)(NOALLOC_SCRATCH_DOUBLES / n2) - 1;  // K slices that fit beside J
+  int nchunk = std::max(1, std::min({n, (4 * sms + n - 1) / n, nmax}));
+  const int jchunk = (n + nchunk - 1) / nchunk;
+  nchunk = (n + jchunk - 1) / jchunk;
+  // every J element and every K slice element is written by the first kernel
+  // before the second reads it, so nothing needs clearing between calls
+  double *J = scr, *Kp = scr + n2;
+  cudaStream_t s = (cudaStream_t)stream;
+  fock_slab_kernel<false><<<dim3(n, nchunk), FOCK_THREADS, 0, s>>>(d_XX, d_D, nullptr, n, jchunk, J, Kp, nullptr);
+  fock_combine_kernel<<<(unsigned)((n2 + 255) / 256), 256, 0, s>>>(J, Kp, nchunk, n2, 0.5, d_G);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return noalloc_fail(msg, msglen, MQ_ECUDA, cudaGetErrorString(e));
+  return MQ_OK;
+}
