@@ -102,8 +102,9 @@ int mq_fock(mq_ctx *ctx, const double *Da, const double *Db, double *Ga, double 
  * total density), d_G (n x n output, G = J - K/2 as mq_fock computes it).
  * No context is needed and nothing is allocated or freed: the kernels'
  * scratch is a fixed 16 MiB array inside the library, held by every GPU that
- * loads it until the process exits, which limits n to 2 n^2 <= 2097152
- * doubles (n <= 1024); larger n returns MQ_EINVAL.  The work is queued on
+ * loads it until the process exits.  It holds G's J part, the split density
+ * and the K partial sums, which limits n to 3 n^2 <= 2097152 doubles
+ * (n <= 836); larger n returns MQ_EINVAL.  The work is queued on
  * `stream` (NULL: the default stream) and the call returns without waiting;
  * G is ready once that stream reaches this point.  All calls share the one
  * scratch array, so calls that overlap on the GPU (other streams, other host

@@ -101,3 +101,25 @@ def test_syev_batched(ctx):
         for b in range(batch):
             assert np.allclose(w[b], np.linalg.eigvalsh(A[b]), atol=1e-12 * n)
             assert np.allclose(A[b] @ V[b], V[b] * w[b], atol=1e-11 * n)
+
+
+def test_fock_water_cluster(ctx, basis_text):
+    """Stored Fock build at a size where the digestion's long sums matter:
+    (H2O)8, n = 56, tight integrals, a random symmetric density and a
+    converged-like one.  G must be symmetric to the last bit and match the
+    FP64 contraction of the same XX to 1e-12 relative."""
+    from myqc_gb300 import MODE_TIGHT, molecules
+    sysm = molecules.water_cluster_system(8, 7.0, 3)
+    basis = formats.parse_mybasis_text(basis_text, sysm.atoms)
+    ctx.set_system(sysm, basis, None, MODE_TIGHT)
+    XX = ctx.eri_full()
+    n = ctx.n
+    X4 = XX.reshape((n, n, n, n), order="F")
+    rng = np.random.default_rng(4)
+    for D in (rng.standard_normal((n, n)), rng.random((n, n)) * 0.2):
+        D = D + D.T
+        G = ctx.fock(D)
+        ref = np.einsum("ijkl,kl->ij", X4, D) - 0.5 * np.einsum("ikjl,kl->ij", X4, D)
+        assert np.array_equal(G, G.T)
+        err = np.max(np.abs(G - ref)) / np.max(np.abs(ref))
+        assert err < 1e-12, err
