@@ -134,6 +134,12 @@ typedef struct mq_scf_opts {
                        2: use D_in (density guess, e.g. the learned guess) */
   const double *C_in;   /* guess orbitals, n x n (x2 for UHF) */
   const double *D_in;   /* guess density, n x n (x2 for UHF: alpha, beta) */
+  int purify;       /* 0: new density from the eigenvectors each iteration (the
+                       reference's DSYGV step); 1: from the spectral projector
+                       by trace-correcting purification (GEMMs only), one
+                       eigensolve at the end for C and eps; an iteration whose
+                       frontier levels are degenerate falls back to the
+                       eigensolver.  Same fixed point either way. */
 } mq_scf_opts;
 
 /* Converged SCF.  Replaces the scf executable's iteration loop

@@ -33,7 +33,7 @@ class ScfOpts(ctypes.Structure):
     _fields_ = [("uhf", ctypes.c_int), ("nalpha", ctypes.c_int), ("nbeta", ctypes.c_int),
                 ("max_iter", ctypes.c_int), ("conv", ctypes.c_double), ("conv_rms", ctypes.c_int),
                 ("diis", ctypes.c_int), ("direct", ctypes.c_int), ("guess", ctypes.c_int),
-                ("C_in", ctypes.c_void_p), ("D_in", ctypes.c_void_p)]
+                ("C_in", ctypes.c_void_p), ("D_in", ctypes.c_void_p), ("purify", ctypes.c_int)]
 
 
 def header_symbols() -> list[str]:

@@ -446,6 +446,8 @@ int mq_stat(const mq_ctx *c, const char *key, double *value) {
   else if (!strcmp(key, "scf")) *value = s.ms_scf;
   else if (!strcmp(key, "fock_calls")) *value = s.fock_calls;
   else if (!strcmp(key, "scf_iters")) *value = s.scf_iters;
+  else if (!strcmp(key, "diag_calls")) *value = s.diag_calls;
+  else if (!strcmp(key, "purify_steps")) *value = s.purify_steps;
   else if (!strcmp(key, "lib_launches")) *value = s.lib_launches;
   else if (!strcmp(key, "launches")) *value = s.launches;
   else if (!strcmp(key, "quartets")) *value = s.quartets;

@@ -54,7 +54,7 @@ struct DeviceBuf {
 // stage; the SCF accumulates over its iterations.
 struct Stats {
   double ms_eri = 0, ms_fock = 0, ms_diag = 0, ms_ao2mo = 0, ms_mp2 = 0, ms_scf = 0;
-  double fock_calls = 0, diag_calls = 0, scf_iters = 0;
+  double fock_calls = 0, diag_calls = 0, scf_iters = 0, purify_steps = 0;
   double launches = 0, lib_launches = 0, quartets = 0, prim_quartets = 0;
 };
 
@@ -162,6 +162,11 @@ int gemm_strided_batched(mq_ctx *c, char ta, char tb, int m, int n, int k, doubl
                          long long sA, const double *B, int ldb, long long sB, double beta, double *C, int ldc,
                          long long sC, int batch);
 int density_device(mq_ctx *c, int n, int nocc, const double *d_C, double factor, double *d_D);
+// spectral projector onto the nocc lowest eigenvectors of the symmetric d_Fp
+// by trace-correcting purification (d_T, d_W: n x n scratch; d_err: >= 120
+// doubles); MQ_ENOCONV when the frontier levels are degenerate
+int purify_projector(mq_ctx *c, int n, int nocc, const double *d_Fp, double *d_P, double *d_T, double *d_W,
+                     double *d_err, int *steps);
 void cublas_destroy(void *handle);
 
 // ao2mo.cu

@@ -1,0 +1,149 @@
+// purify.cu -- SCF density step without a diagonalisation.
+//
+// The reference obtains each new density from the lowest nocc eigenvectors of
+// F C = S C e (DSYGV, src/scf/scf.f90:813-848, then dens.f90:115-124).  The
+// density depends on F only through the spectral projector P onto those
+// eigenvectors (in the orthogonal basis F' = X^T F X, X = S^-1/2):
+// D = occf * X P X.  Trace-correcting purification (Niklasson, Phys. Rev. B 66,
+// 155115 (2002), "TC2") builds P from F' with matrix products only:
+//   X_0 = (hi I - F') / (hi - lo)   (Gershgorin bounds: spectrum mapped into [0,1],
+//                                    occupied levels nearest 1)
+//   X_{k+1} = X_k^2        if |tr X_k^2 - nocc| < |tr(2X_k - X_k^2) - nocc|
+//           = 2X_k - X_k^2 otherwise
+// until the idempotency error tr(X - X^2) vanishes; convergence is quadratic
+// once the occupied and virtual eigenvalues have separated.  Each step is one
+// FP64 GEMM (cuBLAS) and one fused select/update kernel; no host round trip
+// except a convergence poll every few steps.  The SCF fixed point does not
+// change: at a gapped spectrum P is exactly the aufbau projector.  Without a
+// gap (degenerate frontier levels) the error stalls and the caller falls back
+// to the eigensolver for that iteration.
+#include <cmath>
+#include <vector>
+
+#include "internal.h"
+
+namespace mq {
+
+constexpr int PUR_THREADS = 1024;
+
+__device__ __forceinline__ double block_sum(double v, double *red) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  __syncthreads();  // red may still be read from a previous call
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double t = 0.0;
+  for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+  return t;
+}
+
+__device__ __forceinline__ double block_min(double v, double *red) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double t = red[0];
+  for (int w = 1; w < (int)(blockDim.x >> 5); ++w) t = fmin(t, red[w]);
+  return t;
+}
+
+// One CTA: Gershgorin interval [lo, hi] of the symmetric part of F, then
+// X_0 = (hi I - (F + F^T)/2) / (hi - lo).
+__global__ void __launch_bounds__(PUR_THREADS) purify_init_kernel(const double *__restrict__ F, int n,
+                                                                  double *__restrict__ X) {
+  __shared__ double red[PUR_THREADS / 32];
+  const size_t N = n;
+  double lo = INFINITY, nhi = INFINITY;  // min of row lower bounds, min of -(row upper bounds)
+  for (int r = threadIdx.x; r < n; r += blockDim.x) {
+    double off = 0.0;
+    for (int j = 0; j < n; ++j)
+      if (j != r) off += fabs(0.5 * (F[r + N * j] + F[j + N * r]));
+    const double d = F[r + N * r];
+    lo = fmin(lo, d - off);
+    nhi = fmin(nhi, -(d + off));
+  }
+  lo = block_min(lo, red);
+  const double hi = -block_min(nhi, red);
+  const double inv = 1.0 / fmax(hi - lo, 1e-300);
+  for (size_t idx = threadIdx.x; idx < N * N; idx += blockDim.x) {
+    const size_t r = idx % N, col = idx / N;
+    const double f = 0.5 * (F[idx] + F[col + N * r]);
+    X[idx] = ((r == col ? hi : 0.0) - f) * inv;
+  }
+}
+
+// Xn = select(X, T = X X): every CTA reads the two diagonals to make the same
+// choice; CTA 0 records the idempotency error tr X - tr T of step k.
+__global__ void purify_step_kernel(const double *__restrict__ X, const double *__restrict__ T, int n, double nocc,
+                                   double *__restrict__ Xn, double *__restrict__ err, int k) {
+  __shared__ double red[32];
+  const size_t N = n, n2 = N * N;
+  double tx = 0.0, tt = 0.0;
+  for (int r = threadIdx.x; r < n; r += blockDim.x) {
+    tx += X[r + N * r];
+    tt += T[r + N * r];
+  }
+  tx = block_sum(tx, red);
+  tt = block_sum(tt, red);
+  const bool square = fabs(tt - nocc) < fabs(2.0 * tx - tt - nocc);
+  if (blockIdx.x == 0 && threadIdx.x == 0) err[k] = tx - tt;
+  for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < n2; idx += (size_t)gridDim.x * blockDim.x) {
+    const size_t r = idx % N, col = idx / N;
+    const double t = 0.5 * (T[idx] + T[col + N * r]);
+    Xn[idx] = square ? t : 2.0 * X[idx] - t;
+  }
+}
+
+__global__ void identity_kernel(double *__restrict__ A, int n) {
+  const size_t N = n, idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx < N * N) A[idx] = (idx % N == idx / N) ? 1.0 : 0.0;
+}
+
+int purify_projector(mq_ctx *c, int n, int nocc, const double *d_Fp, double *d_P, double *d_T, double *d_W,
+                     double *d_err, int *steps) {
+  const size_t n2 = (size_t)n * n;
+  const unsigned gb = (unsigned)((n2 + 255) / 256);
+  *steps = 0;
+  if (nocc <= 0) {
+    MQ_CUDA(c, cudaMemsetAsync(d_P, 0, n2 * sizeof(double), c->stream));
+    return MQ_OK;
+  }
+  if (nocc >= n) {
+    identity_kernel<<<gb, 256, 0, c->stream>>>(d_P, n);
+    c->stats.launches += 1;
+    MQ_CUDA(c, cudaGetLastError());
+    return MQ_OK;
+  }
+  constexpr int MAX_STEPS = 120, POLL = 4;
+  constexpr double SETTLED = 1e-9;  // idempotency error after which two more steps reach FP64 round-off
+  double *X = d_P, *Xn = d_W;
+  purify_init_kernel<<<1, PUR_THREADS, 0, c->stream>>>(d_Fp, n, X);
+  c->stats.launches += 1;
+  std::vector<double> e(MAX_STEPS);
+  int k = 0, settled_at = -1;
+  while (k < MAX_STEPS) {
+    MQ_TRY(gemm(c, 'N', 'N', n, n, n, 1.0, X, n, X, n, 0.0, d_T, n));
+    purify_step_kernel<<<std::min(gb, 1024u), 256, 0, c->stream>>>(X, d_T, n, (double)nocc, Xn, d_err, k);
+    c->stats.launches += 1;
+    std::swap(X, Xn);
+    ++k;
+    if (settled_at >= 0 && k >= settled_at + 2) break;
+    if (settled_at < 0 && k % POLL == 0) {
+      MQ_CUDA(c, cudaMemcpyAsync(e.data(), d_err, k * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+      MQ_CUDA(c, cudaStreamSynchronize(c->stream));
+      for (int j = 0; j < k; ++j)
+        if (std::fabs(e[j]) < SETTLED) {  // X_j nearly idempotent: X_{j+2} is at round-off
+          settled_at = j;
+          break;
+        }
+      if (settled_at >= 0 && k >= settled_at + 2) break;
+    }
+  }
+  *steps = k;
+  if (settled_at < 0) return set_err(c, MQ_ENOCONV, "purification did not converge (no gap at the Fermi level?)");
+  if (X != d_P) MQ_CUDA(c, cudaMemcpyAsync(d_P, X, n2 * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+  return MQ_OK;
+}
+
+}  // namespace mq

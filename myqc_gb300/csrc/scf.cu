@@ -13,7 +13,10 @@
 //
 // The generalized problem is solved as C = X C' with X = S^-1/2 and
 // X^T F X C' = C' e (Jacobi), which gives the C^T S C = 1 normalisation and
-// ascending eigenvalues that DSYGV(1,'V','L') returns.
+// ascending eigenvalues that DSYGV(1,'V','L') returns.  With opts->purify the
+// iterations build D_{k+1} from the spectral projector of X^T F X by
+// trace-correcting purification instead (purify.cu), and the eigensolver runs
+// once, on the last iteration's F, for the orbitals and eigenvalues.
 #include <cmath>
 #include <vector>
 
@@ -238,17 +241,52 @@ int scf_device(mq_ctx *c, const double *S, const double *H, const mq_scf_opts *o
     }
     return MQ_OK;
   };
-  auto orbitals_to_density = [&]() -> int {
+  auto orbitals_to_density = [&](double *Dout) -> int {
     for (int s = 0; s < ns; ++s) {
       MQ_TRY(gemm(c, 'N', 'N', n, n, n, 1.0, dX, n, dU + n2 * s, n, 0.0, dC + n2 * s, n));
-      MQ_TRY(density_device(c, n, nocc[s], dC + n2 * s, occf, dDn + n2 * s));
+      MQ_TRY(density_device(c, n, nocc[s], dC + n2 * s, occf, Dout + n2 * s));
     }
     return MQ_OK;
   };
+  // new densities from the Fock matrices Fm: the eigensolver, or purification
+  // of F' = X F X into the projector P and D = occf X P X.  Purification that
+  // stalls (degenerate frontier levels) falls back to the eigensolver, cold
+  // started: the warm-start vectors in dU/dW are overwritten by its scratch.
+  const bool purify = o->purify != 0;
+  auto density_step = [&](const double *Fm, double *Dout) -> int {
+    if (purify) {
+      bool ok = true;
+      for (int s = 0; s < ns && ok; ++s) {
+        MQ_TRY(gemm(c, 'T', 'N', n, n, n, 1.0, dX, n, Fm + n2 * s, n, 0.0, dT1, n));
+        MQ_TRY(gemm(c, 'N', 'N', n, n, n, 1.0, dT1, n, dX, n, 0.0, dFp + n2 * s, n));
+        int steps = 0;
+        const int rc = purify_projector(c, n, nocc[s], dFp + n2 * s, dT3, dT2, dW, dScal + 128, &steps);
+        c->stats.purify_steps += steps;
+        if (rc == MQ_ENOCONV) {
+          ok = false;
+          break;
+        }
+        MQ_TRY(rc);
+        MQ_TRY(gemm(c, 'N', 'N', n, n, n, 1.0, dX, n, dT3, n, 0.0, dT1, n));
+        MQ_TRY(gemm(c, 'N', 'N', n, n, n, occf, dT1, n, dX, n, 0.0, Dout + n2 * s, n));
+      }
+      if (ok) return MQ_OK;
+      have_prev = false;
+    }
+    MQ_TRY(diagonalize(Fm));
+    c->stats.diag_calls += 1;
+    return orbitals_to_density(Dout);
+  };
 
   // initial density
+  c->stats.diag_calls = 0;
+  c->stats.purify_steps = 0;
   if (o->guess == 2 && o->D_in) {
     MQ_CUDA(c, cudaMemcpyAsync(dD, o->D_in, n2 * ns * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  } else if (purify && !(o->guess == 1 && o->C_in)) {  // core Hamiltonian, purified
+    for (int s = 0; s < ns; ++s)
+      MQ_CUDA(c, cudaMemcpyAsync(dF + n2 * s, dH, n2 * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+    MQ_TRY(density_step(dF, dD));
   } else {
     if (o->guess == 1 && o->C_in) {
       MQ_CUDA(c, cudaMemcpyAsync(dC, o->C_in, n2 * ns * sizeof(double), cudaMemcpyHostToDevice, c->stream));
@@ -271,6 +309,7 @@ int scf_device(mq_ctx *c, const double *S, const double *H, const mq_scf_opts *o
   bool conv = false;
   int it = 0;
   std::vector<double> hist;
+  const double *lastF = nullptr;
   for (; it < max_iter && !conv; ++it) {
     // G[D_k]
     t_fock.start(c->stream);
@@ -325,9 +364,9 @@ int scf_device(mq_ctx *c, const double *S, const double *H, const mq_scf_opts *o
       head = (head + 1) % ndiis;
     }
     t_diag.start(c->stream);
-    MQ_TRY(diagonalize(Fdiag));
+    MQ_TRY(density_step(Fdiag, dDn));
     t_diag.stop(c->stream);
-    MQ_TRY(orbitals_to_density());
+    lastF = Fdiag;
     diff_kernel<<<1, 1024, 0, c->stream>>>(dDn, dD, n2 * ns, dScal + 8);
     c->stats.launches += 2 + 2 * ns;
     double hs[10];
@@ -346,6 +385,13 @@ int scf_device(mq_ctx *c, const double *S, const double *H, const mq_scf_opts *o
     }
   }
   // outputs: orbitals and eigenvalues of the last diagonalisation, D_k of the last iteration
+  if (purify && lastF) {  // one eigensolve of the last iteration's Fock matrices for C and eps
+    have_prev = false;
+    MQ_TRY(diagonalize(lastF));
+    c->stats.diag_calls += 1;
+    for (int s = 0; s < ns; ++s)
+      MQ_TRY(gemm(c, 'N', 'N', n, n, n, 1.0, dX, n, dU + n2 * s, n, 0.0, dC + n2 * s, n));
+  }
   MQ_CUDA(c, cudaMemcpyAsync(C, dC, n2 * ns * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   MQ_CUDA(c, cudaMemcpyAsync(eps, dEps, (size_t)n * ns * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   if (D) MQ_CUDA(c, cudaMemcpyAsync(D, dD, n2 * ns * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
@@ -356,7 +402,6 @@ int scf_device(mq_ctx *c, const double *S, const double *H, const mq_scf_opts *o
   c->stats.ms_fock = t_fock.total;
   c->stats.ms_diag = t_diag.total;
   c->stats.fock_calls = it;
-  c->stats.diag_calls = it;
   c->stats.scf_iters = it;
   *energy = E;
   *iters = it;

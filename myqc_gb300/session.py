@@ -110,11 +110,11 @@ class Context:
     # ---------------------------------------------------------------- SCF
     def scf(self, S, H, nalpha: int, nbeta: int, uhf: bool = False, conv: float = 1e-7, conv_rms: bool = False,
             diis: int = 0, direct: bool = False, max_iter: int = 0, D_guess=None, C_guess=None,
-            raise_on_noconv: bool = True) -> SCFResult:
+            raise_on_noconv: bool = True, purify: bool = False) -> SCFResult:
         n, ns = self.n, 2 if uhf else 1
         o = _lib.ScfOpts()
         o.uhf, o.nalpha, o.nbeta, o.max_iter = int(uhf), nalpha, nbeta, max_iter
-        o.conv, o.conv_rms, o.diis, o.direct = conv, int(conv_rms), diis, int(direct)
+        o.conv, o.conv_rms, o.diis, o.direct, o.purify = conv, int(conv_rms), diis, int(direct), int(purify)
         keep = []
         if D_guess is not None:
             Dg = f64(np.asarray(D_guess).reshape(ns, n, n).transpose(1, 2, 0))  # (n, n, ns) F-order = ns blocks

@@ -123,3 +123,28 @@ def test_fock_water_cluster(ctx, basis_text):
         assert np.array_equal(G, G.T)
         err = np.max(np.abs(G - ref)) / np.max(np.abs(ref))
         assert err < 1e-12, err
+
+
+@pytest.mark.parametrize("name", ["CO2", "HF", "NO", "O_triplet", "Be", "(H2O)4"])
+def test_scf_purification_same_fixed_point(ctx, ftab, basis_text, name):
+    """Density by purification instead of the eigensolver: same energies,
+    same iteration count under plain Roothaan (the iterates are the same
+    densities), same orbital energies from the final eigensolve.  Open-shell
+    cases with degenerate frontier levels take the eigensolver fallback."""
+    from myqc_gb300 import molecules
+    if name.startswith("("):
+        sysm = molecules.water_cluster_system(4, 5.0, 11)
+    else:
+        sysm = formats.parse_zmat_text(_zmat(name))
+    basis = formats.parse_mybasis_text(basis_text, sysm.atoms)
+    ctx.set_system(sysm, basis, ftab, 0)
+    S, H = ctx.int1e()
+    ctx.eri_store()
+    for diis in (0, 8):
+        a = ctx.scf(S, H, sysm.nelcA, sysm.nelcB, uhf=sysm.uhf, conv=1e-10, diis=diis)
+        b = ctx.scf(S, H, sysm.nelcA, sysm.nelcB, uhf=sysm.uhf, conv=1e-10, diis=diis, purify=True)
+        assert abs(a.energy - b.energy) < 1e-10, (diis, a.energy, b.energy)
+        assert np.max(np.abs(np.asarray(a.eig) - np.asarray(b.eig))) < 1e-8
+        assert np.max(np.abs(a.D - b.D)) < 1e-8
+        if diis == 0:
+            assert abs(a.iterations - b.iterations) <= 1, (a.iterations, b.iterations)
