@@ -31,8 +31,12 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-NMOL, BOX = 32, 9.5  # (H2O)_32 in a 9.5 Angstrom cube
-WORKLOAD = "(H2O)32 RHF/STO-3G: int1e + int2e (full XX in HBM) + FP64 SCF to 1e-10 RMS dD + ao2mo(iajb) + MP2"
+NMOL, BOX = 32, 9.5  # (H2O)_32 in a 9.5 Angstrom cube (--nmol/--box change it, e.g. for profiler captures)
+
+
+def workload() -> str:
+    return (f"(H2O){NMOL} RHF/STO-3G: int1e + int2e (full XX in HBM) + FP64 SCF to 1e-10 RMS dD + ao2mo(iajb)"
+            " + MP2")
 
 
 def env_rank():
@@ -143,8 +147,8 @@ def run_ours(args):
 
     # ---- fast path, device-resident system (value)
     L0 = stat(ctx, "launches")
-    t_fock = t_eri = t_diag = t_ao2mo = 0.0
-    nfock = 0
+    t_fock = t_eri = t_diag = t_ao2mo = t_fock_kernel = 0.0
+    nfock = n_fock_kernel = 0
     iters = []
     barrier()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -154,6 +158,8 @@ def run_ours(args):
             res, mp2, prec = solve(ctx, sysm, basis, True, False)
             t_fock += stat(ctx, "fock")
             nfock += stat(ctx, "fock_calls")
+            t_fock_kernel += stat(ctx, "fock_kernel")
+            n_fock_kernel += stat(ctx, "fock_kernel_launches")
             t_eri += stat(ctx, "eri")
             t_diag += stat(ctx, "diag")
             t_ao2mo += stat(ctx, "ao2mo")
@@ -187,9 +193,12 @@ def run_ours(args):
     h2d = nat * (4 + 24) + basis.bas.nbytes + basis.set.nbytes + basis.basinfo.nbytes + basis.setinfo.nbytes \
         + 2 * n * n * 8 + 4 * n * n * 8 + n * 8
     d2h = 2 * n * n * 8 + n * n * 8 * 2 + n * 8 + 3 * 8
-    # dominant kernel: the stored-XX Fock digestion (one launch per SCF iteration)
-    fock_ms = t_fock / max(nfock, 1)
-    alg_bytes = float(n) ** 4 * 8 + 3 * n * n * 8
+    # dominant kernel: the stored-XX Fock digestion (one launch per SCF
+    # iteration), timed alone by the library's CUDA events on its stream.
+    # Algorithmic bytes: the n^2 (n+1)/2 slabs (i <= j) of n^2 doubles it reads
+    # plus the density in and J/K out (3 n^2 doubles).
+    fock_ms = t_fock_kernel / max(n_fock_kernel, 1)
+    alg_bytes = float(n) ** 3 * (n + 1) / 2 * 8 + 3 * n * n * 8
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -221,8 +230,8 @@ def run_ours(args):
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f64" if prec == 0 else "f64+bf16x3",
-        "data": "synthetic: seeded (H2O)32 cluster, rigid monomers, PCG64 seed %d" % args.seed,
-        "config": {"workload": WORKLOAD, "molecule": "(H2O)32", "n_basis": n, "n_occ": sysm.nelcA,
+        "data": f"synthetic: seeded (H2O){NMOL} cluster, rigid monomers, PCG64 seed {args.seed}",
+        "config": {"workload": workload(), "molecule": f"(H2O){NMOL}", "n_basis": n, "n_occ": sysm.nelcA,
                    "n_vir": n - sysm.nelcA, "box_angstrom": BOX, "seed": args.seed, "basis": "STO-3G",
                    "boys": "tight FP64 table", "scf": "FP64, DIIS(8), conv 1e-10 RMS dD, densities by TC2 purification (FP64 GEMMs), one Jacobi eigensolve at the end",
                    "mp2_precision": "split hi+mid+lo bf16 (tcgen05), fp32 accumulate" if prec else "fp64",
@@ -231,7 +240,7 @@ def run_ours(args):
         "e2e": {"value": world * 1000.0 / ms_e2e, "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": launches,
-        "roofline": {"kernel": "fock_slab_kernel (stored-XX J/K digestion)", "bound": "hbm",
+        "roofline": {"kernel": "fock_pair_kernel (stored-XX J/K digestion, slabs i <= j)", "bound": "hbm",
                      "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
                      "traffic": traffic, "peak_source": "measured" if peaks else "fallback"},
         "clocks": clk.summary(),
@@ -243,7 +252,7 @@ def run_ours(args):
         "accuracy": {"E_scf": res.energy, "E_mp2": mp2["E_MP2"], "dE_scf_vs_plain_Eh": dE_scf,
                      "dE_mp2_vs_fp64_uEh": dE_mp2 * 1e6},
         "eri_quartets_per_s": stat(ctx, "quartets") / (t_eri / args.steps * 1e-3) if t_eri > 0 else None,
-        "fock_builds_per_s": 1000.0 / fock_ms if fock_ms > 0 else None,
+        "fock_builds_per_s": 1000.0 * nfock / t_fock if t_fock > 0 else None,
     }
     if args.cpu_baseline and rank == 0:
         out["cpu_baseline"] = cpu_baseline(res_p.iterations, quick=True)
@@ -347,12 +356,13 @@ def run_reference(args):
            "value": v, "unit": "solves/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
            "ms_per_step": (time.perf_counter() - t0) * 1000.0 / max(args.steps, 1), "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic: seeded water clusters",
-           "config": {"workload": WORKLOAD, "molecule": "(H2O)32"}, "cpu_baseline": cb,
+           "config": {"workload": workload(), "molecule": f"(H2O){NMOL}"}, "cpu_baseline": cb,
            "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
 
 
 def main():
+    global NMOL, BOX
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
@@ -362,7 +372,10 @@ def main():
     ap.add_argument("--plain-iters", type=int, default=30,
                     help="SCF iterations assumed for the reference CPU extrapolation")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--nmol", type=int, default=NMOL, help="water molecules in the cluster")
+    ap.add_argument("--box", type=float, default=BOX, help="cube side in Angstrom")
     args = ap.parse_args()
+    NMOL, BOX = args.nmol, args.box
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

@@ -195,10 +195,14 @@ int mq_sygv(mq_ctx *ctx, int n, const double *F, const double *S, double *w, dou
 
 /* Profiling counters.  Device milliseconds (CUDA events on the context's
  * stream) of the last call of each stage: "eri", "ao2mo", "mp2", "scf" (whole
- * SCF), "fock" and "diag" (summed over the last SCF's iterations);
- * "fock_calls", "scf_iters"; cumulative launch counts "launches" (this
- * library's kernels) and "lib_launches" (cuBLAS calls); "quartets" and
- * "prim_quartets" of the last integral pass.  MQ_EINVAL on an unknown key. */
+ * SCF), "fock" and "diag" (summed over the last SCF's iterations; "diag" is
+ * the density step, eigensolver or purification), "fock_kernel" (the stored
+ * digestion kernel alone) with "fock_kernel_launches"; "fock_calls",
+ * "scf_iters", "diag_calls" (eigensolves), "purify_steps"; "fock_jc" (tile
+ * length the autotuner picked) and "tune_fock_ms" (its best time per build);
+ * cumulative launch counts "launches" (this library's kernels) and
+ * "lib_launches" (cuBLAS calls); "quartets" and "prim_quartets" of the last
+ * integral pass.  MQ_EINVAL on an unknown key. */
 int mq_stat(const mq_ctx *ctx, const char *key, double *value);
 
 #ifdef __cplusplus

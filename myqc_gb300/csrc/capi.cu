@@ -263,6 +263,9 @@ static int fock_common(mq_ctx *c, const double *Da, const double *Db, double *Ga
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   cudaEventRecord(e0, c->stream);
+  c->t_fock_kernel.collect();
+  c->t_fock_kernel.total = 0;
+  c->stats.fock_kernel_launches = 0;
   int rc;
   if (direct) {
     double *J = dG + n2 * ns, *Ka = J + n2, *Kb = Db ? Ka + n2 : nullptr;
@@ -276,6 +279,8 @@ static int fock_common(mq_ctx *c, const double *Da, const double *Db, double *Ga
   float ms = 0;
   cudaEventElapsedTime(&ms, e0, e1);
   c->stats.ms_fock = ms;
+  c->t_fock_kernel.collect();
+  c->stats.ms_fock_kernel = c->t_fock_kernel.total;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (rc != MQ_OK) return rc;
@@ -448,6 +453,10 @@ int mq_stat(const mq_ctx *c, const char *key, double *value) {
   else if (!strcmp(key, "scf_iters")) *value = s.scf_iters;
   else if (!strcmp(key, "diag_calls")) *value = s.diag_calls;
   else if (!strcmp(key, "purify_steps")) *value = s.purify_steps;
+  else if (!strcmp(key, "fock_jc")) *value = s.fock_jc;
+  else if (!strcmp(key, "fock_kernel")) *value = s.ms_fock_kernel;
+  else if (!strcmp(key, "fock_kernel_launches")) *value = s.fock_kernel_launches;
+  else if (!strcmp(key, "tune_fock_ms")) *value = s.tune_fock_ms;
   else if (!strcmp(key, "lib_launches")) *value = s.lib_launches;
   else if (!strcmp(key, "launches")) *value = s.launches;
   else if (!strcmp(key, "quartets")) *value = s.quartets;

@@ -243,9 +243,13 @@ __device__ __forceinline__ void quartet(const EriArgs &g, int P, int Q) {
     atomicMax(g.sch + P, (unsigned long long)__double_as_longlong(sqrt(m)));
     return;
   }
-  if (g.counters && A0 == 0 && B0 == 0) {
-    atomicAdd(g.counters, 1ull);
-    atomicAdd(g.counters + 1, (unsigned long long)nprim);
+  if (g.counters && A0 == 0 && B0 == 0) {  // one atomic pair per warp, not per quartet
+    const unsigned act = __activemask();
+    const unsigned nq_w = __popc(act), np_w = __reduce_add_sync(act, nprim);
+    if ((threadIdx.x & 31) == __ffs(act) - 1) {
+      atomicAdd(g.counters, (unsigned long long)nq_w);
+      atomicAdd(g.counters + 1, (unsigned long long)np_w);
+    }
   }
   const size_t n = (size_t)g.n;
 #pragma unroll

@@ -12,8 +12,10 @@
 // the CTA, and the chunk's partial K column goes to a scratch slice; a second
 // kernel sums the slices in a fixed order.  No atomics, deterministic.
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
+#include <string>
 
 #include "internal.h"
 
@@ -149,38 +151,305 @@ __global__ void fock_combine_kernel(const double *__restrict__ J, const double *
   G[idx] = J[idx] - f * (0.5 * (k + kt));
 }
 
+// ---- pair-slab digestion: only the slabs with i <= j ------------------------
+// Slab (i,j) and slab (j,i) hold the same n^2 values ((kl|ij) = (kl|ji)), so
+// one read of S = XX(:,:,i,j), i <= j, serves
+//   J_ij = J_ji = <S, Dt>,   K[:,i] += S . D(:,j),   K[:,j] += S . D(:,i) (i < j)
+// and half of XX is never read.  A CTA owns one i and a run of up to JC
+// consecutive j >= i (a tile): the l loop loads the density row element once
+// and applies it to all JC slabs, whose XX streams are in flight together.
+// K[:,i] accumulates over the tile in registers and goes to a per-tile slice;
+// the contribution of slab (i,j) to K[:,j] goes to Q[:, i, j].  An assembly
+// kernel then sums, in a fixed order, the row-j tile slices and Q[:, i<j, j]:
+// deterministic, no atomics.  Thread t of T = blockDim.x owns rows k = t + T r,
+// r < R.
+constexpr int PAIR_MAX_THREADS = 256;
+
+template <int R, int JC, bool UHF>
+__global__ void __launch_bounds__(PAIR_MAX_THREADS) fock_pair_kernel(
+    const double *__restrict__ XX, const float2 *__restrict__ DJ, const float2 *__restrict__ DKa,
+    const float2 *__restrict__ DKb, const int4 *__restrict__ tiles, int n, double *__restrict__ J,
+    double *__restrict__ Kpa, double *__restrict__ Kpb, double *__restrict__ Qa, double *__restrict__ Qb) {
+  extern __shared__ float2 dsh[];  // D(:,i) then D(:,j) for the tile's j (alpha; beta after)
+  const int4 tile = tiles[blockIdx.x];
+  const int i = tile.x, j0 = tile.y, nj = tile.z - tile.y;
+  const size_t N = n, n2 = N * N;
+  const int tid = threadIdx.x, T = blockDim.x;
+  float2 *dia = dsh, *dja = dsh + n;
+  float2 *dib = dsh + (size_t)(1 + JC) * n, *djb = dib + n;
+  for (int l = tid; l < n; l += T) {
+    dia[l] = DKa[l + N * i];
+    if (UHF) dib[l] = DKb[l + N * i];
+  }
+  for (int jj = 0; jj < nj; ++jj)
+    for (int l = tid; l < n; l += T) {
+      dja[jj * n + l] = DKa[l + N * (j0 + jj)];
+      if (UHF) djb[jj * n + l] = DKb[l + N * (j0 + jj)];
+    }
+  __syncthreads();
+
+  const float2 z = make_float2(0.f, 0.f);
+  float2 aj[JC][R], aqa[JC][R], aqb[UHF ? JC : 1][R], aka[R], akb[R];
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    aka[r] = z;
+    akb[r] = z;
+#pragma unroll
+    for (int jj = 0; jj < JC; ++jj) {
+      aj[jj][r] = z;
+      aqa[jj][r] = z;
+      if (UHF) aqb[jj][r] = z;
+    }
+  }
+  const double *S0 = XX + n2 * ((size_t)i + N * j0);
+#pragma unroll 2
+  for (int l = 0; l < n; ++l) {
+    const float2 di_a = dia[l];
+    const float2 di_b = UHF ? dib[l] : z;
+    float2 dj[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const int k = tid + r * T;
+      dj[r] = k < n ? DJ[k + N * l] : z;
+    }
+#pragma unroll
+    for (int jj = 0; jj < JC; ++jj) {
+      if (jj < nj) {
+        const float2 dja_l = dja[jj * n + l];
+        const float2 djb_l = UHF ? djb[jj * n + l] : z;
+        const double *S = S0 + n2 * N * jj + N * l;
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+          const int k = tid + r * T;
+          if (k < n) {
+            const float2 x = split_f64(__ldcs(S + k));  // streamed once: keep it out of L2
+            dfma(aj[jj][r], x, dj[r]);
+            dfma(aka[r], x, dja_l);
+            dfma(aqa[jj][r], x, di_a);
+            if (UHF) {
+              dfma(akb[r], x, djb_l);
+              dfma(aqb[jj][r], x, di_b);
+            }
+          }
+        }
+      }
+    }
+  }
+
+  // epilogue: J_ij by block reduction, Q(:, i, j) for j > i, the tile's K(:, i) slice
+  __shared__ double red[PAIR_MAX_THREADS / 32][JC];
+#pragma unroll
+  for (int jj = 0; jj < JC; ++jj) {
+    double v = 0.0;
+#pragma unroll
+    for (int r = 0; r < R; ++r) v += (double)aj[jj][r].x + (double)aj[jj][r].y;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((tid & 31) == 0) red[tid >> 5][jj] = v;
+  }
+  __syncthreads();
+  if (tid < nj) {
+    double t = 0.0;
+    for (int w = 0; w < T / 32; ++w) t += red[w][tid];
+    const int j = j0 + tid;
+    J[i + N * j] = t;
+    J[j + N * i] = t;
+  }
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const int k = tid + r * T;
+    if (k >= n) continue;
+    Kpa[N * blockIdx.x + k] = (double)aka[r].x + (double)aka[r].y;
+    if (UHF) Kpb[N * blockIdx.x + k] = (double)akb[r].x + (double)akb[r].y;
+#pragma unroll
+    for (int jj = 0; jj < JC; ++jj) {
+      const int j = j0 + jj;
+      if (jj < nj && j > i) {
+        Qa[k + N * i + n2 * j] = (double)aqa[jj][r].x + (double)aqa[jj][r].y;
+        if (UHF) Qb[k + N * i + n2 * j] = (double)aqb[jj][r].x + (double)aqb[jj][r].y;
+      }
+    }
+  }
+}
+
+// K(k, j) = sum over row j's tiles of their slices + sum_{i<j} Q(k, i, j)
+__global__ void fock_pair_assemble_kernel(const double *__restrict__ Kp, const double *__restrict__ Q,
+                                          const int *__restrict__ row_first, int n, double *__restrict__ K) {
+  const size_t N = n, n2 = N * N;
+  const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= n2) return;
+  const int k = (int)(idx % N), j = (int)(idx / N);
+  double s = 0.0;
+  for (int b = row_first[j]; b < row_first[j + 1]; ++b) s += Kp[N * b + k];
+  for (int i = 0; i < j; ++i) s += Q[k + N * i + n2 * j];
+  K[idx] = s;
+}
+
+template <int R, int JC>
+static int launch_pair(mq_ctx *c, int ntiles, int threads, size_t smem, bool uhf, const float2 *DJ,
+                       const float2 *DKa, const float2 *DKb, const int4 *tiles, int n, double *J, double *Kpa,
+                       double *Kpb, double *Qa, double *Qb) {
+  if (uhf) {
+    auto k = fock_pair_kernel<R, JC, true>;
+    MQ_CUDA(c, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k<<<ntiles, threads, smem, c->stream>>>(c->d_XX, DJ, DKa, DKb, tiles, n, J, Kpa, Kpb, Qa, Qb);
+  } else {
+    auto k = fock_pair_kernel<R, JC, false>;
+    MQ_CUDA(c, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k<<<ntiles, threads, smem, c->stream>>>(c->d_XX, DJ, DKa, nullptr, tiles, n, J, Kpa, nullptr, Qa, nullptr);
+  }
+  return MQ_OK;
+}
+
+template <int R>
+static int launch_pair_jc(mq_ctx *c, int jc, int ntiles, int threads, size_t smem, bool uhf, const float2 *DJ,
+                          const float2 *DKa, const float2 *DKb, const int4 *tiles, int n, double *J, double *Kpa,
+                          double *Kpb, double *Qa, double *Qb) {
+  switch (jc) {
+    case 1: return launch_pair<R, 1>(c, ntiles, threads, smem, uhf, DJ, DKa, DKb, tiles, n, J, Kpa, Kpb, Qa, Qb);
+    case 2: return launch_pair<R, 2>(c, ntiles, threads, smem, uhf, DJ, DKa, DKb, tiles, n, J, Kpa, Kpb, Qa, Qb);
+    case 4: return launch_pair<R, 4>(c, ntiles, threads, smem, uhf, DJ, DKa, DKb, tiles, n, J, Kpa, Kpb, Qa, Qb);
+    default: return launch_pair<R, 8>(c, ntiles, threads, smem, uhf, DJ, DKa, DKb, tiles, n, J, Kpa, Kpb, Qa, Qb);
+  }
+}
+
+// Tile table for JC slabs per tile: (i, j0, j1) over row i's j in [i, n), and
+// row_first[i] = first tile of row i.  Cached per (n, JC).
+static int pair_tiles(mq_ctx *c, int n, int JC, const int4 **tiles, const int **row_first, int *ntiles) {
+  const size_t N = n;
+  FockTiles &ft = c->fock_tiles[JC];
+  if (ft.n != n) {
+    std::vector<int4> tl;
+    std::vector<int> rf(N + 1);
+    for (int i = 0; i < n; ++i) {
+      rf[i] = (int)tl.size();
+      for (int j = i; j < n; j += JC) tl.push_back(make_int4(i, j, std::min(n, j + JC), 0));
+    }
+    rf[n] = (int)tl.size();
+    const std::string name = "fock_tiles" + std::to_string(JC);
+    char *d = (char *)buf(c, name.c_str(), sizeof(int4) * tl.size() + sizeof(int) * (N + 1));
+    if (!d) return MQ_ENOMEM;
+    MQ_CUDA(c, cudaMemcpyAsync(d, tl.data(), sizeof(int4) * tl.size(), cudaMemcpyHostToDevice, c->stream));
+    MQ_CUDA(c, cudaMemcpyAsync(d + sizeof(int4) * tl.size(), rf.data(), sizeof(int) * (N + 1),
+                               cudaMemcpyHostToDevice, c->stream));
+    MQ_CUDA(c, cudaStreamSynchronize(c->stream));  // the host vectors go out of scope
+    ft.n = n;
+    ft.ntiles = (int)tl.size();
+    ft.d = d;
+  }
+  *tiles = (const int4 *)ft.d;
+  *row_first = (const int *)(ft.d + sizeof(int4) * ft.ntiles);
+  *ntiles = ft.ntiles;
+  return MQ_OK;
+}
+
+// One digestion of the split densities with JC slabs per tile, then assembly of
+// K and G = J - f (K + K^T)/2.
+static int pair_build(mq_ctx *c, int JC, bool uhf, const float2 *DJ, const float2 *DKa, const float2 *DKb,
+                      double *d_Ga, double *d_Gb, bool timed = false) {
+  const int n = c->nao;
+  const size_t N = n, n2 = N * N;
+  const int T = std::min(PAIR_MAX_THREADS, (n + 31) / 32 * 32);
+  const int R0 = (n + T - 1) / T;
+  const int Rp = R0 <= 1 ? 1 : R0 <= 2 ? 2 : 4;
+  const int4 *tiles;
+  const int *row_first;
+  int ntiles;
+  MQ_TRY(pair_tiles(c, n, JC, &tiles, &row_first, &ntiles));
+  const int ns = uhf ? 2 : 1;
+  // J | K slices (ns * ntiles * n) | Q (ns * n^3) | K (ns * n^2)
+  double *J = (double *)buf(c, "fock_partials", sizeof(double) * (n2 + ns * (N * ntiles + N * n2 + n2)));
+  if (!J) return MQ_ENOMEM;
+  double *Kpa = J + n2, *Kpb = uhf ? Kpa + N * ntiles : nullptr;
+  double *Qa = J + n2 + ns * N * ntiles, *Qb = uhf ? Qa + N * n2 : nullptr;
+  double *Ka = J + n2 + ns * (N * ntiles + N * n2), *Kb = uhf ? Ka + n2 : nullptr;
+  const size_t smem = sizeof(float2) * N * (1 + JC) * ns;
+  int rc = MQ_OK;
+  if (timed) c->t_fock_kernel.start(c->stream);
+  switch (Rp) {
+    case 1: rc = launch_pair_jc<1>(c, JC, ntiles, T, smem, uhf, DJ, DKa, DKb, tiles, n, J, Kpa, Kpb, Qa, Qb); break;
+    case 2: rc = launch_pair_jc<2>(c, JC, ntiles, T, smem, uhf, DJ, DKa, DKb, tiles, n, J, Kpa, Kpb, Qa, Qb); break;
+    default: rc = launch_pair_jc<4>(c, JC, ntiles, T, smem, uhf, DJ, DKa, DKb, tiles, n, J, Kpa, Kpb, Qa, Qb); break;
+  }
+  MQ_TRY(rc);
+  if (timed) {
+    c->t_fock_kernel.stop(c->stream);
+    c->stats.fock_kernel_launches += 1;
+  }
+  MQ_CUDA(c, cudaGetLastError());
+  const int tb = 256;
+  const unsigned gb = (unsigned)((n2 + tb - 1) / tb);
+  fock_pair_assemble_kernel<<<gb, tb, 0, c->stream>>>(Kpa, Qa, row_first, n, Ka);
+  if (uhf) fock_pair_assemble_kernel<<<gb, tb, 0, c->stream>>>(Kpb, Qb, row_first, n, Kb);
+  fock_combine_kernel<<<gb, tb, 0, c->stream>>>(J, Ka, 1, n, uhf ? 1.0 : 0.5, d_Ga);
+  if (uhf) fock_combine_kernel<<<gb, tb, 0, c->stream>>>(J, Kb, 1, n, 1.0, d_Gb);
+  c->stats.launches += uhf ? 5 : 3;
+  MQ_CUDA(c, cudaGetLastError());
+  return MQ_OK;
+}
+
+// Autotuner for the tile length JC: on the first build for a given (n, RHF or
+// UHF) each candidate digests the caller's densities twice under CUDA events
+// and the fastest is kept for the context's later builds.  Every candidate
+// computes the same G (the tile length only changes the summation grouping,
+// ~1e-13 relative), and the call's result comes from the chosen one.
+// MYQC_FOCK_JC=1|2|4|8 in the environment pins the choice instead.
+static int pair_choose_jc(mq_ctx *c, bool uhf, const float2 *DJ, const float2 *DKa, const float2 *DKb,
+                          double *d_Ga, double *d_Gb) {
+  const int n = c->nao;
+  int &slot = uhf ? c->fock_jc_uhf : c->fock_jc_rhf;
+  int &slot_n = uhf ? c->fock_jc_uhf_n : c->fock_jc_rhf_n;
+  if (slot_n == n && slot > 0) return slot;
+  if (const char *e = getenv("MYQC_FOCK_JC")) {
+    const int v = atoi(e);
+    slot = v >= 8 ? 8 : v >= 4 ? 4 : v >= 2 ? 2 : 1;
+    slot_n = n;
+    return slot;
+  }
+  const int cand[3] = {1, 2, 4};
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  float best = 1e30f;
+  int best_jc = 2;
+  for (int jc : cand) {
+    if (pair_build(c, jc, uhf, DJ, DKa, DKb, d_Ga, d_Gb) != MQ_OK) continue;  // warm-up, tile table
+    cudaEventRecord(a, c->stream);
+    bool ok = true;
+    for (int r = 0; r < 2 && ok; ++r) ok = pair_build(c, jc, uhf, DJ, DKa, DKb, d_Ga, d_Gb) == MQ_OK;
+    cudaEventRecord(b, c->stream);
+    cudaEventSynchronize(b);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    if (ok && ms < best) {
+      best = ms;
+      best_jc = jc;
+    }
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  c->stats.tune_fock_ms = best / 2;
+  slot = best_jc;
+  slot_n = n;
+  return slot;
+}
+
 int fock_stored_device(mq_ctx *c, const double *d_Da, const double *d_Db, double *d_Ga, double *d_Gb) {
   const int n = c->nao;
   if (!c->d_XX) return set_err(c, MQ_ESTATE, "no integrals on the device (call mq_eri_store or mq_eri_upload)");
-  if (n > 4 * FOCK_THREADS) return set_err(c, MQ_EINVAL, "stored Fock build supports n <= 1024");
+  if (n > 4 * PAIR_MAX_THREADS) return set_err(c, MQ_EINVAL, "stored Fock build supports n <= 1024");
   const bool uhf = d_Db != nullptr;
-  // chunks of j so that the grid covers the GPU about 4 times
-  int sms = 148;
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
-  int nchunk = std::max(1, std::min(n, (4 * sms + n - 1) / n));
-  const int jchunk = (n + nchunk - 1) / nchunk;
-  nchunk = (n + jchunk - 1) / jchunk;
   const size_t n2 = (size_t)n * n;
-  double *J = (double *)buf(c, "fock_partials", sizeof(double) * n2 * (1 + nchunk * (uhf ? 2 : 1)));
   float2 *DJ = (float2 *)buf(c, "fock_dsplit", sizeof(float2) * n2 * (uhf ? 3 : 1));
-  if (!J || !DJ) return MQ_ENOMEM;
-  double *Kpa = J + n2, *Kpb = uhf ? Kpa + n2 * nchunk : nullptr;
+  if (!DJ) return MQ_ENOMEM;
   float2 *DKa = uhf ? DJ + n2 : DJ, *DKb = uhf ? DJ + 2 * n2 : nullptr;
   const int tb = 256;
-  const unsigned gb = (unsigned)((n2 + tb - 1) / tb);
-  split_density_kernel<<<gb, tb, 0, c->stream>>>(d_Da, d_Db, n2, DJ, DKa, DKb);
-  dim3 grid(n, nchunk);
-  if (uhf)
-    fock_slab_kernel<true><<<grid, FOCK_THREADS, 0, c->stream>>>(c->d_XX, DJ, DKa, DKb, n, jchunk, J, Kpa, Kpb);
-  else
-    fock_slab_kernel<false><<<grid, FOCK_THREADS, 0, c->stream>>>(c->d_XX, DJ, DKa, nullptr, n, jchunk, J, Kpa,
-                                                                  nullptr);
-  MQ_CUDA(c, cudaGetLastError());
-  fock_combine_kernel<<<gb, tb, 0, c->stream>>>(J, Kpa, nchunk, n, uhf ? 1.0 : 0.5, d_Ga);
-  if (uhf) fock_combine_kernel<<<gb, tb, 0, c->stream>>>(J, Kpb, nchunk, n, 1.0, d_Gb);
-  c->stats.launches += uhf ? 4 : 3;
-  MQ_CUDA(c, cudaGetLastError());
-  return MQ_OK;
+  split_density_kernel<<<(unsigned)((n2 + tb - 1) / tb), tb, 0, c->stream>>>(d_Da, d_Db, n2, DJ, DKa, DKb);
+  c->stats.launches += 1;
+  const int JC = pair_choose_jc(c, uhf, DJ, DKa, DKb, d_Ga, d_Gb);
+  c->stats.fock_jc = JC;
+  c->t_fock_kernel.collect();  // a previous build's timing not yet collected by its caller
+  return pair_build(c, JC, uhf, DJ, DKa, DKb, d_Ga, d_Gb, true);
 }
 
 // ---------------------------------------------------------------------------

@@ -52,10 +52,17 @@ struct DeviceBuf {
 
 // Device time (CUDA events on the context's stream) of the last call of each
 // stage; the SCF accumulates over its iterations.
+// device tile table of the pair-slab Fock kernel for one tile length
+struct FockTiles {
+  int n = 0, ntiles = 0;
+  char *d = nullptr;  // int4 tiles[ntiles] then int row_first[n + 1], in a named context buffer
+};
+
 struct Stats {
   double ms_eri = 0, ms_fock = 0, ms_diag = 0, ms_ao2mo = 0, ms_mp2 = 0, ms_scf = 0;
-  double fock_calls = 0, diag_calls = 0, scf_iters = 0, purify_steps = 0;
+  double fock_calls = 0, diag_calls = 0, scf_iters = 0, purify_steps = 0, fock_jc = 0, tune_fock_ms = 0;
   double launches = 0, lib_launches = 0, quartets = 0, prim_quartets = 0;
+  double ms_fock_kernel = 0, fock_kernel_launches = 0;  // the digestion kernel alone, last SCF or mq_fock
 };
 
 // Event pair on the context's stream that adds its elapsed time to a counter
@@ -110,6 +117,9 @@ struct mq_ctx {
   mq::PairTable pt{};
   std::vector<void *> pair_allocs;
   double *d_XX = nullptr;    // n^4 full integral array
+  mq::StageTimer t_fock_kernel;  // the digestion kernel alone, collected at the caller's sync points
+  mq::FockTiles fock_tiles[9];  // pair-slab tile tables, indexed by slabs per tile
+  int fock_jc_rhf = 0, fock_jc_rhf_n = 0, fock_jc_uhf = 0, fock_jc_uhf_n = 0;  // autotuned tile lengths
   size_t XX_elems = 0;
   double *d_iajb = nullptr;  // last (ia|jb) block
   size_t iajb_elems = 0;

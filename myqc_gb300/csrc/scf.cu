@@ -302,6 +302,9 @@ int scf_device(mq_ctx *c, const double *S, const double *H, const mq_scf_opts *o
 
   const double enuc = nuclear_repulsion(c);
   StageTimer t_fock, t_diag, t_all;
+  c->t_fock_kernel.collect();
+  c->t_fock_kernel.total = 0;
+  c->stats.fock_kernel_launches = 0;
   t_all.start(c->stream);
   std::vector<double> Bm((size_t)ndiis * ndiis * 4, 0.0);
   int nh = 0, head = 0;
@@ -374,6 +377,7 @@ int scf_device(mq_ctx *c, const double *S, const double *H, const mq_scf_opts *o
     MQ_CUDA(c, cudaStreamSynchronize(c->stream));
     t_fock.collect();
     t_diag.collect();
+    c->t_fock_kernel.collect();
     E = hs[0] + (uhf ? hs[2] : 0.0) + enuc;
     const double diff = o->conv_rms ? hs[9] : hs[8];
     hist.push_back(E);
@@ -400,6 +404,7 @@ int scf_device(mq_ctx *c, const double *S, const double *H, const mq_scf_opts *o
   t_all.collect();
   c->stats.ms_scf = t_all.total;
   c->stats.ms_fock = t_fock.total;
+  c->stats.ms_fock_kernel = c->t_fock_kernel.total;
   c->stats.ms_diag = t_diag.total;
   c->stats.fock_calls = it;
   c->stats.scf_iters = it;
