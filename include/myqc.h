@@ -193,6 +193,44 @@ int mq_syev_batched(mq_ctx *ctx, int n, int batch, double *A, double *w, double 
  * src/scf/scf.f90:478,848) for one n x n pair of host matrices. */
 int mq_sygv(mq_ctx *ctx, int n, const double *F, const double *S, double *w, double *C);
 
+/* ---- Batches of independent closed-shell molecules (no reference
+ * counterpart: the reference runs one molecule per invocation of scf,
+ * src/scf/scf.f90:61-216).  Molecules of uneven size (at most 116 basis
+ * functions each) are added one by one with the arrays buildBasis returns,
+ * then solved together: integrals, Fock builds and the dense per-molecule
+ * steps of every molecule share each launch, and one SCF iteration is a CUDA
+ * graph replayed until every molecule has converged.  Integrals use
+ * MQ_MODE_TIGHT.  Per molecule the iteration and convergence rule are those of
+ * mq_scf (RHF).  Packed arrays hold molecule m's n_m x n_m block (column-major)
+ * after those of molecules 0..m-1; vectors likewise. */
+typedef struct mq_batch_opts {
+  int max_iter;        /* 0 -> 500 */
+  double conv;         /* density threshold; 0 -> 1e-7 */
+  int conv_rms;        /* 0: max|dD|; 1: RMS */
+  int diis;            /* 0: plain Roothaan; >0: DIIS subspace (<= 16) */
+  int graph;           /* 1: replay one captured iteration as a CUDA graph */
+  int check_every;     /* poll the count of unconverged molecules every k iterations (0 -> 4) */
+  const double *D_in;  /* packed guess densities, or NULL for the core-Hamiltonian guess;
+                          a block whose first element is NaN takes the core guess */
+} mq_batch_opts;
+
+/* Empty the context's batch. */
+int mq_batch_clear(mq_ctx *ctx);
+
+/* Append one closed-shell molecule with nocc doubly occupied orbitals. */
+int mq_batch_add(mq_ctx *ctx, int nnuc, const int *Z, const double *xyz, const double *bas, const double *set,
+                 const int *basinfo, const int *setinfo, int nocc);
+
+/* Number of molecules, and (norb may be NULL) each one's basis size. */
+int mq_batch_info(const mq_ctx *ctx, int *nmol, int *norb);
+
+/* Solve every molecule of the batch.  energy, iters, converged: one entry per
+ * molecule (E of the last iteration's input density; iterations taken;
+ * 1 if converged).  D (may be NULL): packed last input densities; eps (may be
+ * NULL): packed orbital energies of the last diagonalisation. */
+int mq_batch_scf(mq_ctx *ctx, const mq_batch_opts *opts, double *energy, int *iters, int *converged, double *D,
+                 double *eps);
+
 /* Profiling counters.  Device milliseconds (CUDA events on the context's
  * stream) of the last call of each stage: "eri", "ao2mo", "mp2", "scf" (whole
  * SCF), "fock" and "diag" (summed over the last SCF's iterations; "diag" is

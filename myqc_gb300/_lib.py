@@ -36,6 +36,12 @@ class ScfOpts(ctypes.Structure):
                 ("C_in", ctypes.c_void_p), ("D_in", ctypes.c_void_p), ("purify", ctypes.c_int)]
 
 
+class BatchOpts(ctypes.Structure):
+    _fields_ = [("max_iter", ctypes.c_int), ("conv", ctypes.c_double), ("conv_rms", ctypes.c_int),
+                ("diis", ctypes.c_int), ("graph", ctypes.c_int), ("check_every", ctypes.c_int),
+                ("D_in", ctypes.c_void_p)]
+
+
 def header_symbols() -> list[str]:
     """Names of every function the public header declares."""
     txt = open(HEADER).read()
@@ -77,6 +83,10 @@ def lib(path: str | None = None):
     L.mq_syev_batched.argtypes = [vp, c_int, c_int, dp, dp, dp]
     L.mq_sygv.argtypes = [vp, c_int, dp, dp, dp, dp]
     L.mq_stat.argtypes = [vp, ctypes.c_char_p, ctypes.POINTER(c_double)]
+    L.mq_batch_clear.argtypes = [vp]
+    L.mq_batch_add.argtypes = [vp, c_int, vp, vp, vp, vp, vp, vp, c_int]
+    L.mq_batch_info.argtypes = [vp, ip, vp]
+    L.mq_batch_scf.argtypes = [vp, ctypes.POINTER(BatchOpts), dp, vp, vp, dp, dp]
     _lib = L
     return L
 

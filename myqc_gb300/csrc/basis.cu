@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <cmath>
 #include <map>
+#include <type_traits>
 
 #include "internal.h"
 
@@ -115,43 +116,33 @@ void free_pairs(mq_ctx *c) {
   c->pt = PairTable{};
 }
 
-template <class T>
-static int upload(mq_ctx *c, T *&dst, const std::vector<T> &src) {
-  dst = nullptr;
-  size_t bytes = std::max<size_t>(1, src.size()) * sizeof(T);
-  cudaError_t e = cudaMalloc((void **)&dst, bytes);
-  if (e != cudaSuccess) return set_err(c, MQ_ENOMEM, "cudaMalloc pair table");
-  c->pair_allocs.push_back(dst);
-  if (!src.empty()) MQ_CUDA(c, cudaMemcpy(dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice));
-  return MQ_OK;
-}
-
-int build_pairs(mq_ctx *c) {
-  free_pairs(c);
-  const int ns = c->nshell;
+// Shell pairs of one molecule, in class order (ss), (sp,s), (sp,sp), with
+// their surviving primitive pairs.
+void pairs_host(const std::vector<HostShell> &shells, const std::vector<double> &xyz, HostPairs &h) {
+  h = HostPairs{};
+  const int ns = (int)shells.size();
   std::vector<std::pair<int, int>> pl[3];
   for (int a = 0; a < ns; ++a)
     for (int b = 0; b <= a; ++b) {
       int A = a, B = b;
-      const HostShell &sa = c->shells[a], &sb = c->shells[b];
+      const HostShell &sa = shells[a], &sb = shells[b];
       if (sb.type > sa.type) std::swap(A, B);
       pl[sa.type + sb.type].push_back({A, B});
     }
-  std::vector<int> shA, shB, off, aoA, aoB;
-  std::vector<double> p, inv2p, beta, Px, Py, Pz, PAx, PAy, PAz, PBx, PBy, PBz, K, c4;
   int idx = 0;
   for (int cl = 0; cl < 3; ++cl) {
-    c->pt.class_off[cl] = idx;
+    h.class_off[cl] = idx;
     for (auto &ab : pl[cl]) {
-      const HostShell &A = c->shells[ab.first], &B = c->shells[ab.second];
-      const double *xa = &c->xyz[3 * A.atom], *xb = &c->xyz[3 * B.atom];
+      const HostShell &A = shells[ab.first], &B = shells[ab.second];
+      const double *xa = &xyz[3 * A.atom], *xb = &xyz[3 * B.atom];
       double AB2 = 0;
       for (int k = 0; k < 3; ++k) AB2 += (xa[k] - xb[k]) * (xa[k] - xb[k]);
-      shA.push_back(ab.first);
-      shB.push_back(ab.second);
-      aoA.push_back(A.ao0);
-      aoB.push_back(B.ao0);
-      off.push_back((int)p.size());
+      h.shA.push_back(ab.first);
+      h.shB.push_back(ab.second);
+      h.aoA.push_back(A.ao0);
+      h.aoB.push_back(B.ao0);
+      h.mol.push_back(0);
+      h.off.push_back((int)h.p.size());
       for (int i = 0; i < A.nprim; ++i)
         for (int j = 0; j < B.nprim; ++j) {
           double a = A.alpha[i], b = B.alpha[j], pp = a + b;
@@ -166,41 +157,88 @@ int build_pairs(mq_ctx *c) {
             PA[k] = P[k] - xa[k];
             PB[k] = P[k] - xb[k];
           }
-          p.push_back(pp);
-          inv2p.push_back(1.0 / (2.0 * pp));
-          beta.push_back(b);
-          Px.push_back(P[0]); Py.push_back(P[1]); Pz.push_back(P[2]);
-          PAx.push_back(PA[0]); PAy.push_back(PA[1]); PAz.push_back(PA[2]);
-          PBx.push_back(PB[0]); PBy.push_back(PB[1]); PBz.push_back(PB[2]);
-          K.push_back(Kab);
+          h.p.push_back(pp);
+          h.inv2p.push_back(1.0 / (2.0 * pp));
+          h.beta.push_back(b);
+          h.Px.push_back(P[0]); h.Py.push_back(P[1]); h.Pz.push_back(P[2]);
+          h.PAx.push_back(PA[0]); h.PAy.push_back(PA[1]); h.PAz.push_back(PA[2]);
+          h.PBx.push_back(PB[0]); h.PBy.push_back(PB[1]); h.PBz.push_back(PB[2]);
+          h.K.push_back(Kab);
           double ca[2] = {A.cs[i], A.cp[i]}, cb[2] = {B.cs[j], B.cp[j]};
           for (int la = 0; la < 2; ++la)
-            for (int lb = 0; lb < 2; ++lb) c4.push_back(Kab * ca[la] * cb[lb]);
+            for (int lb = 0; lb < 2; ++lb) h.c4.push_back(Kab * ca[la] * cb[lb]);
         }
       ++idx;
     }
   }
-  c->pt.class_off[3] = idx;
-  off.push_back((int)p.size());
-  c->pt.npairs = idx;
-  c->pt.npp = (int)p.size();
-  PairTable &t = c->pt;
-  MQ_TRY(upload(c, t.shA, shA));
-  MQ_TRY(upload(c, t.shB, shB));
-  MQ_TRY(upload(c, t.pp_off, off));
-  MQ_TRY(upload(c, t.aoA, aoA));
-  MQ_TRY(upload(c, t.aoB, aoB));
-  std::vector<double> ones(idx, 1.0e300);
-  MQ_TRY(upload(c, t.schwarz, ones));
-  MQ_TRY(upload(c, t.p, p));
-  MQ_TRY(upload(c, t.inv2p, inv2p));
-  MQ_TRY(upload(c, t.beta, beta));
-  MQ_TRY(upload(c, t.Px, Px)); MQ_TRY(upload(c, t.Py, Py)); MQ_TRY(upload(c, t.Pz, Pz));
-  MQ_TRY(upload(c, t.PAx, PAx)); MQ_TRY(upload(c, t.PAy, PAy)); MQ_TRY(upload(c, t.PAz, PAz));
-  MQ_TRY(upload(c, t.PBx, PBx)); MQ_TRY(upload(c, t.PBy, PBy)); MQ_TRY(upload(c, t.PBz, PBz));
-  MQ_TRY(upload(c, t.K, K));
-  MQ_TRY(upload(c, t.c4, c4));
-  c->pair_class_count = {(int)pl[0].size(), (int)pl[1].size(), (int)pl[2].size()};
+  h.class_off[3] = idx;
+  h.off.push_back((int)h.p.size());
+}
+
+// Append the class-cl pairs of one molecule's table to a batch table (whose
+// pairs are ordered class first, then molecule), tagging them with `mol`.
+void append_pairs_class(HostPairs &dst, const HostPairs &src, int cl, int mol) {
+  if (dst.off.empty()) dst.off.push_back(0);
+  for (int P = src.class_off[cl]; P < src.class_off[cl + 1]; ++P) {
+    dst.shA.push_back(src.shA[P]);
+    dst.shB.push_back(src.shB[P]);
+    dst.aoA.push_back(src.aoA[P]);
+    dst.aoB.push_back(src.aoB[P]);
+    dst.mol.push_back(mol);
+    for (int q = src.off[P]; q < src.off[P + 1]; ++q) {
+      dst.p.push_back(src.p[q]);
+      dst.inv2p.push_back(src.inv2p[q]);
+      dst.beta.push_back(src.beta[q]);
+      dst.Px.push_back(src.Px[q]); dst.Py.push_back(src.Py[q]); dst.Pz.push_back(src.Pz[q]);
+      dst.PAx.push_back(src.PAx[q]); dst.PAy.push_back(src.PAy[q]); dst.PAz.push_back(src.PAz[q]);
+      dst.PBx.push_back(src.PBx[q]); dst.PBy.push_back(src.PBy[q]); dst.PBz.push_back(src.PBz[q]);
+      dst.K.push_back(src.K[q]);
+      for (int k = 0; k < 4; ++k) dst.c4.push_back(src.c4[4 * q + k]);
+    }
+    dst.off.push_back((int)dst.p.size());  // end of this pair's primitives = start of the next
+  }
+}
+
+int upload_pairs(mq_ctx *c, const HostPairs &h, std::vector<void *> &allocs, PairTable &t) {
+  t = PairTable{};
+  for (int k = 0; k < 4; ++k) t.class_off[k] = h.class_off[k];
+  t.npairs = (int)h.shA.size();
+  t.npp = (int)h.p.size();
+  auto up = [&](auto *&dst, const auto &src) -> int {
+    using T = typename std::decay<decltype(src)>::type::value_type;
+    dst = nullptr;
+    const size_t bytes = std::max<size_t>(1, src.size()) * sizeof(T);
+    if (cudaMalloc((void **)&dst, bytes) != cudaSuccess) return set_err(c, MQ_ENOMEM, "cudaMalloc pair table");
+    allocs.push_back(dst);
+    if (!src.empty()) MQ_CUDA(c, cudaMemcpy(dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice));
+    return MQ_OK;
+  };
+  MQ_TRY(up(t.shA, h.shA));
+  MQ_TRY(up(t.shB, h.shB));
+  MQ_TRY(up(t.pp_off, h.off));
+  MQ_TRY(up(t.aoA, h.aoA));
+  MQ_TRY(up(t.aoB, h.aoB));
+  MQ_TRY(up(t.mol, h.mol));
+  std::vector<double> ones(h.shA.size(), 1.0e300);
+  MQ_TRY(up(t.schwarz, ones));
+  MQ_TRY(up(t.p, h.p));
+  MQ_TRY(up(t.inv2p, h.inv2p));
+  MQ_TRY(up(t.beta, h.beta));
+  MQ_TRY(up(t.Px, h.Px)); MQ_TRY(up(t.Py, h.Py)); MQ_TRY(up(t.Pz, h.Pz));
+  MQ_TRY(up(t.PAx, h.PAx)); MQ_TRY(up(t.PAy, h.PAy)); MQ_TRY(up(t.PAz, h.PAz));
+  MQ_TRY(up(t.PBx, h.PBx)); MQ_TRY(up(t.PBy, h.PBy)); MQ_TRY(up(t.PBz, h.PBz));
+  MQ_TRY(up(t.K, h.K));
+  MQ_TRY(up(t.c4, h.c4));
+  return MQ_OK;
+}
+
+int build_pairs(mq_ctx *c) {
+  free_pairs(c);
+  HostPairs h;
+  pairs_host(c->shells, c->xyz, h);
+  MQ_TRY(upload_pairs(c, h, c->pair_allocs, c->pt));
+  c->pair_class_count = {h.class_off[1] - h.class_off[0], h.class_off[2] - h.class_off[1],
+                         h.class_off[3] - h.class_off[2]};
   return MQ_OK;
 }
 

@@ -123,6 +123,8 @@ int mq_free(mq_ctx *c) {
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
   free_pairs(c);
+  batch_clear(c);
+  if (c->d_boys_tight) cudaFree(c->d_boys_tight);
   for (auto &kv : c->bufs)
     if (kv.second.ptr) cudaFree(kv.second.ptr);
   if (c->d_XX) cudaFree(c->d_XX);
@@ -440,6 +442,34 @@ int mq_sygv(mq_ctx *c, int n, const double *F, const double *S, double *w, doubl
   return MQ_OK;
 }
 
+int mq_batch_clear(mq_ctx *c) {
+  if (!c) return MQ_EINVAL;
+  return batch_clear(c);
+}
+
+int mq_batch_add(mq_ctx *c, int nnuc, const int *Z, const double *xyz, const double *bas, const double *set,
+                 const int *basinfo, const int *setinfo, int nocc) {
+  if (!c) return MQ_EINVAL;
+  if (nnuc <= 0 || !Z || !xyz || !bas || !set || !basinfo || !setinfo) return set_err(c, MQ_EINVAL, "null argument");
+  return batch_add(c, nnuc, Z, xyz, bas, set, basinfo, setinfo, nocc);
+}
+
+int mq_batch_info(const mq_ctx *c, int *nmol, int *norb) {
+  if (!c || !nmol) return MQ_EINVAL;
+  *nmol = (int)c->bmols.size();
+  if (norb)
+    for (size_t m = 0; m < c->bmols.size(); ++m) norb[m] = c->bmols[m].n;
+  return MQ_OK;
+}
+
+int mq_batch_scf(mq_ctx *c, const mq_batch_opts *o, double *energy, int *iters, int *converged, double *D,
+                 double *eps) {
+  if (!c) return MQ_EINVAL;
+  if (!o || !energy) return set_err(c, MQ_EINVAL, "null argument");
+  cudaSetDevice(c->device);
+  return batch_scf(c, o, energy, iters, converged, D, eps);
+}
+
 int mq_stat(const mq_ctx *c, const char *key, double *value) {
   if (!c || !key || !value) return MQ_EINVAL;
   const Stats &s = c->stats;
@@ -454,6 +484,7 @@ int mq_stat(const mq_ctx *c, const char *key, double *value) {
   else if (!strcmp(key, "diag_calls")) *value = s.diag_calls;
   else if (!strcmp(key, "purify_steps")) *value = s.purify_steps;
   else if (!strcmp(key, "fock_jc")) *value = s.fock_jc;
+  else if (!strcmp(key, "graph_launches")) *value = s.graph_launches;
   else if (!strcmp(key, "fock_kernel")) *value = s.ms_fock_kernel;
   else if (!strcmp(key, "fock_kernel_launches")) *value = s.fock_kernel_launches;
   else if (!strcmp(key, "tune_fock_ms")) *value = s.tune_fock_ms;

@@ -49,6 +49,13 @@ struct EriArgs {
   double *J, *Ka, *Kb;
   int uhf;
   unsigned long long *counters;  // [0] quartets computed, [1] primitive quartets
+  // batch (nmol > 0): the launch covers one class combination of every
+  // molecule; mq_off is the prefix of the molecules' quartet counts, pstart /
+  // pcount the molecules' pair ranges per class in the batch pair table
+  int nmol, cP, cQ;
+  const long long *mq_off;
+  const int *pstart, *pcount;
+  const MolDesc *mols;
 };
 
 __host__ __device__ constexpr int fl(int f, int axis) { return f == axis + 1 ? 1 : 0; }  // f: 0 s, 1 px, 2 py, 3 pz
@@ -120,7 +127,7 @@ __device__ __forceinline__ void pair_E(double PA, double PB, double i2p, double 
 }
 
 template <int LA, int LB, int LC, int LD, int A0, int A1, int B0, int B1, int EPI>
-__device__ __forceinline__ void quartet(const EriArgs &g, int P, int Q) {
+__device__ __forceinline__ void quartet(const EriArgs &g, int P, int Q, size_t n, double *XXout) {
   constexpr int NC = nfun(LC), ND = nfun(LD);
   constexpr int LAB = LA + LB, LT = LA + LB + LC + LD;
   constexpr int QREF = 3 * LT;  // the reference's Boys order for s/sp sets
@@ -251,7 +258,6 @@ __device__ __forceinline__ void quartet(const EriArgs &g, int P, int Q) {
       atomicAdd(g.counters + 1, (unsigned long long)np_w);
     }
   }
-  const size_t n = (size_t)g.n;
 #pragma unroll
   for (int a = A0; a < A1; ++a)
 #pragma unroll
@@ -266,7 +272,7 @@ __device__ __forceinline__ void quartet(const EriArgs &g, int P, int Q) {
           if (P == Q && (size_t)i * n + j < (size_t)k * n + l) continue;
           const double x = acc[a - A0][b - B0][c][d];
           if (EPI == EPI_XX) {
-            double *XX = g.XX;
+            double *XX = XXout;
             const size_t ij = (size_t)i + n * j, ji = (size_t)j + n * i, kl = (size_t)k + n * l,
                          lk = (size_t)l + n * k, n2 = n * n;
             XX[ij + n2 * kl] = x;
@@ -308,22 +314,38 @@ __device__ __forceinline__ void quartet(const EriArgs &g, int P, int Q) {
         }
 }
 
-// decode (P, Q) of quartet index q in the launch; returns false past the end
-__device__ __forceinline__ bool decode(const EriArgs &g, long long q, int &P, int &Q) {
+// decode (P, Q) of quartet index q in the launch, and the molecule m (0 for
+// one system); returns false past the end
+__device__ __forceinline__ bool decode(const EriArgs &g, long long q, int &P, int &Q, int &m) {
   if (q >= g.nq) return false;
+  m = 0;
+  int pOff = g.pOff, qOff = g.qOff, nQ = g.nQ;
+  if (g.nmol) {  // largest m with mq_off[m] <= q
+    int lo = 0, hi = g.nmol - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (g.mq_off[mid] <= q) lo = mid;
+      else hi = mid - 1;
+    }
+    m = lo;
+    q -= g.mq_off[m];
+    pOff = g.pstart[3 * m + g.cP];
+    qOff = g.pstart[3 * m + g.cQ];
+    nQ = g.pcount[3 * m + g.cQ];
+  }
   if (g.diag) {
-    P = Q = g.pOff + (int)q;
+    P = Q = pOff + (int)q;
     return true;
   }
   if (g.tri) {
     long long r = (long long)((sqrt(8.0 * (double)q + 1.0) - 1.0) * 0.5);
     while (r * (r + 1) / 2 > q) --r;
     while ((r + 1) * (r + 2) / 2 <= q) ++r;
-    P = g.pOff + (int)r;
-    Q = g.qOff + (int)(q - r * (r + 1) / 2);
+    P = pOff + (int)r;
+    Q = qOff + (int)(q - r * (r + 1) / 2);
   } else {
-    P = g.pOff + (int)(q / g.nQ);
-    Q = g.qOff + (int)(q % g.nQ);
+    P = pOff + (int)(q / nQ);
+    Q = qOff + (int)(q % nQ);
   }
   if (g.thr > 0.0 && g.t.schwarz[P] * g.t.schwarz[Q] < g.thr) return false;
   return true;
@@ -339,24 +361,30 @@ __global__ void __launch_bounds__(128) eri_kernel(EriArgs g) {
   const int lane = threadIdx.x & 31;
   const int split = (int)(warp % NSPLIT);
   const long long q = (warp / NSPLIT) * 32 + lane;
-  int P, Q;
-  if (!decode(g, q, P, Q)) return;
+  int P, Q, m;
+  if (!decode(g, q, P, Q, m)) return;
+  size_t n = (size_t)g.n;
+  double *XX = g.XX;
+  if (g.nmol) {
+    n = (size_t)g.mols[m].n;
+    XX += g.mols[m].xx;
+  }
   if (NSPLIT == 1) {
-    quartet<LA, LB, LC, LD, 0, NA, 0, NB, EPI>(g, P, Q);
+    quartet<LA, LB, LC, LD, 0, NA, 0, NB, EPI>(g, P, Q, n, XX);
   } else if (NSPLIT == 4) {
     switch (split) {
-      case 0: quartet<LA, LB, LC, LD, 0, 1, 0, NB, EPI>(g, P, Q); break;
-      case 1: quartet<LA, LB, LC, LD, 1, 2, 0, NB, EPI>(g, P, Q); break;
-      case 2: quartet<LA, LB, LC, LD, 2, 3, 0, NB, EPI>(g, P, Q); break;
-      default: quartet<LA, LB, LC, LD, 3, 4, 0, NB, EPI>(g, P, Q); break;
+      case 0: quartet<LA, LB, LC, LD, 0, 1, 0, NB, EPI>(g, P, Q, n, XX); break;
+      case 1: quartet<LA, LB, LC, LD, 1, 2, 0, NB, EPI>(g, P, Q, n, XX); break;
+      case 2: quartet<LA, LB, LC, LD, 2, 3, 0, NB, EPI>(g, P, Q, n, XX); break;
+      default: quartet<LA, LB, LC, LD, 3, 4, 0, NB, EPI>(g, P, Q, n, XX); break;
     }
   } else {
 #define MQ_SPLIT16(s) \
-  case s: quartet<LA, LB, LC, LD, (s) / 4, (s) / 4 + 1, (s) % 4, (s) % 4 + 1, EPI>(g, P, Q); break;
+  case s: quartet<LA, LB, LC, LD, (s) / 4, (s) / 4 + 1, (s) % 4, (s) % 4 + 1, EPI>(g, P, Q, n, XX); break;
     switch (split) {
       MQ_SPLIT16(0) MQ_SPLIT16(1) MQ_SPLIT16(2) MQ_SPLIT16(3) MQ_SPLIT16(4) MQ_SPLIT16(5) MQ_SPLIT16(6)
       MQ_SPLIT16(7) MQ_SPLIT16(8) MQ_SPLIT16(9) MQ_SPLIT16(10) MQ_SPLIT16(11) MQ_SPLIT16(12) MQ_SPLIT16(13)
-      MQ_SPLIT16(14) default: quartet<LA, LB, LC, LD, 3, 4, 3, 4, EPI>(g, P, Q); break;
+      MQ_SPLIT16(14) default: quartet<LA, LB, LC, LD, 3, 4, 3, 4, EPI>(g, P, Q, n, XX); break;
     }
 #undef MQ_SPLIT16
   }
@@ -455,6 +483,38 @@ int eri_full_device(mq_ctx *c, double *d_XX) {
   MQ_CUDA(c, cudaStreamSynchronize(c->stream));
   c->stats.quartets = (double)h[0];
   c->stats.prim_quartets = (double)h[1];
+  return MQ_OK;
+}
+
+// Batch: the full XX of every molecule into the packed XX (offset
+// MolDesc::xx), one launch per class combination for all molecules.  qcount
+// holds, per combination (cP, cQ) with cQ <= cP at index cP*(cP+1)/2 + cQ,
+// the device prefix of the molecules' quartet counts and its total.
+int eri_batch_device(mq_ctx *c, const PairTable &t, const MolDesc *d_mols, int nmol, const int *d_pstart,
+                     const int *d_pcount, const long long *const d_mq_off[6], const long long total[6], double *d_XX,
+                     size_t xx_total) {
+  MQ_CUDA(c, cudaMemsetAsync(d_XX, 0, xx_total * sizeof(double), c->stream));
+  EriArgs g{};
+  g.t = t;
+  g.boys = c->d_boys;
+  g.mode = MQ_MODE_TIGHT;
+  g.XX = d_XX;
+  g.nmol = nmol;
+  g.pstart = d_pstart;
+  g.pcount = d_pcount;
+  g.mols = d_mols;
+  for (int cP = 0; cP < 3; ++cP)
+    for (int cQ = 0; cQ <= cP; ++cQ) {
+      const int k = cP * (cP + 1) / 2 + cQ;
+      if (total[k] == 0) continue;
+      EriArgs h = g;
+      h.cP = cP;
+      h.cQ = cQ;
+      h.tri = cP == cQ;
+      h.nq = total[k];
+      h.mq_off = d_mq_off[k];
+      MQ_TRY(launch_class<EPI_XX>(c, h, cP, cQ));
+    }
   return MQ_OK;
 }
 

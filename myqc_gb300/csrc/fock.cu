@@ -79,6 +79,14 @@ __global__ void split_density_kernel(const double *__restrict__ Da, const double
   }
 }
 
+int split_density(mq_ctx *c, const double *Da, const double *Db, size_t n2, float2 *DJ, float2 *DKa, float2 *DKb) {
+  if (n2 == 0) return MQ_OK;
+  split_density_kernel<<<(unsigned)((n2 + 255) / 256), 256, 0, c->stream>>>(Da, Db, n2, DJ, DKa, DKb);
+  c->stats.launches += 1;
+  MQ_CUDA(c, cudaGetLastError());
+  return MQ_OK;
+}
+
 template <bool UHF>
 __global__ void __launch_bounds__(FOCK_THREADS) fock_slab_kernel(const double *__restrict__ XX,
                                                                  const float2 *__restrict__ DJ,
@@ -165,15 +173,28 @@ __global__ void fock_combine_kernel(const double *__restrict__ J, const double *
 // r < R.
 constexpr int PAIR_MAX_THREADS = 256;
 
+// A tile is (i, j0, j1, molecule); the molecule's descriptor gives its order
+// and where its XX, matrices and Q live, so one launch serves one system or a
+// whole batch.  Tiles of molecules whose `active` flag is 0 do nothing.
 template <int R, int JC, bool UHF>
 __global__ void __launch_bounds__(PAIR_MAX_THREADS) fock_pair_kernel(
     const double *__restrict__ XX, const float2 *__restrict__ DJ, const float2 *__restrict__ DKa,
-    const float2 *__restrict__ DKb, const int4 *__restrict__ tiles, int n, double *__restrict__ J,
-    double *__restrict__ Kpa, double *__restrict__ Kpb, double *__restrict__ Qa, double *__restrict__ Qb) {
+    const float2 *__restrict__ DKb, const int4 *__restrict__ tiles, const MolDesc *__restrict__ mols,
+    const int *__restrict__ active, int kp_stride, double *__restrict__ J, double *__restrict__ Kpa,
+    double *__restrict__ Kpb, double *__restrict__ Qa, double *__restrict__ Qb) {
   extern __shared__ float2 dsh[];  // D(:,i) then D(:,j) for the tile's j (alpha; beta after)
   const int4 tile = tiles[blockIdx.x];
-  const int i = tile.x, j0 = tile.y, nj = tile.z - tile.y;
+  if (active && !active[tile.w]) return;
+  const MolDesc md = mols[tile.w];
+  const int i = tile.x, j0 = tile.y, nj = tile.z - tile.y, n = md.n;
   const size_t N = n, n2 = N * N;
+  XX += md.xx;
+  DJ += md.mat;
+  DKa += md.mat;
+  if (UHF) DKb += md.mat;
+  J += md.mat;
+  Qa += md.q;
+  if (UHF) Qb += md.q;
   const int tid = threadIdx.x, T = blockDim.x;
   float2 *dia = dsh, *dja = dsh + n;
   float2 *dib = dsh + (size_t)(1 + JC) * n, *djb = dib + n;
@@ -259,8 +280,8 @@ __global__ void __launch_bounds__(PAIR_MAX_THREADS) fock_pair_kernel(
   for (int r = 0; r < R; ++r) {
     const int k = tid + r * T;
     if (k >= n) continue;
-    Kpa[N * blockIdx.x + k] = (double)aka[r].x + (double)aka[r].y;
-    if (UHF) Kpb[N * blockIdx.x + k] = (double)akb[r].x + (double)akb[r].y;
+    Kpa[(size_t)kp_stride * blockIdx.x + k] = (double)aka[r].x + (double)aka[r].y;
+    if (UHF) Kpb[(size_t)kp_stride * blockIdx.x + k] = (double)akb[r].x + (double)akb[r].y;
 #pragma unroll
     for (int jj = 0; jj < JC; ++jj) {
       const int j = j0 + jj;
@@ -272,104 +293,124 @@ __global__ void __launch_bounds__(PAIR_MAX_THREADS) fock_pair_kernel(
   }
 }
 
-// K(k, j) = sum over row j's tiles of their slices + sum_{i<j} Q(k, i, j)
+// K(k, j) = sum over row j's tiles of their slices + sum_{i<j} Q(k, i, j);
+// blockIdx.y is the molecule
 __global__ void fock_pair_assemble_kernel(const double *__restrict__ Kp, const double *__restrict__ Q,
-                                          const int *__restrict__ row_first, int n, double *__restrict__ K) {
-  const size_t N = n, n2 = N * N;
+                                          const int *__restrict__ row_first, const MolDesc *__restrict__ mols,
+                                          const int *__restrict__ active, int kp_stride, double *__restrict__ K) {
+  const int m = blockIdx.y;
+  if (active && !active[m]) return;
+  const MolDesc md = mols[m];
+  const size_t N = md.n, n2 = N * N;
   const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= n2) return;
   const int k = (int)(idx % N), j = (int)(idx / N);
+  const int *rf = row_first + md.row_first;
+  Q += md.q;
   double s = 0.0;
-  for (int b = row_first[j]; b < row_first[j + 1]; ++b) s += Kp[N * b + k];
+  for (int b = rf[j]; b < rf[j + 1]; ++b) s += Kp[(size_t)kp_stride * b + k];
   for (int i = 0; i < j; ++i) s += Q[k + N * i + n2 * j];
-  K[idx] = s;
+  K[md.mat + idx] = s;
+}
+
+// G = J - f (K + K^T)/2 per molecule (blockIdx.y)
+__global__ void fock_pair_combine_kernel(const double *__restrict__ J, const double *__restrict__ K,
+                                         const MolDesc *__restrict__ mols, const int *__restrict__ active, double f,
+                                         double *__restrict__ G) {
+  const int m = blockIdx.y;
+  if (active && !active[m]) return;
+  const MolDesc md = mols[m];
+  const size_t N = md.n, n2 = N * N;
+  const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= n2) return;
+  const size_t tdx = (idx % N) * N + idx / N;
+  G[md.mat + idx] = J[md.mat + idx] - f * (0.5 * (K[md.mat + idx] + K[md.mat + tdx]));
 }
 
 template <int R, int JC>
-static int launch_pair(mq_ctx *c, int ntiles, int threads, size_t smem, bool uhf, const float2 *DJ,
-                       const float2 *DKa, const float2 *DKb, const int4 *tiles, int n, double *J, double *Kpa,
-                       double *Kpb, double *Qa, double *Qb) {
+static int launch_pair(mq_ctx *c, const PairLaunch &L, int threads, size_t smem, bool uhf) {
   if (uhf) {
     auto k = fock_pair_kernel<R, JC, true>;
     MQ_CUDA(c, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k<<<ntiles, threads, smem, c->stream>>>(c->d_XX, DJ, DKa, DKb, tiles, n, J, Kpa, Kpb, Qa, Qb);
+    k<<<L.ntiles, threads, smem, c->stream>>>(L.XX, L.DJ, L.DKa, L.DKb, L.tiles, L.mols, L.active, L.nmax, L.J,
+                                              L.Kpa, L.Kpb, L.Qa, L.Qb);
   } else {
     auto k = fock_pair_kernel<R, JC, false>;
     MQ_CUDA(c, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k<<<ntiles, threads, smem, c->stream>>>(c->d_XX, DJ, DKa, nullptr, tiles, n, J, Kpa, nullptr, Qa, nullptr);
+    k<<<L.ntiles, threads, smem, c->stream>>>(L.XX, L.DJ, L.DKa, nullptr, L.tiles, L.mols, L.active, L.nmax, L.J,
+                                              L.Kpa, nullptr, L.Qa, nullptr);
   }
   return MQ_OK;
 }
 
 template <int R>
-static int launch_pair_jc(mq_ctx *c, int jc, int ntiles, int threads, size_t smem, bool uhf, const float2 *DJ,
-                          const float2 *DKa, const float2 *DKb, const int4 *tiles, int n, double *J, double *Kpa,
-                          double *Kpb, double *Qa, double *Qb) {
+static int launch_pair_jc(mq_ctx *c, int jc, const PairLaunch &L, int threads, size_t smem, bool uhf) {
   switch (jc) {
-    case 1: return launch_pair<R, 1>(c, ntiles, threads, smem, uhf, DJ, DKa, DKb, tiles, n, J, Kpa, Kpb, Qa, Qb);
-    case 2: return launch_pair<R, 2>(c, ntiles, threads, smem, uhf, DJ, DKa, DKb, tiles, n, J, Kpa, Kpb, Qa, Qb);
-    case 4: return launch_pair<R, 4>(c, ntiles, threads, smem, uhf, DJ, DKa, DKb, tiles, n, J, Kpa, Kpb, Qa, Qb);
-    default: return launch_pair<R, 8>(c, ntiles, threads, smem, uhf, DJ, DKa, DKb, tiles, n, J, Kpa, Kpb, Qa, Qb);
+    case 1: return launch_pair<R, 1>(c, L, threads, smem, uhf);
+    case 2: return launch_pair<R, 2>(c, L, threads, smem, uhf);
+    case 4: return launch_pair<R, 4>(c, L, threads, smem, uhf);
+    default: return launch_pair<R, 8>(c, L, threads, smem, uhf);
   }
 }
 
-// Tile table for JC slabs per tile: (i, j0, j1) over row i's j in [i, n), and
-// row_first[i] = first tile of row i.  Cached per (n, JC).
-static int pair_tiles(mq_ctx *c, int n, int JC, const int4 **tiles, const int **row_first, int *ntiles) {
+void pair_tiles_host(int n, int JC, int mol, std::vector<int4> &tl, std::vector<int> &rf) {
+  for (int i = 0; i < n; ++i) {
+    rf.push_back((int)tl.size());
+    for (int j = i; j < n; j += JC) tl.push_back(make_int4(i, j, std::min(n, j + JC), mol));
+  }
+  rf.push_back((int)tl.size());
+}
+
+// Tile table of the single system for JC slabs per tile: (i, j0, j1, 0) over
+// row i's j in [i, n), row_first[i] = first tile of row i, and the one
+// molecule descriptor.  Cached per (n, JC).
+static int pair_tiles(mq_ctx *c, int n, int JC, PairLaunch &L) {
   const size_t N = n;
   FockTiles &ft = c->fock_tiles[JC];
   if (ft.n != n) {
     std::vector<int4> tl;
-    std::vector<int> rf(N + 1);
-    for (int i = 0; i < n; ++i) {
-      rf[i] = (int)tl.size();
-      for (int j = i; j < n; j += JC) tl.push_back(make_int4(i, j, std::min(n, j + JC), 0));
-    }
-    rf[n] = (int)tl.size();
+    std::vector<int> rf;
+    pair_tiles_host(n, JC, 0, tl, rf);
+    MolDesc md{};
+    md.n = n;
     const std::string name = "fock_tiles" + std::to_string(JC);
-    char *d = (char *)buf(c, name.c_str(), sizeof(int4) * tl.size() + sizeof(int) * (N + 1));
+    char *d = (char *)buf(c, name.c_str(), sizeof(int4) * tl.size() + sizeof(int) * (N + 1) + sizeof(MolDesc) + 16);
     if (!d) return MQ_ENOMEM;
-    MQ_CUDA(c, cudaMemcpyAsync(d, tl.data(), sizeof(int4) * tl.size(), cudaMemcpyHostToDevice, c->stream));
-    MQ_CUDA(c, cudaMemcpyAsync(d + sizeof(int4) * tl.size(), rf.data(), sizeof(int) * (N + 1),
-                               cudaMemcpyHostToDevice, c->stream));
+    const size_t o1 = sizeof(int4) * tl.size(), o2 = (o1 + sizeof(int) * (N + 1) + 15) / 16 * 16;
+    MQ_CUDA(c, cudaMemcpyAsync(d, tl.data(), o1, cudaMemcpyHostToDevice, c->stream));
+    MQ_CUDA(c, cudaMemcpyAsync(d + o1, rf.data(), sizeof(int) * (N + 1), cudaMemcpyHostToDevice, c->stream));
+    MQ_CUDA(c, cudaMemcpyAsync(d + o2, &md, sizeof(MolDesc), cudaMemcpyHostToDevice, c->stream));
     MQ_CUDA(c, cudaStreamSynchronize(c->stream));  // the host vectors go out of scope
     ft.n = n;
     ft.ntiles = (int)tl.size();
     ft.d = d;
+    ft.rf_off = o1;
+    ft.mol_off = o2;
   }
-  *tiles = (const int4 *)ft.d;
-  *row_first = (const int *)(ft.d + sizeof(int4) * ft.ntiles);
-  *ntiles = ft.ntiles;
+  L.tiles = (const int4 *)ft.d;
+  L.row_first = (const int *)(ft.d + ft.rf_off);
+  L.mols = (const MolDesc *)(ft.d + ft.mol_off);
+  L.ntiles = ft.ntiles;
+  L.nmol = 1;
+  L.nmax = n;
+  L.active = nullptr;
   return MQ_OK;
 }
 
-// One digestion of the split densities with JC slabs per tile, then assembly of
-// K and G = J - f (K + K^T)/2.
-static int pair_build(mq_ctx *c, int JC, bool uhf, const float2 *DJ, const float2 *DKa, const float2 *DKb,
-                      double *d_Ga, double *d_Gb, bool timed = false) {
-  const int n = c->nao;
-  const size_t N = n, n2 = N * N;
+// One digestion of split densities with JC slabs per tile, then assembly of K
+// and G = J - f (K + K^T)/2, for all molecules of L.
+int pair_digest(mq_ctx *c, int JC, bool uhf, const PairLaunch &L, double *d_Ga, double *d_Gb, bool timed) {
+  const int n = L.nmax;
   const int T = std::min(PAIR_MAX_THREADS, (n + 31) / 32 * 32);
   const int R0 = (n + T - 1) / T;
   const int Rp = R0 <= 1 ? 1 : R0 <= 2 ? 2 : 4;
-  const int4 *tiles;
-  const int *row_first;
-  int ntiles;
-  MQ_TRY(pair_tiles(c, n, JC, &tiles, &row_first, &ntiles));
-  const int ns = uhf ? 2 : 1;
-  // J | K slices (ns * ntiles * n) | Q (ns * n^3) | K (ns * n^2)
-  double *J = (double *)buf(c, "fock_partials", sizeof(double) * (n2 + ns * (N * ntiles + N * n2 + n2)));
-  if (!J) return MQ_ENOMEM;
-  double *Kpa = J + n2, *Kpb = uhf ? Kpa + N * ntiles : nullptr;
-  double *Qa = J + n2 + ns * N * ntiles, *Qb = uhf ? Qa + N * n2 : nullptr;
-  double *Ka = J + n2 + ns * (N * ntiles + N * n2), *Kb = uhf ? Ka + n2 : nullptr;
-  const size_t smem = sizeof(float2) * N * (1 + JC) * ns;
+  const size_t smem = sizeof(float2) * (size_t)n * (1 + JC) * (uhf ? 2 : 1);
   int rc = MQ_OK;
   if (timed) c->t_fock_kernel.start(c->stream);
   switch (Rp) {
-    case 1: rc = launch_pair_jc<1>(c, JC, ntiles, T, smem, uhf, DJ, DKa, DKb, tiles, n, J, Kpa, Kpb, Qa, Qb); break;
-    case 2: rc = launch_pair_jc<2>(c, JC, ntiles, T, smem, uhf, DJ, DKa, DKb, tiles, n, J, Kpa, Kpb, Qa, Qb); break;
-    default: rc = launch_pair_jc<4>(c, JC, ntiles, T, smem, uhf, DJ, DKa, DKb, tiles, n, J, Kpa, Kpb, Qa, Qb); break;
+    case 1: rc = launch_pair_jc<1>(c, JC, L, T, smem, uhf); break;
+    case 2: rc = launch_pair_jc<2>(c, JC, L, T, smem, uhf); break;
+    default: rc = launch_pair_jc<4>(c, JC, L, T, smem, uhf); break;
   }
   MQ_TRY(rc);
   if (timed) {
@@ -378,14 +419,40 @@ static int pair_build(mq_ctx *c, int JC, bool uhf, const float2 *DJ, const float
   }
   MQ_CUDA(c, cudaGetLastError());
   const int tb = 256;
-  const unsigned gb = (unsigned)((n2 + tb - 1) / tb);
-  fock_pair_assemble_kernel<<<gb, tb, 0, c->stream>>>(Kpa, Qa, row_first, n, Ka);
-  if (uhf) fock_pair_assemble_kernel<<<gb, tb, 0, c->stream>>>(Kpb, Qb, row_first, n, Kb);
-  fock_combine_kernel<<<gb, tb, 0, c->stream>>>(J, Ka, 1, n, uhf ? 1.0 : 0.5, d_Ga);
-  if (uhf) fock_combine_kernel<<<gb, tb, 0, c->stream>>>(J, Kb, 1, n, 1.0, d_Gb);
+  const dim3 gb((unsigned)(((size_t)n * n + tb - 1) / tb), (unsigned)L.nmol);
+  fock_pair_assemble_kernel<<<gb, tb, 0, c->stream>>>(L.Kpa, L.Qa, L.row_first, L.mols, L.active, L.nmax, L.Ka);
+  if (uhf)
+    fock_pair_assemble_kernel<<<gb, tb, 0, c->stream>>>(L.Kpb, L.Qb, L.row_first, L.mols, L.active, L.nmax, L.Kb);
+  fock_pair_combine_kernel<<<gb, tb, 0, c->stream>>>(L.J, L.Ka, L.mols, L.active, uhf ? 1.0 : 0.5, d_Ga);
+  if (uhf) fock_pair_combine_kernel<<<gb, tb, 0, c->stream>>>(L.J, L.Kb, L.mols, L.active, 1.0, d_Gb);
   c->stats.launches += uhf ? 5 : 3;
   MQ_CUDA(c, cudaGetLastError());
   return MQ_OK;
+}
+
+// Scratch of the single system: J | K slices | Q | K.
+static int pair_build(mq_ctx *c, int JC, bool uhf, const float2 *DJ, const float2 *DKa, const float2 *DKb,
+                      double *d_Ga, double *d_Gb, bool timed = false) {
+  const int n = c->nao;
+  const size_t N = n, n2 = N * N;
+  PairLaunch L{};
+  MQ_TRY(pair_tiles(c, n, JC, L));
+  const int ns = uhf ? 2 : 1;
+  const size_t nt = L.ntiles;
+  double *J = (double *)buf(c, "fock_partials", sizeof(double) * (n2 + ns * (N * nt + N * n2 + n2)));
+  if (!J) return MQ_ENOMEM;
+  L.XX = c->d_XX;
+  L.DJ = DJ;
+  L.DKa = DKa;
+  L.DKb = DKb;
+  L.J = J;
+  L.Kpa = J + n2;
+  L.Kpb = uhf ? L.Kpa + N * nt : nullptr;
+  L.Qa = J + n2 + ns * N * nt;
+  L.Qb = uhf ? L.Qa + N * n2 : nullptr;
+  L.Ka = J + n2 + ns * (N * nt + N * n2);
+  L.Kb = uhf ? L.Ka + n2 : nullptr;
+  return pair_digest(c, JC, uhf, L, d_Ga, d_Gb, timed);
 }
 
 // Autotuner for the tile length JC: on the first build for a given (n, RHF or

@@ -15,6 +15,7 @@ struct Int1eArgs {
   int nnuc, n, mode;
   int pOff, np;
   double *S, *H;
+  const MolDesc *mols;  // batch: per-pair molecule gives n, nuclei and matrix offset (null: one system)
 };
 
 // Hermite coefficients E^{ij}_t of one axis for i <= 1, j <= 3 (kinetic needs
@@ -49,6 +50,18 @@ __global__ void __launch_bounds__(128) int1e_kernel(Int1eArgs g) {
   if (idx >= g.np) return;
   const int P = g.pOff + idx;
   const PairTable &t = g.t;
+  const double *nuc = g.nuc;
+  int nnuc = g.nnuc;
+  size_t n = g.n;
+  double *Sout = g.S, *Hout = g.H;
+  if (g.mols) {
+    const MolDesc md = g.mols[t.mol[P]];
+    nuc += 4 * md.nuc_off;
+    nnuc = md.nnuc;
+    n = md.n;
+    Sout += md.mat;
+    Hout += md.mat;
+  }
   const bool parity = g.mode == MQ_MODE_REFERENCE;
   const double pi = parity ? PI_REF : PI_TRUE;
   double s[NA][NB], h[NA][NB];
@@ -76,12 +89,12 @@ __global__ void __launch_bounds__(128) int1e_kernel(Int1eArgs g) {
       for (int y = 0; y <= L; ++y)
 #pragma unroll
         for (int z = 0; z <= L; ++z) V[x][y][z] = 0.0;
-    for (int cn = 0; cn < g.nnuc; ++cn) {
-      const double X = Px - g.nuc[4 * cn], Y = Py - g.nuc[4 * cn + 1], Z = Pz - g.nuc[4 * cn + 2];
+    for (int cn = 0; cn < nnuc; ++cn) {
+      const double X = Px - nuc[4 * cn], Y = Py - nuc[4 * cn + 1], Z = Pz - nuc[4 * cn + 2];
       const double T = p * (X * X + Y * Y + Z * Z);
       double F[L + 1];
       boys<QREF, L>(g.mode, T, g.boys, F);
-      const double w = -g.nuc[4 * cn + 3] * 2.0 * pi / p;
+      const double w = -nuc[4 * cn + 3] * 2.0 * pi / p;
       // R recursion (auxilary.f90:22-80) with alpha = p
       double Rj[L + 1][L + 1][L + 1][L + 1];
       double pw = 1.0;
@@ -146,18 +159,45 @@ __global__ void __launch_bounds__(128) int1e_kernel(Int1eArgs g) {
       }
   }
   const int A = t.shA[P], B = t.shB[P], i0 = t.aoA[P], j0 = t.aoB[P];
-  const size_t n = g.n;
 #pragma unroll
   for (int a = 0; a < NA; ++a)
 #pragma unroll
     for (int b = 0; b < NB; ++b) {
       const int i = i0 + a, j = j0 + b;
       if (A == B && i < j) continue;
-      g.S[i + n * j] = s[a][b];
-      g.S[j + n * i] = s[a][b];
-      g.H[i + n * j] = h[a][b];
-      g.H[j + n * i] = h[a][b];
+      Sout[i + n * j] = s[a][b];
+      Sout[j + n * i] = s[a][b];
+      Hout[i + n * j] = h[a][b];
+      Hout[j + n * i] = h[a][b];
     }
+}
+
+// Batch: S and H of every molecule of the batch table into the packed n x n
+// arrays (offset MolDesc::mat), one launch per pair class for all molecules.
+int int1e_batch_device(mq_ctx *c, const PairTable &t, const double *d_nuc, const MolDesc *d_mols, size_t mat_total,
+                       double *d_S, double *d_H) {
+  MQ_CUDA(c, cudaMemsetAsync(d_S, 0, mat_total * sizeof(double), c->stream));
+  MQ_CUDA(c, cudaMemsetAsync(d_H, 0, mat_total * sizeof(double), c->stream));
+  Int1eArgs g{};
+  g.t = t;
+  g.boys = c->d_boys;
+  g.nuc = d_nuc;
+  g.mode = MQ_MODE_TIGHT;
+  g.S = d_S;
+  g.H = d_H;
+  g.mols = d_mols;
+  for (int cl = 0; cl < 3; ++cl) {
+    g.pOff = t.class_off[cl];
+    g.np = t.class_off[cl + 1] - g.pOff;
+    if (!g.np) continue;
+    dim3 grid((g.np + 127) / 128);
+    if (cl == 0) int1e_kernel<0, 0><<<grid, 128, 0, c->stream>>>(g);
+    else if (cl == 1) int1e_kernel<1, 0><<<grid, 128, 0, c->stream>>>(g);
+    else int1e_kernel<1, 1><<<grid, 128, 0, c->stream>>>(g);
+    c->stats.launches += 1;
+    MQ_CUDA(c, cudaGetLastError());
+  }
+  return MQ_OK;
 }
 
 int int1e_device(mq_ctx *c, double *d_S, double *d_H) {

@@ -38,11 +38,29 @@ struct PairTable {
   int class_off[4];      // pair index ranges per class: [0]=ss, [1]=(sp,s), [2]=(sp,sp), [3]=end
   int *shA, *shB;        // shells of each pair (type(A) >= type(B))
   int *pp_off;           // primitive-pair offset, npairs+1
-  int *aoA, *aoB;        // first AO of A and B
+  int *aoA, *aoB;        // first AO of A and B (within the pair's molecule)
+  int *mol;              // molecule of each pair (0 for a single system)
   double *schwarz;       // sqrt(max |(ab|ab)|) per pair
   // primitive pairs
   int npp;
   double *p, *inv2p, *beta, *Px, *Py, *Pz, *PAx, *PAy, *PAz, *PBx, *PBy, *PBz, *K, *c4;  // c4: 4 per pp
+};
+
+// Host copy of a pair table (same fields as PairTable), built per molecule
+// and concatenated for batches.
+struct HostPairs {
+  int class_off[4] = {0, 0, 0, 0};
+  std::vector<int> shA, shB, off, aoA, aoB, mol;
+  std::vector<double> p, inv2p, beta, Px, Py, Pz, PAx, PAy, PAz, PBx, PBy, PBz, K, c4;
+};
+
+// One molecule added to a batch: host pair table, nuclei (x, y, z, Z) and
+// closed-shell occupation.
+struct BatchMol {
+  int n = 0, nocc = 0, nnuc = 0;
+  double enuc = 0.0;
+  HostPairs pairs;
+  std::vector<double> nuc;
 };
 
 struct DeviceBuf {
@@ -55,7 +73,18 @@ struct DeviceBuf {
 // device tile table of the pair-slab Fock kernel for one tile length
 struct FockTiles {
   int n = 0, ntiles = 0;
-  char *d = nullptr;  // int4 tiles[ntiles] then int row_first[n + 1], in a named context buffer
+  char *d = nullptr;  // int4 tiles[ntiles], int row_first[n + 1], MolDesc, in a named context buffer
+  size_t rf_off = 0, mol_off = 0;
+};
+
+// One molecule of a (possibly one-molecule) batch as device kernels see it:
+// its order and occupation, its nuclei in the packed nuclear table, and the
+// offsets (in elements) of its XX (n^4), n x n matrices, n-vectors, Q (n^3)
+// and Fock row table in the packed batch arrays.
+struct MolDesc {
+  int n, nocc, nnuc, nuc_off;
+  long long xx, mat, vec, q;
+  int row_first, pad;
 };
 
 struct Stats {
@@ -63,6 +92,7 @@ struct Stats {
   double fock_calls = 0, diag_calls = 0, scf_iters = 0, purify_steps = 0, fock_jc = 0, tune_fock_ms = 0;
   double launches = 0, lib_launches = 0, quartets = 0, prim_quartets = 0;
   double ms_fock_kernel = 0, fock_kernel_launches = 0;  // the digestion kernel alone, last SCF or mq_fock
+  double graph_launches = 0;  // CUDA-graph replays of the last batch SCF
 };
 
 // Event pair on the context's stream that adds its elapsed time to a counter
@@ -117,6 +147,10 @@ struct mq_ctx {
   mq::PairTable pt{};
   std::vector<void *> pair_allocs;
   double *d_XX = nullptr;    // n^4 full integral array
+  // batch of independent closed-shell molecules (mq_batch_*)
+  std::vector<mq::BatchMol> bmols;
+  std::vector<void *> batch_allocs;  // batch pair table
+  double *d_boys_tight = nullptr;    // the tight Boys table, for batches
   mq::StageTimer t_fock_kernel;  // the digestion kernel alone, collected at the caller's sync points
   mq::FockTiles fock_tiles[9];  // pair-slab tile tables, indexed by slabs per tile
   int fock_jc_rhf = 0, fock_jc_rhf_n = 0, fock_jc_uhf = 0, fock_jc_uhf_n = 0;  // autotuned tile lengths
@@ -140,10 +174,42 @@ void *buf(mq_ctx *c, const char *name, size_t bytes);
 // the first failing stage by `label` (a diagnostic; off by default).
 int sync_check(mq_ctx *c, const char *label);
 
+// batched kernels (int1e.cu, eri.cu, fock.cu)
+int int1e_batch_device(mq_ctx *c, const PairTable &t, const double *d_nuc, const MolDesc *d_mols, size_t mat_total,
+                       double *d_S, double *d_H);
+int eri_batch_device(mq_ctx *c, const PairTable &t, const MolDesc *d_mols, int nmol, const int *d_pstart,
+                     const int *d_pcount, const long long *const d_mq_off[6], const long long total[6], double *d_XX,
+                     size_t xx_total);
+void pair_tiles_host(int n, int JC, int mol, std::vector<int4> &tl, std::vector<int> &rf);
+// Everything one pair-slab Fock launch needs; `nmax` is the largest order among
+// the molecules (thread count, shared memory, K-slice stride).
+struct PairLaunch {
+  const double *XX;
+  const float2 *DJ, *DKa, *DKb;
+  const int4 *tiles;
+  const int *row_first;
+  const MolDesc *mols;
+  const int *active;
+  int ntiles, nmol, nmax;
+  double *J, *Kpa, *Kpb, *Qa, *Qb, *Ka, *Kb;
+};
+int pair_digest(mq_ctx *c, int JC, bool uhf, const PairLaunch &L, double *d_Ga, double *d_Gb, bool timed);
+// densities as hi/lo float pairs: DJ from Da (+ Db), DKa from Da, DKb from Db
+int split_density(mq_ctx *c, const double *Da, const double *Db, size_t n2, float2 *DJ, float2 *DKa, float2 *DKb);
+// batch.cu
+int batch_clear(mq_ctx *c);
+int batch_add(mq_ctx *c, int nnuc, const int *Z, const double *xyz, const double *bas, const double *set,
+              const int *basinfo, const int *setinfo, int nocc);
+int batch_scf(mq_ctx *c, const mq_batch_opts *o, double *energy, int *iters, int *converged, double *D_out,
+              double *eps_out);
+
 // basis.cu
 int build_shells(mq_ctx *c, int nnuc, const int *Z, const double *xyz, const double *bas, const double *set,
                  const int *basinfo, const int *setinfo);
 int build_pairs(mq_ctx *c);
+void pairs_host(const std::vector<HostShell> &shells, const std::vector<double> &xyz, HostPairs &h);
+void append_pairs_class(HostPairs &dst, const HostPairs &src, int cl, int mol);
+int upload_pairs(mq_ctx *c, const HostPairs &h, std::vector<void *> &allocs, PairTable &t);
 void free_pairs(mq_ctx *c);
 void tight_boys_table(std::vector<double> &tab);  // TIGHT_NT x TIGHT_NM, row-major [T][m]
 

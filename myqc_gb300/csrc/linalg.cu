@@ -13,27 +13,11 @@
 #include <cublas_v2.h>
 
 #include "internal.h"
+#include "jacobi.cuh"
 
 namespace mq {
 
 constexpr int JAC_THREADS = 512;
-
-__device__ __forceinline__ void rr_pair(int np, int r, int k, int &p, int &q) {
-  // circle method: player 0 fixed, players 1..np-1 rotate
-  const int m = np - 1;
-  if (k == 0) {
-    p = 0;
-    q = 1 + (r % m);
-  } else {
-    p = 1 + (r + k) % m;
-    q = 1 + (r - k + m) % m;
-  }
-  if (p > q) {
-    int t = p;
-    p = q;
-    q = t;
-  }
-}
 
 template <bool SMEM>
 __global__ void __launch_bounds__(JAC_THREADS) jacobi_kernel(int n, double *__restrict__ Ag, double *__restrict__ wg,
@@ -53,120 +37,12 @@ __global__ void __launch_bounds__(JAC_THREADS) jacobi_kernel(int n, double *__re
   }
   __shared__ double cs[2 * 512];  // (c, s) per pair of a round, n <= 1024
   __shared__ double red[JAC_THREADS / 32];
-  __shared__ int done;
-  const int tid = threadIdx.x;
-  for (size_t idx = tid; idx < n2; idx += blockDim.x) {
-    A[idx] = Ain[idx];
-    V[idx] = (idx % (n + 1) == 0) ? 1.0 : 0.0;
-  }
+  __shared__ int flag;
+  for (size_t idx = threadIdx.x; idx < n2; idx += blockDim.x) A[idx] = Ain[idx];
   __syncthreads();
-  // ||A||_F for the stopping rule
-  double fro = 0.0;
-  for (size_t idx = tid; idx < n2; idx += blockDim.x) fro += A[idx] * A[idx];
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) fro += __shfl_xor_sync(0xffffffffu, fro, o);
-  if ((tid & 31) == 0) red[tid >> 5] = fro;
-  __syncthreads();
-  if (tid == 0) {
-    double t = 0;
-    for (int w = 0; w < JAC_THREADS / 32; ++w) t += red[w];
-    red[0] = t;
-    done = 0;
-  }
-  __syncthreads();
-  const double stop2 = tol * tol * red[0];
-  __syncthreads();
-  const int np = n + (n & 1), half = np / 2;
-  int sweep = 0;
-  for (; sweep < max_sweeps; ++sweep) {
-    // off-diagonal norm
-    double off = 0.0;
-    for (size_t idx = tid; idx < n2; idx += blockDim.x) {
-      const int i = (int)(idx % n), j = (int)(idx / n);
-      if (i != j) off += A[idx] * A[idx];
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) off += __shfl_xor_sync(0xffffffffu, off, o);
-    __syncthreads();
-    if ((tid & 31) == 0) red[tid >> 5] = off;
-    __syncthreads();
-    if (tid == 0) {
-      double t = 0;
-      for (int w = 0; w < JAC_THREADS / 32; ++w) t += red[w];
-      done = (t <= stop2);
-    }
-    __syncthreads();
-    if (done) break;
-    for (int r = 0; r < np - 1; ++r) {
-      // 1) rotation angles
-      for (int k = tid; k < half; k += blockDim.x) {
-        int p, q;
-        rr_pair(np, r, k, p, q);
-        double c = 1.0, s = 0.0;
-        if (q < n) {
-          const double apq = A[p + (size_t)n * q];
-          const double app = A[p + (size_t)n * p], aqq = A[q + (size_t)n * q];
-          if (fabs(apq) > 0x1p-60 * (fabs(app) + fabs(aqq))) {  // negligible rotations are skipped
-            const double theta = (aqq - app) / (2.0 * apq);
-            const double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
-            c = rsqrt(t * t + 1.0);
-            s = t * c;
-          }
-        }
-        cs[2 * k] = c;
-        cs[2 * k + 1] = s;
-      }
-      __syncthreads();
-      // 2) rows p, q of A:  A <- J^T A
-      for (int idx = tid; idx < half * n; idx += blockDim.x) {
-        const int k = idx / n, j = idx % n;
-        int p, q;
-        rr_pair(np, r, k, p, q);
-        if (q >= n) continue;
-        const double c = cs[2 * k], s = cs[2 * k + 1];
-        if (s == 0.0) continue;
-        const double ap = A[p + (size_t)n * j], aq = A[q + (size_t)n * j];
-        A[p + (size_t)n * j] = c * ap - s * aq;
-        A[q + (size_t)n * j] = s * ap + c * aq;
-      }
-      __syncthreads();
-      // 3) columns p, q of A and V:  A <- A J, V <- V J
-      for (int idx = tid; idx < half * n; idx += blockDim.x) {
-        const int k = idx / n, i = idx % n;
-        int p, q;
-        rr_pair(np, r, k, p, q);
-        if (q >= n) continue;
-        const double c = cs[2 * k], s = cs[2 * k + 1];
-        if (s == 0.0) continue;
-        double *ap = A + (size_t)n * p, *aq = A + (size_t)n * q;
-        const double x = ap[i], y = aq[i];
-        ap[i] = c * x - s * y;
-        aq[i] = s * x + c * y;
-        double *vp = V + (size_t)n * p, *vq = V + (size_t)n * q;
-        const double vx = vp[i], vy = vq[i];
-        vp[i] = c * vx - s * vy;
-        vq[i] = s * vx + c * vy;
-      }
-      __syncthreads();
-    }
-  }
-  if (tid == 0 && sweep >= max_sweeps) atomicExch(status, 1);
-  // sort ascending: rank of each eigenvalue, ties broken by index
-  for (int i = tid; i < n; i += blockDim.x) {
-    const double wi = A[i + (size_t)n * i];
-    int rank = 0;
-    for (int j = 0; j < n; ++j) {
-      const double wj = A[j + (size_t)n * j];
-      rank += (wj < wi) || (wj == wi && j < i);
-    }
-    wg[(size_t)n * b + rank] = wi;
-    // eigenvector i -> column rank, sign fixed so the largest component is positive
-    double big = 0.0;
-    for (int k = 0; k < n; ++k)
-      if (fabs(V[k + (size_t)n * i]) > fabs(big)) big = V[k + (size_t)n * i];
-    const double sg = big < 0 ? -1.0 : 1.0;
-    for (int k = 0; k < n; ++k) Vg[n2 * b + k + (size_t)n * rank] = sg * V[k + (size_t)n * i];
-  }
+  const bool ok = jacobi_block(n, A, V, cs, red, &flag, max_sweeps, tol);
+  if (threadIdx.x == 0 && !ok) atomicExch(status, 1);
+  jacobi_sorted_out(n, A, V, wg + (size_t)n * b, Vg + n2 * b);
 }
 
 // ---------------------------------------------------------------------------

@@ -74,6 +74,61 @@ class Context:
         self.n = n.value
         self.sys = sysm
 
+    # ---------------------------------------------------------------- batches
+    def batch_clear(self):
+        self._check(self.L.mq_batch_clear(self.h))
+
+    def batch_add(self, sysm: System, basis: BasisArrays):
+        """Append one closed-shell molecule (nelcA doubly occupied orbitals)."""
+        if sysm.nelcA != sysm.nelcB:
+            raise ValueError("batches hold closed-shell molecules")
+        Z = np.ascontiguousarray(sysm.atoms, dtype=np.int32)
+        xyz = f64(np.asarray(sysm.xyz).reshape(-1, 3))
+        k = (Z, xyz, np.ascontiguousarray(basis.bas, dtype=np.float64),
+             np.ascontiguousarray(basis.set, dtype=np.float64), np.ascontiguousarray(basis.basinfo, dtype=np.int32),
+             np.ascontiguousarray(basis.setinfo, dtype=np.int32))
+        self._check(self.L.mq_batch_add(self.h, len(Z), ptr(k[0]), ptr(k[1]), ptr(k[2]), ptr(k[3]), ptr(k[4]),
+                                        ptr(k[5]), sysm.nelcA))
+
+    def batch_sizes(self) -> np.ndarray:
+        nm = ctypes.c_int()
+        self._check(self.L.mq_batch_info(self.h, ctypes.byref(nm), None))
+        out = np.zeros(nm.value, dtype=np.int32)
+        self._check(self.L.mq_batch_info(self.h, ctypes.byref(nm), ptr(out)))
+        return out
+
+    def batch_scf(self, conv: float = 1e-7, conv_rms: bool = False, diis: int = 0, max_iter: int = 0,
+                  graph: bool = True, check_every: int = 4, D_guess=None):
+        """Solve the batch.  D_guess: list of n x n arrays (None entries take the
+        core guess).  Returns dict with energy, iterations, converged, D, eps
+        (lists of per-molecule arrays)."""
+        sizes = self.batch_sizes()
+        M = len(sizes)
+        mat = np.concatenate([[0], np.cumsum(sizes.astype(np.int64) ** 2)])
+        vec = np.concatenate([[0], np.cumsum(sizes.astype(np.int64))])
+        o = _lib.BatchOpts()
+        o.max_iter, o.conv, o.conv_rms, o.diis = max_iter, conv, int(conv_rms), diis
+        o.graph, o.check_every = int(graph), check_every
+        keep = None
+        if D_guess is not None:
+            keep = np.empty(int(mat[-1]))
+            for m in range(M):
+                g = D_guess[m]
+                if g is None:
+                    keep[mat[m]] = np.nan
+                else:
+                    keep[mat[m]:mat[m + 1]] = np.asarray(g, dtype=np.float64).reshape(-1, order="F")
+            o.D_in = keep.ctypes.data
+        E = np.zeros(M)
+        it = np.zeros(M, dtype=np.int32)
+        cv = np.zeros(M, dtype=np.int32)
+        D = np.zeros(int(mat[-1]))
+        eps = np.zeros(int(vec[-1]))
+        self._check(self.L.mq_batch_scf(self.h, ctypes.byref(o), ptr(E), ptr(it), ptr(cv), ptr(D), ptr(eps)))
+        Ds = [D[mat[m]:mat[m + 1]].reshape(sizes[m], sizes[m], order="F") for m in range(M)]
+        es = [eps[vec[m]:vec[m + 1]].copy() for m in range(M)]
+        return {"energy": E, "iterations": it, "converged": cv.astype(bool), "D": Ds, "eps": es}
+
     def set_schwarz(self, thr: float):
         self._check(self.L.mq_set_schwarz(self.h, thr))
 
