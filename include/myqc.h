@@ -231,6 +231,24 @@ int mq_batch_info(const mq_ctx *ctx, int *nmol, int *norb);
 int mq_batch_scf(mq_ctx *ctx, const mq_batch_opts *opts, double *energy, int *iters, int *converged, double *D,
                  double *eps);
 
+/* ---- The learned density guess's network (no reference counterpart).  A
+ * 3-layer MLP nin -> width -> width -> nout with SiLU activations, BF16
+ * weights and activations and FP32 accumulation on the tensor cores, trained
+ * by Adam on the device.  One network per context.  Parameters are packed as
+ * FP32: W1 [width][nin], b1, W2 [width][width], b2, W3 [nout][width], b3.
+ * Rows of X (nin floats), T and W (nout floats) are samples. */
+int mq_mlp_init(mq_ctx *ctx, int nin, int width, int nout); /* width, nout <= 256; nin % 8 == 0 */
+int mq_mlp_param_count(mq_ctx *ctx, int *n);
+int mq_mlp_set_params(mq_ctx *ctx, const float *params);   /* also resets the Adam moments */
+int mq_mlp_get_params(mq_ctx *ctx, float *params);
+int mq_mlp_forward(mq_ctx *ctx, int rows, const float *X, float *Y);
+/* Loss sum W (Y - T)^2 / sum W over the rows and its gradient (packed like the parameters). */
+int mq_mlp_grad(mq_ctx *ctx, int rows, const float *X, const float *T, const float *W, float *grads, double *loss);
+/* Training set kept on the device, then one epoch of Adam minibatches in the order perm (a
+ * permutation of 0..n-1); batch a multiple of 128; mean minibatch loss to *loss. */
+int mq_mlp_set_data(mq_ctx *ctx, long long n, const float *X, const float *T, const float *W);
+int mq_mlp_train_epoch(mq_ctx *ctx, const int *perm, int batch, float lr, double *loss);
+
 /* Profiling counters.  Device milliseconds (CUDA events on the context's
  * stream) of the last call of each stage: "eri", "ao2mo", "mp2", "scf" (whole
  * SCF), "fock" and "diag" (summed over the last SCF's iterations; "diag" is

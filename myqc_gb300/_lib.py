@@ -83,6 +83,14 @@ def lib(path: str | None = None):
     L.mq_syev_batched.argtypes = [vp, c_int, c_int, dp, dp, dp]
     L.mq_sygv.argtypes = [vp, c_int, dp, dp, dp, dp]
     L.mq_stat.argtypes = [vp, ctypes.c_char_p, ctypes.POINTER(c_double)]
+    L.mq_mlp_init.argtypes = [vp, c_int, c_int, c_int]
+    L.mq_mlp_param_count.argtypes = [vp, ip]
+    L.mq_mlp_set_params.argtypes = [vp, vp]
+    L.mq_mlp_get_params.argtypes = [vp, vp]
+    L.mq_mlp_forward.argtypes = [vp, c_int, vp, vp]
+    L.mq_mlp_grad.argtypes = [vp, c_int, vp, vp, vp, vp, ctypes.POINTER(c_double)]
+    L.mq_mlp_set_data.argtypes = [vp, ctypes.c_longlong, vp, vp, vp]
+    L.mq_mlp_train_epoch.argtypes = [vp, vp, c_int, ctypes.c_float, ctypes.POINTER(c_double)]
     L.mq_batch_clear.argtypes = [vp]
     L.mq_batch_add.argtypes = [vp, c_int, vp, vp, vp, vp, vp, vp, c_int]
     L.mq_batch_info.argtypes = [vp, ip, vp]

@@ -124,6 +124,7 @@ int mq_free(mq_ctx *c) {
   cudaStreamSynchronize(c->stream);
   free_pairs(c);
   batch_clear(c);
+  mlp_free(c);
   if (c->d_boys_tight) cudaFree(c->d_boys_tight);
   for (auto &kv : c->bufs)
     if (kv.second.ptr) cudaFree(kv.second.ptr);
@@ -468,6 +469,55 @@ int mq_batch_scf(mq_ctx *c, const mq_batch_opts *o, double *energy, int *iters, 
   if (!o || !energy) return set_err(c, MQ_EINVAL, "null argument");
   cudaSetDevice(c->device);
   return batch_scf(c, o, energy, iters, converged, D, eps);
+}
+
+int mq_mlp_init(mq_ctx *c, int nin, int width, int nout) {
+  if (!c) return MQ_EINVAL;
+  cudaSetDevice(c->device);
+  return mlp_init(c, nin, width, nout);
+}
+
+int mq_mlp_param_count(mq_ctx *c, int *n) {
+  if (!c || !n) return MQ_EINVAL;
+  if (!c->mlp) return set_err(c, MQ_ESTATE, "no MLP (mq_mlp_init)");
+  *n = mlp_param_count(c);
+  return MQ_OK;
+}
+
+int mq_mlp_set_params(mq_ctx *c, const float *params) {
+  if (!c || !params) return MQ_EINVAL;
+  cudaSetDevice(c->device);
+  return mlp_set_params(c, params);
+}
+
+int mq_mlp_get_params(mq_ctx *c, float *params) {
+  if (!c || !params) return MQ_EINVAL;
+  cudaSetDevice(c->device);
+  return mlp_get_params(c, params);
+}
+
+int mq_mlp_forward(mq_ctx *c, int rows, const float *X, float *Y) {
+  if (!c || rows < 0 || (rows && (!X || !Y))) return MQ_EINVAL;
+  cudaSetDevice(c->device);
+  return mlp_forward(c, rows, X, Y);
+}
+
+int mq_mlp_grad(mq_ctx *c, int rows, const float *X, const float *T, const float *W, float *grads, double *loss) {
+  if (!c || rows <= 0 || !X || !T || !W || !grads || !loss) return MQ_EINVAL;
+  cudaSetDevice(c->device);
+  return mlp_grad(c, rows, X, T, W, grads, loss);
+}
+
+int mq_mlp_set_data(mq_ctx *c, long long n, const float *X, const float *T, const float *W) {
+  if (!c || n <= 0 || !X || !T || !W) return MQ_EINVAL;
+  cudaSetDevice(c->device);
+  return mlp_set_data(c, n, X, T, W);
+}
+
+int mq_mlp_train_epoch(mq_ctx *c, const int *perm, int batch, float lr, double *loss) {
+  if (!c || !perm || !loss) return MQ_EINVAL;
+  cudaSetDevice(c->device);
+  return mlp_train_epoch(c, perm, batch, lr, loss);
 }
 
 int mq_stat(const mq_ctx *c, const char *key, double *value) {

@@ -151,6 +151,7 @@ struct mq_ctx {
   std::vector<mq::BatchMol> bmols;
   std::vector<void *> batch_allocs;  // batch pair table
   double *d_boys_tight = nullptr;    // the tight Boys table, for batches
+  void *mlp = nullptr;               // the learned guess's network (mlp.cu)
   mq::StageTimer t_fock_kernel;  // the digestion kernel alone, collected at the caller's sync points
   mq::FockTiles fock_tiles[9];  // pair-slab tile tables, indexed by slabs per tile
   int fock_jc_rhf = 0, fock_jc_rhf_n = 0, fock_jc_uhf = 0, fock_jc_uhf_n = 0;  // autotuned tile lengths
@@ -196,6 +197,16 @@ struct PairLaunch {
 int pair_digest(mq_ctx *c, int JC, bool uhf, const PairLaunch &L, double *d_Ga, double *d_Gb, bool timed);
 // densities as hi/lo float pairs: DJ from Da (+ Db), DKa from Da, DKb from Db
 int split_density(mq_ctx *c, const double *Da, const double *Db, size_t n2, float2 *DJ, float2 *DKa, float2 *DKb);
+// mlp.cu
+int mlp_init(mq_ctx *c, int nin, int width, int nout);
+int mlp_param_count(mq_ctx *c);
+int mlp_set_params(mq_ctx *c, const float *h);
+int mlp_get_params(mq_ctx *c, float *h);
+int mlp_forward(mq_ctx *c, int rows, const float *X, float *Y);
+int mlp_grad(mq_ctx *c, int rows, const float *X, const float *T, const float *Wl, float *grads, double *loss);
+int mlp_set_data(mq_ctx *c, long long n, const float *X, const float *T, const float *Wl);
+int mlp_train_epoch(mq_ctx *c, const int *perm, int batch, float lr, double *loss);
+void mlp_free(mq_ctx *c);
 // batch.cu
 int batch_clear(mq_ctx *c);
 int batch_add(mq_ctx *c, int nnuc, const int *Z, const double *xyz, const double *bas, const double *set,

@@ -129,6 +129,49 @@ class Context:
         es = [eps[vec[m]:vec[m + 1]].copy() for m in range(M)]
         return {"energy": E, "iterations": it, "converged": cv.astype(bool), "D": Ds, "eps": es}
 
+    # ---------------------------------------------------------------- learned-guess network
+    def mlp_init(self, nin: int, width: int, nout: int):
+        self._check(self.L.mq_mlp_init(self.h, nin, width, nout))
+        self.mlp_dims = (nin, width, width, nout)
+
+    def mlp_param_count(self) -> int:
+        n = ctypes.c_int()
+        self._check(self.L.mq_mlp_param_count(self.h, ctypes.byref(n)))
+        return n.value
+
+    def mlp_set_params(self, params):
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        self._check(self.L.mq_mlp_set_params(self.h, ptr(p)))
+
+    def mlp_get_params(self) -> np.ndarray:
+        p = np.zeros(self.mlp_param_count(), dtype=np.float32)
+        self._check(self.L.mq_mlp_get_params(self.h, ptr(p)))
+        return p
+
+    def mlp_forward(self, X) -> np.ndarray:
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        Y = np.zeros((X.shape[0], self.mlp_dims[3]), dtype=np.float32)
+        self._check(self.L.mq_mlp_forward(self.h, X.shape[0], ptr(X), ptr(Y)))
+        return Y
+
+    def mlp_grad(self, X, T, W):
+        X, T, W = (np.ascontiguousarray(a, dtype=np.float32) for a in (X, T, W))
+        g = np.zeros(self.mlp_param_count(), dtype=np.float32)
+        loss = ctypes.c_double()
+        self._check(self.L.mq_mlp_grad(self.h, X.shape[0], ptr(X), ptr(T), ptr(W), ptr(g), ctypes.byref(loss)))
+        return loss.value, g
+
+    def mlp_set_data(self, X, T, W):
+        X, T, W = (np.ascontiguousarray(a, dtype=np.float32) for a in (X, T, W))
+        self._check(self.L.mq_mlp_set_data(self.h, X.shape[0], ptr(X), ptr(T), ptr(W)))
+        self._mlp_n = X.shape[0]
+
+    def mlp_train_epoch(self, batch: int, lr: float, seed: int) -> float:
+        perm = np.random.default_rng(seed).permutation(self._mlp_n).astype(np.int32)
+        loss = ctypes.c_double()
+        self._check(self.L.mq_mlp_train_epoch(self.h, ptr(perm), batch, ctypes.c_float(lr), ctypes.byref(loss)))
+        return loss.value
+
     def set_schwarz(self, thr: float):
         self._check(self.L.mq_set_schwarz(self.h, thr))
 

@@ -85,3 +85,33 @@ def test_mp2_sum_identity(ftab, basis_text):
     D = e[:no, None, None, None] - e[None, no:, None, None] + e[None, None, :no, None] - e[None, None, None, no:]
     E = np.sum(Om * (2 * Om - Om.transpose(0, 3, 2, 1)) / D)
     assert abs(E - r["mp2"]["E_MP2"]) < 1e-12
+
+
+def test_mlp_oracle_gradient_finite_differences():
+    """The MLP oracle's analytic gradient (float64, no BF16 rounding) against
+    central differences."""
+    import mlp_ref as M
+    dims = (16, 12, 12, 5)
+    p = M.init_params(dims, 3)
+    rng = np.random.default_rng(4)
+    X = rng.standard_normal((40, dims[0]))
+    T = rng.standard_normal((40, dims[3]))
+    Wl = rng.random((40, dims[3]))
+    _, g = M.loss_grad(p, dims, X, T, Wl, bf=False)
+    idx = rng.choice(len(p), 30, replace=False)
+    h = 1e-6
+    for i in idx:
+        e = np.zeros_like(p)
+        e[i] = h
+        lp, _ = M.loss_grad(p + e, dims, X, T, Wl, bf=False)
+        lm, _ = M.loss_grad(p - e, dims, X, T, Wl, bf=False)
+        assert abs((lp - lm) / (2 * h) - g[i]) < 1e-6 * max(1.0, abs(g[i]))
+
+
+def test_bf16_rounding():
+    import mlp_ref as M
+    x = np.array([1.0, 1.0 + 2 ** -8, 1.0 + 3 * 2 ** -9, -3.14159, 0.0])
+    r = M.bf16(x)
+    assert r[0] == 1.0 and r[1] == 1.0  # halfway between 1 and 1 + 2^-7: ties to even
+    assert r[2] == 1.0 + 2 ** -7  # 1.5 BF16 ulp above 1 rounds up to the even neighbour
+    assert abs(r[3] + 3.140625) < 1e-12 and r[4] == 0.0
