@@ -53,7 +53,11 @@ class ClockSampler:
     def __init__(self, gpu: int):
         self.gpu = gpu
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_bench_{os.getpid()}.csv")
+        # raw samples go to MYQC_CLOCKS_DIR (default: the system temp folder); the
+        # summary is part of the JSON line
+        import tempfile
+        folder = os.environ.get("MYQC_CLOCKS_DIR", tempfile.gettempdir())
+        self.path = os.path.join(folder, f"clocks_bench_{os.getpid()}.csv")
 
     def __enter__(self):
         try:
@@ -99,18 +103,43 @@ def load_workload(seed: int):
     return sysm, basis
 
 
+MODEL = os.path.join(ROOT, "myqc_gb300", "data", "guess_mlp.npz")
+SCHWARZ = 1e-12  # fast arm: contracted quartets with a Schwarz bound below this are skipped
+_learned = {}
+
+
+def learned_guess(ctx):
+    """The trained density-guess network on this context (None without a model file)."""
+    if id(ctx) not in _learned:
+        from myqc_gb300 import guess
+        _learned[id(ctx)] = guess.LearnedGuess(ctx, MODEL) if os.path.exists(MODEL) else None
+    return _learned[id(ctx)]
+
+
 def solve(ctx, sysm, basis, fast: bool, set_system: bool):
-    """One solve through the public API.  fast: densities by purification
-    (one eigensolve at the end) and split-precision MP2; plain: the
-    eigensolver every iteration and the FP64 transform.  Both start from the
-    core Hamiltonian and use DIIS(8) (plain Roothaan iterations, the
-    reference's scheme, oscillate without converging on this cluster)."""
-    from myqc_gb300 import MODE_TIGHT, PREC_FP64, PREC_SPLIT_BF16X3
+    """One solve through the public API.  fast: the learned initial density
+    (core guess when the prediction fails its checks or the SCF does not
+    converge from it), Schwarz screening at 1e-12, the double-float Fock
+    digestion, densities by purification (one eigensolve at the end)
+    and split-precision MP2; plain: the core-Hamiltonian guess, the
+    eigensolver every iteration and the FP64 transform.  Both use DIIS(8)
+    (plain Roothaan iterations, the reference's scheme, oscillate without
+    converging on this cluster)."""
+    from myqc_gb300 import FOCK_DF32, FOCK_FP64, MODE_TIGHT, PREC_FP64, PREC_SPLIT_BF16X3
+    ctx.set_schwarz(SCHWARZ if fast else 0.0)
+    ctx.set_fock_precision(FOCK_DF32 if fast else FOCK_FP64)
     if set_system:
         ctx.set_system(sysm, basis, None, MODE_TIGHT)
     S, H = ctx.int1e()
     ctx.eri_store()
-    res = ctx.scf(S, H, sysm.nelcA, sysm.nelcB, conv=1e-10, conv_rms=True, diis=8, max_iter=200, purify=fast)
+    kw = dict(conv=1e-10, conv_rms=True, diis=8, max_iter=200, purify=fast)
+    D0 = None
+    if fast and learned_guess(ctx) is not None:
+        D0 = learned_guess(ctx).guess(sysm, S)
+    res = ctx.scf(S, H, sysm.nelcA, sysm.nelcB, D_guess=D0, raise_on_noconv=D0 is None, **kw)
+    if D0 is not None and res.iterations >= kw["max_iter"]:  # fallback: the core guess
+        res = ctx.scf(S, H, sysm.nelcA, sysm.nelcB, **kw)
+    res.learned_guess = D0 is not None
     prec = PREC_SPLIT_BF16X3 if fast else PREC_FP64
     mp2 = ctx.mp2_rhf(res.eig, sysm.nelcA, prec, C=res.C)
     return res, mp2, prec
@@ -237,7 +266,8 @@ def run_ours(args):
         "data": f"synthetic: seeded (H2O){NMOL} cluster, rigid monomers, PCG64 seed {args.seed}",
         "config": {"workload": workload(), "molecule": f"(H2O){NMOL}", "n_basis": n, "n_occ": sysm.nelcA,
                    "n_vir": n - sysm.nelcA, "box_angstrom": BOX, "seed": args.seed, "basis": "STO-3G",
-                   "boys": "tight FP64 table", "scf": "FP64, DIIS(8), conv 1e-10 RMS dD, densities by TC2 purification (FP64 GEMMs), one Jacobi eigensolve at the end",
+                   "boys": "tight FP64 table", "schwarz": SCHWARZ, "scf": "FP64 (Fock digestion in double-float on the FP32 pipes), DIIS(8), conv 1e-10 RMS dD, initial density from the learned guess (core guess fallback), densities by TC2 purification (FP64 GEMMs), one Jacobi eigensolve at the end",
+                   "guess_model": os.path.relpath(MODEL, ROOT) if learned_guess(ctx) is not None else None,
                    "mp2_precision": "split hi+mid+lo bf16 (tcgen05), fp32 accumulate" if prec else "fp64",
                    "l2": "inputs larger than L2: the 20 GB integral array is rebuilt and streamed every step",
                    "parallelism": f"replicas x{world}"},
@@ -250,7 +280,8 @@ def run_ours(args):
         "clocks": clk.summary(),
         "breakdown_ms_per_solve": {"eri": t_eri / args.steps, "scf_fock": t_fock / args.steps,
                                    "scf_diag": t_diag / args.steps, "ao2mo": t_ao2mo / args.steps},
-        "scf_iterations": {"fast": float(np.mean(iters)), "plain": res_p.iterations},
+        "scf_iterations": {"fast": float(np.mean(iters)), "plain": res_p.iterations,
+                           "fast_used_learned_guess": bool(getattr(res, "learned_guess", False))},
         "plain_fp64": {"ms_per_solve": ms_plain, "solves_per_s": 1000.0 / ms_plain,
                        "speedup_fast_vs_plain": ms_plain / ms_value},
         "accuracy": {"E_scf": res.energy, "E_mp2": mp2["E_MP2"], "dE_scf_vs_plain_Eh": dE_scf,

@@ -94,6 +94,15 @@ int mq_eri_upload(mq_ctx *ctx, const double *XX);
  * All matrices n x n column-major host arrays. */
 int mq_fock(mq_ctx *ctx, const double *Da, const double *Db, double *Ga, double *Gb);
 
+/* Arithmetic of the stored-integral Fock digestion (mq_fock, mq_scf, batches).
+ * MQ_FOCK_FP64 (default): FP64 products and sums, the reference's arithmetic.
+ * MQ_FOCK_DF32: each integral split into a float pair, products and row sums
+ * in double-float on the FP32 pipes (~2^-48 relative per product, below 1e-12
+ * relative on G), sums over slabs in FP64; no reference counterpart. */
+#define MQ_FOCK_FP64 0
+#define MQ_FOCK_DF32 1
+int mq_set_fock_precision(mq_ctx *ctx, int precision);
+
 /* Allocation-free RHF Fock build.  No counterpart in the reference: it exists
  * for callers that cannot allocate device memory themselves (device arrays
  * owned by an OpenACC / OpenMP-offload runtime or a preallocated pool, code
@@ -102,9 +111,9 @@ int mq_fock(mq_ctx *ctx, const double *Da, const double *Db, double *Ga, double 
  * total density), d_G (n x n output, G = J - K/2 as mq_fock computes it).
  * No context is needed and nothing is allocated or freed: the kernels'
  * scratch is a fixed 16 MiB array inside the library, held by every GPU that
- * loads it until the process exits.  It holds G's J part, the split density
- * and the K partial sums, which limits n to 3 n^2 <= 2097152 doubles
- * (n <= 836); larger n returns MQ_EINVAL.  The work is queued on
+ * loads it until the process exits.  It holds G's J part and the K partial
+ * sums (FP64 arithmetic), which with n <= 1024 always fit (2 n^2 <= 2097152
+ * doubles); larger n returns MQ_EINVAL.  The work is queued on
  * `stream` (NULL: the default stream) and the call returns without waiting;
  * G is ready once that stream reaches this point.  All calls share the one
  * scratch array, so calls that overlap on the GPU (other streams, other host
@@ -182,6 +191,15 @@ int mq_mp2_rhf(mq_ctx *ctx, const double *eig, int nocc, int nvir, double *e_out
  * eA, eB n.  e_out = {E(AA), E(BB), E(AB), E(MBPT2)}. */
 int mq_mp2_uhf(mq_ctx *ctx, const double *CA, const double *CB, const double *eA, const double *eB, int noA,
                int noB, int precision, double *e_out);
+
+/* MP2 pair sums of a given (ia|jb) block (host array, i fastest, as
+ * mq_ao2mo_iajb returns it), e.g. the records of the ijab_* files that
+ * src/mp2/mp2.f90:79-232 reads: e1 = energies of the first pair's occupied
+ * then virtual orbitals (no1 + nv1), e2 likewise.  e_out[0] =
+ * sum_{ijab} (ia|jb)^2 / D; e_out[1] = sum_{i<j, a<b} [(ia|jb) - (ib|ja)]^2 / D
+ * when same_spin (else 0), D = e_i + e_j - e_a - e_b.  No system is needed. */
+int mq_mp2_pairs(mq_ctx *ctx, const double *iajb, int no1, int nv1, int no2, int nv2, const double *e1,
+                 const double *e2, int same_spin, double *e_out);
 
 /* Batched symmetric eigensolver (FP64 Jacobi): `batch` matrices of order n,
  * A (n*n each, column-major, overwritten) -> eigenvalues w (ascending, n each)

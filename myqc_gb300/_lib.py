@@ -19,6 +19,7 @@ HEADER = os.path.join(HERE, "..", "include", "myqc.h")
 MQ_OK, MQ_EINVAL, MQ_ENOMEM, MQ_ECUDA, MQ_ETIMEOUT, MQ_ENOCONV, MQ_ESTATE = range(7)
 MODE_REFERENCE, MODE_TIGHT = 0, 1
 PREC_FP64, PREC_SPLIT_BF16, PREC_SPLIT_BF16X3 = 0, 1, 2
+FOCK_FP64, FOCK_DF32 = 0, 1
 _NAMES = {0: "MQ_OK", 1: "MQ_EINVAL", 2: "MQ_ENOMEM", 3: "MQ_ECUDA", 4: "MQ_ETIMEOUT", 5: "MQ_ENOCONV",
           6: "MQ_ESTATE"}
 
@@ -80,6 +81,7 @@ def lib(path: str | None = None):
     L.mq_ao2mo_iajb.argtypes = [vp, dp, c_int, dp, c_int, dp, c_int, dp, c_int, c_int, dp]
     L.mq_mp2_rhf.argtypes = [vp, dp, c_int, c_int, dp]
     L.mq_mp2_uhf.argtypes = [vp, dp, dp, dp, dp, c_int, c_int, c_int, dp]
+    L.mq_mp2_pairs.argtypes = [vp, dp, c_int, c_int, c_int, c_int, dp, dp, c_int, dp]
     L.mq_syev_batched.argtypes = [vp, c_int, c_int, dp, dp, dp]
     L.mq_sygv.argtypes = [vp, c_int, dp, dp, dp, dp]
     L.mq_stat.argtypes = [vp, ctypes.c_char_p, ctypes.POINTER(c_double)]
@@ -91,6 +93,7 @@ def lib(path: str | None = None):
     L.mq_mlp_grad.argtypes = [vp, c_int, vp, vp, vp, vp, ctypes.POINTER(c_double)]
     L.mq_mlp_set_data.argtypes = [vp, ctypes.c_longlong, vp, vp, vp]
     L.mq_mlp_train_epoch.argtypes = [vp, vp, c_int, ctypes.c_float, ctypes.POINTER(c_double)]
+    L.mq_set_fock_precision.argtypes = [vp, c_int]
     L.mq_batch_clear.argtypes = [vp]
     L.mq_batch_add.argtypes = [vp, c_int, vp, vp, vp, vp, vp, vp, c_int]
     L.mq_batch_info.argtypes = [vp, ip, vp]

@@ -68,9 +68,36 @@ def build(force: bool = False, verbose: bool = False, extra=()) -> str:
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stderr}")
+    build_stages(force)
     if verbose:
         print(LIB)
     return LIB
+
+
+STAGES = ("int1e", "int2e", "scf", "ao2mo", "mp2")
+BINDIR = os.path.join(HERE, "bin")
+STAGE_BIN = os.path.join(BINDIR, "myqc-stage")
+
+
+def build_stages(force: bool = False) -> str:
+    """The drop-in stage executables: one C++ program on the C ABI, linked to
+    lib/libmyqc.so (found through its run path), with a link per stage name."""
+    src = os.path.join(HERE, "dropin", "stages.cpp")
+    os.makedirs(BINDIR, exist_ok=True)
+    if force or _stale(STAGE_BIN, [src, LIB, os.path.join(HERE, "..", "include", "myqc.h")]):
+        cxx = shutil.which("g++") or shutil.which("c++")
+        if not cxx:
+            raise RuntimeError("no C++ compiler for the stage executables")
+        cmd = [cxx, "-O2", "-std=c++17", "-o", STAGE_BIN, src, "-L" + LIBDIR, "-lmyqc", "-Wl,-rpath,$ORIGIN/../lib"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"stage executables failed to build:\n{r.stderr}")
+    for st in STAGES:
+        link = os.path.join(BINDIR, st)
+        if os.path.lexists(link):
+            os.remove(link)
+        os.symlink("myqc-stage", link)
+    return STAGE_BIN
 
 
 if __name__ == "__main__":

@@ -1,3 +1,4 @@
+#include <algorithm>
 // capi.cu -- the extern "C" entry points of libmyqc (include/myqc.h).
 #include <cuda_runtime.h>
 
@@ -397,6 +398,26 @@ int mq_mp2_uhf(mq_ctx *c, const double *CA, const double *CB, const double *eA, 
   return MQ_OK;
 }
 
+int mq_mp2_pairs(mq_ctx *c, const double *iajb, int no1, int nv1, int no2, int nv2, const double *e1,
+                 const double *e2, int same_spin, double *e_out) {
+  if (!c) return MQ_EINVAL;
+  if (!iajb || !e1 || !e2 || !e_out || no1 < 0 || nv1 < 0 || no2 < 0 || nv2 < 0)
+    return set_err(c, MQ_EINVAL, "bad mp2 pair arguments");
+  cudaSetDevice(c->device);
+  const size_t nel = (size_t)no1 * nv1 * no2 * nv2;
+  double *d = to_dev(c, "mp2_pairs_in", iajb, std::max<size_t>(nel, 1));
+  if (!d) return MQ_ENOMEM;
+  double *de = (double *)buf(c, "mp2_pairs_eig", sizeof(double) * ((size_t)no1 + nv1 + no2 + nv2 + 2));
+  if (!de) return MQ_ENOMEM;
+  MQ_CUDA(c, cudaMemcpyAsync(de, e1, sizeof(double) * (no1 + nv1), cudaMemcpyHostToDevice, c->stream));
+  MQ_CUDA(c, cudaMemcpyAsync(de + no1 + nv1, e2, sizeof(double) * (no2 + nv2), cudaMemcpyHostToDevice, c->stream));
+  double s[2] = {0.0, 0.0};
+  MQ_TRY(mp2_pair_sums(c, d, no1, nv1, no2, nv2, de, de + no1 + nv1, same_spin, s));
+  e_out[0] = s[0];
+  e_out[1] = s[1];
+  return MQ_OK;
+}
+
 int mq_syev_batched(mq_ctx *c, int n, int batch, double *A, double *w, double *V) {
   if (!c || !A || !w || !V || n <= 0 || batch <= 0) return MQ_EINVAL;
   cudaSetDevice(c->device);
@@ -440,6 +461,13 @@ int mq_sygv(mq_ctx *c, int n, const double *F, const double *S, double *w, doubl
   MQ_TRY(gemm(c, 'N', 'N', n, n, n, 1.0, dX, n, dT, n, 0.0, dF, n));
   MQ_CUDA(c, cudaMemcpyAsync(C, dF, n2 * 8, cudaMemcpyDeviceToHost, c->stream));
   MQ_CUDA(c, cudaStreamSynchronize(c->stream));
+  return MQ_OK;
+}
+
+int mq_set_fock_precision(mq_ctx *c, int precision) {
+  if (!c) return MQ_EINVAL;
+  if (precision != MQ_FOCK_FP64 && precision != MQ_FOCK_DF32) return set_err(c, MQ_EINVAL, "bad Fock precision");
+  c->fock_df32 = precision == MQ_FOCK_DF32;
   return MQ_OK;
 }
 
@@ -535,6 +563,7 @@ int mq_stat(const mq_ctx *c, const char *key, double *value) {
   else if (!strcmp(key, "purify_steps")) *value = s.purify_steps;
   else if (!strcmp(key, "fock_jc")) *value = s.fock_jc;
   else if (!strcmp(key, "graph_launches")) *value = s.graph_launches;
+  else if (!strcmp(key, "fock_precision")) *value = c->fock_df32;
   else if (!strcmp(key, "fock_kernel")) *value = s.ms_fock_kernel;
   else if (!strcmp(key, "fock_kernel_launches")) *value = s.fock_kernel_launches;
   else if (!strcmp(key, "tune_fock_ms")) *value = s.tune_fock_ms;

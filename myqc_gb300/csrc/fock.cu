@@ -25,29 +25,22 @@ constexpr int FOCK_THREADS = 256;
 
 // ---- double-float arithmetic on the FP32 pipes ----------------------------
 // GB300 issues FP32 at many times its FP64 rate, so the digestion keeps its
-// sums as unevaluated float pairs (hi + lo, ~48-bit significand).  An integral
-// x is split into hi + lo floats with integer operations only: hi takes the
-// top 24 significand bits, lo the next 24 of the remainder (both truncated;
-// |x - hi - lo| < 2^-47 |x|; values below the FP32 normal range become 0).
+// sums as unevaluated float pairs (hi + lo, ~48-bit significand).  A double x
+// is split with integer operations only, without branches:
+//   hi = x truncated to 24 significant bits: the sign, the exponent rebiased
+//        from 1023 to 127, the top 23 fraction bits;
+//   lo = the remaining 29 fraction bits (an integer r times the ulp
+//        2^(E-1075) of x) converted to float (rounded to 24 bits) and scaled.
+// |x - hi - lo| <= 2^-48 |x| for 2^-74 <= |x| < 2^128; below 2^-74 lo is 0
+// (an absolute error under 2^-97) and below 2^-126 hi is 0 as well.
 __device__ __forceinline__ float2 split_f64(double x) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-  const unsigned hi32 = (unsigned)(b >> 32);
-  const unsigned sign = hi32 & 0x80000000u;
-  const int E = (int)((hi32 >> 20) & 0x7ff);
-  const int e8 = E - 896;  // FP32 biased exponent of x
-  if (e8 <= 0 || e8 >= 255) return make_float2(0.f, 0.f);
-  const unsigned long long frac = b & 0xfffffffffffffull;
-  const float h = __uint_as_float(sign | ((unsigned)e8 << 23) | (unsigned)(frac >> 29));
-  const unsigned rem = (unsigned)(frac & 0x1fffffffu);  // value rem * 2^(E - 1075)
-  float l = 0.f;
-  if (rem) {
-    const int msb = 31 - __clz(rem);  // 0..28
-    const int el = msb + E - 948;     // FP32 biased exponent of the remainder
-    if (el > 0) {
-      const unsigned mant = msb >= 23 ? (rem >> (msb - 23)) : (rem << (23 - msb));
-      l = __uint_as_float(sign | ((unsigned)el << 23) | (mant & 0x7fffffu));
-    }
-  }
+  const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+  const unsigned sign = hi & 0x80000000u;
+  const unsigned E = (hi >> 20) & 0x7ffu;
+  const unsigned hb = sign | (((hi & 0x7fffffffu) - 0x38000000u) << 3) | (lo >> 29);
+  const float h = __uint_as_float(E > 896u ? hb : sign);
+  const unsigned sc = E > 948u ? (((E - 948u) << 23) | sign) : 0u;
+  const float l = __uint2float_rn(lo & 0x1fffffffu) * __uint_as_float(sc);
   return make_float2(h, l);
 }
 
@@ -63,37 +56,76 @@ __device__ __forceinline__ void dfma(float2 &s, float2 x, float2 d) {
   s.y += err + (pe + cr);
 }
 
-// density hi/lo pairs: DJ from Da (+ Db), DKa from Da, DKb from Db (UHF)
+// Arithmetic of the digestion.  ArithF64 is plain FP64, the reference's
+// arithmetic (the default).  ArithDF32 keeps each integral as a float pair and
+// the row sums as double-float on the FP32 pipes (opt-in, mq_set_fock_precision):
+// about 2^-48 relative per product, below 1e-12 relative on G.  Either way
+// the sums over slabs and the assembly are FP64.
+struct ArithDF32 {
+  typedef float2 Den;  // a density element as the kernels read it
+  typedef float2 Acc;
+  __device__ static Acc zero() { return make_float2(0.f, 0.f); }
+  __device__ static float2 load(const double *p) { return split_f64(__ldcs(p)); }
+  __device__ static void fma(Acc &s, float2 x, Den d) { dfma(s, x, d); }
+  __device__ static double val(Acc s) { return (double)s.x + (double)s.y; }
+};
+struct ArithF64 {
+  typedef double Den;
+  typedef double Acc;
+  __device__ static Acc zero() { return 0.0; }
+  __device__ static double load(const double *p) { return __ldcs(p); }
+  __device__ static void fma(Acc &s, double x, Den d) { s = ::fma(x, d, s); }
+  __device__ static double val(Acc s) { return s; }
+};
+
+// FP64 density prepared for J: the lower-triangle weights of the total density
+// (2 D(k,l) for l < k, D(k,k), 0 above) for a system of order tri_n
+__global__ void prep_density_f64_kernel(const double *__restrict__ Da, const double *__restrict__ Db, size_t n2,
+                                        double *__restrict__ DJ, int tri_n) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n2) return;
+  const size_t k = i % (size_t)tri_n, l = i / (size_t)tri_n;
+  const double w = l < k ? 2.0 : (l == k ? 1.0 : 0.0);
+  DJ[i] = w * (Da[i] + (Db ? Db[i] : 0.0));
+}
+
+// density hi/lo pairs: DJ from Da (+ Db), DKa from Da, DKb from Db (UHF).
+// With tri_n > 0 (the order n of one system) DJ holds the lower-triangle
+// weights for J over half of a symmetric slab: 2 D(k,l) for l < k, D(k,k) on
+// the diagonal, 0 above; DKa must then be a separate array.
 __global__ void split_density_kernel(const double *__restrict__ Da, const double *__restrict__ Db, size_t n2,
-                                     float2 *__restrict__ DJ, float2 *__restrict__ DKa, float2 *__restrict__ DKb) {
+                                     float2 *__restrict__ DJ, float2 *__restrict__ DKa, float2 *__restrict__ DKb,
+                                     int tri_n) {
   const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n2) return;
   const double a = Da[i];
-  if (Db) {
-    const double b = Db[i];
-    DJ[i] = split_f64(a + b);
-    DKa[i] = split_f64(a);
-    DKb[i] = split_f64(b);
-  } else {
-    DJ[i] = split_f64(a);
+  const double b = Db ? Db[i] : 0.0;
+  double wj = 1.0;
+  if (tri_n > 0) {
+    const size_t k = i % (size_t)tri_n, l = i / (size_t)tri_n;
+    wj = l < k ? 2.0 : (l == k ? 1.0 : 0.0);
   }
+  DJ[i] = split_f64(wj * (a + b));
+  if (tri_n > 0 || Db) DKa[i] = split_f64(a);
+  if (Db) DKb[i] = split_f64(b);
 }
 
-int split_density(mq_ctx *c, const double *Da, const double *Db, size_t n2, float2 *DJ, float2 *DKa, float2 *DKb) {
+int split_density(mq_ctx *c, const double *Da, const double *Db, size_t n2, float2 *DJ, float2 *DKa, float2 *DKb,
+                  int tri_n) {
   if (n2 == 0) return MQ_OK;
-  split_density_kernel<<<(unsigned)((n2 + 255) / 256), 256, 0, c->stream>>>(Da, Db, n2, DJ, DKa, DKb);
+  split_density_kernel<<<(unsigned)((n2 + 255) / 256), 256, 0, c->stream>>>(Da, Db, n2, DJ, DKa, DKb, tri_n);
   c->stats.launches += 1;
   MQ_CUDA(c, cudaGetLastError());
   return MQ_OK;
 }
 
-template <bool UHF>
+template <class P, bool UHF>
 __global__ void __launch_bounds__(FOCK_THREADS) fock_slab_kernel(const double *__restrict__ XX,
-                                                                 const float2 *__restrict__ DJ,
-                                                                 const float2 *__restrict__ DKa,
-                                                                 const float2 *__restrict__ DKb, int n, int jchunk,
-                                                                 double *__restrict__ J, double *__restrict__ Kpa,
-                                                                 double *__restrict__ Kpb) {
+                                                                 const typename P::Den *__restrict__ DJ,
+                                                                 const typename P::Den *__restrict__ DKa,
+                                                                 const typename P::Den *__restrict__ DKb, int n,
+                                                                 int jchunk, double *__restrict__ J,
+                                                                 double *__restrict__ Kpa, double *__restrict__ Kpb) {
   const int i = blockIdx.x, chunk = blockIdx.y;
   const int j0 = chunk * jchunk, j1 = min(n, j0 + jchunk);
   const size_t N = n, n2 = N * N;
@@ -107,17 +139,17 @@ __global__ void __launch_bounds__(FOCK_THREADS) fock_slab_kernel(const double *_
     for (int r = 0; r < 4; ++r) {
       const int k = threadIdx.x + r * FOCK_THREADS;
       if (k >= n) break;
-      float2 sa = make_float2(0.f, 0.f), sb = sa, sj = sa;
+      typename P::Acc sa = P::zero(), sb = sa, sj = sa;
 #pragma unroll 4
       for (int l = 0; l < n; ++l) {
-        const float2 x = split_f64(__ldcs(S + k + N * l));  // streamed once: do not keep in L2
-        dfma(sj, x, DJ[k + N * l]);
-        dfma(sa, x, DKa[l + N * j]);
-        if (UHF) dfma(sb, x, DKb[l + N * j]);
+        const auto x = P::load(S + k + N * l);  // streamed once: do not keep in L2
+        P::fma(sj, x, DJ[k + N * l]);
+        P::fma(sa, x, DKa[l + N * j]);
+        if (UHF) P::fma(sb, x, DKb[l + N * j]);
       }
-      jsum += (double)sj.x + (double)sj.y;
-      ka[r] += (double)sa.x + (double)sa.y;
-      if (UHF) kb[r] += (double)sb.x + (double)sb.y;
+      jsum += P::val(sj);
+      ka[r] += P::val(sa);
+      if (UHF) kb[r] += P::val(sb);
     }
     // block reduction of J_ij
 #pragma unroll
@@ -176,13 +208,15 @@ constexpr int PAIR_MAX_THREADS = 256;
 // A tile is (i, j0, j1, molecule); the molecule's descriptor gives its order
 // and where its XX, matrices and Q live, so one launch serves one system or a
 // whole batch.  Tiles of molecules whose `active` flag is 0 do nothing.
-template <int R, int JC, bool UHF>
+template <class P, int R, int JC, bool UHF>
 __global__ void __launch_bounds__(PAIR_MAX_THREADS) fock_pair_kernel(
-    const double *__restrict__ XX, const float2 *__restrict__ DJ, const float2 *__restrict__ DKa,
-    const float2 *__restrict__ DKb, const int4 *__restrict__ tiles, const MolDesc *__restrict__ mols,
-    const int *__restrict__ active, int kp_stride, double *__restrict__ J, double *__restrict__ Kpa,
+    const double *__restrict__ XX, const typename P::Den *__restrict__ DJ, const typename P::Den *__restrict__ DKa,
+    const typename P::Den *__restrict__ DKb, const int4 *__restrict__ tiles, const MolDesc *__restrict__ mols,
+    const int *__restrict__ active, int kp_stride, int tri, double *__restrict__ J, double *__restrict__ Kpa,
     double *__restrict__ Kpb, double *__restrict__ Qa, double *__restrict__ Qb) {
-  extern __shared__ float2 dsh[];  // D(:,i) then D(:,j) for the tile's j (alpha; beta after)
+  typedef typename P::Den Den;
+  extern __shared__ __align__(16) unsigned char dsh_raw[];
+  Den *dsh = (Den *)dsh_raw;  // D(:,i) then D(:,j) for the tile's j (alpha; beta after)
   const int4 tile = tiles[blockIdx.x];
   if (active && !active[tile.w]) return;
   const MolDesc md = mols[tile.w];
@@ -196,8 +230,8 @@ __global__ void __launch_bounds__(PAIR_MAX_THREADS) fock_pair_kernel(
   Qa += md.q;
   if (UHF) Qb += md.q;
   const int tid = threadIdx.x, T = blockDim.x;
-  float2 *dia = dsh, *dja = dsh + n;
-  float2 *dib = dsh + (size_t)(1 + JC) * n, *djb = dib + n;
+  Den *dia = dsh, *dja = dsh + n;
+  Den *dib = dsh + (size_t)(1 + JC) * n, *djb = dib + n;
   for (int l = tid; l < n; l += T) {
     dia[l] = DKa[l + N * i];
     if (UHF) dib[l] = DKb[l + N * i];
@@ -209,8 +243,9 @@ __global__ void __launch_bounds__(PAIR_MAX_THREADS) fock_pair_kernel(
     }
   __syncthreads();
 
-  const float2 z = make_float2(0.f, 0.f);
-  float2 aj[JC][R], aqa[JC][R], aqb[UHF ? JC : 1][R], aka[R], akb[R];
+  const typename P::Acc z = P::zero();
+  const Den dz = Den();
+  typename P::Acc aj[JC][R], aqa[JC][R], aqb[UHF ? JC : 1][R], aka[R], akb[R];
 #pragma unroll
   for (int r = 0; r < R; ++r) {
     aka[r] = z;
@@ -225,31 +260,32 @@ __global__ void __launch_bounds__(PAIR_MAX_THREADS) fock_pair_kernel(
   const double *S0 = XX + n2 * ((size_t)i + N * j0);
 #pragma unroll 2
   for (int l = 0; l < n; ++l) {
-    const float2 di_a = dia[l];
-    const float2 di_b = UHF ? dib[l] : z;
-    float2 dj[R];
+    const Den di_a = dia[l];
+    const Den di_b = UHF ? dib[l] : dz;
+    Den dj[R];
 #pragma unroll
     for (int r = 0; r < R; ++r) {
       const int k = tid + r * T;
-      dj[r] = k < n ? DJ[k + N * l] : z;
+      dj[r] = k < n ? DJ[k + N * l] : dz;
     }
 #pragma unroll
     for (int jj = 0; jj < JC; ++jj) {
       if (jj < nj) {
-        const float2 dja_l = dja[jj * n + l];
-        const float2 djb_l = UHF ? djb[jj * n + l] : z;
+        const Den dja_l = dja[jj * n + l];
+        const Den djb_l = UHF ? djb[jj * n + l] : dz;
         const double *S = S0 + n2 * N * jj + N * l;
 #pragma unroll
         for (int r = 0; r < R; ++r) {
           const int k = tid + r * T;
           if (k < n) {
-            const float2 x = split_f64(__ldcs(S + k));  // streamed once: keep it out of L2
-            dfma(aj[jj][r], x, dj[r]);
-            dfma(aka[r], x, dja_l);
-            dfma(aqa[jj][r], x, di_a);
+            const auto x = P::load(S + k);  // streamed once: keep it out of L2
+            // triangle weights are 0 for l > k: skip once l passes the warp's last row
+            if (!tri || l <= (tid | 31) + r * T) P::fma(aj[jj][r], x, dj[r]);
+            P::fma(aka[r], x, dja_l);
+            P::fma(aqa[jj][r], x, di_a);
             if (UHF) {
-              dfma(akb[r], x, djb_l);
-              dfma(aqb[jj][r], x, di_b);
+              P::fma(akb[r], x, djb_l);
+              P::fma(aqb[jj][r], x, di_b);
             }
           }
         }
@@ -263,7 +299,7 @@ __global__ void __launch_bounds__(PAIR_MAX_THREADS) fock_pair_kernel(
   for (int jj = 0; jj < JC; ++jj) {
     double v = 0.0;
 #pragma unroll
-    for (int r = 0; r < R; ++r) v += (double)aj[jj][r].x + (double)aj[jj][r].y;
+    for (int r = 0; r < R; ++r) v += P::val(aj[jj][r]);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     if ((tid & 31) == 0) red[tid >> 5][jj] = v;
@@ -280,14 +316,14 @@ __global__ void __launch_bounds__(PAIR_MAX_THREADS) fock_pair_kernel(
   for (int r = 0; r < R; ++r) {
     const int k = tid + r * T;
     if (k >= n) continue;
-    Kpa[(size_t)kp_stride * blockIdx.x + k] = (double)aka[r].x + (double)aka[r].y;
-    if (UHF) Kpb[(size_t)kp_stride * blockIdx.x + k] = (double)akb[r].x + (double)akb[r].y;
+    Kpa[(size_t)kp_stride * blockIdx.x + k] = P::val(aka[r]);
+    if (UHF) Kpb[(size_t)kp_stride * blockIdx.x + k] = P::val(akb[r]);
 #pragma unroll
     for (int jj = 0; jj < JC; ++jj) {
       const int j = j0 + jj;
       if (jj < nj && j > i) {
-        Qa[k + N * i + n2 * j] = (double)aqa[jj][r].x + (double)aqa[jj][r].y;
-        if (UHF) Qb[k + N * i + n2 * j] = (double)aqb[jj][r].x + (double)aqb[jj][r].y;
+        Qa[k + N * i + n2 * j] = P::val(aqa[jj][r]);
+        if (UHF) Qb[k + N * i + n2 * j] = P::val(aqb[jj][r]);
       }
     }
   }
@@ -327,29 +363,39 @@ __global__ void fock_pair_combine_kernel(const double *__restrict__ J, const dou
   G[md.mat + idx] = J[md.mat + idx] - f * (0.5 * (K[md.mat + idx] + K[md.mat + tdx]));
 }
 
-template <int R, int JC>
+template <class P, int R, int JC>
 static int launch_pair(mq_ctx *c, const PairLaunch &L, int threads, size_t smem, bool uhf) {
+  typedef typename P::Den Den;
+  const Den *DJ = (const Den *)L.DJ, *DKa = (const Den *)L.DKa, *DKb = (const Den *)L.DKb;
   if (uhf) {
-    auto k = fock_pair_kernel<R, JC, true>;
+    auto k = fock_pair_kernel<P, R, JC, true>;
     MQ_CUDA(c, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k<<<L.ntiles, threads, smem, c->stream>>>(L.XX, L.DJ, L.DKa, L.DKb, L.tiles, L.mols, L.active, L.nmax, L.J,
+    k<<<L.ntiles, threads, smem, c->stream>>>(L.XX, DJ, DKa, DKb, L.tiles, L.mols, L.active, L.nmax, L.tri, L.J,
                                               L.Kpa, L.Kpb, L.Qa, L.Qb);
   } else {
-    auto k = fock_pair_kernel<R, JC, false>;
+    auto k = fock_pair_kernel<P, R, JC, false>;
     MQ_CUDA(c, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k<<<L.ntiles, threads, smem, c->stream>>>(L.XX, L.DJ, L.DKa, nullptr, L.tiles, L.mols, L.active, L.nmax, L.J,
+    k<<<L.ntiles, threads, smem, c->stream>>>(L.XX, DJ, DKa, nullptr, L.tiles, L.mols, L.active, L.nmax, L.tri, L.J,
                                               L.Kpa, nullptr, L.Qa, nullptr);
   }
   return MQ_OK;
 }
 
-template <int R>
+template <class P, int R>
 static int launch_pair_jc(mq_ctx *c, int jc, const PairLaunch &L, int threads, size_t smem, bool uhf) {
   switch (jc) {
-    case 1: return launch_pair<R, 1>(c, L, threads, smem, uhf);
-    case 2: return launch_pair<R, 2>(c, L, threads, smem, uhf);
-    case 4: return launch_pair<R, 4>(c, L, threads, smem, uhf);
-    default: return launch_pair<R, 8>(c, L, threads, smem, uhf);
+    case 1: return launch_pair<P, R, 1>(c, L, threads, smem, uhf);
+    case 2: return launch_pair<P, R, 2>(c, L, threads, smem, uhf);
+    default: return launch_pair<P, R, 4>(c, L, threads, smem, uhf);
+  }
+}
+
+template <class P>
+static int launch_pair_r(mq_ctx *c, int Rp, int jc, const PairLaunch &L, int threads, size_t smem, bool uhf) {
+  switch (Rp) {
+    case 1: return launch_pair_jc<P, 1>(c, jc, L, threads, smem, uhf);
+    case 2: return launch_pair_jc<P, 2>(c, jc, L, threads, smem, uhf);
+    default: return launch_pair_jc<P, 4>(c, jc, L, threads, smem, uhf);
   }
 }
 
@@ -404,15 +450,9 @@ int pair_digest(mq_ctx *c, int JC, bool uhf, const PairLaunch &L, double *d_Ga, 
   const int T = std::min(PAIR_MAX_THREADS, (n + 31) / 32 * 32);
   const int R0 = (n + T - 1) / T;
   const int Rp = R0 <= 1 ? 1 : R0 <= 2 ? 2 : 4;
-  const size_t smem = sizeof(float2) * (size_t)n * (1 + JC) * (uhf ? 2 : 1);
-  int rc = MQ_OK;
+  const size_t smem = 8 * (size_t)n * (1 + JC) * (uhf ? 2 : 1);  // float2 or double density columns
   if (timed) c->t_fock_kernel.start(c->stream);
-  switch (Rp) {
-    case 1: rc = launch_pair_jc<1>(c, JC, L, T, smem, uhf); break;
-    case 2: rc = launch_pair_jc<2>(c, JC, L, T, smem, uhf); break;
-    default: rc = launch_pair_jc<4>(c, JC, L, T, smem, uhf); break;
-  }
-  MQ_TRY(rc);
+  MQ_TRY(L.df32 ? launch_pair_r<ArithDF32>(c, Rp, JC, L, T, smem, uhf) : launch_pair_r<ArithF64>(c, Rp, JC, L, T, smem, uhf));
   if (timed) {
     c->t_fock_kernel.stop(c->stream);
     c->stats.fock_kernel_launches += 1;
@@ -431,7 +471,7 @@ int pair_digest(mq_ctx *c, int JC, bool uhf, const PairLaunch &L, double *d_Ga, 
 }
 
 // Scratch of the single system: J | K slices | Q | K.
-static int pair_build(mq_ctx *c, int JC, bool uhf, const float2 *DJ, const float2 *DKa, const float2 *DKb,
+static int pair_build(mq_ctx *c, int JC, bool uhf, const void *DJ, const void *DKa, const void *DKb,
                       double *d_Ga, double *d_Gb, bool timed = false) {
   const int n = c->nao;
   const size_t N = n, n2 = N * N;
@@ -442,6 +482,8 @@ static int pair_build(mq_ctx *c, int JC, bool uhf, const float2 *DJ, const float
   double *J = (double *)buf(c, "fock_partials", sizeof(double) * (n2 + ns * (N * nt + N * n2 + n2)));
   if (!J) return MQ_ENOMEM;
   L.XX = c->d_XX;
+  L.tri = 1;
+  L.df32 = c->fock_df32;
   L.DJ = DJ;
   L.DKa = DKa;
   L.DKb = DKb;
@@ -456,20 +498,20 @@ static int pair_build(mq_ctx *c, int JC, bool uhf, const float2 *DJ, const float
 }
 
 // Autotuner for the tile length JC: on the first build for a given (n, RHF or
-// UHF) each candidate digests the caller's densities twice under CUDA events
-// and the fastest is kept for the context's later builds.  Every candidate
-// computes the same G (the tile length only changes the summation grouping,
-// ~1e-13 relative), and the call's result comes from the chosen one.
-// MYQC_FOCK_JC=1|2|4|8 in the environment pins the choice instead.
-static int pair_choose_jc(mq_ctx *c, bool uhf, const float2 *DJ, const float2 *DKa, const float2 *DKb,
-                          double *d_Ga, double *d_Gb) {
+// UHF, arithmetic) each candidate digests the caller's densities twice under
+// CUDA events and the fastest is kept for the context's later builds.  Every
+// candidate computes the same G (the tile length only changes the summation
+// grouping, ~1e-13 relative), and the call's result comes from the chosen one.
+// MYQC_FOCK_JC=1|2|4 in the environment pins the choice instead.
+static int pair_choose_jc(mq_ctx *c, bool uhf, const void *DJ, const void *DKa, const void *DKb, double *d_Ga,
+                          double *d_Gb) {
   const int n = c->nao;
-  int &slot = uhf ? c->fock_jc_uhf : c->fock_jc_rhf;
-  int &slot_n = uhf ? c->fock_jc_uhf_n : c->fock_jc_rhf_n;
+  int &slot = c->fock_jc[uhf ? 1 : 0][c->fock_df32 ? 1 : 0];
+  int &slot_n = c->fock_jc_n[uhf ? 1 : 0][c->fock_df32 ? 1 : 0];
   if (slot_n == n && slot > 0) return slot;
   if (const char *e = getenv("MYQC_FOCK_JC")) {
     const int v = atoi(e);
-    slot = v >= 8 ? 8 : v >= 4 ? 4 : v >= 2 ? 2 : 1;
+    slot = v >= 4 ? 4 : v >= 2 ? 2 : 1;
     slot_n = n;
     return slot;
   }
@@ -501,18 +543,40 @@ static int pair_choose_jc(mq_ctx *c, bool uhf, const float2 *DJ, const float2 *D
   return slot;
 }
 
+// Density operands for the digestion, in the context's arithmetic: DJ the
+// triangle-weighted total density, DKa / DKb the spin densities (FP64: the
+// caller's arrays themselves; double-float: split copies).
+int fock_densities(mq_ctx *c, int n, const double *d_Da, const double *d_Db, const void **DJ, const void **DKa,
+                   const void **DKb) {
+  const size_t n2 = (size_t)n * n;
+  const bool uhf = d_Db != nullptr;
+  if (c->fock_df32) {
+    float2 *d = (float2 *)buf(c, "fock_dsplit", sizeof(float2) * n2 * (uhf ? 3 : 2));
+    if (!d) return MQ_ENOMEM;
+    MQ_TRY(split_density(c, d_Da, d_Db, n2, d, d + n2, uhf ? d + 2 * n2 : nullptr, n));
+    *DJ = d;
+    *DKa = d + n2;
+    *DKb = uhf ? d + 2 * n2 : nullptr;
+  } else {
+    double *d = (double *)buf(c, "fock_dsplit", sizeof(double) * n2);
+    if (!d) return MQ_ENOMEM;
+    prep_density_f64_kernel<<<(unsigned)((n2 + 255) / 256), 256, 0, c->stream>>>(d_Da, d_Db, n2, d, n);
+    c->stats.launches += 1;
+    MQ_CUDA(c, cudaGetLastError());
+    *DJ = d;
+    *DKa = d_Da;
+    *DKb = d_Db;
+  }
+  return MQ_OK;
+}
+
 int fock_stored_device(mq_ctx *c, const double *d_Da, const double *d_Db, double *d_Ga, double *d_Gb) {
   const int n = c->nao;
   if (!c->d_XX) return set_err(c, MQ_ESTATE, "no integrals on the device (call mq_eri_store or mq_eri_upload)");
   if (n > 4 * PAIR_MAX_THREADS) return set_err(c, MQ_EINVAL, "stored Fock build supports n <= 1024");
   const bool uhf = d_Db != nullptr;
-  const size_t n2 = (size_t)n * n;
-  float2 *DJ = (float2 *)buf(c, "fock_dsplit", sizeof(float2) * n2 * (uhf ? 3 : 1));
-  if (!DJ) return MQ_ENOMEM;
-  float2 *DKa = uhf ? DJ + n2 : DJ, *DKb = uhf ? DJ + 2 * n2 : nullptr;
-  const int tb = 256;
-  split_density_kernel<<<(unsigned)((n2 + tb - 1) / tb), tb, 0, c->stream>>>(d_Da, d_Db, n2, DJ, DKa, DKb);
-  c->stats.launches += 1;
+  const void *DJ, *DKa, *DKb;
+  MQ_TRY(fock_densities(c, n, d_Da, d_Db, &DJ, &DKa, &DKb));
   const int JC = pair_choose_jc(c, uhf, DJ, DKa, DKb, d_Ga, d_Gb);
   c->stats.fock_jc = JC;
   c->t_fock_kernel.collect();  // a previous build's timing not yet collected by its caller
@@ -525,9 +589,9 @@ int fock_stored_device(mq_ctx *c, const double *d_Da, const double *d_Db, double
 // For callers that may not allocate device memory themselves -- a Fortran or
 // C host whose device arrays are owned by an OpenACC / OpenMP-offload runtime
 // or by a preallocated pool, or code that must not call cudaMalloc while it
-// runs -- the same two kernels as fock_stored_device run on caller-owned
-// device buffers, with their scratch (J and the per-chunk K columns) in the
-// fixed array below instead of a context buffer.  The array is part of the
+// runs -- a slab digestion (FP64, full slabs) and the combine kernel run on
+// caller-owned device buffers, with their scratch (J and the per-chunk K
+// columns) in the fixed array below instead of a context buffer.  The array is part of the
 // loaded library: every GPU that loads libmyqc holds its 16 MiB until the
 // process exits.  Host code cannot use the array's name as a device address;
 // the first call on each device looks the address up with
@@ -554,10 +618,10 @@ extern "C" int mq_fock_rhf_noalloc(int n, const double *d_XX, const double *d_D,
   if (n <= 0 || !d_XX || !d_D || !d_G) return noalloc_fail(msg, msglen, MQ_EINVAL, "null pointer or n <= 0");
   if (n > 4 * FOCK_THREADS) return noalloc_fail(msg, msglen, MQ_EINVAL, "n > 1024 is not supported");
   const size_t n2 = (size_t)n * n;
-  // J, the split density (one float pair per element) and at least one K
-  // slice must fit the fixed scratch: 3 n^2 <= 2 Mi doubles (n <= 836)
-  if (3 * n2 > NOALLOC_SCRATCH_DOUBLES)
-    return noalloc_fail(msg, msglen, MQ_EINVAL, "scratch too small: 3 n^2 must not exceed 2097152 doubles (n <= 836)");
+  // J and at least one K slice must fit the fixed scratch: 2 n^2 <= 2 Mi
+  // doubles, which n <= 1024 always meets
+  if (2 * n2 > NOALLOC_SCRATCH_DOUBLES)
+    return noalloc_fail(msg, msglen, MQ_EINVAL, "scratch too small: 2 n^2 must not exceed 2097152 doubles");
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= NOALLOC_MAX_DEVICES)
     return noalloc_fail(msg, msglen, MQ_ECUDA, "cudaGetDevice failed");
@@ -574,18 +638,16 @@ extern "C" int mq_fock_rhf_noalloc(int n, const double *d_XX, const double *d_D,
   }
   int sms = 148;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const int nmax = (int)(NOALLOC_SCRATCH_DOUBLES / n2) - 2;  // K slices that fit beside J and the density
+  const int nmax = (int)(NOALLOC_SCRATCH_DOUBLES / n2) - 1;  // K slices that fit beside J
   int nchunk = std::max(1, std::min({n, (4 * sms + n - 1) / n, nmax}));
   const int jchunk = (n + nchunk - 1) / nchunk;
   nchunk = (n + jchunk - 1) / jchunk;
-  // every split-density, J and K-slice element is written by an earlier
-  // kernel before a later one reads it, so nothing needs clearing between calls
-  double *J = scr;
-  float2 *Ds = (float2 *)(scr + n2);
-  double *Kp = scr + 2 * n2;
+  // every J and K-slice element is written by the first kernel before the
+  // second reads it, so nothing needs clearing between calls (FP64 throughout)
+  double *J = scr, *Kp = scr + n2;
   cudaStream_t s = (cudaStream_t)stream;
-  split_density_kernel<<<(unsigned)((n2 + 255) / 256), 256, 0, s>>>(d_D, nullptr, n2, Ds, Ds, nullptr);
-  fock_slab_kernel<false><<<dim3(n, nchunk), FOCK_THREADS, 0, s>>>(d_XX, Ds, Ds, nullptr, n, jchunk, J, Kp, nullptr);
+  fock_slab_kernel<ArithF64, false><<<dim3(n, nchunk), FOCK_THREADS, 0, s>>>(d_XX, d_D, d_D, nullptr, n, jchunk, J, Kp,
+                                                                             nullptr);
   fock_combine_kernel<<<(unsigned)((n2 + 255) / 256), 256, 0, s>>>(J, Kp, nchunk, n, 0.5, d_G);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return noalloc_fail(msg, msglen, MQ_ECUDA, cudaGetErrorString(e));

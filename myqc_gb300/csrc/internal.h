@@ -154,7 +154,8 @@ struct mq_ctx {
   void *mlp = nullptr;               // the learned guess's network (mlp.cu)
   mq::StageTimer t_fock_kernel;  // the digestion kernel alone, collected at the caller's sync points
   mq::FockTiles fock_tiles[9];  // pair-slab tile tables, indexed by slabs per tile
-  int fock_jc_rhf = 0, fock_jc_rhf_n = 0, fock_jc_uhf = 0, fock_jc_uhf_n = 0;  // autotuned tile lengths
+  int fock_jc[2][2] = {{0, 0}, {0, 0}}, fock_jc_n[2][2] = {{0, 0}, {0, 0}};  // autotuned tile length [uhf][df32]
+  int fock_df32 = 0;  // digestion arithmetic: 0 FP64, 1 double-float (mq_set_fock_precision)
   size_t XX_elems = 0;
   double *d_iajb = nullptr;  // last (ia|jb) block
   size_t iajb_elems = 0;
@@ -186,17 +187,24 @@ void pair_tiles_host(int n, int JC, int mol, std::vector<int4> &tl, std::vector<
 // the molecules (thread count, shared memory, K-slice stride).
 struct PairLaunch {
   const double *XX;
-  const float2 *DJ, *DKa, *DKb;
+  const void *DJ, *DKa, *DKb;  // float2 (df32) or double arrays
   const int4 *tiles;
   const int *row_first;
   const MolDesc *mols;
   const int *active;
   int ntiles, nmol, nmax;
+  int tri;   // DJ carries lower-triangle weights: J sums over l <= k only
+  int df32;  // densities are float pairs and the digestion double-float (else FP64 arrays)
   double *J, *Kpa, *Kpb, *Qa, *Qb, *Ka, *Kb;
 };
+// density operands of the digestion in the context's arithmetic (fock.cu)
+int fock_densities(mq_ctx *c, int n, const double *d_Da, const double *d_Db, const void **DJ, const void **DKa,
+                   const void **DKb);
 int pair_digest(mq_ctx *c, int JC, bool uhf, const PairLaunch &L, double *d_Ga, double *d_Gb, bool timed);
-// densities as hi/lo float pairs: DJ from Da (+ Db), DKa from Da, DKb from Db
-int split_density(mq_ctx *c, const double *Da, const double *Db, size_t n2, float2 *DJ, float2 *DKa, float2 *DKb);
+// densities as hi/lo float pairs: DJ from Da (+ Db), DKa from Da, DKb from Db;
+// tri_n > 0: DJ with lower-triangle weights for a system of order tri_n
+int split_density(mq_ctx *c, const double *Da, const double *Db, size_t n2, float2 *DJ, float2 *DKa, float2 *DKb,
+                  int tri_n);
 // mlp.cu
 int mlp_init(mq_ctx *c, int nin, int width, int nout);
 int mlp_param_count(mq_ctx *c);

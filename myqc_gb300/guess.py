@@ -215,3 +215,49 @@ def check_density(D: np.ndarray, S: np.ndarray, nelec: int, tol_count: float = 0
     idem = float(np.linalg.norm(0.5 * D @ S @ D - D) / max(np.linalg.norm(D), 1e-30))
     ok = np.isfinite(cnt) and abs(cnt - nelec) < tol_count and idem < tol_idem
     return ok, cnt - nelec, idem
+
+
+# ---------------------------------------------------------------- model I/O and inference
+def system_geometry(sysm):
+    """(atoms, xyz in Angstrom) of a System (whose xyz is in bohr)."""
+    return np.asarray(sysm.atoms), np.asarray(sysm.xyz, dtype=float) / BOHR
+
+
+def pair_data(atoms, xyz_angstrom):
+    """Pairs, descriptors, frames, block types and output masks of one geometry."""
+    pairs = pairs_of(atoms, xyz_angstrom)
+    feat, Q = descriptors(atoms, xyz_angstrom, pairs)
+    za, zb = np.asarray(atoms)[pairs[:, 0]], np.asarray(atoms)[pairs[:, 1]]
+    t = block_type(za, zb, pairs[:, 0] == pairs[:, 1])
+    return pairs, feat, Q, t, output_mask(atoms, pairs)
+
+
+class LearnedGuess:
+    """Trained network + normalisation, evaluated through a Context's MLP
+    kernels.  The file holds params (FP32), dims, mu_x/sd_x (feature
+    standardisation) and mu_y/sd_y (per block type and output entry)."""
+
+    def __init__(self, ctx, path: str):
+        z = np.load(path)
+        self.ctx = ctx
+        self.dims = tuple(int(v) for v in z["dims"])
+        self.mu_x, self.sd_x = z["mu_x"], z["sd_x"]
+        self.mu_y, self.sd_y = z["mu_y"], z["sd_y"]
+        ctx.mlp_init(self.dims[0], self.dims[1], self.dims[3])
+        ctx.mlp_set_params(z["params"])
+
+    def predict(self, atoms, xyz_angstrom) -> np.ndarray:
+        pairs, feat, Q, t, mask = pair_data(atoms, xyz_angstrom)
+        Xn = (feat - self.mu_x) / self.sd_x
+        Yn = self.ctx.mlp_forward(Xn.astype(np.float32)).astype(np.float64)
+        Y = (Yn * self.sd_y[t] + self.mu_y[t]) * mask
+        return assemble(atoms, Y, pairs, Q)
+
+    def guess(self, sysm, S: np.ndarray):
+        """Predicted closed-shell density, or None when it fails the
+        electron-count or idempotency check (the caller then uses the core
+        guess)."""
+        atoms, xyz = system_geometry(sysm)
+        D = self.predict(atoms, xyz)
+        ok, _, _ = check_density(D, S, sysm.nelcA + sysm.nelcB)
+        return D if ok else None

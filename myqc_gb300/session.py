@@ -172,6 +172,10 @@ class Context:
         self._check(self.L.mq_mlp_train_epoch(self.h, ptr(perm), batch, ctypes.c_float(lr), ctypes.byref(loss)))
         return loss.value
 
+    def set_fock_precision(self, precision: int):
+        """_lib.FOCK_FP64 (default) or _lib.FOCK_DF32 (double-float digestion)."""
+        self._check(self.L.mq_set_fock_precision(self.h, precision))
+
     def set_schwarz(self, thr: float):
         self._check(self.L.mq_set_schwarz(self.h, thr))
 

@@ -1,0 +1,197 @@
+"""Train the learned density guess on densities from the batched SCF.
+
+    python -m myqc_gb300.train_guess --train 20000 --test 2048 --out myqc_gb300/data/guess_mlp.npz
+
+Seeded (H2O)_n clusters, n uniform in 2..16, rigid monomers in cubes of side
+(27 n)^(1/3) A (about one molecule per 27 A^3), are solved by the batched SCF
+(RHF/STO-3G, tight integrals, DIIS(8), RMS dD < 1e-10).  Each converged
+density is cut into local-frame pair blocks (guess.py) which, with the pair
+descriptors, are the training samples of the MLP (3 layers, width 256, BF16
+weights, FP32 accumulation, Adam; mlp.cu).  Held-out geometries are then
+solved twice by the batched SCF, from the core-Hamiltonian guess and from the
+learned guess (with the core guess as fallback), and the iteration counts and
+energy differences are written next to the model.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, ROOT)
+
+from myqc_gb300 import formats, guess, molecules  # noqa: E402
+from myqc_gb300.session import Context  # noqa: E402
+
+BASIS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data", "sto3g.mybasis")
+
+
+def geometries(count: int, seed: int, kmin: int = 2, kmax: int = 16):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    out = []
+    for i in range(count):
+        k = int(rng.integers(kmin, kmax + 1))
+        sym, xyz = molecules.water_cluster(k, (27.0 * k) ** (1 / 3), seed * 1000003 + i)
+        out.append(formats.system_from_geometry(sym, xyz, calc_mp2=False))
+    return out
+
+
+def solve_batches(ctx, systems, budget_bytes=1.2e11, guesses=None, **kw):
+    """Batched SCF over `systems` in chunks of at most budget_bytes of XX;
+    returns per-molecule energy, iterations, converged, D and the wall time."""
+    btext = open(BASIS).read()
+    E, it, cv, Ds = [], [], [], []
+    wall = 0.0
+    i = 0
+    while i < len(systems):
+        ctx.batch_clear()
+        used, j = 0.0, i
+        while j < len(systems):
+            n = sum(1 if z == 1 else 5 for z in systems[j].atoms)
+            if j > i and used + 8.0 * n ** 4 > budget_bytes:
+                break
+            used += 8.0 * n ** 4
+            ctx.batch_add(systems[j], formats.parse_mybasis_text(btext, systems[j].atoms))
+            j += 1
+        t = time.perf_counter()
+        out = ctx.batch_scf(D_guess=None if guesses is None else guesses[i:j], **kw)
+        wall += time.perf_counter() - t
+        E.extend(out["energy"])
+        it.extend(out["iterations"])
+        cv.extend(out["converged"])
+        Ds.extend(out["D"])
+        i = j
+    return np.array(E), np.array(it), np.array(cv), Ds, wall
+
+
+SCF = dict(conv=1e-10, conv_rms=True, diis=8, max_iter=100, graph=True)
+
+
+def _samples(item):
+    atoms, xyz, D = item
+    pairs, f, Q, t, m = guess.pair_data(atoms, xyz)
+    return f, guess.extract_blocks(atoms, D, pairs, Q).astype(np.float32), t, m
+
+
+def build_dataset(systems, Ds, workers: int = 0):
+    """Pair samples of every converged density; host work spread over a pool of
+    spawned processes (no GPU use in the workers)."""
+    items = [(*guess.system_geometry(s), D) for s, D in zip(systems, Ds)]
+    if workers > 1:
+        import multiprocessing as mp
+        with mp.get_context("spawn").Pool(workers) as pool:
+            res = pool.map(_samples, items, chunksize=16)
+    else:
+        res = [_samples(it) for it in items]
+    return tuple(np.concatenate([r[k] for r in res]) for k in range(4))
+
+
+def normalisation(X, Y, t, M):
+    mu_x = X.mean(0)
+    sd_x = X.std(0)
+    sd_x[sd_x < 1e-6] = 1.0
+    mu_y = np.zeros((guess.NTYPES, guess.NOUT))
+    sd_y = np.ones((guess.NTYPES, guess.NOUT))
+    for k in range(guess.NTYPES):
+        sel = t == k
+        if not sel.any():
+            continue
+        m = M[sel] > 0
+        y = Y[sel]
+        cnt = np.maximum(m.sum(0), 1)
+        mu = (y * m).sum(0) / cnt
+        sd = np.sqrt((((y - mu) * m) ** 2).sum(0) / cnt)
+        mu_y[k] = np.where(m.any(0), mu, 0.0)
+        sd_y[k] = np.where(sd > 1e-8, sd, 1.0)
+    return mu_x, sd_x, mu_y, sd_y
+
+
+def train(ctx, X, Y, t, M, epochs: int, batch: int, lr: float, seed: int):
+    mu_x, sd_x, mu_y, sd_y = normalisation(X, Y, t, M)
+    Xn = ((X - mu_x) / sd_x).astype(np.float32)
+    Yn = (((Y - mu_y[t]) / sd_y[t]) * M).astype(np.float32)
+    dims = (guess.NFEAT, 256, 256, guess.NOUT)
+    ctx.mlp_init(dims[0], dims[1], dims[3])
+    rng = np.random.default_rng(seed)
+    parts = []
+    for l in range(3):  # fan-in scaled normal weights, zero biases
+        W = rng.standard_normal((dims[l + 1], dims[l])) * np.sqrt(1.0 / dims[l])
+        parts.append(np.concatenate([W.ravel(), np.zeros(dims[l + 1])]))
+    ctx.mlp_set_params(np.concatenate(parts).astype(np.float32))
+    ctx.mlp_set_data(Xn, Yn, M.astype(np.float32))
+    hist = []
+    for e in range(epochs):
+        lr_e = lr * 0.5 * (1 + np.cos(np.pi * e / epochs)) + 1e-5
+        hist.append(ctx.mlp_train_epoch(batch, lr_e, seed + e))
+        print(f"epoch {e} lr {lr_e:.2e} loss {hist[-1]:.5f}", flush=True)
+    return ctx.mlp_get_params(), dims, (mu_x, sd_x, mu_y, sd_y), hist
+
+
+def evaluate(ctx, model_path, systems):
+    """Held-out geometries: batched SCF from the core guess and from the learned
+    guess (core guess where the prediction fails its checks)."""
+    E0, it0, cv0, _, t0 = solve_batches(ctx, systems, **SCF)
+    lg = guess.LearnedGuess(ctx, model_path)
+    btext = open(BASIS).read()
+    gs, nfail = [], 0
+    tp = time.perf_counter()
+    for s in systems:
+        ctx.set_system(s, formats.parse_mybasis_text(btext, s.atoms), None, 1)
+        S, _ = ctx.int1e()
+        D = lg.guess(s, S)
+        nfail += D is None
+        gs.append(D)
+    tpred = time.perf_counter() - tp
+    E1, it1, cv1, _, t1 = solve_batches(ctx, systems, guesses=gs, **SCF)
+    both = cv0 & cv1
+    return {"n": len(systems), "predictions_failed_checks": int(nfail),
+            "iterations_core_mean": float(it0.mean()), "iterations_learned_mean": float(it1.mean()),
+            "iteration_ratio": float(it0.mean() / it1.mean()),
+            "converged_core": int(cv0.sum()), "converged_learned": int(cv1.sum()),
+            "max_abs_dE_Eh": float(np.max(np.abs(E1[both] - E0[both]))) if both.any() else None,
+            "scf_wall_s_core": t0, "scf_wall_s_learned": t1, "prediction_wall_s": tpred}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--train", type=int, default=20000)
+    ap.add_argument("--test", type=int, default=2048)
+    ap.add_argument("--kmax", type=int, default=16)
+    ap.add_argument("--epochs", type=int, default=30)
+    ap.add_argument("--batch", type=int, default=4096)
+    ap.add_argument("--lr", type=float, default=2e-3)
+    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--out", default=os.path.join(os.path.dirname(os.path.abspath(__file__)), "data", "guess_mlp.npz"))
+    args = ap.parse_args()
+    ctx = Context()
+    t = time.perf_counter()
+    train_sys = geometries(args.train, args.seed, kmax=args.kmax)
+    E, it, cv, Ds, wall = solve_batches(ctx, train_sys, **SCF)
+    print(f"training SCF: {len(train_sys)} clusters, {cv.mean():.4f} converged, {wall:.1f} s SCF, "
+          f"{time.perf_counter() - t:.1f} s total", flush=True)
+    keep = [i for i in range(len(train_sys)) if cv[i]]
+    X, Y, ty, M = build_dataset([train_sys[i] for i in keep], [Ds[i] for i in keep],
+                                workers=min(16, os.cpu_count() or 1))
+    del Ds
+    print(f"dataset: {len(X)} pair samples", flush=True)
+    params, dims, (mu_x, sd_x, mu_y, sd_y), hist = train(ctx, X, Y, ty, M, args.epochs, args.batch, args.lr,
+                                                         args.seed)
+    os.makedirs(os.path.dirname(args.out), exist_ok=True)
+    np.savez(args.out, params=params, dims=np.array(dims), mu_x=mu_x, sd_x=sd_x, mu_y=mu_y, sd_y=sd_y,
+             loss=np.array(hist))
+    test_sys = geometries(args.test, args.seed + 7777, kmax=args.kmax)
+    ev = evaluate(ctx, args.out, test_sys)
+    ev.update({"train_clusters": len(keep), "pair_samples": int(len(X)), "epochs": args.epochs,
+               "final_loss": hist[-1]})
+    print(json.dumps(ev), flush=True)
+    with open(os.path.splitext(args.out)[0] + "_eval.json", "w") as f:
+        json.dump(ev, f, indent=1)
+
+
+if __name__ == "__main__":
+    main()
