@@ -401,11 +401,15 @@ int mq_mp2_uhf(mq_ctx *c, const double *CA, const double *CB, const double *eA, 
 int mq_mp2_pairs(mq_ctx *c, const double *iajb, int no1, int nv1, int no2, int nv2, const double *e1,
                  const double *e2, int same_spin, double *e_out) {
   if (!c) return MQ_EINVAL;
-  if (!iajb || !e1 || !e2 || !e_out || no1 < 0 || nv1 < 0 || no2 < 0 || nv2 < 0)
-    return set_err(c, MQ_EINVAL, "bad mp2 pair arguments");
-  cudaSetDevice(c->device);
   const size_t nel = (size_t)no1 * nv1 * no2 * nv2;
-  double *d = to_dev(c, "mp2_pairs_in", iajb, std::max<size_t>(nel, 1));
+  if ((nel && !iajb) || !e1 || !e2 || !e_out || no1 < 0 || nv1 < 0 || no2 < 0 || nv2 < 0)
+    return set_err(c, MQ_EINVAL, "bad mp2 pair arguments");
+  if (nel == 0) {  // no occupied or no virtual orbitals on one side: no pairs
+    e_out[0] = e_out[1] = 0.0;
+    return MQ_OK;
+  }
+  cudaSetDevice(c->device);
+  double *d = to_dev(c, "mp2_pairs_in", iajb, nel);
   if (!d) return MQ_ENOMEM;
   double *de = (double *)buf(c, "mp2_pairs_eig", sizeof(double) * ((size_t)no1 + nv1 + no2 + nv2 + 2));
   if (!de) return MQ_ENOMEM;

@@ -262,6 +262,9 @@ int density_device(mq_ctx *c, int n, int nocc, const double *d_C, double factor,
 // doubles); MQ_ENOCONV when the frontier levels are degenerate
 int purify_projector(mq_ctx *c, int n, int nocc, const double *d_Fp, double *d_P, double *d_T, double *d_W,
                      double *d_err, int *steps);
+// X = S^-1/2 by the coupled Newton-Schulz iteration (w: 5 n^2 doubles of
+// scratch, d_err: >= 101 doubles); MQ_ENOCONV when it does not settle
+int inv_sqrt_ns(mq_ctx *c, int n, const double *d_S, double *d_X, double *w, double *d_err, int *steps);
 void cublas_destroy(void *handle);
 
 // ao2mo.cu

@@ -17,6 +17,7 @@
 // change: at a gapped spectrum P is exactly the aufbau projector.  Without a
 // gap (degenerate frontier levels) the error stalls and the caller falls back
 // to the eigensolver for that iteration.
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -143,6 +144,93 @@ int purify_projector(mq_ctx *c, int n, int nocc, const double *d_Fp, double *d_P
   *steps = k;
   if (settled_at < 0) return set_err(c, MQ_ENOCONV, "purification did not converge (no gap at the Fermi level?)");
   if (X != d_P) MQ_CUDA(c, cudaMemcpyAsync(d_P, X, n2 * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+  return MQ_OK;
+}
+
+// ---- S^-1/2 by the coupled Newton-Schulz iteration (Higham, "Functions of
+// Matrices", 2008, eq. 6.35): with Y_0 = S / c, Z_0 = I and
+//   T_k = (3 I - Z_k Y_k) / 2,  Y_{k+1} = Y_k T_k,  Z_{k+1} = T_k Z_k,
+// Y -> (S/c)^(1/2) and Z -> (S/c)^(-1/2) quadratically once the spectrum of
+// Z Y is near 1; c >= lambda_max(S) (Gershgorin) keeps every eigenvalue of
+// S/c in (0, 1].  X = Z / sqrt(c).  Three FP64 GEMMs per step, no eigensolver.
+
+// T = 1.5 I - 0.5 A (A = Z Y); err[k] = ||I - A||_F^2 (block 0)
+__global__ void ns_step_kernel(const double *__restrict__ A, int n, double *__restrict__ T, double *__restrict__ err,
+                               int k) {
+  __shared__ double red[32];
+  const size_t N = n, n2 = N * N;
+  double e = 0.0;
+  for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < n2; idx += (size_t)gridDim.x * blockDim.x) {
+    const double d = (idx % (N + 1) == 0) ? 1.0 - A[idx] : -A[idx];
+    e += d * d;
+    T[idx] = 0.5 * d + ((idx % (N + 1) == 0) ? 1.0 : 0.0);
+  }
+  e = block_sum(e, red);
+  if (threadIdx.x == 0) atomicAdd(err + k, e);
+}
+
+// Y = S / c with c the Gershgorin bound of S; Z = I; scal[0] = c
+__global__ void __launch_bounds__(PUR_THREADS) ns_init_kernel(const double *__restrict__ S, int n,
+                                                              double *__restrict__ Y, double *__restrict__ Z,
+                                                              double *__restrict__ scal) {
+  __shared__ double red[PUR_THREADS / 32];
+  const size_t N = n;
+  double nhi = INFINITY;
+  for (int r = threadIdx.x; r < n; r += blockDim.x) {
+    double s = 0.0;
+    for (int j = 0; j < n; ++j) s += fabs(S[r + N * j]);
+    nhi = fmin(nhi, -s);
+  }
+  const double c = -block_min(nhi, red);
+  for (size_t idx = threadIdx.x; idx < N * N; idx += blockDim.x) {
+    Y[idx] = S[idx] / c;
+    Z[idx] = (idx % (N + 1) == 0) ? 1.0 : 0.0;
+  }
+  if (threadIdx.x == 0) scal[0] = c;
+}
+
+__global__ void scale_kernel(const double *__restrict__ A, size_t n2, const double *__restrict__ c,
+                             double *__restrict__ out) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n2) out[i] = A[i] * rsqrt(c[0]);
+}
+
+int inv_sqrt_ns(mq_ctx *c, int n, const double *d_S, double *d_X, double *w, double *d_err, int *steps) {
+  const size_t n2 = (size_t)n * n;
+  double *Y = w, *Z = w + n2, *T = w + 2 * n2, *A = w + 3 * n2, *Y2 = w + 4 * n2;
+  constexpr int MAX_STEPS = 100, POLL = 4;
+  const unsigned gb = (unsigned)std::min<size_t>((n2 + 255) / 256, 1024);
+  MQ_CUDA(c, cudaMemsetAsync(d_err, 0, (MAX_STEPS + 1) * sizeof(double), c->stream));
+  ns_init_kernel<<<1, PUR_THREADS, 0, c->stream>>>(d_S, n, Y, Z, d_err + MAX_STEPS);
+  c->stats.launches += 1;
+  std::vector<double> e(MAX_STEPS);
+  int k = 0, done_at = -1;
+  while (k < MAX_STEPS) {
+    MQ_TRY(gemm(c, 'N', 'N', n, n, n, 1.0, Z, n, Y, n, 0.0, A, n));
+    ns_step_kernel<<<gb, 256, 0, c->stream>>>(A, n, T, d_err, k);
+    c->stats.launches += 1;
+    MQ_TRY(gemm(c, 'N', 'N', n, n, n, 1.0, Y, n, T, n, 0.0, Y2, n));
+    MQ_TRY(gemm(c, 'N', 'N', n, n, n, 1.0, T, n, Z, n, 0.0, A, n));
+    std::swap(Y, Y2);
+    std::swap(Z, A);  // A is scratch again
+    ++k;
+    if (done_at >= 0 && k >= done_at + 2) break;
+    if (done_at < 0 && k % POLL == 0) {
+      MQ_CUDA(c, cudaMemcpyAsync(e.data(), d_err, k * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+      MQ_CUDA(c, cudaStreamSynchronize(c->stream));
+      for (int j = 0; j < k; ++j)
+        if (e[j] < 1e-16 * n) {  // ||I - Z_j Y_j|| ~ 1e-8: two more steps reach round-off
+          done_at = j;
+          break;
+        }
+      if (done_at >= 0 && k >= done_at + 2) break;
+    }
+  }
+  *steps = k;
+  if (done_at < 0) return set_err(c, MQ_ENOCONV, "Newton-Schulz S^-1/2 did not converge");
+  scale_kernel<<<(unsigned)((n2 + 255) / 256), 256, 0, c->stream>>>(Z, n2, d_err + MAX_STEPS, d_X);
+  c->stats.launches += 1;
+  MQ_CUDA(c, cudaGetLastError());
   return MQ_OK;
 }
 

@@ -206,15 +206,25 @@ int scf_device(mq_ctx *c, const double *S, const double *H, const mq_scf_opts *o
   MQ_CUDA(c, cudaMemcpyAsync(dS, S, n2 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
   MQ_CUDA(c, cudaMemcpyAsync(dH, H, n2 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
 
-  // X = S^-1/2
-  MQ_CUDA(c, cudaMemcpyAsync(dT1, dS, n2 * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
-  MQ_TRY(syev_batched_device(c, n, 1, dT1, dEps, dU));
-  std::vector<double> sev(n);
-  MQ_CUDA(c, cudaMemcpyAsync(sev.data(), dEps, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
-  MQ_CUDA(c, cudaStreamSynchronize(c->stream));
-  if (sev[0] <= 0.0) return set_err(c, MQ_EINVAL, "overlap matrix is not positive definite");
-  scale_cols_kernel<<<blocks(n2), 256, 0, c->stream>>>(dU, dEps, dW, n, -0.5);
-  MQ_TRY(gemm(c, 'N', 'T', n, n, n, 1.0, dW, n, dU, n, 0.0, dX, n));
+  // X = S^-1/2: Newton-Schulz (GEMMs only) with purification, else (and as its
+  // fallback) the eigendecomposition S = U s U^T
+  bool have_x = false;
+  if (o->purify) {
+    int ns_steps = 0;
+    const int rc = inv_sqrt_ns(c, n, dS, dX, dT1, dScal + 128, &ns_steps);  // scratch dT1..dW (5 n^2)
+    if (rc != MQ_OK && rc != MQ_ENOCONV) return rc;
+    have_x = rc == MQ_OK;
+  }
+  if (!have_x) {
+    MQ_CUDA(c, cudaMemcpyAsync(dT1, dS, n2 * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+    MQ_TRY(syev_batched_device(c, n, 1, dT1, dEps, dU));
+    std::vector<double> sev(n);
+    MQ_CUDA(c, cudaMemcpyAsync(sev.data(), dEps, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    MQ_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (sev[0] <= 0.0) return set_err(c, MQ_EINVAL, "overlap matrix is not positive definite");
+    scale_cols_kernel<<<blocks(n2), 256, 0, c->stream>>>(dU, dEps, dW, n, -0.5);
+    MQ_TRY(gemm(c, 'N', 'T', n, n, n, 1.0, dW, n, dU, n, 0.0, dX, n));
+  }
 
   // solve F C = S C e for ns Fock matrices in dF -> dC, dEps.  Eigenvectors
   // (orthogonal basis) go to dU (and dW, which follows it, for beta).  Large

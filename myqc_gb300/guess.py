@@ -86,17 +86,13 @@ def pairs_of(atoms, xyz_angstrom: np.ndarray, cutoff: float = CUTOFF) -> np.ndar
     """Atom pairs (A, B), each unordered pair once and within the cutoff, plus
     the diagonal (A, A); the heavier element comes first."""
     atoms = np.asarray(atoms)
-    n = len(atoms)
-    out = []
-    for a in range(n):
-        for b in range(a, n):
-            if a != b and np.linalg.norm(xyz_angstrom[a] - xyz_angstrom[b]) > cutoff:
-                continue
-            if atoms[b] > atoms[a]:
-                out.append((b, a))
-            else:
-                out.append((a, b))
-    return np.array(out, dtype=np.int64).reshape(-1, 2)
+    xyz = np.asarray(xyz_angstrom, dtype=float)
+    d = np.linalg.norm(xyz[:, None, :] - xyz[None, :, :], axis=-1)
+    a, b = np.triu_indices(len(atoms))
+    keep = (a == b) | (d[a, b] <= cutoff)
+    a, b = a[keep], b[keep]
+    swap = atoms[b] > atoms[a]
+    return np.stack([np.where(swap, b, a), np.where(swap, a, b)], axis=1).astype(np.int64)
 
 
 def block_type(za: np.ndarray, zb: np.ndarray, diag: np.ndarray) -> np.ndarray:
@@ -202,10 +198,10 @@ def assemble(atoms, blocks: np.ndarray, pairs: np.ndarray, Q: np.ndarray) -> np.
 def output_mask(atoms, pairs: np.ndarray) -> np.ndarray:
     """(npairs, NOUT) 1 where the padded 5 x 5 block holds a real entry."""
     _, nao = ao_layout(atoms)
-    m = np.zeros((len(pairs), 5, 5), dtype=np.float32)
-    for p, (a, b) in enumerate(pairs):
-        m[p, :nao[a], :nao[b]] = 1.0
-    return m.reshape(len(pairs), NOUT)
+    r = np.arange(5)
+    va = r[None, :] < nao[pairs[:, 0]][:, None]
+    vb = r[None, :] < nao[pairs[:, 1]][:, None]
+    return (va[:, :, None] & vb[:, None, :]).reshape(len(pairs), NOUT).astype(np.float32)
 
 
 def check_density(D: np.ndarray, S: np.ndarray, nelec: int, tol_count: float = 0.5, tol_idem: float = 0.25):

@@ -51,7 +51,8 @@ def test_stage_chain(tmp_path, ftab, basis_text, name):
     E = _number(r"Total SCF energy \(a\.u\)", out)
     assert abs(E - ref["scf"].energy) < 1e-9, (E, ref["scf"].energy)
     Emp2 = _number(r"E\(MBPT2\) =", out)
-    assert abs(Emp2 - ref["mp2"]["E_MP2"]) < 1e-8, (Emp2, ref["mp2"])
+    mp2 = ref["mp2"] if "mp2" in ref else O.mp2(ref["mol"], ref["scf"], ref["XX"])
+    assert abs(Emp2 - mp2["E_MP2"]) < 1e-8, (Emp2, mp2)
     for f in ("Cui", "eig", "MOLDEN", "ijab_AB", "basinfo", "setinfo"):
         assert (tmp_path / f).exists(), f
     # a stage started after a failure does nothing
