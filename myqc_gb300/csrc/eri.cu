@@ -126,21 +126,27 @@ __device__ __forceinline__ void pair_E(double PA, double PB, double i2p, double 
   e[1][1][2] = i2p * i2p;
 }
 
-template <int LA, int LB, int LC, int LD, int A0, int A1, int B0, int B1, int EPI>
+// One contracted quartet (P, Q), the bra functions a in [A0, A1), b in [B0, B1)
+// and ket functions c in [C0, C1), d in [D0, D1) of it (a thread's share when a
+// quartet is split over threads).  With the whole bra in one thread (ONFLY)
+// the bra Hermite products are formed on the fly from the per-axis
+// coefficients instead of being kept for every (a, b): a ket-split thread then
+// forms each ket contraction W once and applies it to all 16 bra functions.
+template <int LA, int LB, int LC, int LD, int A0, int A1, int B0, int B1, int C0, int C1, int D0, int D1, int EPI>
 __device__ __forceinline__ void quartet(const EriArgs &g, int P, int Q, size_t n, double *XXout) {
-  constexpr int NC = nfun(LC), ND = nfun(LD);
   constexpr int LAB = LA + LB, LT = LA + LB + LC + LD;
   constexpr int QREF = 3 * LT;  // the reference's Boys order for s/sp sets
+  constexpr bool ONFLY = (A1 - A0) * (B1 - B0) > 4;
   const PairTable &t = g.t;
-  double acc[A1 - A0][B1 - B0][NC][ND];
+  double acc[A1 - A0][B1 - B0][C1 - C0][D1 - D0];
 #pragma unroll
   for (int a = 0; a < A1 - A0; ++a)
 #pragma unroll
     for (int b = 0; b < B1 - B0; ++b)
 #pragma unroll
-      for (int c = 0; c < NC; ++c)
+      for (int c = 0; c < C1 - C0; ++c)
 #pragma unroll
-        for (int d = 0; d < ND; ++d) acc[a][b][c][d] = 0.0;
+        for (int d = 0; d < D1 - D0; ++d) acc[a][b][c][d] = 0.0;
 
   const int p0 = t.pp_off[P], p1 = t.pp_off[P + 1];
   const int q0 = t.pp_off[Q], q1 = t.pp_off[Q + 1];
@@ -157,20 +163,24 @@ __device__ __forceinline__ void quartet(const EriArgs &g, int P, int Q, size_t n
     double cab[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) cab[k] = t.c4[4 * ip + k];
-    // bra products E^{ab}_{tuv} * c_a c_b K_ab
-    double eb[A1 - A0][B1 - B0][3][3][3];
+    // bra products E^{ab}_{tuv} * c_a c_b K_ab (kept per (a, b) unless ONFLY)
+    double eb[ONFLY ? 1 : A1 - A0][ONFLY ? 1 : B1 - B0][3][3][3];
+    if (!ONFLY) {
 #pragma unroll
-    for (int a = A0; a < A1; ++a)
+      for (int a = A0; a < A1; ++a)
 #pragma unroll
-      for (int b = B0; b < B1; ++b)
+        for (int b = B0; b < B1; ++b)
 #pragma unroll
-        for (int x = 0; x <= fl(a, 0) + fl(b, 0); ++x)
+          for (int x = 0; x <= fl(a, 0) + fl(b, 0); ++x)
 #pragma unroll
-          for (int y = 0; y <= fl(a, 1) + fl(b, 1); ++y)
+            for (int y = 0; y <= fl(a, 1) + fl(b, 1); ++y)
 #pragma unroll
-            for (int z = 0; z <= fl(a, 2) + fl(b, 2); ++z)
-              eb[a - A0][b - B0][x][y][z] = ex[fl(a, 0)][fl(b, 0)][x] * ey[fl(a, 1)][fl(b, 1)][y] *
-                                            ez[fl(a, 2)][fl(b, 2)][z] * cab[2 * fang(a) + fang(b)];
+              for (int z = 0; z <= fl(a, 2) + fl(b, 2); ++z)
+                eb[ONFLY ? 0 : a - A0][ONFLY ? 0 : b - B0][x][y][z] = ex[fl(a, 0)][fl(b, 0)][x] *
+                                                                     ey[fl(a, 1)][fl(b, 1)][y] *
+                                                                     ez[fl(a, 2)][fl(b, 2)][z] *
+                                                                     cab[2 * fang(a) + fang(b)];
+    }
     for (int iq = q0; iq < q1; ++iq) {
       const double Kcd = t.K[iq];
       if (Kab * Kcd < 1.0e-14) continue;  // int2e.f90:257
@@ -197,9 +207,9 @@ __device__ __forceinline__ void quartet(const EriArgs &g, int P, int Q, size_t n
 #pragma unroll
       for (int k = 0; k < 4; ++k) ccd[k] = t.c4[4 * iq + k];
 #pragma unroll
-      for (int c = 0; c < NC; ++c)
+      for (int c = C0; c < C1; ++c)
 #pragma unroll
-        for (int d = 0; d < ND; ++d) {
+        for (int d = D0; d < D1; ++d) {
           const double cf = ccd[2 * fang(c) + fang(d)];
           double W[LAB + 1][LAB + 1][LAB + 1];
 #pragma unroll
@@ -230,8 +240,13 @@ __device__ __forceinline__ void quartet(const EriArgs &g, int P, int Q, size_t n
 #pragma unroll
                 for (int y = 0; y <= fl(a, 1) + fl(b, 1); ++y)
 #pragma unroll
-                  for (int z = 0; z <= fl(a, 2) + fl(b, 2); ++z) v += eb[a - A0][b - B0][x][y][z] * W[x][y][z];
-              acc[a - A0][b - B0][c][d] += v;
+                  for (int z = 0; z <= fl(a, 2) + fl(b, 2); ++z) {
+                    const double e = ONFLY ? ex[fl(a, 0)][fl(b, 0)][x] * ey[fl(a, 1)][fl(b, 1)][y] *
+                                                 ez[fl(a, 2)][fl(b, 2)][z]
+                                           : eb[ONFLY ? 0 : a - A0][ONFLY ? 0 : b - B0][x][y][z];
+                    v += e * W[x][y][z];
+                  }
+              acc[a - A0][b - B0][c - C0][d - D0] += ONFLY ? v * cab[2 * fang(a) + fang(b)] : v;
             }
         }
     }
@@ -246,11 +261,11 @@ __device__ __forceinline__ void quartet(const EriArgs &g, int P, int Q, size_t n
     for (int a = A0; a < A1; ++a)
 #pragma unroll
       for (int b = B0; b < B1; ++b)
-        if (a < NC && b < ND) m = fmax(m, fabs(acc[a - A0][b - B0][a][b]));
+        if (a >= C0 && a < C1 && b >= D0 && b < D1) m = fmax(m, fabs(acc[a - A0][b - B0][a - C0][b - D0]));
     atomicMax(g.sch + P, (unsigned long long)__double_as_longlong(sqrt(m)));
     return;
   }
-  if (g.counters && A0 == 0 && B0 == 0) {  // one atomic pair per warp, not per quartet
+  if (g.counters && A0 == 0 && B0 == 0 && C0 == 0 && D0 == 0) {  // one atomic pair per warp, not per quartet
     const unsigned act = __activemask();
     const unsigned nq_w = __popc(act), np_w = __reduce_add_sync(act, nprim);
     if ((threadIdx.x & 31) == __ffs(act) - 1) {
@@ -263,14 +278,14 @@ __device__ __forceinline__ void quartet(const EriArgs &g, int P, int Q, size_t n
 #pragma unroll
     for (int b = B0; b < B1; ++b)
 #pragma unroll
-      for (int c = 0; c < NC; ++c)
+      for (int c = C0; c < C1; ++c)
 #pragma unroll
-        for (int d = 0; d < ND; ++d) {
+        for (int d = D0; d < D1; ++d) {
           const int i = i0 + a, j = j0 + b, k = k0 + c, l = l0 + d;
           if (A == B && i < j) continue;
           if (C == D && k < l) continue;
           if (P == Q && (size_t)i * n + j < (size_t)k * n + l) continue;
-          const double x = acc[a - A0][b - B0][c][d];
+          const double x = acc[a - A0][b - B0][c - C0][d - D0];
           if (EPI == EPI_XX) {
             double *XX = XXout;
             const size_t ij = (size_t)i + n * j, ji = (size_t)j + n * i, kl = (size_t)k + n * l,
@@ -369,22 +384,23 @@ __global__ void __launch_bounds__(128) eri_kernel(EriArgs g) {
     n = (size_t)g.mols[m].n;
     XX += g.mols[m].xx;
   }
+  constexpr int NC = nfun(LC), ND = nfun(LD);
   if (NSPLIT == 1) {
-    quartet<LA, LB, LC, LD, 0, NA, 0, NB, EPI>(g, P, Q, n, XX);
-  } else if (NSPLIT == 4) {
+    quartet<LA, LB, LC, LD, 0, NA, 0, NB, 0, NC, 0, ND, EPI>(g, P, Q, n, XX);
+  } else if (NSPLIT == 4) {  // (sp sp|sp s): one ket function c per thread, the whole bra
     switch (split) {
-      case 0: quartet<LA, LB, LC, LD, 0, 1, 0, NB, EPI>(g, P, Q, n, XX); break;
-      case 1: quartet<LA, LB, LC, LD, 1, 2, 0, NB, EPI>(g, P, Q, n, XX); break;
-      case 2: quartet<LA, LB, LC, LD, 2, 3, 0, NB, EPI>(g, P, Q, n, XX); break;
-      default: quartet<LA, LB, LC, LD, 3, 4, 0, NB, EPI>(g, P, Q, n, XX); break;
+      case 0: quartet<LA, LB, LC, LD, 0, NA, 0, NB, 0, 1, 0, ND, EPI>(g, P, Q, n, XX); break;
+      case 1: quartet<LA, LB, LC, LD, 0, NA, 0, NB, 1, 2, 0, ND, EPI>(g, P, Q, n, XX); break;
+      case 2: quartet<LA, LB, LC, LD, 0, NA, 0, NB, 2, 3, 0, ND, EPI>(g, P, Q, n, XX); break;
+      default: quartet<LA, LB, LC, LD, 0, NA, 0, NB, 3, 4, 0, ND, EPI>(g, P, Q, n, XX); break;
     }
-  } else {
+  } else {  // (sp sp|sp sp): one ket pair (c, d) per thread, the whole bra
 #define MQ_SPLIT16(s) \
-  case s: quartet<LA, LB, LC, LD, (s) / 4, (s) / 4 + 1, (s) % 4, (s) % 4 + 1, EPI>(g, P, Q, n, XX); break;
+  case s: quartet<LA, LB, LC, LD, 0, NA, 0, NB, (s) / 4, (s) / 4 + 1, (s) % 4, (s) % 4 + 1, EPI>(g, P, Q, n, XX); break;
     switch (split) {
       MQ_SPLIT16(0) MQ_SPLIT16(1) MQ_SPLIT16(2) MQ_SPLIT16(3) MQ_SPLIT16(4) MQ_SPLIT16(5) MQ_SPLIT16(6)
       MQ_SPLIT16(7) MQ_SPLIT16(8) MQ_SPLIT16(9) MQ_SPLIT16(10) MQ_SPLIT16(11) MQ_SPLIT16(12) MQ_SPLIT16(13)
-      MQ_SPLIT16(14) default: quartet<LA, LB, LC, LD, 3, 4, 3, 4, EPI>(g, P, Q, n, XX); break;
+      MQ_SPLIT16(14) default: quartet<LA, LB, LC, LD, 0, NA, 0, NB, 3, 4, 3, 4, EPI>(g, P, Q, n, XX); break;
     }
 #undef MQ_SPLIT16
   }
