@@ -25,6 +25,7 @@
 // bra function; the split index is constant per warp (warp w serves split
 // w % nsplit for 32 consecutive quartets), so no lane diverges.
 #include <algorithm>
+#include <vector>
 
 #include "boys.cuh"
 #include "internal.h"
@@ -56,6 +57,9 @@ struct EriArgs {
   const long long *mq_off;
   const int *pstart, *pcount;
   const MolDesc *mols;
+  // Schwarz-compacted launch: the quartet indices that pass the screen, in
+  // ascending order, nq of them (null: every index below nq, screened inline)
+  const long long *list;
 };
 
 __host__ __device__ constexpr int fl(int f, int axis) { return f == axis + 1 ? 1 : 0; }  // f: 0 s, 1 px, 2 py, 3 pz
@@ -183,7 +187,10 @@ __device__ __forceinline__ void quartet(const EriArgs &g, int P, int Q, size_t n
     }
     for (int iq = q0; iq < q1; ++iq) {
       const double Kcd = t.K[iq];
-      if (Kab * Kcd < 1.0e-14) continue;  // int2e.f90:257
+      // int2e.f90:257; not for the Schwarz bounds, which must bound the exact
+      // (ab|ab): the screen removes every primitive quartet of (ab|ab) for a
+      // distant pair while (ab|cd) with a compact partner survives it
+      if (EPI != EPI_SCHWARZ && Kab * Kcd < 1.0e-14) continue;
       ++nprim;
       const double q = t.p[iq], i2q = t.inv2p[iq];
       const double X = Px - t.Px[iq], Y = Py - t.Py[iq], Z = Pz - t.Pz[iq];
@@ -333,6 +340,8 @@ __device__ __forceinline__ void quartet(const EriArgs &g, int P, int Q, size_t n
 // one system); returns false past the end
 __device__ __forceinline__ bool decode(const EriArgs &g, long long q, int &P, int &Q, int &m) {
   if (q >= g.nq) return false;
+  const bool listed = g.list != nullptr;
+  if (listed) q = g.list[q];
   m = 0;
   int pOff = g.pOff, qOff = g.qOff, nQ = g.nQ;
   if (g.nmol) {  // largest m with mq_off[m] <= q
@@ -362,8 +371,39 @@ __device__ __forceinline__ bool decode(const EriArgs &g, long long q, int &P, in
     P = pOff + (int)(q / nQ);
     Q = qOff + (int)(q % nQ);
   }
-  if (g.thr > 0.0 && g.t.schwarz[P] * g.t.schwarz[Q] < g.thr) return false;
+  if (!listed && g.thr > 0.0 && g.t.schwarz[P] * g.t.schwarz[Q] < g.thr) return false;
   return true;
+}
+
+// Schwarz compaction of one class combination: every quartet index whose bound
+// passes goes to `list`.  Each CTA writes its survivors, in index order, to
+// its own slot of `part` (blockDim entries) and their number to `counts`; a
+// second kernel packs the slots in CTA order, so the list is ascending and the
+// same on every run.
+__global__ void quartet_screen_kernel(EriArgs g, long long *__restrict__ part, int *__restrict__ counts) {
+  __shared__ int warp_cnt[32], warp_off[33];
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  int P = 0, Q = 0, m = 0;
+  EriArgs h = g;
+  h.list = nullptr;
+  const bool keep = q < g.nq && decode(h, q, P, Q, m);
+  const unsigned bal = __ballot_sync(0xffffffffu, keep);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) warp_cnt[w] = __popc(bal);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    warp_off[0] = 0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) warp_off[k + 1] = warp_off[k] + warp_cnt[k];
+    counts[blockIdx.x] = warp_off[blockDim.x >> 5];
+  }
+  __syncthreads();
+  if (keep) part[(size_t)blockIdx.x * blockDim.x + warp_off[w] + __popc(bal & ((1u << lane) - 1))] = q;
+}
+
+__global__ void quartet_pack_kernel(const long long *__restrict__ part, const int *__restrict__ counts,
+                                    const long long *__restrict__ offs, int block, long long *__restrict__ list) {
+  const int b = blockIdx.x;
+  for (int k = threadIdx.x; k < counts[b]; k += blockDim.x) list[offs[b] + k] = part[(size_t)b * block + k];
 }
 
 template <int LA, int LB, int LC, int LD, int EPI>
@@ -444,6 +484,40 @@ static EriArgs base_args(mq_ctx *c) {
 }
 
 // all unique (bra class >= ket class) combinations
+// The surviving quartet indices of launch h (Schwarz screen) into a context
+// buffer; h.list / h.nq are set to the compacted list.  Warps of the integral
+// kernel then hold only quartets that compute, instead of mostly screened
+// lanes that idle while the others loop over their primitives.
+static int compact_quartets(mq_ctx *c, EriArgs &h) {
+  const int block = 256;
+  const long long nb = (h.nq + block - 1) / block;
+  if (nb == 0) return MQ_OK;
+  char *w = (char *)buf(c, "eri_screen", (size_t)nb * block * sizeof(long long) + (size_t)nb * (sizeof(int) + sizeof(long long)) + (size_t)h.nq * sizeof(long long) + 256);
+  if (!w) return MQ_ENOMEM;
+  long long *part = (long long *)w;
+  long long *list = part + (size_t)nb * block;
+  long long *offs = list + h.nq;
+  int *counts = (int *)(offs + nb);
+  quartet_screen_kernel<<<(unsigned)nb, block, 0, c->stream>>>(h, part, counts);
+  std::vector<int> hc((size_t)nb);
+  std::vector<long long> ho((size_t)nb);
+  MQ_CUDA(c, cudaMemcpyAsync(hc.data(), counts, nb * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  MQ_CUDA(c, cudaStreamSynchronize(c->stream));
+  long long tot = 0;
+  for (long long b = 0; b < nb; ++b) {
+    ho[b] = tot;
+    tot += hc[b];
+  }
+  MQ_CUDA(c, cudaMemcpyAsync(offs, ho.data(), nb * sizeof(long long), cudaMemcpyHostToDevice, c->stream));
+  quartet_pack_kernel<<<(unsigned)nb, 128, 0, c->stream>>>(part, counts, offs, block, list);
+  c->stats.launches += 2;
+  MQ_CUDA(c, cudaGetLastError());
+  MQ_CUDA(c, cudaStreamSynchronize(c->stream));  // offs (host vector) goes out of scope
+  h.list = list;
+  h.nq = tot;
+  return MQ_OK;
+}
+
 template <int EPI>
 static int run_all(mq_ctx *c, EriArgs g) {
   const int *off = c->pt.class_off;
@@ -459,6 +533,9 @@ static int run_all(mq_ctx *c, EriArgs g) {
       h.tri = cP == cQ;
       h.diag = 0;
       h.nq = h.tri ? (long long)nP * (nP + 1) / 2 : (long long)nP * nQ;
+      h.list = nullptr;
+      if (h.thr > 0.0) MQ_TRY(compact_quartets(c, h));
+      if (h.nq == 0) continue;
       MQ_TRY(launch_class<EPI>(c, h, cP, cQ));
     }
   return MQ_OK;

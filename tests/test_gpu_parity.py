@@ -173,3 +173,33 @@ def test_fock_double_float_matches_fp64(ctx, basis_text):
         ctx.set_fock_precision(FOCK_FP64)
     for a, b in ((G32, G64), (Ga32, Ga64), (Gb32, Gb64)):
         assert np.max(np.abs(a - b)) < 1e-12 * np.max(np.abs(b))
+
+
+def test_schwarz_screened_integrals(ctx, basis_text):
+    """Schwarz screening at 1e-12 (quartet lists compacted before the integral
+    launches): every dropped integral is below the bound, kept ones are
+    unchanged, and the direct Fock build from the screened quartets matches
+    the stored unscreened one."""
+    from myqc_gb300 import MODE_TIGHT, molecules
+    sysm = molecules.water_cluster_system(8, 8.0, 2)
+    basis = formats.parse_mybasis_text(basis_text, sysm.atoms)
+    ctx.set_schwarz(0.0)
+    ctx.set_system(sysm, basis, None, MODE_TIGHT)
+    XX = ctx.eri_full()
+    n = ctx.n
+    rng = np.random.default_rng(9)
+    D = rng.random((n, n)) * 0.1
+    D = D + D.T
+    G = ctx.fock(D)
+    try:
+        ctx.set_schwarz(1e-12)
+        XXs = ctx.eri_full()
+        nq = ctx.stat("quartets")
+        Gd = ctx.fock(D, direct=True)
+    finally:
+        ctx.set_schwarz(0.0)
+    kept = XXs != 0.0
+    assert np.array_equal(XXs[kept], XX[kept])
+    assert np.max(np.abs(XX[~kept])) < 1e-11
+    assert nq > 0
+    assert np.max(np.abs(Gd - G)) < 1e-9 * np.max(np.abs(G))
