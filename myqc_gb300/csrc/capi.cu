@@ -219,18 +219,13 @@ int mq_eri_store(mq_ctx *c) {
   MQ_TRY(need_system(c));
   cudaSetDevice(c->device);
   MQ_TRY(ensure_xx(c));
-  cudaEvent_t e0, e1;
-  cudaEventCreate(&e0);
-  cudaEventCreate(&e1);
-  cudaEventRecord(e0, c->stream);
-  int rc = eri_full_device(c, c->d_XX);
-  cudaEventRecord(e1, c->stream);
-  cudaEventSynchronize(e1);
-  float ms = 0;
-  cudaEventElapsedTime(&ms, e0, e1);
-  c->stats.ms_eri = ms;
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
+  // queued on the context's stream; the call returns without waiting (later
+  // calls on the context order after it)
+  c->t_eri.collect_sync();
+  c->t_eri.total = 0;
+  c->t_eri.start(c->stream);
+  const int rc = eri_full_device(c, c->d_XX);
+  c->t_eri.stop(c->stream);
   return rc;
 }
 
@@ -555,7 +550,11 @@ int mq_mlp_train_epoch(mq_ctx *c, const int *perm, int batch, float lr, double *
 int mq_stat(const mq_ctx *c, const char *key, double *value) {
   if (!c || !key || !value) return MQ_EINVAL;
   const Stats &s = c->stats;
-  if (!strcmp(key, "eri")) *value = s.ms_eri;
+  mq_ctx *mut = const_cast<mq_ctx *>(c);  // lazily collected device timings and counters
+  if (!strcmp(key, "eri")) {
+    mut->t_eri.collect_sync();
+    *value = c->t_eri.total;
+  }
   else if (!strcmp(key, "fock")) *value = s.ms_fock;
   else if (!strcmp(key, "diag")) *value = s.ms_diag;
   else if (!strcmp(key, "ao2mo")) *value = s.ms_ao2mo;
@@ -573,8 +572,14 @@ int mq_stat(const mq_ctx *c, const char *key, double *value) {
   else if (!strcmp(key, "tune_fock_ms")) *value = s.tune_fock_ms;
   else if (!strcmp(key, "lib_launches")) *value = s.lib_launches;
   else if (!strcmp(key, "launches")) *value = s.launches;
-  else if (!strcmp(key, "quartets")) *value = s.quartets;
-  else if (!strcmp(key, "prim_quartets")) *value = s.prim_quartets;
+  else if (!strcmp(key, "quartets") || !strcmp(key, "prim_quartets")) {
+    unsigned long long h[2] = {0, 0};
+    if (c->d_eri_counters) {
+      cudaMemcpyAsync(h, c->d_eri_counters, sizeof(h), cudaMemcpyDeviceToHost, mut->stream);
+      cudaStreamSynchronize(mut->stream);
+    }
+    *value = (double)h[key[0] == 'q' ? 0 : 1];
+  }
   else return MQ_EINVAL;
   return MQ_OK;
 }

@@ -25,6 +25,7 @@
 // bra function; the split index is constant per warp (warp w serves split
 // w % nsplit for 32 consecutive quartets), so no lane diverges.
 #include <algorithm>
+#include <string>
 #include <vector>
 
 #include "boys.cuh"
@@ -58,8 +59,10 @@ struct EriArgs {
   const int *pstart, *pcount;
   const MolDesc *mols;
   // Schwarz-compacted launch: the quartet indices that pass the screen, in
-  // ascending order, nq of them (null: every index below nq, screened inline)
+  // ascending order, *list_n of them (null: every index below nq, screened
+  // inline); nq is then only the bound the grid is sized for
   const long long *list;
+  const long long *list_n;
 };
 
 __host__ __device__ constexpr int fl(int f, int axis) { return f == axis + 1 ? 1 : 0; }  // f: 0 s, 1 px, 2 py, 3 pz
@@ -341,7 +344,10 @@ __device__ __forceinline__ void quartet(const EriArgs &g, int P, int Q, size_t n
 __device__ __forceinline__ bool decode(const EriArgs &g, long long q, int &P, int &Q, int &m) {
   if (q >= g.nq) return false;
   const bool listed = g.list != nullptr;
-  if (listed) q = g.list[q];
+  if (listed) {
+    if (q >= *g.list_n) return false;
+    q = g.list[q];
+  }
   m = 0;
   int pOff = g.pOff, qOff = g.qOff, nQ = g.nQ;
   if (g.nmol) {  // largest m with mq_off[m] <= q
@@ -398,6 +404,43 @@ __global__ void quartet_screen_kernel(EriArgs g, long long *__restrict__ part, i
   }
   __syncthreads();
   if (keep) part[(size_t)blockIdx.x * blockDim.x + warp_off[w] + __popc(bal & ((1u << lane) - 1))] = q;
+}
+
+// exclusive prefix sum of the CTA counts (one CTA) and the total
+__global__ void __launch_bounds__(1024) quartet_scan_kernel(const int *__restrict__ counts, long long nb,
+                                                            long long *__restrict__ offs, long long *__restrict__ total) {
+  __shared__ long long warp_sum[32];
+  __shared__ long long carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (long long base = 0; base < nb; base += blockDim.x) {
+    const long long i = base + threadIdx.x;
+    long long v = i < nb ? counts[i] : 0, x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const long long y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_sum[w] = x;
+    __syncthreads();
+    if (w == 0) {
+      long long t = lane < (int)(blockDim.x >> 5) ? warp_sum[lane] : 0;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const long long y = __shfl_up_sync(0xffffffffu, t, o);
+        if (lane >= o) t += y;
+      }
+      warp_sum[lane] = t;  // inclusive sums of the warps
+    }
+    __syncthreads();
+    const long long incl = x + (w ? warp_sum[w - 1] : 0) + carry;
+    if (i < nb) offs[i] = incl - v;
+    __syncthreads();
+    if (threadIdx.x == blockDim.x - 1) carry = incl;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *total = carry;
 }
 
 __global__ void quartet_pack_kernel(const long long *__restrict__ part, const int *__restrict__ counts,
@@ -488,33 +531,28 @@ static EriArgs base_args(mq_ctx *c) {
 // buffer; h.list / h.nq are set to the compacted list.  Warps of the integral
 // kernel then hold only quartets that compute, instead of mostly screened
 // lanes that idle while the others loop over their primitives.
-static int compact_quartets(mq_ctx *c, EriArgs &h) {
+static int compact_quartets(mq_ctx *c, EriArgs &h, int slot) {
   const int block = 256;
   const long long nb = (h.nq + block - 1) / block;
   if (nb == 0) return MQ_OK;
-  char *w = (char *)buf(c, "eri_screen", (size_t)nb * block * sizeof(long long) + (size_t)nb * (sizeof(int) + sizeof(long long)) + (size_t)h.nq * sizeof(long long) + 256);
+  // one buffer per class combination: the lists of all six stay alive until
+  // their integral launches have run (nothing here waits for the device)
+  const std::string name = "eri_screen" + std::to_string(slot);
+  char *w = (char *)buf(c, name.c_str(), (size_t)nb * block * sizeof(long long) + (size_t)nb * (sizeof(int) + sizeof(long long)) +
+                                             (size_t)h.nq * sizeof(long long) + 256);
   if (!w) return MQ_ENOMEM;
   long long *part = (long long *)w;
   long long *list = part + (size_t)nb * block;
   long long *offs = list + h.nq;
-  int *counts = (int *)(offs + nb);
+  long long *total = offs + nb;
+  int *counts = (int *)(total + 1);
   quartet_screen_kernel<<<(unsigned)nb, block, 0, c->stream>>>(h, part, counts);
-  std::vector<int> hc((size_t)nb);
-  std::vector<long long> ho((size_t)nb);
-  MQ_CUDA(c, cudaMemcpyAsync(hc.data(), counts, nb * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-  MQ_CUDA(c, cudaStreamSynchronize(c->stream));
-  long long tot = 0;
-  for (long long b = 0; b < nb; ++b) {
-    ho[b] = tot;
-    tot += hc[b];
-  }
-  MQ_CUDA(c, cudaMemcpyAsync(offs, ho.data(), nb * sizeof(long long), cudaMemcpyHostToDevice, c->stream));
+  quartet_scan_kernel<<<1, 1024, 0, c->stream>>>(counts, nb, offs, total);
   quartet_pack_kernel<<<(unsigned)nb, 128, 0, c->stream>>>(part, counts, offs, block, list);
-  c->stats.launches += 2;
+  c->stats.launches += 3;
   MQ_CUDA(c, cudaGetLastError());
-  MQ_CUDA(c, cudaStreamSynchronize(c->stream));  // offs (host vector) goes out of scope
   h.list = list;
-  h.nq = tot;
+  h.list_n = total;  // h.nq stays the bound: the grid covers every quartet, idle past *total
   return MQ_OK;
 }
 
@@ -534,8 +572,8 @@ static int run_all(mq_ctx *c, EriArgs g) {
       h.diag = 0;
       h.nq = h.tri ? (long long)nP * (nP + 1) / 2 : (long long)nP * nQ;
       h.list = nullptr;
-      if (h.thr > 0.0) MQ_TRY(compact_quartets(c, h));
-      if (h.nq == 0) continue;
+      h.list_n = nullptr;
+      if (h.thr > 0.0) MQ_TRY(compact_quartets(c, h, cP * (cP + 1) / 2 + cQ));
       MQ_TRY(launch_class<EPI>(c, h, cP, cQ));
     }
   return MQ_OK;
@@ -571,11 +609,7 @@ int eri_full_device(mq_ctx *c, double *d_XX) {
   MQ_CUDA(c, cudaMemsetAsync(cnt, 0, 2 * sizeof(unsigned long long), c->stream));
   g.counters = cnt;
   MQ_TRY(run_all<EPI_XX>(c, g));
-  unsigned long long h[2];
-  MQ_CUDA(c, cudaMemcpyAsync(h, cnt, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
-  MQ_CUDA(c, cudaStreamSynchronize(c->stream));
-  c->stats.quartets = (double)h[0];
-  c->stats.prim_quartets = (double)h[1];
+  c->d_eri_counters = cnt;  // read when the quartet statistics are asked for
   return MQ_OK;
 }
 

@@ -112,6 +112,10 @@ struct StageTimer {
     cudaEventRecord(b, s);
     pending = true;
   }
+  void collect_sync() {  // wait for the end event first
+    if (pending) cudaEventSynchronize(b);
+    collect();
+  }
   void collect() {  // call after the stream has been synchronised
     if (!pending) return;
     float ms = 0;
@@ -152,7 +156,9 @@ struct mq_ctx {
   std::vector<void *> batch_allocs;  // batch pair table
   double *d_boys_tight = nullptr;    // the tight Boys table, for batches
   void *mlp = nullptr;               // the learned guess's network (mlp.cu)
-  mq::StageTimer t_fock_kernel;  // the digestion kernel alone, collected at the caller's sync points
+  mq::StageTimer t_fock_kernel;
+  mq::StageTimer t_eri;                       // the last integral pass, collected when asked for
+  unsigned long long *d_eri_counters = nullptr;  // its quartet counters (device)  // the digestion kernel alone, collected at the caller's sync points
   mq::FockTiles fock_tiles[9];  // pair-slab tile tables, indexed by slabs per tile
   int fock_jc[2][2] = {{0, 0}, {0, 0}}, fock_jc_n[2][2] = {{0, 0}, {0, 0}};  // autotuned tile length [uhf][df32]
   int fock_df32 = 0;  // digestion arithmetic: 0 FP64, 1 double-float (mq_set_fock_precision)
@@ -257,6 +263,7 @@ int gemm_strided_batched(mq_ctx *c, char ta, char tb, int m, int n, int k, doubl
                          long long sA, const double *B, int ldb, long long sB, double beta, double *C, int ldc,
                          long long sC, int batch);
 int density_device(mq_ctx *c, int n, int nocc, const double *d_C, double factor, double *d_D);
+int syrk_lower(mq_ctx *c, int n, int k, double alpha, const double *A, int lda, double beta, double *C, int ldc);
 // spectral projector onto the nocc lowest eigenvectors of the symmetric d_Fp
 // by trace-correcting purification (d_T, d_W: n x n scratch; d_err: >= 120
 // doubles); MQ_ENOCONV when the frontier levels are degenerate

@@ -333,6 +333,16 @@ int gemm(mq_ctx *c, char ta, char tb, int m, int n, int k, double alpha, const d
   return MQ_OK;
 }
 
+// lower triangle of C = alpha A A^T + beta C (n x n, A n x k); the upper triangle is not written
+int syrk_lower(mq_ctx *c, int n, int k, double alpha, const double *A, int lda, double beta, double *C, int ldc) {
+  cublasHandle_t h = handle(c);
+  if (!h) return set_err(c, MQ_ECUDA, "cublasCreate failed");
+  if (cublasDsyrk(h, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, n, k, &alpha, A, lda, &beta, C, ldc) != CUBLAS_STATUS_SUCCESS)
+    return set_err(c, MQ_ECUDA, "cublasDsyrk failed");
+  c->stats.lib_launches += 1;
+  return MQ_OK;
+}
+
 int gemm_strided_batched(mq_ctx *c, char ta, char tb, int m, int n, int k, double alpha, const double *A, int lda,
                          long long sA, const double *B, int ldb, long long sB, double beta, double *C, int ldc,
                          long long sC, int batch) {

@@ -74,8 +74,9 @@ __global__ void __launch_bounds__(PUR_THREADS) purify_init_kernel(const double *
   }
 }
 
-// Xn = select(X, T = X X): every CTA reads the two diagonals to make the same
-// choice; CTA 0 records the idempotency error tr X - tr T of step k.
+// Xn = select(X, T = X X), T given by its lower triangle (DSYRK; X is
+// symmetric so X X = X X^T): every CTA reads the two diagonals to make the
+// same choice; CTA 0 records the idempotency error tr X - tr T of step k.
 __global__ void purify_step_kernel(const double *__restrict__ X, const double *__restrict__ T, int n, double nocc,
                                    double *__restrict__ Xn, double *__restrict__ err, int k) {
   __shared__ double red[32];
@@ -91,7 +92,7 @@ __global__ void purify_step_kernel(const double *__restrict__ X, const double *_
   if (blockIdx.x == 0 && threadIdx.x == 0) err[k] = tx - tt;
   for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < n2; idx += (size_t)gridDim.x * blockDim.x) {
     const size_t r = idx % N, col = idx / N;
-    const double t = 0.5 * (T[idx] + T[col + N * r]);
+    const double t = r >= col ? T[idx] : T[col + N * r];  // the lower triangle holds X X
     Xn[idx] = square ? t : 2.0 * X[idx] - t;
   }
 }
@@ -124,7 +125,7 @@ int purify_projector(mq_ctx *c, int n, int nocc, const double *d_Fp, double *d_P
   std::vector<double> e(MAX_STEPS);
   int k = 0, settled_at = -1;
   while (k < MAX_STEPS) {
-    MQ_TRY(gemm(c, 'N', 'N', n, n, n, 1.0, X, n, X, n, 0.0, d_T, n));
+    MQ_TRY(syrk_lower(c, n, n, 1.0, X, n, 0.0, d_T, n));
     purify_step_kernel<<<std::min(gb, 1024u), 256, 0, c->stream>>>(X, d_T, n, (double)nocc, Xn, d_err, k);
     c->stats.launches += 1;
     std::swap(X, Xn);
