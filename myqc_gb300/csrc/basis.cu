@@ -129,6 +129,28 @@ void pairs_host(const std::vector<HostShell> &shells, const std::vector<double> 
       if (sb.type > sa.type) std::swap(A, B);
       pl[sa.type + sb.type].push_back({A, B});
     }
+  // within a class, pairs with more primitive pairs first: neighbouring quartets
+  // of an integral launch (one warp) then loop over similar primitive counts
+  auto live = [&](const std::pair<int, int> &ab) {
+    const HostShell &A = shells[ab.first], &B = shells[ab.second];
+    const double *xa = &xyz[3 * A.atom], *xb = &xyz[3 * B.atom];
+    double AB2 = 0;
+    for (int k = 0; k < 3; ++k) AB2 += (xa[k] - xb[k]) * (xa[k] - xb[k]);
+    int cnt = 0;
+    for (int i = 0; i < A.nprim; ++i)
+      for (int j = 0; j < B.nprim; ++j) {
+        const double a = A.alpha[i], b = B.alpha[j];
+        cnt += std::exp(-a * b * AB2 / (a + b)) >= 1.0e-14;
+      }
+    return cnt;
+  };
+  for (int cl = 0; cl < 3; ++cl) {
+    std::vector<std::pair<int, std::pair<int, int>>> keyed;
+    for (auto &ab : pl[cl]) keyed.push_back({live(ab), ab});
+    std::stable_sort(keyed.begin(), keyed.end(),
+                     [](const auto &x, const auto &y) { return x.first > y.first; });
+    for (size_t k = 0; k < keyed.size(); ++k) pl[cl][k] = keyed[k].second;
+  }
   int idx = 0;
   for (int cl = 0; cl < 3; ++cl) {
     h.class_off[cl] = idx;
