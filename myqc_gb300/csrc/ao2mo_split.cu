@@ -289,45 +289,100 @@ __device__ __forceinline__ void decompose(float x, long long &mant, int &ex) {
   ex = E - 150;
 }
 
-// one warp per row: r-th row at in + r*ld (kvalid values), slices to planes of
-// `plane` elements at out + r*Kp, row exponent to e[r]
-template <int S, class T>
-__global__ void slice_rows_kernel(const T *__restrict__ in, long long rows, int kvalid, long long ld, int Kp,
-                                  long long plane, bf16 *__restrict__ out, int *__restrict__ e) {
+// One warp per row: the r-th row at in + r*ld (kvalid values) becomes S planes
+// of `plane` elements at out + r*Kp, its exponent e[r].  Lane l owns the
+// 8-element chunks l and l+32 of the row (Kp <= 512): the row is read once into
+// registers (16-byte loads when `vec`), and each plane gets one 16-byte store per
+// chunk.  `vec` requires 16-byte aligned rows and kvalid a multiple of the
+// elements per 16 bytes.
+template <class T>
+__device__ __forceinline__ void load_chunk(const T *__restrict__ x, int k0, int kvalid, bool vec, T (&v)[8]) {
+  if (vec && k0 + 8 <= kvalid) {
+    if (sizeof(T) == 8) {
+      const double2 *p = reinterpret_cast<const double2 *>(x + k0);
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const double2 t = __ldg(p + j);
+        v[2 * j] = (T)t.x;
+        v[2 * j + 1] = (T)t.y;
+      }
+    } else {
+      const float4 *p = reinterpret_cast<const float4 *>(x + k0);
+#pragma unroll
+      for (int j = 0; j < 2; ++j) {
+        const float4 t = __ldg(p + j);
+        v[4 * j] = (T)t.x;
+        v[4 * j + 1] = (T)t.y;
+        v[4 * j + 2] = (T)t.z;
+        v[4 * j + 3] = (T)t.w;
+      }
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < 8; ++j) v[j] = (k0 + j < kvalid) ? __ldg(x + k0 + j) : (T)0;
+  }
+}
+
+template <int S, class T, int H>
+__global__ void __launch_bounds__(256, 4) slice_rows_kernel(const T *__restrict__ in, long long rows, int kvalid,
+                                                         long long ld, int Kp, long long plane, bf16 *__restrict__ out,
+                                                         int *__restrict__ e, int vec) {
   const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
   const int lane = threadIdx.x & 31;
+  const int nchunk = Kp >> 3;
   for (long long r = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); r < rows; r += warps) {
     const T *x = in + r * ld;
+    T v[H][8];
     int emax = 0;
-    for (int k = lane; k < kvalid; k += 32) emax = max(emax, exp_field(x[k]));
+#pragma unroll
+    for (int h = 0; h < H; ++h) {
+      const int c = lane + 32 * h;
+      if (c < nchunk) {
+        load_chunk(x, 8 * c, kvalid, vec != 0, v[h]);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) emax = max(emax, exp_field(v[h][j]));
+      }
+    }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o));
     // |x| < 2^erow with erow = unbiased exponent of the largest element + 1
     const int erow = emax == 0 ? -200 : emax - (sizeof(T) == 8 ? 1022 : 126);
     if (lane == 0) e[r] = erow;
-    for (int k = lane; k < Kp; k += 32) {
-      long long q = 0;
-      if (k < kvalid) {
-        long long mant;
-        int ex;
-        decompose(x[k], mant, ex);
-        // q = round(mant * 2^(ex + 8S - 1 - erow)); the shift is negative for every nonzero x
-        const int sh = -(ex + 8 * S - 1 - erow);
-        if (mant != 0 && sh < 62) {
-          const long long half = sh > 0 ? (1ll << (sh - 1)) : 0;
-          q = sh > 0 ? ((mant + half) >> sh) : (mant << -sh);
+#pragma unroll
+    for (int h = 0; h < H; ++h) {
+      const int c = lane + 32 * h;
+      if (c >= nchunk) continue;
+      unsigned packed[S][4];
+#pragma unroll
+      for (int j = 0; j < 8; j += 2) {
+        float dig[2][S];
+#pragma unroll
+        for (int t = 0; t < 2; ++t) {
+          long long mant;
+          int ex;
+          decompose(v[h][j + t], mant, ex);
+          // q = round(mant * 2^(ex + 8S - 1 - erow)); the shift is negative for every nonzero x
+          const int sh = -(ex + 8 * S - 1 - erow);
+          int q = 0;
+          if (mant != 0 && sh < 62) q = (int)(sh > 0 ? ((mant + (1ll << (sh - 1))) >> sh) : (mant << -sh));
+#pragma unroll
+          for (int d = S - 1; d > 0; --d) {
+            const int hi = (q + 128) >> 8;  // balanced digit: q = hi*256 + lo, lo in [-128, 127]
+            dig[t][d] = (float)(q - hi * 256);
+            q = hi;
+          }
+          dig[t][0] = (float)q;
+        }
+#pragma unroll
+        for (int d = 0; d < S; ++d) {
+          const __nv_bfloat162 b2 = __floats2bfloat162_rn(dig[0][d], dig[1][d]);
+          packed[d][j >> 1] = *reinterpret_cast<const unsigned *>(&b2);
         }
       }
-      float dig[S];
 #pragma unroll
-      for (int d = S - 1; d > 0; --d) {
-        const long long hi = (q + 128) >> 8;  // balanced digit: q = hi*256 + lo, lo in [-128, 127]
-        dig[d] = (float)(q - hi * 256);
-        q = hi;
-      }
-      dig[0] = (float)q;
-#pragma unroll
-      for (int d = 0; d < S; ++d) out[d * plane + r * Kp + k] = __float2bfloat16_rn(dig[d]);
+      for (int d = 0; d < S; ++d)
+        *reinterpret_cast<uint4 *>(out + d * plane + r * Kp + 8 * c) =
+            make_uint4(packed[d][0], packed[d][1], packed[d][2], packed[d][3]);
     }
   }
 }
@@ -382,9 +437,17 @@ static int slice_gemm(mq_ctx *c, Sliced A, long long M, int batch, long long a_b
 
 template <int S, class T>
 static int slice_rows(mq_ctx *c, const T *in, long long rows, int kvalid, long long ld, int Kp, Sliced o) {
+  if (Kp % 8 || Kp > 512) return set_err(c, MQ_EINVAL, "slice_rows: Kp must be a multiple of 8 up to 512");
   const int tb = 256;
   const long long blocks = std::max<long long>(1, std::min<long long>((rows + 7) / 8, 1 << 20));
-  slice_rows_kernel<S, T><<<(unsigned)blocks, tb, 0, c->stream>>>(in, rows, kvalid, ld, Kp, o.plane, o.base, o.e);
+  const int per16 = 16 / (int)sizeof(T);
+  const int vec = ((uintptr_t)in % 16 == 0) && (ld % per16 == 0) && (kvalid % per16 == 0);
+  if (Kp <= 256)
+    slice_rows_kernel<S, T, 1><<<(unsigned)blocks, tb, 0, c->stream>>>(in, rows, kvalid, ld, Kp, o.plane, o.base, o.e,
+                                                                       vec);
+  else
+    slice_rows_kernel<S, T, 2><<<(unsigned)blocks, tb, 0, c->stream>>>(in, rows, kvalid, ld, Kp, o.plane, o.base, o.e,
+                                                                       vec);
   c->stats.launches += 1;
   MQ_CUDA(c, cudaGetLastError());
   return sync_check(c, "slice_rows");
@@ -412,9 +475,7 @@ static int ao2mo_slices(mq_ctx *c, const double *Ci, int no1, const double *Ca, 
   int *err = (int *)buf(c, "split_err", 64);
   if (!pa || !ea || !pb || !eb || !y1 || !y2 || !err) return MQ_ENOMEM;
   MQ_CUDA(c, cudaMemsetAsync(err, 0, sizeof(int), c->stream));
-  // the padding columns Kp > n of the intermediates stay zero
-  MQ_CUDA(c, cudaMemsetAsync(y1, 0, std::max(r1, r3) * Kp * sizeof(float), c->stream));
-  MQ_CUDA(c, cudaMemsetAsync(y2, 0, r2 * Kp * sizeof(float), c->stream));
+  // the padding columns Kp > n of the intermediates are never read: slicing reads n values per row
   // coefficient blocks: column p of C (n contiguous) becomes row p of B (K-major)
   const long long plB = rB * Kp;
   Sliced Bi{pb, plB, eb}, Ba{pb + (long long)no1 * Kp, plB, eb + no1};
