@@ -105,6 +105,7 @@ def load_workload(seed: int):
 
 MODEL = os.path.join(ROOT, "myqc_gb300", "data", "guess_mlp.npz")
 SCHWARZ = 1e-12  # fast arm: contracted quartets with a Schwarz bound below this are skipped
+ERI_F32_TAU = 1e-5  # fast arm: quartets with a bound below this in FP32 (max |dG| 3e-11 on (H2O)32)
 _learned = {}
 
 
@@ -119,7 +120,8 @@ def learned_guess(ctx):
 def solve(ctx, sysm, basis, fast: bool, set_system: bool):
     """One solve through the public API.  fast: the learned initial density
     (core guess when the prediction fails its checks or the SCF does not
-    converge from it), Schwarz screening at 1e-12, the double-float Fock
+    converge from it), Schwarz screening at 1e-12, quartets with a bound below
+    1e-5 in FP32, the double-float Fock
     digestion, densities by purification (one eigensolve at the end)
     and split-precision MP2; plain: the core-Hamiltonian guess, the
     eigensolver every iteration and the FP64 transform.  Both use DIIS(8)
@@ -130,6 +132,7 @@ def solve(ctx, sysm, basis, fast: bool, set_system: bool):
     ctx.set_fock_precision(FOCK_DF32 if fast else FOCK_FP64)
     if set_system:
         ctx.set_system(sysm, basis, None, MODE_TIGHT)
+    ctx.set_eri_mixed(ERI_F32_TAU if fast else 0.0)
     S, H = ctx.int1e()
     ctx.eri_store()
     kw = dict(conv=1e-10, conv_rms=True, diis=8, max_iter=200, purify=fast)
@@ -266,7 +269,8 @@ def run_ours(args):
         "data": f"synthetic: seeded (H2O){NMOL} cluster, rigid monomers, PCG64 seed {args.seed}",
         "config": {"workload": workload(), "molecule": f"(H2O){NMOL}", "n_basis": n, "n_occ": sysm.nelcA,
                    "n_vir": n - sysm.nelcA, "box_angstrom": BOX, "seed": args.seed, "basis": "STO-3G",
-                   "boys": "tight FP64 table", "schwarz": SCHWARZ, "scf": "FP64 (Fock digestion in double-float on the FP32 pipes), DIIS(8), conv 1e-10 RMS dD, initial density from the learned guess (core guess fallback), densities by TC2 purification (FP64 GEMMs), one Jacobi eigensolve at the end",
+                   "boys": "tight FP64 table (FP32 copy for the FP32 quartets)", "schwarz": SCHWARZ,
+                   "eri_fp32_below_bound": ERI_F32_TAU, "scf": "FP64 (Fock digestion in double-float on the FP32 pipes), DIIS(8), conv 1e-10 RMS dD, initial density from the learned guess (core guess fallback), densities by TC2 purification (FP64 GEMMs), one Jacobi eigensolve at the end",
                    "guess_model": os.path.relpath(MODEL, ROOT) if learned_guess(ctx) is not None else None,
                    "mp2_precision": "split hi+mid+lo bf16 (tcgen05), fp32 accumulate" if prec else "fp64",
                    "l2": "inputs larger than L2: the 20 GB integral array is rebuilt and streamed every step",
@@ -287,6 +291,7 @@ def run_ours(args):
         "accuracy": {"E_scf": res.energy, "E_mp2": mp2["E_MP2"], "dE_scf_vs_plain_Eh": dE_scf,
                      "dE_mp2_vs_fp64_uEh": dE_mp2 * 1e6},
         "eri_quartets_per_s": stat(ctx, "quartets") / (t_eri / args.steps * 1e-3) if t_eri > 0 else None,
+        "eri_fp32_share": stat(ctx, "quartets_f32") / max(stat(ctx, "quartets"), 1.0),
         "fock_builds_per_s": 1000.0 * nfock / t_fock if t_fock > 0 else None,
     }
     if args.secondary and world == 1:

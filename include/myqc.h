@@ -69,6 +69,13 @@ int mq_norb(const mq_ctx *ctx, int *norb);
  * (0 = off, the reference's behaviour; 1e-12 for direct SCF at scale). */
 int mq_set_schwarz(mq_ctx *ctx, double threshold);
 
+/* Mixed-precision integral pass (MQ_MODE_TIGHT only; 0 = off, every quartet
+ * in FP64): contracted quartets whose Schwarz bound is below tau are computed
+ * in FP32, the rest in FP64 (dynamic precision as in Luehr, Ufimtsev and
+ * Martinez, J. Chem. Theory Comput. 7, 949 (2011)); an integral's FP32 error
+ * stays a small multiple of tau * 1e-6.  Applies to mq_eri_store/mq_eri_full. */
+int mq_set_eri_mixed(mq_ctx *ctx, double tau);
+
 /* One-electron integrals S and H = T + V, n x n column-major host arrays.
  * Replaces proc1e (src/integrals/int1e.f90:132-280). */
 int mq_int1e(mq_ctx *ctx, double *S, double *H);
@@ -206,6 +213,13 @@ int mq_mp2_pairs(mq_ctx *ctx, const double *iajb, int no1, int nv1, int no2, int
  * and eigenvectors V (n*n each).  Replaces DSYEV/DSYGV's eigen step
  * (src/scf/scf.f90:692,848). */
 int mq_syev_batched(mq_ctx *ctx, int n, int batch, double *A, double *w, double *V);
+
+/* C = alpha op(A) op(B) + beta C on the device, host arrays column-major
+ * (BLAS DGEMM semantics; transa/transb 'N' or 'T'), e.g. the DGEMM products of
+ * the reference's SCF (src/scf/scf.f90:1306-1307).  Orders up to ~1000 run
+ * on the library's own FP64 kernel spread over all SMs. */
+int mq_dgemm(mq_ctx *ctx, char transa, char transb, int m, int n, int k, double alpha, const double *A, int lda,
+             const double *B, int ldb, double beta, double *C, int ldc);
 
 /* Generalized problem F C = S C eps (DSYGV itype 1, 'V', 'L',
  * src/scf/scf.f90:478,848) for one n x n pair of host matrices. */

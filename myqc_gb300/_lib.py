@@ -70,6 +70,7 @@ def lib(path: str | None = None):
     L.mq_set_system.argtypes = [vp, c_int, vp, vp, vp, vp, vp, vp, vp, c_int]
     L.mq_norb.argtypes = [vp, ip]
     L.mq_set_schwarz.argtypes = [vp, c_double]
+    L.mq_set_eri_mixed.argtypes = [vp, c_double]
     L.mq_int1e.argtypes = [vp, dp, dp]
     L.mq_eri_full.argtypes = [vp, dp]
     L.mq_eri_store.argtypes = [vp]
@@ -83,6 +84,8 @@ def lib(path: str | None = None):
     L.mq_mp2_uhf.argtypes = [vp, dp, dp, dp, dp, c_int, c_int, c_int, dp]
     L.mq_mp2_pairs.argtypes = [vp, dp, c_int, c_int, c_int, c_int, dp, dp, c_int, dp]
     L.mq_syev_batched.argtypes = [vp, c_int, c_int, dp, dp, dp]
+    L.mq_dgemm.argtypes = [vp, ctypes.c_char, ctypes.c_char, c_int, c_int, c_int, ctypes.c_double, dp, c_int, dp, c_int,
+                           ctypes.c_double, dp, c_int]
     L.mq_sygv.argtypes = [vp, c_int, dp, dp, dp, dp]
     L.mq_stat.argtypes = [vp, ctypes.c_char_p, ctypes.POINTER(c_double)]
     L.mq_mlp_init.argtypes = [vp, c_int, c_int, c_int]

@@ -251,6 +251,15 @@ int upload_pairs(mq_ctx *c, const HostPairs &h, std::vector<void *> &allocs, Pai
   MQ_TRY(up(t.PBx, h.PBx)); MQ_TRY(up(t.PBy, h.PBy)); MQ_TRY(up(t.PBz, h.PBz));
   MQ_TRY(up(t.K, h.K));
   MQ_TRY(up(t.c4, h.c4));
+  std::vector<float4> pf(4 * h.p.size());
+  for (size_t i = 0; i < h.p.size(); ++i) {
+    pf[4 * i] = make_float4((float)h.p[i], (float)h.inv2p[i], (float)h.K[i], (float)h.Px[i]);
+    pf[4 * i + 1] = make_float4((float)h.Py[i], (float)h.Pz[i], (float)h.PAx[i], (float)h.PAy[i]);
+    pf[4 * i + 2] = make_float4((float)h.PAz[i], (float)h.PBx[i], (float)h.PBy[i], (float)h.PBz[i]);
+    pf[4 * i + 3] = make_float4((float)h.c4[4 * i], (float)h.c4[4 * i + 1], (float)h.c4[4 * i + 2],
+                                (float)h.c4[4 * i + 3]);
+  }
+  MQ_TRY(up(t.pf, pf));
   return MQ_OK;
 }
 

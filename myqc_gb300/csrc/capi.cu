@@ -111,6 +111,7 @@ int mq_init(mq_ctx **ctx, int device) {
   if (cudaSetDevice(device) != cudaSuccess) return MQ_ECUDA;
   mq_ctx *c = new mq_ctx();
   c->device = device;
+  if (const char *e = getenv("MYQC_DGEMM")) c->dgemm_cublas = !strcmp(e, "cublas");
   if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
     delete c;
     return MQ_ECUDA;
@@ -130,6 +131,7 @@ int mq_free(mq_ctx *c) {
   for (auto &kv : c->bufs)
     if (kv.second.ptr) cudaFree(kv.second.ptr);
   if (c->d_XX) cudaFree(c->d_XX);
+  if (c->d_boys_f32) cudaFree(c->d_boys_f32);
   if (c->d_boys) cudaFree(c->d_boys);
   if (c->d_nuc) cudaFree(c->d_nuc);
   if (c->cublas) cublas_destroy(c->cublas);
@@ -167,6 +169,15 @@ int mq_set_system(mq_ctx *c, int nnuc, const int *Z, const double *xyz, const do
   }
   if (c->d_boys) cudaFree(c->d_boys);
   c->d_boys = nullptr;
+  if (c->d_boys_f32) cudaFree(c->d_boys_f32);
+  c->d_boys_f32 = nullptr;
+  if (mode == MQ_MODE_TIGHT) {  // single-precision copy for the mixed-precision integral pass
+    std::vector<float> tf(tab.begin(), tab.end());
+    MQ_CUDA(c, cudaMalloc((void **)&c->d_boys_f32, tf.size() * sizeof(float)));
+    MQ_CUDA(c, cudaMemcpy(c->d_boys_f32, tf.data(), tf.size() * sizeof(float), cudaMemcpyHostToDevice));
+  } else {
+    c->eri_f32_tau = 0.0;
+  }
   MQ_CUDA(c, cudaMalloc((void **)&c->d_boys, tab.size() * sizeof(double)));
   MQ_CUDA(c, cudaMemcpy(c->d_boys, tab.data(), tab.size() * sizeof(double), cudaMemcpyHostToDevice));
   std::vector<double> nuc(4 * (size_t)nnuc);
@@ -198,6 +209,15 @@ int mq_set_schwarz(mq_ctx *c, double threshold) {
   if (!c || threshold < 0) return MQ_EINVAL;
   c->schwarz_thr = threshold;
   if (c->have_system && threshold > 0) return eri_schwarz(c);
+  return MQ_OK;
+}
+
+int mq_set_eri_mixed(mq_ctx *c, double tau) {
+  if (!c || !(tau >= 0)) return MQ_EINVAL;
+  if (tau > 0 && c->have_system && c->mode != MQ_MODE_TIGHT)
+    return set_err(c, MQ_EINVAL, "mixed-precision integrals need MQ_MODE_TIGHT (reference mode reproduces the "
+                                 "reference's FP64 Boys table)");
+  c->eri_f32_tau = tau;
   return MQ_OK;
 }
 
@@ -432,6 +452,23 @@ int mq_syev_batched(mq_ctx *c, int n, int batch, double *A, double *w, double *V
   return MQ_OK;
 }
 
+int mq_dgemm(mq_ctx *c, char transa, char transb, int m, int n, int k, double alpha, const double *A, int lda,
+             const double *B, int ldb, double beta, double *C, int ldc) {
+  if (!c || !A || !B || !C || m <= 0 || n <= 0 || k <= 0) return MQ_EINVAL;
+  const bool ta = transa == 'T' || transa == 't', tb = transb == 'T' || transb == 't';
+  if ((!ta && transa != 'N' && transa != 'n') || (!tb && transb != 'N' && transb != 'n'))
+    return set_err(c, MQ_EINVAL, "mq_dgemm: trans must be N or T");
+  if (lda < (ta ? k : m) || ldb < (tb ? n : k) || ldc < m) return set_err(c, MQ_EINVAL, "mq_dgemm: leading dimension");
+  cudaSetDevice(c->device);
+  const size_t na = (size_t)lda * (ta ? m : k), nb = (size_t)ldb * (tb ? k : n), nc = (size_t)ldc * n;
+  double *dA = to_dev(c, "dgemm_A", A, na), *dB = to_dev(c, "dgemm_B", B, nb), *dC = to_dev(c, "dgemm_C", C, nc);
+  if (!dA || !dB || !dC) return MQ_ENOMEM;
+  MQ_TRY(gemm(c, transa, transb, m, n, k, alpha, dA, lda, dB, ldb, beta, dC, ldc));
+  MQ_CUDA(c, cudaMemcpyAsync(C, dC, nc * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  MQ_CUDA(c, cudaStreamSynchronize(c->stream));
+  return MQ_OK;
+}
+
 int mq_sygv(mq_ctx *c, int n, const double *F, const double *S, double *w, double *C) {
   if (!c || !F || !S || !w || !C || n <= 0) return MQ_EINVAL;
   cudaSetDevice(c->device);
@@ -566,20 +603,32 @@ int mq_stat(const mq_ctx *c, const char *key, double *value) {
   else if (!strcmp(key, "purify_steps")) *value = s.purify_steps;
   else if (!strcmp(key, "fock_jc")) *value = s.fock_jc;
   else if (!strcmp(key, "graph_launches")) *value = s.graph_launches;
+  else if (!strcmp(key, "eig_cluster")) *value = s.eig_cluster;
+  else if (!strcmp(key, "eig_final")) *value = s.ms_eig_final;
+  else if (!strcmp(key, "eig_f32_sweeps")) *value = s.eig_f32_sweeps;
+  else if (!strcmp(key, "eig_f32_off")) *value = s.eig_f32_off;
+  else if (!strcmp(key, "eig_f32")) *value = s.ms_eig_f32;
+  else if (!strcmp(key, "eig_refine")) *value = s.ms_eig_refine;
+  else if (!strcmp(key, "eig_jacobi")) *value = s.ms_eig_jacobi;
+  else if (!strcmp(key, "eig_jacobi_sweeps")) *value = s.eig_jacobi_sweeps;
   else if (!strcmp(key, "fock_precision")) *value = c->fock_df32;
   else if (!strcmp(key, "fock_kernel")) *value = s.ms_fock_kernel;
   else if (!strcmp(key, "fock_kernel_launches")) *value = s.fock_kernel_launches;
   else if (!strcmp(key, "tune_fock_ms")) *value = s.tune_fock_ms;
   else if (!strcmp(key, "lib_launches")) *value = s.lib_launches;
   else if (!strcmp(key, "launches")) *value = s.launches;
-  else if (!strcmp(key, "quartets") || !strcmp(key, "prim_quartets")) {
-    unsigned long long h[2] = {0, 0};
+  else if (!strcmp(key, "quartets") || !strcmp(key, "prim_quartets") || !strcmp(key, "quartets_f32") ||
+           !strcmp(key, "prim_quartets_f32")) {
+    // [0], [1]: all quartets and primitive quartets; [2], [3]: those computed in FP32
+    unsigned long long h[4] = {0, 0, 0, 0};
     if (c->d_eri_counters) {
       cudaMemcpyAsync(h, c->d_eri_counters, sizeof(h), cudaMemcpyDeviceToHost, mut->stream);
       cudaStreamSynchronize(mut->stream);
     }
-    *value = (double)h[key[0] == 'q' ? 0 : 1];
+    const bool f32 = strstr(key, "f32") != nullptr, prim = key[0] == 'p';
+    *value = (double)(f32 ? h[prim ? 3 : 2] : h[prim ? 1 : 0] + h[prim ? 3 : 2]);
   }
+  else if (!strcmp(key, "eri_f32_tau")) *value = c->eri_f32_tau;
   else return MQ_EINVAL;
   return MQ_OK;
 }

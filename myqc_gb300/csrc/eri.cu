@@ -45,6 +45,8 @@ struct EriArgs {
   int diag;      // Schwarz: quartet (P,P) only
   long long nq;  // quartets in this launch
   double thr;    // Schwarz threshold (0: off)
+  double thr_hi; // > 0: only quartets whose bound is below it (the FP32 window of a mixed-precision pass)
+  const float *boys_f;  // FP32 Boys table (tight layout) for the FP32 instances
   double *XX;
   unsigned long long *sch;  // Schwarz output (bit pattern of a positive double)
   const double *Da, *Db;
@@ -78,11 +80,11 @@ __host__ __device__ constexpr bool bra_needs(int A0, int A1, int B0, int B1, int
 }
 
 // Hermite R_{tuv} (t+u+v <= L) from F_j already scaled by the prefactor.
-template <int L>
-__device__ __forceinline__ void hermite_R(const double (&F)[L + 1], double m2a, double X, double Y, double Z,
-                                          double (&R)[L + 1][L + 1][L + 1]) {
-  double Rj[L + 1][L + 1][L + 1][L + 1];
-  double pw = 1.0;
+template <int L, class RT>
+__device__ __forceinline__ void hermite_R(const RT (&F)[L + 1], RT m2a, RT X, RT Y, RT Z,
+                                          RT (&R)[L + 1][L + 1][L + 1]) {
+  RT Rj[L + 1][L + 1][L + 1][L + 1];
+  RT pw = RT(1);
 #pragma unroll
   for (int j = 0; j <= L; ++j) {
     Rj[j][0][0][0] = pw * F[j];
@@ -97,16 +99,16 @@ __device__ __forceinline__ void hermite_R(const double (&F)[L + 1], double m2a, 
 #pragma unroll
         for (int v = 0; v <= L; ++v) {
           if (t + u + v == 0 || t + u + v > L - j) continue;
-          double r;
+          RT r;
           if (t > 0) {
             r = X * Rj[j + 1][t - 1][u][v];
-            if (t > 1) r += (t - 1) * Rj[j + 1][t - 2][u][v];
+            if (t > 1) r += RT(t - 1) * Rj[j + 1][t - 2][u][v];
           } else if (u > 0) {
             r = Y * Rj[j + 1][t][u - 1][v];
-            if (u > 1) r += (u - 1) * Rj[j + 1][t][u - 2][v];
+            if (u > 1) r += RT(u - 1) * Rj[j + 1][t][u - 2][v];
           } else {
             r = Z * Rj[j + 1][t][u][v - 1];
-            if (v > 1) r += (v - 1) * Rj[j + 1][t][u][v - 2];
+            if (v > 1) r += RT(v - 1) * Rj[j + 1][t][u][v - 2];
           }
           Rj[j][t][u][v] = r;
         }
@@ -122,8 +124,9 @@ __device__ __forceinline__ void hermite_R(const double (&F)[L + 1], double m2a, 
 
 // Per-axis Hermite coefficients of a primitive pair for l_a, l_b in {0,1}:
 // e[la][lb][t], t <= la+lb (sign folded in for the ket when sgn = -1).
-__device__ __forceinline__ void pair_E(double PA, double PB, double i2p, double sgn, double (&e)[2][2][3]) {
-  e[0][0][0] = 1.0;
+template <class RT>
+__device__ __forceinline__ void pair_E(RT PA, RT PB, RT i2p, RT sgn, RT (&e)[2][2][3]) {
+  e[0][0][0] = RT(1);
   e[1][0][0] = PA;
   e[1][0][1] = sgn * i2p;
   e[0][1][0] = PB;
@@ -133,19 +136,107 @@ __device__ __forceinline__ void pair_E(double PA, double PB, double i2p, double 
   e[1][1][2] = i2p * i2p;
 }
 
+// One primitive pair's data in the arithmetic type of the instance: FP64 from
+// the pair table's arrays, FP32 from its packed copy (4 float4 per primitive
+// pair: p 1/2p K Px | Py Pz PAx PAy | PAz PBx PBy PBz | c4).
+template <class RT>
+struct PrimPair {
+  RT p, i2p, K, Px, Py, Pz, PAx, PAy, PAz, PBx, PBy, PBz, c[4];
+};
+__device__ __forceinline__ void load_pp(const PairTable &t, int ip, PrimPair<double> &d) {
+  d.p = t.p[ip];
+  d.i2p = t.inv2p[ip];
+  d.K = t.K[ip];
+  d.Px = t.Px[ip];
+  d.Py = t.Py[ip];
+  d.Pz = t.Pz[ip];
+  d.PAx = t.PAx[ip];
+  d.PAy = t.PAy[ip];
+  d.PAz = t.PAz[ip];
+  d.PBx = t.PBx[ip];
+  d.PBy = t.PBy[ip];
+  d.PBz = t.PBz[ip];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) d.c[k] = t.c4[4 * ip + k];
+}
+__device__ __forceinline__ void load_pp(const PairTable &t, int ip, PrimPair<float> &d) {
+  const float4 a = __ldg(t.pf + 4 * ip), b = __ldg(t.pf + 4 * ip + 1), c = __ldg(t.pf + 4 * ip + 2),
+               e = __ldg(t.pf + 4 * ip + 3);
+  d.p = a.x;
+  d.i2p = a.y;
+  d.K = a.z;
+  d.Px = a.w;
+  d.Py = b.x;
+  d.Pz = b.y;
+  d.PAx = b.z;
+  d.PAy = b.w;
+  d.PAz = c.x;
+  d.PBx = c.y;
+  d.PBy = c.z;
+  d.PBz = c.w;
+  d.c[0] = e.x;
+  d.c[1] = e.y;
+  d.c[2] = e.z;
+  d.c[3] = e.w;
+}
+__device__ __forceinline__ double rsq(double x) { return rsqrt(x); }
+__device__ __forceinline__ float rsq(float x) { return rsqrtf(x); }
+
+// FP32 Boys values F_0..F_L from the tight table in single precision: 6-term
+// Taylor of F_L about the nearest grid point (|d| <= 0.05: remainder below
+// 1e-10 relative), downward recursion; above 36 the asymptotic F_0 and upward
+// recursion.  Serves the FP32 instances, whose quartets are below a bound
+// where single-precision relative errors stay far under the integral
+// tolerance.
+template <int L>
+__device__ __forceinline__ void boys_f32(float T, const float *__restrict__ tab, float (&F)[L + 1]) {
+  static_assert(L + 5 < TIGHT_NM, "Boys order");
+  if (T < 36.0f) {
+    const int tk = (int)(T * 10.0f + 0.5f);
+    const float d = __ldg(tab + BOYS_TIGHT_GRID + tk) - T;
+    const float *row = tab + tk * TIGHT_NM + L;
+    float f = __ldg(row + 5);
+    f = __ldg(row + 4) + f * (d * 0.2f);
+    f = __ldg(row + 3) + f * (d * 0.25f);
+    f = __ldg(row + 2) + f * (d * (1.0f / 3.0f));
+    f = __ldg(row + 1) + f * (d * 0.5f);
+    f = __ldg(row + 0) + f * d;
+    F[L] = f;
+    if (L > 0) {
+      const float e = expf(-T), t2 = 2.0f * T;
+#pragma unroll
+      for (int j = L - 1; j >= 0; --j) F[j] = (t2 * F[j + 1] + e) * (1.0f / (2 * j + 1));
+    }
+  } else {
+    const float rT = rsqrtf(T), i2T = 0.5f * rT * rT;
+    F[0] = 0.886226925f * rT;  // sqrt(pi)/2
+#pragma unroll
+    for (int j = 1; j <= L; ++j) F[j] = i2T * float(2 * j - 1) * F[j - 1];
+  }
+}
+template <int Q, int L>
+__device__ __forceinline__ void boys_any(const EriArgs &g, double T, double (&F)[L + 1]) {
+  boys<Q, L>(g.mode, T, g.boys, F);
+}
+template <int Q, int L>
+__device__ __forceinline__ void boys_any(const EriArgs &g, float T, float (&F)[L + 1]) {
+  boys_f32<L>(T, g.boys_f, F);
+}
+
 // One contracted quartet (P, Q), the bra functions a in [A0, A1), b in [B0, B1)
 // and ket functions c in [C0, C1), d in [D0, D1) of it (a thread's share when a
 // quartet is split over threads).  With the whole bra in one thread (ONFLY)
 // the bra Hermite products are formed on the fly from the per-axis
 // coefficients instead of being kept for every (a, b): a ket-split thread then
 // forms each ket contraction W once and applies it to all 16 bra functions.
-template <int LA, int LB, int LC, int LD, int A0, int A1, int B0, int B1, int C0, int C1, int D0, int D1, int EPI>
+template <int LA, int LB, int LC, int LD, int A0, int A1, int B0, int B1, int C0, int C1, int D0, int D1, int EPI,
+          class RT = double>
 __device__ __forceinline__ void quartet(const EriArgs &g, int P, int Q, size_t n, double *XXout) {
   constexpr int LAB = LA + LB, LT = LA + LB + LC + LD;
   constexpr int QREF = 3 * LT;  // the reference's Boys order for s/sp sets
   constexpr bool ONFLY = (A1 - A0) * (B1 - B0) > 4;
   const PairTable &t = g.t;
-  double acc[A1 - A0][B1 - B0][C1 - C0][D1 - D0];
+  RT acc[A1 - A0][B1 - B0][C1 - C0][D1 - D0];
 #pragma unroll
   for (int a = 0; a < A1 - A0; ++a)
 #pragma unroll
@@ -153,25 +244,27 @@ __device__ __forceinline__ void quartet(const EriArgs &g, int P, int Q, size_t n
 #pragma unroll
       for (int c = 0; c < C1 - C0; ++c)
 #pragma unroll
-        for (int d = 0; d < D1 - D0; ++d) acc[a][b][c][d] = 0.0;
+        for (int d = 0; d < D1 - D0; ++d) acc[a][b][c][d] = RT(0);
 
   const int p0 = t.pp_off[P], p1 = t.pp_off[P + 1];
   const int q0 = t.pp_off[Q], q1 = t.pp_off[Q + 1];
   const bool parity = g.mode == MQ_MODE_REFERENCE;
-  const double pref0 = parity ? 2.0 * 17.493419544621675 : 2.0 * 17.493418327624862;  // 2 pi^2.5
+  const RT pref0 = parity ? RT(2.0 * 17.493419544621675) : RT(2.0 * 17.493418327624862);  // 2 pi^2.5
   unsigned nprim = 0;
   for (int ip = p0; ip < p1; ++ip) {
-    const double p = t.p[ip], i2p = t.inv2p[ip], Kab = t.K[ip];
-    const double Px = t.Px[ip], Py = t.Py[ip], Pz = t.Pz[ip];
-    double ex[2][2][3], ey[2][2][3], ez[2][2][3];
-    pair_E(t.PAx[ip], t.PBx[ip], i2p, 1.0, ex);
-    pair_E(t.PAy[ip], t.PBy[ip], i2p, 1.0, ey);
-    pair_E(t.PAz[ip], t.PBz[ip], i2p, 1.0, ez);
-    double cab[4];
+    PrimPair<RT> ab;
+    load_pp(t, ip, ab);
+    const RT p = ab.p, i2p = ab.i2p, Kab = ab.K;
+    const RT Px = ab.Px, Py = ab.Py, Pz = ab.Pz;
+    RT ex[2][2][3], ey[2][2][3], ez[2][2][3];
+    pair_E(ab.PAx, ab.PBx, i2p, RT(1), ex);
+    pair_E(ab.PAy, ab.PBy, i2p, RT(1), ey);
+    pair_E(ab.PAz, ab.PBz, i2p, RT(1), ez);
+    RT cab[4];
 #pragma unroll
-    for (int k = 0; k < 4; ++k) cab[k] = t.c4[4 * ip + k];
+    for (int k = 0; k < 4; ++k) cab[k] = ab.c[k];
     // bra products E^{ab}_{tuv} * c_a c_b K_ab (kept per (a, b) unless ONFLY)
-    double eb[ONFLY ? 1 : A1 - A0][ONFLY ? 1 : B1 - B0][3][3][3];
+    RT eb[ONFLY ? 1 : A1 - A0][ONFLY ? 1 : B1 - B0][3][3][3];
     if (!ONFLY) {
 #pragma unroll
       for (int a = A0; a < A1; ++a)
@@ -189,39 +282,41 @@ __device__ __forceinline__ void quartet(const EriArgs &g, int P, int Q, size_t n
                                                                      cab[2 * fang(a) + fang(b)];
     }
     for (int iq = q0; iq < q1; ++iq) {
-      const double Kcd = t.K[iq];
+      PrimPair<RT> cd;
+      load_pp(t, iq, cd);
+      const RT Kcd = cd.K;
       // int2e.f90:257; not for the Schwarz bounds, which must bound the exact
       // (ab|ab): the screen removes every primitive quartet of (ab|ab) for a
       // distant pair while (ab|cd) with a compact partner survives it
-      if (EPI != EPI_SCHWARZ && Kab * Kcd < 1.0e-14) continue;
+      if (EPI != EPI_SCHWARZ && Kab * Kcd < RT(1.0e-14)) continue;
       ++nprim;
-      const double q = t.p[iq], i2q = t.inv2p[iq];
-      const double X = Px - t.Px[iq], Y = Py - t.Py[iq], Z = Pz - t.Pz[iq];
-      const double s = p + q;
-      const double rs = rsqrt(s);
-      const double ipq = 4.0 * i2p * i2q;  // 1/(pq)
-      const double alpha = (p * q) * (rs * rs);
-      const double T = alpha * (X * X + Y * Y + Z * Z);
-      const double pref = pref0 * rs * ipq;
-      double F[LT + 1];
-      boys<QREF, LT>(g.mode, T, g.boys, F);
+      const RT q = cd.p, i2q = cd.i2p;
+      const RT X = Px - cd.Px, Y = Py - cd.Py, Z = Pz - cd.Pz;
+      const RT s = p + q;
+      const RT rs = rsq(s);
+      const RT ipq = RT(4) * i2p * i2q;  // 1/(pq)
+      const RT alpha = (p * q) * (rs * rs);
+      const RT T = alpha * (X * X + Y * Y + Z * Z);
+      const RT pref = pref0 * rs * ipq;
+      RT F[LT + 1];
+      boys_any<QREF, LT>(g, T, F);
 #pragma unroll
       for (int j = 0; j <= LT; ++j) F[j] *= pref;
-      double R[LT + 1][LT + 1][LT + 1];
-      hermite_R<LT>(F, -2.0 * alpha, X, Y, Z, R);
-      double fx[2][2][3], fy[2][2][3], fz[2][2][3];
-      pair_E(t.PAx[iq], t.PBx[iq], i2q, -1.0, fx);
-      pair_E(t.PAy[iq], t.PBy[iq], i2q, -1.0, fy);
-      pair_E(t.PAz[iq], t.PBz[iq], i2q, -1.0, fz);
-      double ccd[4];
+      RT R[LT + 1][LT + 1][LT + 1];
+      hermite_R<LT>(F, RT(-2) * alpha, X, Y, Z, R);
+      RT fx[2][2][3], fy[2][2][3], fz[2][2][3];
+      pair_E(cd.PAx, cd.PBx, i2q, RT(-1), fx);
+      pair_E(cd.PAy, cd.PBy, i2q, RT(-1), fy);
+      pair_E(cd.PAz, cd.PBz, i2q, RT(-1), fz);
+      RT ccd[4];
 #pragma unroll
-      for (int k = 0; k < 4; ++k) ccd[k] = t.c4[4 * iq + k];
+      for (int k = 0; k < 4; ++k) ccd[k] = cd.c[k];
 #pragma unroll
       for (int c = C0; c < C1; ++c)
 #pragma unroll
         for (int d = D0; d < D1; ++d) {
-          const double cf = ccd[2 * fang(c) + fang(d)];
-          double W[LAB + 1][LAB + 1][LAB + 1];
+          const RT cf = ccd[2 * fang(c) + fang(d)];
+          RT W[LAB + 1][LAB + 1][LAB + 1];
 #pragma unroll
           for (int x = 0; x <= LAB; ++x)
 #pragma unroll
@@ -229,7 +324,7 @@ __device__ __forceinline__ void quartet(const EriArgs &g, int P, int Q, size_t n
 #pragma unroll
               for (int z = 0; z <= LAB; ++z) {
                 if (x + y + z > LAB || !bra_needs(A0, A1, B0, B1, x, y, z)) continue;
-                double w = 0.0;
+                RT w = RT(0);
 #pragma unroll
                 for (int xx = 0; xx <= fl(c, 0) + fl(d, 0); ++xx)
 #pragma unroll
@@ -244,16 +339,16 @@ __device__ __forceinline__ void quartet(const EriArgs &g, int P, int Q, size_t n
           for (int a = A0; a < A1; ++a)
 #pragma unroll
             for (int b = B0; b < B1; ++b) {
-              double v = 0.0;
+              RT v = RT(0);
 #pragma unroll
               for (int x = 0; x <= fl(a, 0) + fl(b, 0); ++x)
 #pragma unroll
                 for (int y = 0; y <= fl(a, 1) + fl(b, 1); ++y)
 #pragma unroll
                   for (int z = 0; z <= fl(a, 2) + fl(b, 2); ++z) {
-                    const double e = ONFLY ? ex[fl(a, 0)][fl(b, 0)][x] * ey[fl(a, 1)][fl(b, 1)][y] *
-                                                 ez[fl(a, 2)][fl(b, 2)][z]
-                                           : eb[ONFLY ? 0 : a - A0][ONFLY ? 0 : b - B0][x][y][z];
+                    const RT e = ONFLY ? ex[fl(a, 0)][fl(b, 0)][x] * ey[fl(a, 1)][fl(b, 1)][y] *
+                                             ez[fl(a, 2)][fl(b, 2)][z]
+                                       : eb[ONFLY ? 0 : a - A0][ONFLY ? 0 : b - B0][x][y][z];
                     v += e * W[x][y][z];
                   }
               acc[a - A0][b - B0][c - C0][d - D0] += ONFLY ? v * cab[2 * fang(a) + fang(b)] : v;
@@ -271,7 +366,7 @@ __device__ __forceinline__ void quartet(const EriArgs &g, int P, int Q, size_t n
     for (int a = A0; a < A1; ++a)
 #pragma unroll
       for (int b = B0; b < B1; ++b)
-        if (a >= C0 && a < C1 && b >= D0 && b < D1) m = fmax(m, fabs(acc[a - A0][b - B0][a - C0][b - D0]));
+        if (a >= C0 && a < C1 && b >= D0 && b < D1) m = fmax(m, fabs((double)acc[a - A0][b - B0][a - C0][b - D0]));
     atomicMax(g.sch + P, (unsigned long long)__double_as_longlong(sqrt(m)));
     return;
   }
@@ -295,7 +390,7 @@ __device__ __forceinline__ void quartet(const EriArgs &g, int P, int Q, size_t n
           if (A == B && i < j) continue;
           if (C == D && k < l) continue;
           if (P == Q && (size_t)i * n + j < (size_t)k * n + l) continue;
-          const double x = acc[a - A0][b - B0][c - C0][d - D0];
+          const double x = (double)acc[a - A0][b - B0][c - C0][d - D0];
           if (EPI == EPI_XX) {
             double *XX = XXout;
             const size_t ij = (size_t)i + n * j, ji = (size_t)j + n * i, kl = (size_t)k + n * l,
@@ -377,7 +472,10 @@ __device__ __forceinline__ bool decode(const EriArgs &g, long long q, int &P, in
     P = pOff + (int)(q / nQ);
     Q = qOff + (int)(q % nQ);
   }
-  if (!listed && g.thr > 0.0 && g.t.schwarz[P] * g.t.schwarz[Q] < g.thr) return false;
+  if (!listed && g.thr > 0.0) {
+    const double b = g.t.schwarz[P] * g.t.schwarz[Q];
+    if (b < g.thr || (g.thr_hi > 0.0 && b >= g.thr_hi)) return false;
+  }
   return true;
 }
 
@@ -449,7 +547,7 @@ __global__ void quartet_pack_kernel(const long long *__restrict__ part, const in
   for (int k = threadIdx.x; k < counts[b]; k += blockDim.x) list[offs[b] + k] = part[(size_t)b * block + k];
 }
 
-template <int LA, int LB, int LC, int LD, int EPI>
+template <int LA, int LB, int LC, int LD, int EPI, class RT = double>
 __global__ void __launch_bounds__(128) eri_kernel(EriArgs g) {
   constexpr int NA = nfun(LA), NB = nfun(LB);
   constexpr int NOUT = NA * NB * nfun(LC) * nfun(LD);
@@ -469,21 +567,21 @@ __global__ void __launch_bounds__(128) eri_kernel(EriArgs g) {
   }
   constexpr int NC = nfun(LC), ND = nfun(LD);
   if (NSPLIT == 1) {
-    quartet<LA, LB, LC, LD, 0, NA, 0, NB, 0, NC, 0, ND, EPI>(g, P, Q, n, XX);
+    quartet<LA, LB, LC, LD, 0, NA, 0, NB, 0, NC, 0, ND, EPI, RT>(g, P, Q, n, XX);
   } else if (NSPLIT == 4) {  // (sp sp|sp s): one ket function c per thread, the whole bra
     switch (split) {
-      case 0: quartet<LA, LB, LC, LD, 0, NA, 0, NB, 0, 1, 0, ND, EPI>(g, P, Q, n, XX); break;
-      case 1: quartet<LA, LB, LC, LD, 0, NA, 0, NB, 1, 2, 0, ND, EPI>(g, P, Q, n, XX); break;
-      case 2: quartet<LA, LB, LC, LD, 0, NA, 0, NB, 2, 3, 0, ND, EPI>(g, P, Q, n, XX); break;
-      default: quartet<LA, LB, LC, LD, 0, NA, 0, NB, 3, 4, 0, ND, EPI>(g, P, Q, n, XX); break;
+      case 0: quartet<LA, LB, LC, LD, 0, NA, 0, NB, 0, 1, 0, ND, EPI, RT>(g, P, Q, n, XX); break;
+      case 1: quartet<LA, LB, LC, LD, 0, NA, 0, NB, 1, 2, 0, ND, EPI, RT>(g, P, Q, n, XX); break;
+      case 2: quartet<LA, LB, LC, LD, 0, NA, 0, NB, 2, 3, 0, ND, EPI, RT>(g, P, Q, n, XX); break;
+      default: quartet<LA, LB, LC, LD, 0, NA, 0, NB, 3, 4, 0, ND, EPI, RT>(g, P, Q, n, XX); break;
     }
   } else {  // (sp sp|sp sp): one ket pair (c, d) per thread, the whole bra
 #define MQ_SPLIT16(s) \
-  case s: quartet<LA, LB, LC, LD, 0, NA, 0, NB, (s) / 4, (s) / 4 + 1, (s) % 4, (s) % 4 + 1, EPI>(g, P, Q, n, XX); break;
+  case s: quartet<LA, LB, LC, LD, 0, NA, 0, NB, (s) / 4, (s) / 4 + 1, (s) % 4, (s) % 4 + 1, EPI, RT>(g, P, Q, n, XX); break;
     switch (split) {
       MQ_SPLIT16(0) MQ_SPLIT16(1) MQ_SPLIT16(2) MQ_SPLIT16(3) MQ_SPLIT16(4) MQ_SPLIT16(5) MQ_SPLIT16(6)
       MQ_SPLIT16(7) MQ_SPLIT16(8) MQ_SPLIT16(9) MQ_SPLIT16(10) MQ_SPLIT16(11) MQ_SPLIT16(12) MQ_SPLIT16(13)
-      MQ_SPLIT16(14) default: quartet<LA, LB, LC, LD, 0, NA, 0, NB, 3, 4, 3, 4, EPI>(g, P, Q, n, XX); break;
+      MQ_SPLIT16(14) default: quartet<LA, LB, LC, LD, 0, NA, 0, NB, 3, 4, 3, 4, EPI, RT>(g, P, Q, n, XX); break;
     }
 #undef MQ_SPLIT16
   }
@@ -494,7 +592,7 @@ static int nsplit_of(int cP, int cQ) {
   return nout <= 16 ? 1 : (nout <= 64 ? 4 : 16);
 }
 
-template <int EPI>
+template <int EPI, class RT = double>
 static int launch_class(mq_ctx *c, EriArgs g, int cP, int cQ) {
   const int nsplit = nsplit_of(cP, cQ);
   const long long warps = (g.nq + 31) / 32 * nsplit;
@@ -504,7 +602,7 @@ static int launch_class(mq_ctx *c, EriArgs g, int cP, int cQ) {
   if (grid == 0) return MQ_OK;
   if (grid > 2147483647LL) return set_err(c, MQ_EINVAL, "integral launch too large");
   dim3 gd((unsigned)grid);
-#define MQ_LAUNCH(a, b, cc, d) eri_kernel<a, b, cc, d, EPI><<<gd, block, 0, c->stream>>>(g)
+#define MQ_LAUNCH(a, b, cc, d) eri_kernel<a, b, cc, d, EPI, RT><<<gd, block, 0, c->stream>>>(g)
   if (cP == 0 && cQ == 0) MQ_LAUNCH(0, 0, 0, 0);
   else if (cP == 1 && cQ == 0) MQ_LAUNCH(1, 0, 0, 0);
   else if (cP == 1 && cQ == 1) MQ_LAUNCH(1, 0, 1, 0);
@@ -573,7 +671,24 @@ static int run_all(mq_ctx *c, EriArgs g) {
       h.nq = h.tri ? (long long)nP * (nP + 1) / 2 : (long long)nP * nQ;
       h.list = nullptr;
       h.list_n = nullptr;
-      if (h.thr > 0.0) MQ_TRY(compact_quartets(c, h, cP * (cP + 1) / 2 + cQ));
+      const int slot = cP * (cP + 1) / 2 + cQ;
+      if constexpr (EPI == EPI_XX) {
+        if (g.boys_f && c->eri_f32_tau > h.thr) {
+          // mixed precision: bounds >= tau in FP64, [thr, tau) in FP32
+          EriArgs h64 = h, h32 = h;
+          h64.thr = c->eri_f32_tau;
+          h64.thr_hi = 0.0;
+          MQ_TRY(compact_quartets(c, h64, slot));
+          MQ_TRY(launch_class<EPI>(c, h64, cP, cQ));
+          h32.thr = std::max(h.thr, 1e-300);
+          h32.thr_hi = c->eri_f32_tau;
+          h32.counters = h.counters ? h.counters + 2 : nullptr;
+          MQ_TRY(compact_quartets(c, h32, slot + 8));
+          MQ_TRY((launch_class<EPI, float>(c, h32, cP, cQ)));
+          continue;
+        }
+      }
+      if (h.thr > 0.0) MQ_TRY(compact_quartets(c, h, slot));
       MQ_TRY(launch_class<EPI>(c, h, cP, cQ));
     }
   return MQ_OK;
@@ -603,10 +718,12 @@ int eri_full_device(mq_ctx *c, double *d_XX) {
   EriArgs g = base_args(c);
   g.XX = d_XX;
   g.thr = c->schwarz_thr;
-  if (g.thr > 0) MQ_TRY(eri_schwarz(c));
-  unsigned long long *cnt = (unsigned long long *)buf(c, "eri_counters", 2 * sizeof(unsigned long long));
+  const bool mixed = c->eri_f32_tau > 0.0 && c->mode == MQ_MODE_TIGHT && c->d_boys_f32;
+  if (mixed) g.boys_f = c->d_boys_f32;
+  if (g.thr > 0 || mixed) MQ_TRY(eri_schwarz(c));
+  unsigned long long *cnt = (unsigned long long *)buf(c, "eri_counters", 4 * sizeof(unsigned long long));
   if (!cnt) return MQ_ENOMEM;
-  MQ_CUDA(c, cudaMemsetAsync(cnt, 0, 2 * sizeof(unsigned long long), c->stream));
+  MQ_CUDA(c, cudaMemsetAsync(cnt, 0, 4 * sizeof(unsigned long long), c->stream));
   g.counters = cnt;
   MQ_TRY(run_all<EPI_XX>(c, g));
   c->d_eri_counters = cnt;  // read when the quartet statistics are asked for

@@ -44,6 +44,9 @@ struct PairTable {
   // primitive pairs
   int npp;
   double *p, *inv2p, *beta, *Px, *Py, *Pz, *PAx, *PAy, *PAz, *PBx, *PBy, *PBz, *K, *c4;  // c4: 4 per pp
+  // single-precision copy, 4 float4 per primitive pair:
+  // p 1/2p K Px | Py Pz PAx PAy | PAz PBx PBy PBz | c4
+  float4 *pf;
 };
 
 // Host copy of a pair table (same fields as PairTable), built per molecule
@@ -93,6 +96,12 @@ struct Stats {
   double launches = 0, lib_launches = 0, quartets = 0, prim_quartets = 0;
   double ms_fock_kernel = 0, fock_kernel_launches = 0;  // the digestion kernel alone, last SCF or mq_fock
   double graph_launches = 0;  // CUDA-graph replays of the last batch SCF
+  double eig_cluster = 0;     // CTAs of the last FP32 cluster eigensolve (0: none)
+  double ms_eig_final = 0;    // the last SCF's final eigensolve (purification mode)
+  // last cold eigensolve: FP32 cluster sweeps and off-norm ratio reached, its
+  // phases' times, FP64 Jacobi sweeps
+  double eig_f32_sweeps = 0, eig_f32_off = 0, ms_eig_f32 = 0, ms_eig_refine = 0, ms_eig_jacobi = 0;
+  double eig_jacobi_sweeps = 0;
 };
 
 // Event pair on the context's stream that adds its elapsed time to a counter
@@ -135,6 +144,7 @@ struct mq_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
   void *cublas = nullptr;
+  int dgemm_cublas = 0;  // MYQC_DGEMM=cublas: every FP64 product through cuBLAS (comparison runs)
   std::string err;
   // system
   int have_system = 0;
@@ -147,6 +157,8 @@ struct mq_ctx {
   std::vector<int> pair_class_count;
   // device data
   double *d_boys = nullptr;  // Ftab (parity) or own table (tight)
+  float *d_boys_f32 = nullptr;  // tight table in single precision (mixed-precision integrals)
+  double eri_f32_tau = 0.0;     // quartets with a Schwarz bound below this are computed in FP32 (0: off)
   double *d_nuc = nullptr;   // nnuc x 4: x, y, z, Z
   mq::PairTable pt{};
   std::vector<void *> pair_allocs;
@@ -257,6 +269,13 @@ int syev_batched_device(mq_ctx *c, int n, int batch, double *d_A, double *d_w, d
 // one matrix of order n > JAC_SMEM_MAX on all SMs; d_V0 (optional) are start
 // vectors and d_A must then already be V0^T A V0
 int syev_large_device(mq_ctx *c, int n, double *d_A, const double *d_V0, double *d_w, double *d_V);
+// one matrix of order n > JAC_SMEM_MAX without start vectors: FP32 Jacobi on a
+// thread-block cluster, FP64 refinement, then syev_large_device (eigen.cu)
+int syev_large_cold(mq_ctx *c, int n, double *d_A, double *d_w, double *d_V);
+// small FP64 products on all SMs (dgemm.cu); gemm() takes them when they fit
+bool dgemm_small_fits(int m, int n, int k);
+int dgemm_small(mq_ctx *c, char ta, char tb, int m, int n, int k, double alpha, const double *A, int lda,
+                const double *B, int ldb, double beta, double *C, int ldc);
 int gemm(mq_ctx *c, char ta, char tb, int m, int n, int k, double alpha, const double *A, int lda, const double *B,
          int ldb, double beta, double *C, int ldc);
 int gemm_strided_batched(mq_ctx *c, char ta, char tb, int m, int n, int k, double alpha, const double *A, int lda,

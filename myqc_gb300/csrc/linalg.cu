@@ -13,6 +13,7 @@
 #include <cublas_v2.h>
 
 #include "internal.h"
+#include "gridsync.cuh"
 #include "jacobi.cuh"
 
 namespace mq {
@@ -52,49 +53,14 @@ __global__ void __launch_bounds__(JAC_THREADS) jacobi_kernel(int n, double *__re
 // transpose), and V <- V J row by row; no element is touched by two threads,
 // so a round needs a single grid barrier.  Every CTA recomputes the round's
 // rotation angles from the diagonal it reads after the barrier.  The barrier
-// is this file's own: arrive on a counter, wait on a generation word with an
-// iteration limit; on time-out it raises the error flag and every CTA leaves.
+// (gridsync.cuh) raises an error flag on time-out and every CTA leaves.
 // Launched cooperatively so that all CTAs are resident.
 constexpr int JG_THREADS = 256;
-constexpr long long BARRIER_SPIN_LIMIT = 20000000;  // ~ seconds of polling
-
-struct GridSync {
-  unsigned *count;
-  unsigned *gen;
-  int *err;
-};
-
-__device__ __forceinline__ bool grid_barrier(const GridSync &gs, unsigned nblocks) {
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    volatile unsigned *genv = gs.gen;
-    const unsigned g = *genv;
-    __threadfence();
-    if (atomicAdd(gs.count, 1u) == nblocks - 1) {
-      *gs.count = 0;
-      __threadfence();
-      atomicAdd(gs.gen, 1u);
-    } else {
-      long long it = 0;
-      while (*genv == g) {
-        if (++it > BARRIER_SPIN_LIMIT) {
-          atomicExch(gs.err, 2);
-          break;
-        }
-        if (*(volatile int *)gs.err) break;
-        __nanosleep(64);
-      }
-    }
-    __threadfence();
-  }
-  __syncthreads();
-  return *(volatile int *)gs.err == 0;
-}
-
 __global__ void __launch_bounds__(JG_THREADS) jacobi_grid_kernel(int n, double *__restrict__ A,
                                                                   double *__restrict__ V, double *__restrict__ w,
                                                                   double *__restrict__ Vout, double *part,
-                                                                  GridSync gs, int max_sweeps, double tol) {
+                                                                  GridSync gs, int max_sweeps, double tol,
+                                                                  int *__restrict__ info) {
   __shared__ double cs[2 * 512];
   __shared__ double red[JG_THREADS / 32];
   const int np = n + (n & 1), half = np / 2;
@@ -126,6 +92,7 @@ __global__ void __launch_bounds__(JG_THREADS) jacobi_grid_kernel(int n, double *
   }
   if (!grid_barrier(gs, nb)) return;
   const double stop2 = tol * tol * reduce_all();
+  const double skip = sqrt(stop2) / n;
   if (!grid_barrier(gs, nb)) return;
   int sweep = 0;
   for (; sweep < max_sweeps; ++sweep) {
@@ -140,6 +107,7 @@ __global__ void __launch_bounds__(JG_THREADS) jacobi_grid_kernel(int n, double *
     if (!grid_barrier(gs, nb)) return;  // everyone has read part[] before it is rewritten
     if (done) break;
     for (int r = 0; r < np - 1; ++r) {
+      int active = 0;
       for (int k = tid; k < half; k += blockDim.x) {
         int p, q;
         rr_pair(np, r, k, p, q);
@@ -147,17 +115,23 @@ __global__ void __launch_bounds__(JG_THREADS) jacobi_grid_kernel(int n, double *
         if (q < n) {
           const double apq = A[p + N * q];
           const double app = A[p + N * p], aqq = A[q + N * q];
-          if (fabs(apq) > 0x1p-60 * (fabs(app) + fabs(aqq))) {  // negligible rotations are skipped
+          // negligible rotations are skipped: below 2^-60 of the diagonal, or
+          // below skip = tol ||A||_F / n (all such pairs together stay under
+          // the stopping threshold)
+          if (fabs(apq) > fmax(0x1p-60 * (fabs(app) + fabs(aqq)), skip)) {
             const double theta = (aqq - app) / (2.0 * apq);
             const double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
             c = rsqrt(t * t + 1.0);
             s = t * c;
+            active = 1;
           }
         }
         cs[2 * k] = c;
         cs[2 * k + 1] = s;
       }
-      __syncthreads();
+      // every CTA reads the same A, so all skip a round without rotations
+      // together, barrier included
+      if (!__syncthreads_or(active)) continue;
       // blocks (P, Q) with P >= Q, and V rows
       const long long nblk = (long long)half * (half + 1) / 2;
       for (long long idx = gtid; idx < nblk + (long long)N * half; idx += gstride) {
@@ -220,6 +194,7 @@ __global__ void __launch_bounds__(JG_THREADS) jacobi_grid_kernel(int n, double *
     }
   }
   if (sweep >= max_sweeps && blockIdx.x == 0 && tid == 0) atomicExch(gs.err, 1);
+  if (blockIdx.x == 0 && tid == 0) info[0] = sweep;
   // sorted output: each global thread ranks one eigenvalue
   for (long long i = gtid; i < n; i += gstride) {
     const double wi = A[i + N * i];
@@ -266,13 +241,16 @@ int syev_large_device(mq_ctx *c, int n, double *d_A, const double *d_V0, double 
   }
   int max_sweeps = 40;
   double tol = 1e-14;  // ||offdiag||_F / ||A||_F at stop; eigenvalue error ~ tol^2 ||A|| / gap
-  void *args[] = {&n, &d_A, &V, &d_w, &d_V, &part, &gs, &max_sweeps, &tol};
+  int *info = (int *)(ws + 192);
+  void *args[] = {&n, &d_A, &V, &d_w, &d_V, &part, &gs, &max_sweeps, &tol, &info};
   MQ_CUDA(c, cudaLaunchCooperativeKernel((void *)jacobi_grid_kernel, dim3(nblocks), dim3(JG_THREADS), args, 0,
                                          c->stream));
   c->stats.launches += 2;
-  int h = 0;
+  int h = 0, sw = 0;
   MQ_CUDA(c, cudaMemcpyAsync(&h, gs.err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  MQ_CUDA(c, cudaMemcpyAsync(&sw, info, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   MQ_CUDA(c, cudaStreamSynchronize(c->stream));
+  c->stats.eig_jacobi_sweeps = sw;
   if (h == 2) return set_err(c, MQ_ETIMEOUT, "Jacobi grid barrier timed out");
   if (h == 1) return set_err(c, MQ_ENOCONV, "Jacobi eigensolver did not converge");
   return MQ_OK;
@@ -283,7 +261,7 @@ int syev_batched_device(mq_ctx *c, int n, int batch, double *d_A, double *d_w, d
   if (n > 1024) return set_err(c, MQ_EINVAL, "syev: n > 1024");
   const size_t n2 = (size_t)n * n;
   if (n > JAC_SMEM_MAX) {
-    for (int b = 0; b < batch; ++b) MQ_TRY(syev_large_device(c, n, d_A + n2 * b, nullptr, d_w + (size_t)n * b, d_V + n2 * b));
+    for (int b = 0; b < batch; ++b) MQ_TRY(syev_large_cold(c, n, d_A + n2 * b, d_w + (size_t)n * b, d_V + n2 * b));
     return MQ_OK;
   }
   const size_t smem = 2 * n2 * sizeof(double);
@@ -325,6 +303,8 @@ static cublasOperation_t op(char t) { return (t == 'T' || t == 't') ? CUBLAS_OP_
 
 int gemm(mq_ctx *c, char ta, char tb, int m, int n, int k, double alpha, const double *A, int lda, const double *B,
          int ldb, double beta, double *C, int ldc) {
+  if (dgemm_small_fits(m, n, k) && !c->dgemm_cublas)
+    return dgemm_small(c, ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
   cublasHandle_t h = handle(c);
   if (!h) return set_err(c, MQ_ECUDA, "cublasCreate failed");
   if (cublasDgemm(h, op(ta), op(tb), m, n, k, &alpha, A, lda, B, ldb, &beta, C, ldc) != CUBLAS_STATUS_SUCCESS)

@@ -21,6 +21,7 @@
 #include <cmath>
 #include <vector>
 
+#include "gridsync.cuh"
 #include "internal.h"
 
 namespace mq {
@@ -102,6 +103,168 @@ __global__ void identity_kernel(double *__restrict__ A, int n) {
   if (idx < N * N) A[idx] = (idx % N == idx / N) ? 1.0 : 0.0;
 }
 
+// ---- All TC2 steps in one cooperative launch (n <= PUR_PERSIST_MAX).
+// CTA b owns the lower-triangle 16x16 tiles b, b + grid, ... of X^2.  X is
+// symmetric, so (X^2)_ij = sum_k X_ki X_kj: the tile's 16 + 16 columns are
+// staged in shared memory and each thread forms one element.  The selection
+// needs tr X and tr X^2 of the matrix being squared; tr X^2 = ||X||_F^2, so
+// both come from per-tile partial sums that the previous step wrote with X
+// itself (double-buffered by step parity), and a step is: read the partials,
+// decide, square, write the next X and its partials, one grid barrier.  Every
+// CTA sums the partials in the same order, so all make the same choices and
+// stop together: at step j + 2 after the first step j whose idempotency error
+// tr(X_j - X_j^2) is below SETTLED, as the polled loop does.
+constexpr int PUR_TILE = 16;
+constexpr int PUR_PERSIST_MAX = 640;  // 2 x 16 staged columns of n doubles fit in shared memory
+constexpr int PUR_MAX_STEPS = 120;
+constexpr double PUR_SETTLED = 1e-9;
+
+__device__ __forceinline__ void tile_of(int t, int &I, int &J) {
+  I = (int)((sqrt(8.0 * t + 1.0) - 1.0) * 0.5);
+  while (I * (I + 1) / 2 > t) --I;
+  while ((I + 1) * (I + 2) / 2 <= t) ++I;
+  J = t - I * (I + 1) / 2;
+}
+
+// partial sums of one tile of X (lower triangle): [0] diagonal, [1] squares
+// weighted by 2 off the diagonal tiles; written to part[2 * tile + 0/1]
+__device__ __forceinline__ void tile_partials(double tr, double sq, double *red, double *part, int tile) {
+  tr = block_sum(tr, red);
+  sq = block_sum(sq, red);
+  if (threadIdx.x == 0) {
+    part[2 * tile] = tr;
+    part[2 * tile + 1] = sq;
+  }
+}
+
+__global__ void __launch_bounds__(256) purify_persist_kernel(int n, double nocc, double *X0,
+                                                             double *X1, double *part,
+                                                             double *__restrict__ err, int *__restrict__ info,
+                                                             GridSync gs) {
+  extern __shared__ double cols[];  // [2][16][ld], ld = n + 1: the 16 columns of a warp hit 16 bank pairs
+  __shared__ double red[32];
+  const int nt = (n + PUR_TILE - 1) / PUR_TILE, ntiles = nt * (nt + 1) / 2;
+  const int tid = threadIdx.x, ti = tid % PUR_TILE, tj = tid / PUR_TILE;
+  const int ld = n | 1;
+  const unsigned nb = gridDim.x;
+  const size_t N = n;
+  // partials of X_0
+  for (int tile = blockIdx.x; tile < ntiles; tile += nb) {
+    int I, J;
+    tile_of(tile, I, J);
+    const int i = I * PUR_TILE + ti, j = J * PUR_TILE + tj;
+    double tr = 0.0, sq = 0.0;
+    if (i < n && j < n) {
+      const double x = X0[i + N * j];
+      tr = (i == j) ? x : 0.0;
+      sq = (I == J ? 1.0 : 2.0) * x * x;
+    }
+    tile_partials(tr, sq, red, part, tile);
+  }
+  if (!grid_barrier(gs, nb)) return;
+  int settled_at = -1, k = 0;
+  for (; k < PUR_MAX_STEPS; ++k) {
+    const double *pk = part + (size_t)2 * ntiles * (k & 1);
+    double tr = 0.0, sq = 0.0;
+    for (int t = tid; t < ntiles; t += blockDim.x) {
+      tr += pk[2 * t];
+      sq += pk[2 * t + 1];
+    }
+    const double tx = block_sum(tr, red), tt = block_sum(sq, red);
+    const double e = tx - tt;
+    if (blockIdx.x == 0 && tid == 0) err[k] = e;
+    if (settled_at < 0 && fabs(e) < PUR_SETTLED) settled_at = k;
+    if (settled_at >= 0 && k >= settled_at + 2) break;
+    const bool square = fabs(tt - nocc) < fabs(2.0 * tx - tt - nocc);
+    const double *X = (k & 1) ? X1 : X0;
+    double *Y = (k & 1) ? X0 : X1;
+    double *pn = part + (size_t)2 * ntiles * ((k + 1) & 1);
+    for (int tile = blockIdx.x; tile < ntiles; tile += nb) {
+      int I, J;
+      tile_of(tile, I, J);
+      __syncthreads();  // the previous tile's columns are no longer read
+      // 32 columns of n values: loads batched 8 per thread before the stores
+      for (int base = tid; base < 2 * PUR_TILE * n; base += 8 * blockDim.x) {
+        double v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int idx = base + u * blockDim.x;
+          v[u] = 0.0;
+          if (idx < 2 * PUR_TILE * n) {
+            const int cc = idx / n, r = idx % n;  // cc: 0..31 over the I then the J columns
+            const int col = (cc < PUR_TILE ? I * PUR_TILE + cc : J * PUR_TILE + cc - PUR_TILE);
+            if (col < n) v[u] = X[r + N * col];
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int idx = base + u * blockDim.x;
+          if (idx < 2 * PUR_TILE * n) cols[(idx / n) * ld + idx % n] = v[u];
+        }
+      }
+      __syncthreads();
+      const int i = I * PUR_TILE + ti, j = J * PUR_TILE + tj;
+      const double *ci = cols + (size_t)ti * ld, *cj = cols + (size_t)(PUR_TILE + tj) * ld;
+      double t0 = 0.0, t1 = 0.0;
+      int r = 0;
+      for (; r + 1 < n; r += 2) {
+        t0 = fma(ci[r], cj[r], t0);
+        t1 = fma(ci[r + 1], cj[r + 1], t1);
+      }
+      if (r < n) t0 = fma(ci[r], cj[r], t0);
+      const double t = t0 + t1;
+      double ptr = 0.0, psq = 0.0;
+      if (i < n && j < n) {
+        const double y = square ? t : 2.0 * cj[i] - t;  // cj[i] = X(i, j)
+        Y[i + N * j] = y;
+        if (I != J) Y[j + N * i] = y;
+        ptr = (i == j) ? y : 0.0;
+        psq = (I == J ? 1.0 : 2.0) * y * y;
+      }
+      tile_partials(ptr, psq, red, pn, tile);
+    }
+    if (!grid_barrier(gs, nb)) return;
+  }
+  if (blockIdx.x == 0 && tid == 0) {
+    info[0] = k;                 // steps taken; the result is X_k
+    info[1] = settled_at >= 0;   // converged
+  }
+}
+
+static int purify_persistent(mq_ctx *c, int n, int nocc, double *d_P, double *d_W, double *d_err, int *steps) {
+  const size_t n2 = (size_t)n * n;
+  const int nt = (n + PUR_TILE - 1) / PUR_TILE, ntiles = nt * (nt + 1) / 2;
+  const size_t smem = (size_t)2 * PUR_TILE * (n | 1) * sizeof(double);
+  char *ws = (char *)buf(c, "purify_persist", 256 + 64 + sizeof(double) * 4 * ntiles);
+  if (!ws) return MQ_ENOMEM;
+  GridSync gs{(unsigned *)ws, (unsigned *)(ws + 64), (int *)(ws + 128)};
+  int *info = (int *)(ws + 192);
+  double *part = (double *)(ws + 320);
+  MQ_CUDA(c, cudaMemsetAsync(ws, 0, 320, c->stream));
+  MQ_CUDA(c, cudaFuncSetAttribute(purify_persist_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int sms = 0, per_sm = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+  MQ_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, purify_persist_kernel, 256, smem));
+  if (per_sm < 1) return set_err(c, MQ_EINVAL, "purification kernel does not fit on an SM");
+  // one tile per CTA where the tiles allow; every CTA must be resident
+  int grid = std::min(ntiles, sms * per_sm);
+  double *X0 = d_P, *X1 = d_W;
+  double noccd = (double)nocc;
+  void *args[] = {&n, &noccd, &X0, &X1, &part, &d_err, &info, &gs};
+  MQ_CUDA(c, cudaLaunchCooperativeKernel((void *)purify_persist_kernel, dim3(grid), dim3(256), args, smem,
+                                         c->stream));
+  c->stats.launches += 1;
+  int h[2] = {0, 0}, berr = 0;
+  MQ_CUDA(c, cudaMemcpyAsync(h, info, 2 * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  MQ_CUDA(c, cudaMemcpyAsync(&berr, gs.err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  MQ_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (berr) return set_err(c, MQ_ETIMEOUT, "purification grid barrier timed out");
+  *steps = h[0];
+  if (!h[1]) return set_err(c, MQ_ENOCONV, "purification did not converge (no gap at the Fermi level?)");
+  if (h[0] & 1) MQ_CUDA(c, cudaMemcpyAsync(d_P, d_W, n2 * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+  return MQ_OK;
+}
+
 int purify_projector(mq_ctx *c, int n, int nocc, const double *d_Fp, double *d_P, double *d_T, double *d_W,
                      double *d_err, int *steps) {
   const size_t n2 = (size_t)n * n;
@@ -117,11 +280,12 @@ int purify_projector(mq_ctx *c, int n, int nocc, const double *d_Fp, double *d_P
     MQ_CUDA(c, cudaGetLastError());
     return MQ_OK;
   }
-  constexpr int MAX_STEPS = 120, POLL = 4;
-  constexpr double SETTLED = 1e-9;  // idempotency error after which two more steps reach FP64 round-off
+  constexpr int MAX_STEPS = PUR_MAX_STEPS, POLL = 4;
+  constexpr double SETTLED = PUR_SETTLED;  // idempotency error after which two more steps reach FP64 round-off
   double *X = d_P, *Xn = d_W;
   purify_init_kernel<<<1, PUR_THREADS, 0, c->stream>>>(d_Fp, n, X);
   c->stats.launches += 1;
+  if (n <= PUR_PERSIST_MAX) return purify_persistent(c, n, nocc, d_P, d_W, d_err, steps);
   std::vector<double> e(MAX_STEPS);
   int k = 0, settled_at = -1;
   while (k < MAX_STEPS) {

@@ -245,7 +245,10 @@ int scf_device(mq_ctx *c, const double *S, const double *H, const mq_scf_opts *o
           MQ_TRY(gemm(c, 'T', 'N', n, n, n, 1.0, U, n, A, n, 0.0, dT1, n));
           MQ_TRY(gemm(c, 'N', 'N', n, n, n, 1.0, dT1, n, U, n, 0.0, A, n));
         }
-        MQ_TRY(syev_large_device(c, n, A, have_prev ? U : nullptr, dEps + (size_t)n * s, U));
+        if (have_prev)
+          MQ_TRY(syev_large_device(c, n, A, U, dEps + (size_t)n * s, U));
+        else
+          MQ_TRY(syev_large_cold(c, n, A, dEps + (size_t)n * s, U));
       }
       have_prev = true;
     }
@@ -399,12 +402,18 @@ int scf_device(mq_ctx *c, const double *S, const double *H, const mq_scf_opts *o
     }
   }
   // outputs: orbitals and eigenvalues of the last diagonalisation, D_k of the last iteration
+  c->stats.ms_eig_final = 0;
   if (purify && lastF) {  // one eigensolve of the last iteration's Fock matrices for C and eps
+    StageTimer t_eig;
+    t_eig.start(c->stream);
     have_prev = false;
     MQ_TRY(diagonalize(lastF));
     c->stats.diag_calls += 1;
     for (int s = 0; s < ns; ++s)
       MQ_TRY(gemm(c, 'N', 'N', n, n, n, 1.0, dX, n, dU + n2 * s, n, 0.0, dC + n2 * s, n));
+    t_eig.stop(c->stream);
+    t_eig.collect_sync();
+    c->stats.ms_eig_final = t_eig.total;
   }
   MQ_CUDA(c, cudaMemcpyAsync(C, dC, n2 * ns * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   MQ_CUDA(c, cudaMemcpyAsync(eps, dEps, (size_t)n * ns * sizeof(double), cudaMemcpyDeviceToHost, c->stream));

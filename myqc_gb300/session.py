@@ -179,6 +179,10 @@ class Context:
     def set_schwarz(self, thr: float):
         self._check(self.L.mq_set_schwarz(self.h, thr))
 
+    def set_eri_mixed(self, tau: float):
+        """Quartets with a Schwarz bound below tau in FP32 (tight mode; 0: all FP64)."""
+        self._check(self.L.mq_set_eri_mixed(self.h, float(tau)))
+
     # ---------------------------------------------------------------- integrals
     def int1e(self):
         n = self.n
@@ -270,6 +274,18 @@ class Context:
         return {"E_AA": e[0], "E_BB": e[1], "E_AB": e[2], "E_MP2": e[3]}
 
     # ---------------------------------------------------------------- linear algebra
+    def dgemm(self, A: np.ndarray, B: np.ndarray, transa: str = "N", transb: str = "N", alpha: float = 1.0,
+              beta: float = 0.0, C: np.ndarray = None):
+        """alpha op(A) op(B) + beta C through mq_dgemm (FP64 on the device)."""
+        A_, B_ = f64(A), f64(B)
+        m = A_.shape[1] if transa == "T" else A_.shape[0]
+        k = A_.shape[0] if transa == "T" else A_.shape[1]
+        n = B_.shape[0] if transb == "T" else B_.shape[1]
+        C_ = np.zeros((m, n), order="F") if C is None else np.asfortranarray(np.array(C, dtype=np.float64))
+        self._check(self.L.mq_dgemm(self.h, transa.encode(), transb.encode(), m, n, k, alpha, ptr(A_), A_.shape[0],
+                                    ptr(B_), B_.shape[0], beta, ptr(C_), m))
+        return C_
+
     def syev_batched(self, A: np.ndarray):
         A = np.asarray(A, dtype=np.float64)
         batch, n = A.shape[0], A.shape[1]

@@ -103,6 +103,81 @@ def test_syev_batched(ctx):
             assert np.allclose(A[b] @ V[b], V[b] * w[b], atol=1e-11 * n)
 
 
+def test_eri_mixed_precision(ctx, basis_text):
+    """Quartets with a Schwarz bound below tau computed in FP32: every integral
+    of (H2O)8 within 1e-6 tau of the FP64 pass (tau = 1e-4 and 1e-6), the
+    FP32 share counted, and FP64 again once tau is 0."""
+    from myqc_gb300 import MODE_TIGHT, molecules
+    sysm = molecules.water_cluster_system(8, 7.0, 3)
+    basis = formats.parse_mybasis_text(basis_text, sysm.atoms)
+    ctx.set_system(sysm, basis, None, MODE_TIGHT)
+    try:
+        ctx.set_schwarz(1e-12)
+        ctx.set_eri_mixed(0.0)
+        X64 = ctx.eri_full()
+        assert ctx.stat("quartets_f32") == 0
+        for tau in (1e-4, 1e-6):
+            ctx.set_eri_mixed(tau)
+            Xm = ctx.eri_full()
+            nf = ctx.stat("quartets_f32")
+            assert 0 < nf < ctx.stat("quartets")
+            err = np.max(np.abs(Xm - X64))
+            assert err < 1e-6 * tau, (tau, err)
+        ctx.set_eri_mixed(0.0)
+        assert np.array_equal(ctx.eri_full(), X64)
+    finally:
+        ctx.set_eri_mixed(0.0)
+        ctx.set_schwarz(0.0)
+
+
+def test_dgemm_small_and_large(ctx):
+    """mq_dgemm: the library's split-K FP64 kernel (small orders) and cuBLAS
+    (large) against NumPy, every transpose case, alpha/beta, odd sizes."""
+    rng = np.random.default_rng(6)
+    for (m, n, k) in ((1, 1, 1), (5, 7, 3), (33, 17, 65), (224, 224, 224), (150, 64, 300), (1100, 1000, 40)):
+        for ta in "NT":
+            for tb in "NT":
+                A = rng.standard_normal((k, m) if ta == "T" else (m, k))
+                B = rng.standard_normal((n, k) if tb == "T" else (k, n))
+                C0 = rng.standard_normal((m, n))
+                ref = 0.7 * ((A.T if ta == "T" else A) @ (B.T if tb == "T" else B)) - 1.3 * C0
+                out = ctx.dgemm(A, B, ta, tb, alpha=0.7, beta=-1.3, C=C0)
+                assert np.max(np.abs(out - ref)) < 1e-13 * k * max(1.0, np.max(np.abs(ref)))
+    # beta = 0 ignores C (NaN in C must not leak)
+    A = rng.standard_normal((40, 30))
+    out = ctx.dgemm(A, A, "T", "N", C=np.full((30, 30), np.nan))
+    assert np.allclose(out, A.T @ A, atol=1e-12)
+
+
+def test_syev_cluster_refined(ctx):
+    """Orders 111..512 without start vectors take the FP32 cluster Jacobi, the
+    FP64 first-order refinement and the FP64 Jacobi.  Spectra: random, and
+    bands of near-degenerate levels (gaps down to ~1e-6 of the norm) like a
+    molecular cluster's Fock matrix.  Eigenvalues within 1e-13 of the
+    norm, orthonormal vectors, residual ||A V - V w|| within 1e-12 of the norm."""
+    rng = np.random.default_rng(5)
+    cases = []
+    for n in (111, 224, 333):
+        M = rng.standard_normal((n, n))
+        cases.append(M + M.T)
+    n = 224
+    bands = [(-20.55, 0.02), (-1.35, 0.08), (-0.72, 0.1), (-0.55, 0.1), (-0.45, 0.1)]
+    w0 = np.concatenate([c + s * rng.random(32) for c, s in bands] + [0.6 + 0.4 * rng.random(64)])
+    Q, _ = np.linalg.qr(rng.standard_normal((n, n)))
+    A = (Q * w0) @ Q.T
+    cases.append(0.5 * (A + A.T))
+    for A in cases:
+        n = A.shape[0]
+        w, V = ctx.syev_batched(A[None])
+        w, V = w[0], V[0]
+        nrm = np.linalg.norm(A, 2)
+        assert np.max(np.abs(w - np.linalg.eigvalsh(A))) < 1e-13 * nrm * np.sqrt(n)
+        assert np.max(np.abs(V.T @ V - np.eye(n))) < 1e-13
+        assert np.max(np.abs(A @ V - V * w)) < 1e-12 * nrm
+        assert np.all(np.diff(w) >= 0)
+    assert ctx.stat("eig_cluster") in (8, 16)
+
+
 def test_fock_water_cluster(ctx, basis_text):
     """Stored Fock build at a size where the digestion's long sums matter:
     (H2O)8, n = 56, tight integrals, a random symmetric density and a
