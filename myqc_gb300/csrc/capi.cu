@@ -190,6 +190,7 @@ int mq_set_system(mq_ctx *c, int nnuc, const int *Z, const double *xyz, const do
   MQ_CUDA(c, cudaMalloc((void **)&c->d_nuc, nuc.size() * sizeof(double)));
   MQ_CUDA(c, cudaMemcpy(c->d_nuc, nuc.data(), nuc.size() * sizeof(double), cudaMemcpyHostToDevice));
   // integrals of a previous system are stale
+  c->slab_live_valid = 0;
   if (c->d_XX) cudaFree(c->d_XX);
   c->d_XX = nullptr;
   c->XX_elems = 0;
@@ -264,6 +265,7 @@ int mq_eri_upload(mq_ctx *c, const double *XX) {
   MQ_TRY(ensure_xx(c));
   MQ_CUDA(c, cudaMemcpyAsync(c->d_XX, XX, c->XX_elems * sizeof(double), cudaMemcpyHostToDevice, c->stream));
   MQ_CUDA(c, cudaStreamSynchronize(c->stream));
+  c->slab_live_valid = 0;  // any slab of the uploaded integrals may be nonzero
   return MQ_OK;
 }
 
@@ -629,6 +631,16 @@ int mq_stat(const mq_ctx *c, const char *key, double *value) {
     *value = (double)(f32 ? h[prim ? 3 : 2] : h[prim ? 1 : 0] + h[prim ? 3 : 2]);
   }
   else if (!strcmp(key, "eri_f32_tau")) *value = c->eri_f32_tau;
+  else if (!strcmp(key, "live_slabs")) {  // fraction of XX slabs the digestion reads (1: all)
+    unsigned long long h = 0;
+    if (c->slab_live_valid && c->d_slab_live_count) {
+      cudaMemcpyAsync(&h, c->d_slab_live_count, sizeof(h), cudaMemcpyDeviceToHost, mut->stream);
+      cudaStreamSynchronize(mut->stream);
+      *value = (double)h / ((double)c->nao * c->nao);
+    } else {
+      *value = 1.0;
+    }
+  }
   else return MQ_EINVAL;
   return MQ_OK;
 }

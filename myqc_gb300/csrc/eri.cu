@@ -712,6 +712,42 @@ int eri_schwarz(mq_ctx *c) {
   return MQ_OK;
 }
 
+// largest Schwarz bound (one CTA)
+__global__ void schwarz_max_kernel(const double *__restrict__ sch, int npairs, double *__restrict__ out) {
+  __shared__ double red[32];
+  double m = 0.0;
+  for (int p = threadIdx.x; p < npairs; p += blockDim.x) m = fmax(m, sch[p]);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) m = fmax(m, red[w]);
+    out[0] = fmax(m, red[0]);
+  }
+}
+
+// live[i + n j] for the AO pairs of shell pair P: Q_P * max_Q Q_Q >= thr, the
+// condition for some quartet of the slab to pass the integral screen
+// (Q_P Q_Q >= thr); counts the live slabs in cnt
+__global__ void slab_live_kernel(PairTable t, int n, double thr, const double *__restrict__ qmax,
+                                 unsigned char *__restrict__ live, unsigned long long *__restrict__ cnt) {
+  const int P = blockIdx.x * blockDim.x + threadIdx.x;
+  if (P >= t.npairs) return;
+  const int nA = P >= t.class_off[1] ? 4 : 1, nB = P >= t.class_off[2] ? 4 : 1;
+  const unsigned char v = t.schwarz[P] * qmax[0] >= thr ? 1 : 0;
+  const size_t N = n;
+  unsigned long long c = 0;
+  for (int a = 0; a < nA; ++a)
+    for (int b = 0; b < nB; ++b) {
+      const size_t i = t.aoA[P] + a, j = t.aoB[P] + b;
+      live[i + N * j] = v;
+      live[j + N * i] = v;
+      c += v ? (i == j ? 1 : 2) : 0;
+    }
+  if (c) atomicAdd(cnt, c);
+}
+
 int eri_full_device(mq_ctx *c, double *d_XX) {
   const size_t n = (size_t)c->nao;
   MQ_CUDA(c, cudaMemsetAsync(d_XX, 0, n * n * n * n * sizeof(double), c->stream));
@@ -727,6 +763,23 @@ int eri_full_device(mq_ctx *c, double *d_XX) {
   g.counters = cnt;
   MQ_TRY(run_all<EPI_XX>(c, g));
   c->d_eri_counters = cnt;  // read when the quartet statistics are asked for
+  c->slab_live_valid = 0;
+  if (g.thr > 0) {  // zero slabs of XX for the digestion to skip
+    const size_t n2 = n * n;
+    char *w = (char *)buf(c, "slab_live", n2 + 64);
+    if (!w) return MQ_ENOMEM;
+    double *qmax = (double *)w;
+    unsigned long long *lc = (unsigned long long *)(w + 8);
+    MQ_CUDA(c, cudaMemsetAsync(lc, 0, 8, c->stream));
+    schwarz_max_kernel<<<1, 1024, 0, c->stream>>>(c->pt.schwarz, c->pt.npairs, qmax);
+    slab_live_kernel<<<(c->pt.npairs + 127) / 128, 128, 0, c->stream>>>(c->pt, (int)n, g.thr, qmax,
+                                                                        (unsigned char *)(w + 64), lc);
+    c->stats.launches += 2;
+    MQ_CUDA(c, cudaGetLastError());
+    c->d_slab_live = (unsigned char *)(w + 64);
+    c->d_slab_live_count = lc;
+    c->slab_live_valid = 1;
+  }
   return MQ_OK;
 }
 

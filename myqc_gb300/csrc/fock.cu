@@ -17,44 +17,12 @@
 #include <mutex>
 #include <string>
 
+#include "df32.cuh"
 #include "internal.h"
 
 namespace mq {
 
 constexpr int FOCK_THREADS = 256;
-
-// ---- double-float arithmetic on the FP32 pipes ----------------------------
-// GB300 issues FP32 at many times its FP64 rate, so the digestion keeps its
-// sums as unevaluated float pairs (hi + lo, ~48-bit significand).  A double x
-// is split with integer operations only, without branches:
-//   hi = x truncated to 24 significant bits: the sign, the exponent rebiased
-//        from 1023 to 127, the top 23 fraction bits;
-//   lo = the remaining 29 fraction bits (an integer r times the ulp
-//        2^(E-1075) of x) converted to float (rounded to 24 bits) and scaled.
-// |x - hi - lo| <= 2^-48 |x| for 2^-74 <= |x| < 2^128; below 2^-74 lo is 0
-// (an absolute error under 2^-97) and below 2^-126 hi is 0 as well.
-__device__ __forceinline__ float2 split_f64(double x) {
-  const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
-  const unsigned sign = hi & 0x80000000u;
-  const unsigned E = (hi >> 20) & 0x7ffu;
-  const unsigned hb = sign | (((hi & 0x7fffffffu) - 0x38000000u) << 3) | (lo >> 29);
-  const float h = __uint_as_float(E > 896u ? hb : sign);
-  const unsigned sc = E > 948u ? (((E - 948u) << 23) | sign) : 0u;
-  const float l = __uint2float_rn(lo & 0x1fffffffu) * __uint_as_float(sc);
-  return make_float2(h, l);
-}
-
-// s += x * d in double-float: exact hi product (FMA), cross terms, two-sum
-__device__ __forceinline__ void dfma(float2 &s, float2 x, float2 d) {
-  const float ph = x.x * d.x;
-  const float pe = fmaf(x.x, d.x, -ph);
-  const float cr = fmaf(x.x, d.y, x.y * d.x);
-  const float t = s.x + ph;
-  const float bb = t - s.x;
-  const float err = (s.x - (t - bb)) + (ph - bb);
-  s.x = t;
-  s.y += err + (pe + cr);
-}
 
 // Arithmetic of the digestion.  ArithF64 is plain FP64, the reference's
 // arithmetic (the default).  ArithDF32 keeps each integral as a float pair and
@@ -212,8 +180,9 @@ template <class P, int R, int JC, bool UHF>
 __global__ void __launch_bounds__(PAIR_MAX_THREADS) fock_pair_kernel(
     const double *__restrict__ XX, const typename P::Den *__restrict__ DJ, const typename P::Den *__restrict__ DKa,
     const typename P::Den *__restrict__ DKb, const int4 *__restrict__ tiles, const MolDesc *__restrict__ mols,
-    const int *__restrict__ active, int kp_stride, int tri, double *__restrict__ J, double *__restrict__ Kpa,
-    double *__restrict__ Kpb, double *__restrict__ Qa, double *__restrict__ Qb) {
+    const int *__restrict__ active, int kp_stride, int tri, const unsigned char *__restrict__ live,
+    double *__restrict__ J, double *__restrict__ Kpa, double *__restrict__ Kpb, double *__restrict__ Qa,
+    double *__restrict__ Qb) {
   typedef typename P::Den Den;
   extern __shared__ __align__(16) unsigned char dsh_raw[];
   Den *dsh = (Den *)dsh_raw;  // D(:,i) then D(:,j) for the tile's j (alpha; beta after)
@@ -257,9 +226,17 @@ __global__ void __launch_bounds__(PAIR_MAX_THREADS) fock_pair_kernel(
       if (UHF) aqb[jj][r] = z;
     }
   }
+  // slabs known to be zero (every quartet screened out) are not read
+  bool lv[JC];
+  bool any = false;
+#pragma unroll
+  for (int jj = 0; jj < JC; ++jj) {
+    lv[jj] = jj < nj && (!live || live[i + N * (j0 + jj)]);
+    any |= lv[jj];
+  }
   const double *S0 = XX + n2 * ((size_t)i + N * j0);
 #pragma unroll 2
-  for (int l = 0; l < n; ++l) {
+  for (int l = 0; any && l < n; ++l) {
     const Den di_a = dia[l];
     const Den di_b = UHF ? dib[l] : dz;
     Den dj[R];
@@ -270,7 +247,7 @@ __global__ void __launch_bounds__(PAIR_MAX_THREADS) fock_pair_kernel(
     }
 #pragma unroll
     for (int jj = 0; jj < JC; ++jj) {
-      if (jj < nj) {
+      if (lv[jj]) {
         const Den dja_l = dja[jj * n + l];
         const Den djb_l = UHF ? djb[jj * n + l] : dz;
         const double *S = S0 + n2 * N * jj + N * l;
@@ -370,13 +347,13 @@ static int launch_pair(mq_ctx *c, const PairLaunch &L, int threads, size_t smem,
   if (uhf) {
     auto k = fock_pair_kernel<P, R, JC, true>;
     MQ_CUDA(c, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k<<<L.ntiles, threads, smem, c->stream>>>(L.XX, DJ, DKa, DKb, L.tiles, L.mols, L.active, L.nmax, L.tri, L.J,
-                                              L.Kpa, L.Kpb, L.Qa, L.Qb);
+    k<<<L.ntiles, threads, smem, c->stream>>>(L.XX, DJ, DKa, DKb, L.tiles, L.mols, L.active, L.nmax, L.tri, L.live,
+                                              L.J, L.Kpa, L.Kpb, L.Qa, L.Qb);
   } else {
     auto k = fock_pair_kernel<P, R, JC, false>;
     MQ_CUDA(c, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k<<<L.ntiles, threads, smem, c->stream>>>(L.XX, DJ, DKa, nullptr, L.tiles, L.mols, L.active, L.nmax, L.tri, L.J,
-                                              L.Kpa, nullptr, L.Qa, nullptr);
+    k<<<L.ntiles, threads, smem, c->stream>>>(L.XX, DJ, DKa, nullptr, L.tiles, L.mols, L.active, L.nmax, L.tri,
+                                              L.live, L.J, L.Kpa, nullptr, L.Qa, nullptr);
   }
   return MQ_OK;
 }
@@ -483,6 +460,7 @@ static int pair_build(mq_ctx *c, int JC, bool uhf, const void *DJ, const void *D
   if (!J) return MQ_ENOMEM;
   L.XX = c->d_XX;
   L.tri = 1;
+  L.live = c->slab_live_valid ? c->d_slab_live : nullptr;
   L.df32 = c->fock_df32;
   L.DJ = DJ;
   L.DKa = DKa;

@@ -170,6 +170,13 @@ struct mq_ctx {
   void *mlp = nullptr;               // the learned guess's network (mlp.cu)
   mq::StageTimer t_fock_kernel;
   mq::StageTimer t_eri;                       // the last integral pass, collected when asked for
+  // live[i + n j] = 0 when every integral of slab XX(:,:,i,j) was screened out
+  // (Schwarz bound of the slab's shell pair times the largest bound below the
+  // threshold): the slab is zero and the digestion skips it.  Valid for the
+  // integrals of the last mq_eri_store with a threshold; null otherwise.
+  unsigned char *d_slab_live = nullptr;
+  int slab_live_valid = 0;
+  unsigned long long *d_slab_live_count = nullptr;  // live slabs (i, j), both orders counted
   unsigned long long *d_eri_counters = nullptr;  // its quartet counters (device)  // the digestion kernel alone, collected at the caller's sync points
   mq::FockTiles fock_tiles[9];  // pair-slab tile tables, indexed by slabs per tile
   int fock_jc[2][2] = {{0, 0}, {0, 0}}, fock_jc_n[2][2] = {{0, 0}, {0, 0}};  // autotuned tile length [uhf][df32]
@@ -212,6 +219,7 @@ struct PairLaunch {
   const int *active;
   int ntiles, nmol, nmax;
   int tri;   // DJ carries lower-triangle weights: J sums over l <= k only
+  const unsigned char *live;  // slab (i,j) may be nonzero (n x n, single system); null: every slab
   int df32;  // densities are float pairs and the digestion double-float (else FP64 arrays)
   double *J, *Kpa, *Kpb, *Qa, *Qb, *Ka, *Kb;
 };

@@ -21,6 +21,7 @@
 #include <cmath>
 #include <vector>
 
+#include "df32.cuh"
 #include "gridsync.cuh"
 #include "internal.h"
 
@@ -50,29 +51,68 @@ __device__ __forceinline__ double block_min(double v, double *red) {
   return t;
 }
 
-// One CTA: Gershgorin interval [lo, hi] of the symmetric part of F, then
-// X_0 = (hi I - (F + F^T)/2) / (hi - lo).
-__global__ void __launch_bounds__(PUR_THREADS) purify_init_kernel(const double *__restrict__ F, int n,
-                                                                  double *__restrict__ X) {
-  __shared__ double red[PUR_THREADS / 32];
+// Gershgorin bounds in three launches (one warp per row, a one-CTA min/max,
+// an elementwise build) rather than on one SM: row r of the symmetric part
+// (F + F^T)/2 gives [d - off, d + off] with off = sum_{j != r} |f_rj|, or with
+// sym = 0 the row's absolute sum sum_j |s_rj| in rowhi (Newton-Schulz scale).
+__global__ void gersh_rows_kernel(const double *__restrict__ F, int n, int sym, double *__restrict__ rowlo,
+                                  double *__restrict__ rowhi) {
+  const int r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (r >= n) return;
   const size_t N = n;
-  double lo = INFINITY, nhi = INFINITY;  // min of row lower bounds, min of -(row upper bounds)
-  for (int r = threadIdx.x; r < n; r += blockDim.x) {
-    double off = 0.0;
-    for (int j = 0; j < n; ++j)
+  double off = 0.0;
+  for (int j = lane; j < n; j += 32) {
+    if (sym) {
       if (j != r) off += fabs(0.5 * (F[r + N * j] + F[j + N * r]));
-    const double d = F[r + N * r];
-    lo = fmin(lo, d - off);
-    nhi = fmin(nhi, -(d + off));
+    } else {
+      off += fabs(F[r + N * j]);
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) off += __shfl_xor_sync(0xffffffffu, off, o);
+  if (lane == 0) {
+    const double d = sym ? F[r + N * r] : 0.0;
+    rowlo[r] = d - off;
+    rowhi[r] = d + off;
+  }
+}
+
+// lohi[0] = min rowlo, lohi[1] = max rowhi (one CTA, fixed order per thread)
+__global__ void __launch_bounds__(PUR_THREADS) gersh_final_kernel(const double *__restrict__ rowlo,
+                                                                  const double *__restrict__ rowhi, int n,
+                                                                  double *__restrict__ lohi) {
+  __shared__ double red[PUR_THREADS / 32];
+  double lo = INFINITY, nhi = INFINITY;
+  for (int r = threadIdx.x; r < n; r += blockDim.x) {
+    lo = fmin(lo, rowlo[r]);
+    nhi = fmin(nhi, -rowhi[r]);
   }
   lo = block_min(lo, red);
-  const double hi = -block_min(nhi, red);
-  const double inv = 1.0 / fmax(hi - lo, 1e-300);
-  for (size_t idx = threadIdx.x; idx < N * N; idx += blockDim.x) {
-    const size_t r = idx % N, col = idx / N;
-    const double f = 0.5 * (F[idx] + F[col + N * r]);
-    X[idx] = ((r == col ? hi : 0.0) - f) * inv;
+  nhi = block_min(nhi, red);
+  if (threadIdx.x == 0) {
+    lohi[0] = lo;
+    lohi[1] = -nhi;
   }
+}
+
+// X_0 = (hi I - (F + F^T)/2) / (hi - lo)
+__global__ void purify_build_kernel(const double *__restrict__ F, int n, const double *__restrict__ lohi,
+                                    double *__restrict__ X) {
+  const size_t N = n, idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= N * N) return;
+  const double lo = lohi[0], hi = lohi[1];
+  const size_t r = idx % N, col = idx / N;
+  const double f = 0.5 * (F[idx] + F[col + N * r]);
+  X[idx] = ((r == col ? hi : 0.0) - f) / fmax(hi - lo, 1e-300);
+}
+
+static int gershgorin(mq_ctx *c, const double *F, int n, int sym, double *lohi) {
+  double *rows = (double *)buf(c, "gersh_rows", 2 * (size_t)n * sizeof(double));
+  if (!rows) return MQ_ENOMEM;
+  gersh_rows_kernel<<<(n * 32 + 255) / 256, 256, 0, c->stream>>>(F, n, sym, rows, rows + n);
+  gersh_final_kernel<<<1, PUR_THREADS, 0, c->stream>>>(rows, rows + n, n, lohi);
+  c->stats.launches += 2;
+  return MQ_OK;
 }
 
 // Xn = select(X, T = X X), T given by its lower triangle (DSYRK; X is
@@ -106,7 +146,10 @@ __global__ void identity_kernel(double *__restrict__ A, int n) {
 // ---- All TC2 steps in one cooperative launch (n <= PUR_PERSIST_MAX).
 // CTA b owns the lower-triangle 16x16 tiles b, b + grid, ... of X^2.  X is
 // symmetric, so (X^2)_ij = sum_k X_ki X_kj: the tile's 16 + 16 columns are
-// staged in shared memory and each thread forms one element.  The selection
+// staged in shared memory as double-float pairs and each thread forms one
+// element in double-float arithmetic on the FP32 pipes (FP64 issues at a small
+// fraction of the FP32 rate here); X itself, the selection and the traces stay
+// FP64.  The selection
 // needs tr X and tr X^2 of the matrix being squared; tr X^2 = ||X||_F^2, so
 // both come from per-tile partial sums that the previous step wrote with X
 // itself (double-buffered by step parity), and a step is: read the partials,
@@ -141,7 +184,7 @@ __global__ void __launch_bounds__(256) purify_persist_kernel(int n, double nocc,
                                                              double *X1, double *part,
                                                              double *__restrict__ err, int *__restrict__ info,
                                                              GridSync gs) {
-  extern __shared__ double cols[];  // [2][16][ld], ld = n + 1: the 16 columns of a warp hit 16 bank pairs
+  extern __shared__ float2 cols[];  // [2][16][ld] as double-float pairs, ld = n | 1: a warp's 16 columns hit 16 bank pairs
   __shared__ double red[32];
   const int nt = (n + PUR_TILE - 1) / PUR_TILE, ntiles = nt * (nt + 1) / 2;
   const int tid = threadIdx.x, ti = tid % PUR_TILE, tj = tid / PUR_TILE;
@@ -199,23 +242,26 @@ __global__ void __launch_bounds__(256) purify_persist_kernel(int n, double nocc,
 #pragma unroll
         for (int u = 0; u < 8; ++u) {
           const int idx = base + u * blockDim.x;
-          if (idx < 2 * PUR_TILE * n) cols[(idx / n) * ld + idx % n] = v[u];
+          if (idx < 2 * PUR_TILE * n) cols[(idx / n) * ld + idx % n] = split_f64(v[u]);
         }
       }
       __syncthreads();
       const int i = I * PUR_TILE + ti, j = J * PUR_TILE + tj;
-      const double *ci = cols + (size_t)ti * ld, *cj = cols + (size_t)(PUR_TILE + tj) * ld;
-      double t0 = 0.0, t1 = 0.0;
+      const double xij = (i < n && j < n) ? X[i + N * j] : 0.0;
+      const float2 *ci = cols + (size_t)ti * ld, *cj = cols + (size_t)(PUR_TILE + tj) * ld;
+      // (X^2)_ij in double-float on the FP32 pipes (about 2^-48 relative per
+      // product), two interleaved sums
+      float2 t0 = make_float2(0.f, 0.f), t1 = t0;
       int r = 0;
       for (; r + 1 < n; r += 2) {
-        t0 = fma(ci[r], cj[r], t0);
-        t1 = fma(ci[r + 1], cj[r + 1], t1);
+        dfma(t0, ci[r], cj[r]);
+        dfma(t1, ci[r + 1], cj[r + 1]);
       }
-      if (r < n) t0 = fma(ci[r], cj[r], t0);
-      const double t = t0 + t1;
+      if (r < n) dfma(t0, ci[r], cj[r]);
+      const double t = df_val(t0) + df_val(t1);
       double ptr = 0.0, psq = 0.0;
       if (i < n && j < n) {
-        const double y = square ? t : 2.0 * cj[i] - t;  // cj[i] = X(i, j)
+        const double y = square ? t : 2.0 * xij - t;
         Y[i + N * j] = y;
         if (I != J) Y[j + N * i] = y;
         ptr = (i == j) ? y : 0.0;
@@ -234,7 +280,7 @@ __global__ void __launch_bounds__(256) purify_persist_kernel(int n, double nocc,
 static int purify_persistent(mq_ctx *c, int n, int nocc, double *d_P, double *d_W, double *d_err, int *steps) {
   const size_t n2 = (size_t)n * n;
   const int nt = (n + PUR_TILE - 1) / PUR_TILE, ntiles = nt * (nt + 1) / 2;
-  const size_t smem = (size_t)2 * PUR_TILE * (n | 1) * sizeof(double);
+  const size_t smem = (size_t)2 * PUR_TILE * (n | 1) * sizeof(float2);
   char *ws = (char *)buf(c, "purify_persist", 256 + 64 + sizeof(double) * 4 * ntiles);
   if (!ws) return MQ_ENOMEM;
   GridSync gs{(unsigned *)ws, (unsigned *)(ws + 64), (int *)(ws + 128)};
@@ -283,7 +329,8 @@ int purify_projector(mq_ctx *c, int n, int nocc, const double *d_Fp, double *d_P
   constexpr int MAX_STEPS = PUR_MAX_STEPS, POLL = 4;
   constexpr double SETTLED = PUR_SETTLED;  // idempotency error after which two more steps reach FP64 round-off
   double *X = d_P, *Xn = d_W;
-  purify_init_kernel<<<1, PUR_THREADS, 0, c->stream>>>(d_Fp, n, X);
+  MQ_TRY(gershgorin(c, d_Fp, n, 1, d_err + PUR_MAX_STEPS));  // [lo, hi] after the step errors
+  purify_build_kernel<<<gb, 256, 0, c->stream>>>(d_Fp, n, d_err + PUR_MAX_STEPS, X);
   c->stats.launches += 1;
   if (n <= PUR_PERSIST_MAX) return purify_persistent(c, n, nocc, d_P, d_W, d_err, steps);
   std::vector<double> e(MAX_STEPS);
@@ -334,24 +381,16 @@ __global__ void ns_step_kernel(const double *__restrict__ A, int n, double *__re
   if (threadIdx.x == 0) atomicAdd(err + k, e);
 }
 
-// Y = S / c with c the Gershgorin bound of S; Z = I; scal[0] = c
-__global__ void __launch_bounds__(PUR_THREADS) ns_init_kernel(const double *__restrict__ S, int n,
-                                                              double *__restrict__ Y, double *__restrict__ Z,
-                                                              double *__restrict__ scal) {
-  __shared__ double red[PUR_THREADS / 32];
-  const size_t N = n;
-  double nhi = INFINITY;
-  for (int r = threadIdx.x; r < n; r += blockDim.x) {
-    double s = 0.0;
-    for (int j = 0; j < n; ++j) s += fabs(S[r + N * j]);
-    nhi = fmin(nhi, -s);
-  }
-  const double c = -block_min(nhi, red);
-  for (size_t idx = threadIdx.x; idx < N * N; idx += blockDim.x) {
-    Y[idx] = S[idx] / c;
-    Z[idx] = (idx % (N + 1) == 0) ? 1.0 : 0.0;
-  }
-  if (threadIdx.x == 0) scal[0] = c;
+// Y = S / c with c = lohi[1] the largest row absolute sum of S (>= lambda_max);
+// Z = I; scal[0] = c
+__global__ void ns_build_kernel(const double *__restrict__ S, int n, const double *__restrict__ lohi,
+                                double *__restrict__ Y, double *__restrict__ Z, double *__restrict__ scal) {
+  const size_t N = n, idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= N * N) return;
+  const double c = lohi[1];
+  Y[idx] = S[idx] / c;
+  Z[idx] = (idx % (N + 1) == 0) ? 1.0 : 0.0;
+  if (idx == 0) scal[0] = c;
 }
 
 __global__ void scale_kernel(const double *__restrict__ A, size_t n2, const double *__restrict__ c,
@@ -366,7 +405,10 @@ int inv_sqrt_ns(mq_ctx *c, int n, const double *d_S, double *d_X, double *w, dou
   constexpr int MAX_STEPS = 100, POLL = 4;
   const unsigned gb = (unsigned)std::min<size_t>((n2 + 255) / 256, 1024);
   MQ_CUDA(c, cudaMemsetAsync(d_err, 0, (MAX_STEPS + 1) * sizeof(double), c->stream));
-  ns_init_kernel<<<1, PUR_THREADS, 0, c->stream>>>(d_S, n, Y, Z, d_err + MAX_STEPS);
+  double *lohi = (double *)buf(c, "ns_lohi", 2 * sizeof(double));
+  if (!lohi) return MQ_ENOMEM;
+  MQ_TRY(gershgorin(c, d_S, n, 0, lohi));
+  ns_build_kernel<<<(unsigned)((n2 + 255) / 256), 256, 0, c->stream>>>(d_S, n, lohi, Y, Z, d_err + MAX_STEPS);
   c->stats.launches += 1;
   std::vector<double> e(MAX_STEPS);
   int k = 0, done_at = -1;

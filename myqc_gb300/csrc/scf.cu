@@ -29,54 +29,80 @@ __global__ void add_kernel(const double *a, const double *b, double *c, size_t n
   if (i < n) c[i] = a[i] + b[i];
 }
 
-// out[0] += 1/2 sum D (F + H), out[1] = max |Dn - Do| (single block, fixed order)
-__global__ void energy_diff_kernel(const double *D, const double *F, const double *H, const double *Dn,
-                                   const double *Do, size_t n2, double *out, int slot) {
-  __shared__ double se[1024], sd[1024];
-  double e = 0.0, d = 0.0;
-  for (size_t i = threadIdx.x; i < n2; i += blockDim.x) {
-    e += D[i] * (F[i] + H[i]);
-    if (Dn) d = fmax(d, fabs(Dn[i] - Do[i]));
-  }
-  se[threadIdx.x] = e;
-  sd[threadIdx.x] = d;
+// Reductions over n^2 elements in two launches: RED_BLOCKS CTAs write
+// partial sums, one CTA adds them in CTA order (deterministic).  A single CTA
+// would run the FP64 arithmetic of the whole matrix on one SM.
+constexpr int RED_BLOCKS = 64, RED_THREADS = 256;
+
+__device__ __forceinline__ double red_sum(double v, double *sh) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   __syncthreads();
-  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-    if (threadIdx.x < s) {
-      se[threadIdx.x] += se[threadIdx.x + s];
-      sd[threadIdx.x] = fmax(sd[threadIdx.x], sd[threadIdx.x + s]);
-    }
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) {
-    out[2 * slot] = 0.5 * se[0];
-    out[2 * slot + 1] = sd[0];
-  }
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double t = 0.0;
+  for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += sh[w];
+  return t;
+}
+__device__ __forceinline__ double red_max(double v, double *sh) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double t = 0.0;
+  for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t = fmax(t, sh[w]);
+  return t;
 }
 
-// max |Dn - Do| and RMS over all spin blocks -> out[0], out[1]
-__global__ void diff_kernel(const double *Dn, const double *Do, size_t n2, double *out) {
-  __shared__ double sm[1024], ss[1024];
+// part[b] = partial of sum D (F + H)
+__global__ void __launch_bounds__(RED_THREADS) energy_part_kernel(const double *__restrict__ D,
+                                                                  const double *__restrict__ F,
+                                                                  const double *__restrict__ H, size_t n2,
+                                                                  double *__restrict__ part) {
+  __shared__ double sh[RED_THREADS / 32];
+  double e = 0.0;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += (size_t)gridDim.x * blockDim.x)
+    e += D[i] * (F[i] + H[i]);
+  e = red_sum(e, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = e;
+}
+// out[2 slot] = 1/2 sum of the partials
+__global__ void energy_final_kernel(const double *__restrict__ part, int nb, double *__restrict__ out, int slot) {
+  if (threadIdx.x != 0) return;
+  double e = 0.0;
+  for (int b = 0; b < nb; ++b) e += part[b];
+  out[2 * slot] = 0.5 * e;
+}
+
+// part[2b], part[2b+1] = partial max |Dn - Do| and sum (Dn - Do)^2
+__global__ void __launch_bounds__(RED_THREADS) diff_part_kernel(const double *__restrict__ Dn,
+                                                                const double *__restrict__ Do, size_t n2,
+                                                                double *__restrict__ part) {
+  __shared__ double sh[RED_THREADS / 32];
   double m = 0.0, s2 = 0.0;
-  for (size_t i = threadIdx.x; i < n2; i += blockDim.x) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += (size_t)gridDim.x * blockDim.x) {
     const double d = Dn[i] - Do[i];
     m = fmax(m, fabs(d));
     s2 += d * d;
   }
-  sm[threadIdx.x] = m;
-  ss[threadIdx.x] = s2;
-  __syncthreads();
-  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-    if (threadIdx.x < s) {
-      sm[threadIdx.x] = fmax(sm[threadIdx.x], sm[threadIdx.x + s]);
-      ss[threadIdx.x] += ss[threadIdx.x + s];
-    }
-    __syncthreads();
-  }
+  m = red_max(m, sh);
+  s2 = red_sum(s2, sh);
   if (threadIdx.x == 0) {
-    out[0] = sm[0];
-    out[1] = sqrt(ss[0] / (double)n2);
+    part[2 * blockIdx.x] = m;
+    part[2 * blockIdx.x + 1] = s2;
   }
+}
+// out[0] = max |Dn - Do|, out[1] = RMS over all spin blocks
+__global__ void diff_final_kernel(const double *__restrict__ part, int nb, size_t n2, double *__restrict__ out) {
+  if (threadIdx.x != 0) return;
+  double m = 0.0, s2 = 0.0;
+  for (int b = 0; b < nb; ++b) {
+    m = fmax(m, part[2 * b]);
+    s2 += part[2 * b + 1];
+  }
+  out[0] = m;
+  out[1] = sqrt(s2 / (double)n2);
 }
 
 // X = U diag(s^-1/2) U^T: scale columns of U into W = U diag(s^-1/2)
@@ -95,20 +121,33 @@ __global__ void antisym_kernel(const double *A, double *E, int n) {
   E[i] = A[i] - A[c + (size_t)n * r];
 }
 
-// B[row, j] = <E_row, E_j> for j < m (one block per j)
-__global__ void dots_kernel(const double *E, size_t n2, int row, int m, size_t stride, double *B) {
-  __shared__ double sh[256];
-  const int j = blockIdx.x;
-  if (j >= m) return;
-  double s = 0.0;
-  for (size_t i = threadIdx.x; i < n2; i += blockDim.x) s += E[stride * row + i] * E[stride * j + i];
-  sh[threadIdx.x] = s;
-  __syncthreads();
-  for (int k = blockDim.x / 2; k > 0; k >>= 1) {
-    if (threadIdx.x < k) sh[threadIdx.x] += sh[threadIdx.x + k];
-    __syncthreads();
+// part[16 b + j] = partial of <E_row, E_j> for j < m (m <= 16)
+__global__ void __launch_bounds__(RED_THREADS) dots_part_kernel(const double *__restrict__ E, size_t n2, int row,
+                                                                int m, size_t stride, double *__restrict__ part) {
+  __shared__ double sh[RED_THREADS / 32];
+  double s[16];
+#pragma unroll
+  for (int j = 0; j < 16; ++j) s[j] = 0.0;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += (size_t)gridDim.x * blockDim.x) {
+    const double er = E[stride * row + i];
+#pragma unroll
+    for (int j = 0; j < 16; ++j)
+      if (j < m) s[j] += er * E[stride * j + i];
   }
-  if (threadIdx.x == 0) B[j] = sh[0];
+#pragma unroll
+  for (int j = 0; j < 16; ++j) {
+    if (j >= m) break;
+    const double t = red_sum(s[j], sh);
+    if (threadIdx.x == 0) part[16 * blockIdx.x + j] = t;
+  }
+}
+// B[j] = sum over CTAs of the partials, j < m
+__global__ void dots_final_kernel(const double *__restrict__ part, int nb, int m, double *__restrict__ B) {
+  const int j = threadIdx.x;
+  if (j >= m) return;
+  double t = 0.0;
+  for (int b = 0; b < nb; ++b) t += part[16 * b + j];
+  B[j] = t;
 }
 
 __global__ void lincomb_kernel(const double *F, size_t stride, const double *coef, int m, double *out, size_t n2) {
@@ -189,7 +228,7 @@ int scf_device(mq_ctx *c, const double *S, const double *H, const mq_scf_opts *o
 
   // device workspace
   const size_t nmat = 8 + 6 * ns + (size_t)2 * ndiis * ns;
-  double *w = (double *)buf(c, "scf_work", sizeof(double) * (n2 * nmat + 256 + n * ns));
+  double *w = (double *)buf(c, "scf_work", sizeof(double) * (n2 * nmat + 256 + n * ns + 16 * RED_BLOCKS));
   if (!w) return MQ_ENOMEM;
   double *dS = w, *dH = dS + n2, *dX = dH + n2, *dT1 = dX + n2, *dT2 = dT1 + n2, *dT3 = dT2 + n2;
   double *dU = dT3 + n2, *dW = dU + n2;
@@ -203,6 +242,7 @@ int scf_device(mq_ctx *c, const double *S, const double *H, const mq_scf_opts *o
   double *dEh = dFh + n2 * ns * ndiis;  // DIIS error history
   double *dScal = dEh + n2 * ns * ndiis;  // 256 scalars
   double *dEps = dScal + 256;           // n * ns
+  double *dRed = dEps + n * ns;         // reduction partials, 16 per CTA
   MQ_CUDA(c, cudaMemcpyAsync(dS, S, n2 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
   MQ_CUDA(c, cudaMemcpyAsync(dH, H, n2 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
 
@@ -338,8 +378,10 @@ int scf_device(mq_ctx *c, const double *S, const double *H, const mq_scf_opts *o
     }
     t_fock.stop(c->stream);
     for (int s = 0; s < ns; ++s) add_kernel<<<blocks(n2), 256, 0, c->stream>>>(dH, dG + n2 * s, dF + n2 * s, n2);
-    for (int s = 0; s < ns; ++s)
-      energy_diff_kernel<<<1, 1024, 0, c->stream>>>(dD + n2 * s, dF + n2 * s, dH, nullptr, nullptr, n2, dScal, s);
+    for (int s = 0; s < ns; ++s) {
+      energy_part_kernel<<<RED_BLOCKS, RED_THREADS, 0, c->stream>>>(dD + n2 * s, dF + n2 * s, dH, n2, dRed);
+      energy_final_kernel<<<1, 32, 0, c->stream>>>(dRed, RED_BLOCKS, dScal, s);
+    }
     const double *Fdiag = dF;
     if (ndiis > 0) {
       // commutator errors e_s = F D S - S D F, stored with F in ring slot `head`
@@ -355,7 +397,8 @@ int scf_device(mq_ctx *c, const double *S, const double *H, const mq_scf_opts *o
       for (int j = 0; j < ndiis; ++j) Bm[(size_t)head * ndiis + j] = Bm[(size_t)j * ndiis + head] = 0.0;
       std::vector<double> row(ndiis, 0.0);
       for (int s = 0; s < ns; ++s) {
-        dots_kernel<<<ndiis, 256, 0, c->stream>>>(dEh + n2 * s, n2, head, nh, n2 * ns, dScal + 16 + 16 * s);
+        dots_part_kernel<<<RED_BLOCKS, RED_THREADS, 0, c->stream>>>(dEh + n2 * s, n2, head, nh, n2 * ns, dRed);
+        dots_final_kernel<<<1, 32, 0, c->stream>>>(dRed, RED_BLOCKS, nh, dScal + 16 + 16 * s);
       }
       std::vector<double> hrow(32);
       MQ_CUDA(c, cudaMemcpyAsync(hrow.data(), dScal + 16, 32 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
@@ -383,7 +426,8 @@ int scf_device(mq_ctx *c, const double *S, const double *H, const mq_scf_opts *o
     MQ_TRY(density_step(Fdiag, dDn));
     t_diag.stop(c->stream);
     lastF = Fdiag;
-    diff_kernel<<<1, 1024, 0, c->stream>>>(dDn, dD, n2 * ns, dScal + 8);
+    diff_part_kernel<<<RED_BLOCKS, RED_THREADS, 0, c->stream>>>(dDn, dD, n2 * ns, dRed);
+    diff_final_kernel<<<1, 32, 0, c->stream>>>(dRed, RED_BLOCKS, n2 * ns, dScal + 8);
     c->stats.launches += 2 + 2 * ns;
     double hs[10];
     MQ_CUDA(c, cudaMemcpyAsync(hs, dScal, 10 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));

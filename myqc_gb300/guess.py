@@ -125,7 +125,7 @@ def descriptors(atoms, xyz_angstrom: np.ndarray, pairs: np.ndarray, Q: np.ndarra
         pi, ci = np.nonzero(keep)
         c = cand[pi, ci]
         k = rank[pi, ci]
-        loc = np.einsum("pji,pj->pi", Q[pi], xyz[c] - xyz[X[pi]])
+        loc = np.matmul((xyz[c] - xyz[X[pi]])[:, None, :], Q[pi])[:, 0, :]  # Q^T v
         base = 4 + side * K_ENV * 5 + k * 5
         for j in range(3):
             f[pi, base + j] = loc[:, j]
@@ -171,7 +171,7 @@ def extract_blocks(atoms, D: np.ndarray, pairs: np.ndarray, Q: np.ndarray) -> np
     ia, ib, va, vb = _ao_index(atoms, pairs)
     blk = D[ia[:, :, None], ib[:, None, :]] * (va[:, :, None] & vb[:, None, :])
     Ra, Rb = _rots(atoms, pairs, Q)
-    out = np.einsum("pki,pkl,plj->pij", Ra, blk, Rb)
+    out = np.matmul(np.matmul(Ra.transpose(0, 2, 1), blk), Rb)  # Ra^T blk Rb
     return out.reshape(len(pairs), NOUT)
 
 
@@ -184,7 +184,7 @@ def assemble(atoms, blocks: np.ndarray, pairs: np.ndarray, Q: np.ndarray) -> np.
     m = (va[:, :, None] & vb[:, None, :])
     Ra, Rb = _rots(atoms, pairs, Q)
     b5 = blocks.reshape(len(pairs), 5, 5) * m
-    blk = np.einsum("pik,pkl,pjl->pij", Ra, b5, Rb)
+    blk = np.matmul(np.matmul(Ra, b5), Rb.transpose(0, 2, 1))  # Ra b5 Rb^T
     diag = pairs[:, 0] == pairs[:, 1]
     blk[diag] = 0.5 * (blk[diag] + np.transpose(blk[diag], (0, 2, 1)))
     D = np.zeros((n, n))

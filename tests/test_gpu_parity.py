@@ -130,6 +130,36 @@ def test_eri_mixed_precision(ctx, basis_text):
         ctx.set_schwarz(0.0)
 
 
+def test_fock_skips_screened_slabs(ctx, basis_text):
+    """With a Schwarz threshold the integral pass marks slabs XX(:,:,i,j) whose
+    quartets were all screened out; the digestion skips them.  G must equal,
+    bit for bit, G from the same integrals uploaded (every slab read)."""
+    from myqc_gb300 import MODE_TIGHT, molecules
+    sysm = molecules.water_cluster_system(8, 9.0, 5)
+    basis = formats.parse_mybasis_text(basis_text, sysm.atoms)
+    ctx.set_system(sysm, basis, None, MODE_TIGHT)
+    try:
+        ctx.set_schwarz(1e-9)
+        XX = ctx.eri_full()
+        frac = ctx.stat("live_slabs")
+        assert 0.0 < frac < 1.0, frac
+        n = ctx.n
+        rng = np.random.default_rng(8)
+        D = rng.standard_normal((n, n))
+        D = D + D.T
+        for prec in (0, 1):
+            ctx.set_fock_precision(prec)
+            G_skip = ctx.fock(D)
+            ctx.eri_upload(XX)
+            assert ctx.stat("live_slabs") == 1.0
+            G_all = ctx.fock(D)
+            assert np.array_equal(G_skip, G_all), prec
+            ctx.eri_store()
+    finally:
+        ctx.set_fock_precision(0)
+        ctx.set_schwarz(0.0)
+
+
 def test_dgemm_small_and_large(ctx):
     """mq_dgemm: the library's split-K FP64 kernel (small orders) and cuBLAS
     (large) against NumPy, every transpose case, alpha/beta, odd sizes."""
