@@ -38,9 +38,32 @@ constexpr int CJ_MAX = 512;
 // partner of index j in round r of the circle-method tournament of rr_pair
 // (np players, m = np - 1 rounds; player 0 fixed)
 __device__ __forceinline__ int cj_partner(int j, int r, int m) {
-  if (j == 0) return 1 + r % m;
-  if (((j - 1 - r) % m + m) % m == 0) return 0;
-  return 1 + ((2 * r - j + 1) % m + m) % m;
+  // j in [0, m], r in [0, m): every residue below is one conditional step away
+  if (j == 0) return 1 + r;
+  if (j - 1 == r) return 0;
+  int x = 2 * r - j + 1;  // in (-m, 2m)
+  if (x < 0) x += m;
+  if (x >= m) x -= m;
+  return 1 + x;
+}
+// pair k of round r as rr_pair gives it, without integer division
+__device__ __forceinline__ void cj_pair(int np, int r, int k, int &p, int &q) {
+  const int m = np - 1;
+  if (k == 0) {
+    p = 0;
+    q = 1 + r;
+    return;
+  }
+  int a = r + k, b = r - k;
+  if (a >= m) a -= m;
+  if (b < 0) b += m;
+  p = 1 + a;
+  q = 1 + b;
+  if (p > q) {
+    const int t = p;
+    p = q;
+    q = t;
+  }
 }
 
 // rotation halves with a fixed rounding sequence: c x - s y and s x + c y
@@ -49,11 +72,13 @@ __device__ __forceinline__ float rhi(float c, float s, float x, float y) { retur
 
 constexpr int CJ_TX = 128;  // threads along a pair / row index; CJ_THREADS / CJ_TX along own columns
 
+template <int LC>  // cluster of C = 2^LC CTAs
 __global__ void __launch_bounds__(CJ_THREADS, 1)
     jacobi_cluster_f32_kernel(int n, const double *__restrict__ Ain, double *__restrict__ Vout, int max_sweeps,
                               float tol, int *__restrict__ info) {
+  constexpr int C = 1 << LC;
   cg::cluster_group cl = cg::this_cluster();
-  const int C = (int)cl.num_blocks(), rank = (int)cl.block_rank();
+  const int rank = (int)cl.block_rank();
   const int tid = threadIdx.x, nt = blockDim.x;
   const int tx = tid % CJ_TX, ty = tid / CJ_TX, ny = nt / CJ_TX;
   const int np = n + (n & 1), m = np - 1, half = np / 2;
@@ -128,13 +153,13 @@ __global__ void __launch_bounds__(CJ_THREADS, 1)
       // phase 1: the round's pairs and angles, this CTA's partner columns
       for (int k = tid; k < half; k += nt) {
         int p, q;
-        rr_pair(np, r, k, p, q);
+        cj_pair(np, r, k, p, q);
         pu[k] = p;
         pv[k] = q;
         float c = 1.f, s = 0.f, t = 0.f;
         if (q < n) {
-          const float *Aq = cl.map_shared_rank(A, q % C) + (size_t)(q / C) * ld;
-          const float *Ap = cl.map_shared_rank(A, p % C) + (size_t)(p / C) * ld;
+          const float *Aq = cl.map_shared_rank(A, q & (C - 1)) + (size_t)(q >> LC) * ld;
+          const float *Ap = cl.map_shared_rank(A, p & (C - 1)) + (size_t)(p >> LC) * ld;
           const float apq = Aq[p], aqq = Aq[q], app = Ap[p];
           if (fabsf(apq) > 0x1p-26f * (fabsf(app) + fabsf(aqq)) && apq != 0.f) {
             const float theta = (aqq - app) / (2.f * apq);
@@ -148,15 +173,18 @@ __global__ void __launch_bounds__(CJ_THREADS, 1)
         ang[3 * p + 2] = t;
       }
       for (int t = tid; t < T; t += nt) pt[t] = cj_partner(rank + C * t, r, m);
-      for (int idx = tid; idx < T * L4; idx += nt) {
-        const int t = idx / L4, e = idx - t * L4;
-        const int pj = cj_partner(rank + C * t, r, m);
-        if (pj < n) {
-          const size_t off_src = (size_t)(pj / C) * ld;
-          const float4 *sa = reinterpret_cast<const float4 *>(cl.map_shared_rank(A, pj % C) + off_src);
-          const float4 *sv = reinterpret_cast<const float4 *>(cl.map_shared_rank(V, pj % C) + off_src);
-          reinterpret_cast<float4 *>(BA + (size_t)t * ld)[e] = sa[e];
-          reinterpret_cast<float4 *>(BV + (size_t)t * ld)[e] = sv[e];
+      __syncthreads();
+      // partner columns: warp w copies column t = w, w + 16, ..; lane e its float4s
+      for (int t = tid >> 5; t < T; t += nt >> 5) {
+        const int pj = pt[t];
+        if (pj >= n) continue;
+        const size_t off_src = (size_t)(pj >> LC) * ld;
+        const float4 *sa = reinterpret_cast<const float4 *>(cl.map_shared_rank(A, pj & (C - 1)) + off_src);
+        const float4 *sv = reinterpret_cast<const float4 *>(cl.map_shared_rank(V, pj & (C - 1)) + off_src);
+        float4 *da = reinterpret_cast<float4 *>(BA + (size_t)t * ld), *dv = reinterpret_cast<float4 *>(BV + (size_t)t * ld);
+        for (int e = tid & 31; e < L4; e += 32) {
+          da[e] = sa[e];
+          dv[e] = sv[e];
         }
       }
       __syncthreads();
@@ -232,14 +260,12 @@ static int jacobi_cluster_f32(mq_ctx *c, int n, const double *A, double *V, int 
     const int Tmax = (n + C - 1) / C, ld = (n + 3) & ~3, np = n + (n & 1);
     const size_t smem = (size_t)(6 * Tmax * ld + 3 * np + 2 * C + Tmax + np) * sizeof(float) + 16;
     if (smem > 200 * 1024) continue;
-    if (cudaFuncSetAttribute(jacobi_cluster_f32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-        cudaSuccess) {
+    const void *kern = C == 16 ? (const void *)jacobi_cluster_f32_kernel<4> : (const void *)jacobi_cluster_f32_kernel<3>;
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
       cudaGetLastError();
       continue;
     }
-    if (C > 8 &&
-        cudaFuncSetAttribute(jacobi_cluster_f32_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
-            cudaSuccess) {
+    if (C > 8 && cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
       cudaGetLastError();
       continue;
     }
@@ -256,11 +282,14 @@ static int jacobi_cluster_f32(mq_ctx *c, int n, const double *A, double *V, int 
     cfg.attrs = at;
     cfg.numAttrs = 1;
     int ncl = 0;
-    if (cudaOccupancyMaxActiveClusters(&ncl, (void *)jacobi_cluster_f32_kernel, &cfg) != cudaSuccess || ncl < 1) {
+    if (cudaOccupancyMaxActiveClusters(&ncl, kern, &cfg) != cudaSuccess || ncl < 1) {
       cudaGetLastError();
       continue;
     }
-    MQ_CUDA(c, cudaLaunchKernelEx(&cfg, jacobi_cluster_f32_kernel, n, A, V, max_sweeps, tol, info));
+    if (C == 16)
+      MQ_CUDA(c, cudaLaunchKernelEx(&cfg, jacobi_cluster_f32_kernel<4>, n, A, V, max_sweeps, tol, info));
+    else
+      MQ_CUDA(c, cudaLaunchKernelEx(&cfg, jacobi_cluster_f32_kernel<3>, n, A, V, max_sweeps, tol, info));
     c->stats.launches += 1;
     c->stats.eig_cluster = C;
     return MQ_OK;

@@ -226,23 +226,24 @@ __global__ void __launch_bounds__(256) purify_persist_kernel(int n, double nocc,
       int I, J;
       tile_of(tile, I, J);
       __syncthreads();  // the previous tile's columns are no longer read
-      // 32 columns of n values: loads batched 8 per thread before the stores
-      for (int base = tid; base < 2 * PUR_TILE * n; base += 8 * blockDim.x) {
-        double v[8];
+      // 32 columns of n values, warp w staging columns w, w + 8, ..: lane e
+      // loads rows e, e + 32, .. (8 loads in flight per batch), no division
+      for (int cc = tid >> 5; cc < 2 * PUR_TILE; cc += blockDim.x >> 5) {
+        const int col = cc < PUR_TILE ? I * PUR_TILE + cc : J * PUR_TILE + cc - PUR_TILE;
+        float2 *dst = cols + (size_t)cc * ld;
+        const double *src = X + N * col;
+        for (int r0 = tid & 31; r0 < n; r0 += 8 * 32) {
+          double v[8];
 #pragma unroll
-        for (int u = 0; u < 8; ++u) {
-          const int idx = base + u * blockDim.x;
-          v[u] = 0.0;
-          if (idx < 2 * PUR_TILE * n) {
-            const int cc = idx / n, r = idx % n;  // cc: 0..31 over the I then the J columns
-            const int col = (cc < PUR_TILE ? I * PUR_TILE + cc : J * PUR_TILE + cc - PUR_TILE);
-            if (col < n) v[u] = X[r + N * col];
+          for (int u = 0; u < 8; ++u) {
+            const int r = r0 + 32 * u;
+            v[u] = (col < n && r < n) ? src[r] : 0.0;
           }
-        }
 #pragma unroll
-        for (int u = 0; u < 8; ++u) {
-          const int idx = base + u * blockDim.x;
-          if (idx < 2 * PUR_TILE * n) cols[(idx / n) * ld + idx % n] = split_f64(v[u]);
+          for (int u = 0; u < 8; ++u) {
+            const int r = r0 + 32 * u;
+            if (r < n) dst[r] = split_f64(v[u]);
+          }
         }
       }
       __syncthreads();
@@ -250,15 +251,17 @@ __global__ void __launch_bounds__(256) purify_persist_kernel(int n, double nocc,
       const double xij = (i < n && j < n) ? X[i + N * j] : 0.0;
       const float2 *ci = cols + (size_t)ti * ld, *cj = cols + (size_t)(PUR_TILE + tj) * ld;
       // (X^2)_ij in double-float on the FP32 pipes (about 2^-48 relative per
-      // product), two interleaved sums
-      float2 t0 = make_float2(0.f, 0.f), t1 = t0;
+      // product), four interleaved sums
+      float2 t0 = make_float2(0.f, 0.f), t1 = t0, t2 = t0, t3 = t0;
       int r = 0;
-      for (; r + 1 < n; r += 2) {
+      for (; r + 3 < n; r += 4) {
         dfma(t0, ci[r], cj[r]);
         dfma(t1, ci[r + 1], cj[r + 1]);
+        dfma(t2, ci[r + 2], cj[r + 2]);
+        dfma(t3, ci[r + 3], cj[r + 3]);
       }
-      if (r < n) dfma(t0, ci[r], cj[r]);
-      const double t = df_val(t0) + df_val(t1);
+      for (; r < n; ++r) dfma(t0, ci[r], cj[r]);
+      const double t = (df_val(t0) + df_val(t1)) + (df_val(t2) + df_val(t3));
       double ptr = 0.0, psq = 0.0;
       if (i < n && j < n) {
         const double y = square ? t : 2.0 * xij - t;
