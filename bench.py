@@ -106,6 +106,8 @@ def load_workload(seed: int):
 MODEL = os.path.join(ROOT, "myqc_gb300", "data", "guess_mlp.npz")
 SCHWARZ = 1e-12  # fast arm: contracted quartets with a Schwarz bound below this are skipped
 ERI_F32_TAU = 1e-5  # fast arm: quartets with a bound below this in FP32 (max |dG| 3e-11 on (H2O)32)
+FOCK_INC_TAU = 1e-6  # fast arm: FP32 incremental Fock builds once max|D_k - D_(k-1)| is below this
+AO2MO_PREFETCH = 3  # fast arm: XX cut into 3 BF16 planes beside the SCF's final eigensolve
 _learned = {}
 
 
@@ -121,15 +123,18 @@ def solve(ctx, sysm, basis, fast: bool, set_system: bool):
     """One solve through the public API.  fast: the learned initial density
     (core guess when the prediction fails its checks or the SCF does not
     converge from it), Schwarz screening at 1e-12, quartets with a bound below
-    1e-5 in FP32, the double-float Fock
-    digestion, densities by purification (one eigensolve at the end)
-    and split-precision MP2; plain: the core-Hamiltonian guess, the
+    1e-5 in FP32, the double-float Fock digestion with FP32 incremental builds
+    once the density moves by less than 1e-6, densities by purification (one
+    eigensolve at the end, with the XX slices of the transform formed beside
+    it) and split-precision MP2; plain: the core-Hamiltonian guess, the
     eigensolver every iteration and the FP64 transform.  Both use DIIS(8)
     (plain Roothaan iterations, the reference's scheme, oscillate without
     converging on this cluster)."""
     from myqc_gb300 import FOCK_DF32, FOCK_FP64, MODE_TIGHT, PREC_FP64, PREC_SPLIT_BF16X3
     ctx.set_schwarz(SCHWARZ if fast else 0.0)
     ctx.set_fock_precision(FOCK_DF32 if fast else FOCK_FP64)
+    ctx.set_fock_incremental(FOCK_INC_TAU if fast else 0.0)
+    ctx.set_ao2mo_prefetch(AO2MO_PREFETCH if fast else 0)
     if set_system:
         ctx.set_system(sysm, basis, None, MODE_TIGHT)
     ctx.set_eri_mixed(ERI_F32_TAU if fast else 0.0)
@@ -181,7 +186,7 @@ def run_ours(args):
     L0 = stat(ctx, "launches")
     t_fock = t_eri = t_diag = t_ao2mo = t_fock_kernel = 0.0
     nq = nq32 = 0.0
-    nfock = n_fock_kernel = 0
+    nfock = n_fock_kernel = n_inc = 0
     iters = []
     barrier()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -194,6 +199,7 @@ def run_ours(args):
             t_fock += stat(ctx, "fock")
             nfock += stat(ctx, "fock_calls")
             t_fock_kernel += stat(ctx, "fock_kernel")
+            n_inc += stat(ctx, "fock_inc_builds")
             n_fock_kernel += stat(ctx, "fock_kernel_launches")
             t_eri += stat(ctx, "eri")
             nq32 += stat(ctx, "quartets_f32")
@@ -279,7 +285,8 @@ def run_ours(args):
         "config": {"workload": workload(), "molecule": f"(H2O){NMOL}", "n_basis": n, "n_occ": sysm.nelcA,
                    "n_vir": n - sysm.nelcA, "box_angstrom": BOX, "seed": args.seed, "basis": "STO-3G",
                    "boys": "tight FP64 table (FP32 copy for the FP32 quartets)", "schwarz": SCHWARZ,
-                   "eri_fp32_below_bound": ERI_F32_TAU, "scf": "FP64 (Fock digestion in double-float on the FP32 pipes), DIIS(8), conv 1e-10 RMS dD, initial density from the learned guess (core guess fallback), densities by TC2 purification (FP64 GEMMs), one Jacobi eigensolve at the end",
+                   "eri_fp32_below_bound": ERI_F32_TAU, "fock_fp32_increments_below": FOCK_INC_TAU,
+                   "scf": "FP64 (Fock digestion in double-float on the FP32 pipes, FP32 increments near convergence), DIIS(8), conv 1e-10 RMS dD, initial density from the learned guess (core guess fallback), densities by TC2 purification (FP64 GEMMs), one Jacobi eigensolve at the end",
                    "guess_model": os.path.relpath(MODEL, ROOT) if learned_guess(ctx) is not None else None,
                    "mp2_precision": "split hi+mid+lo bf16 (tcgen05), fp32 accumulate" if prec else "fp64",
                    "l2": "inputs larger than L2: the 20 GB integral array is rebuilt and streamed every step",
@@ -303,6 +310,7 @@ def run_ours(args):
         "eri_quartets_per_s": nq / (t_eri * 1e-3) if t_eri > 0 else None,
         "eri_fp32_share": nq32 / max(nq, 1.0),
         "fock_builds_per_s": 1000.0 * nfock / t_fock if t_fock > 0 else None,
+        "fock_fp32_increments_per_solve": n_inc / args.steps,
     }
     if args.secondary and world == 1:
         out["secondary"] = {"batched": measure_batched(ctx, args.batch_count), "direct_h2o64": measure_direct(ctx)}
@@ -310,6 +318,10 @@ def run_ours(args):
         out["cpu_baseline"] = cpu_baseline(res_p.iterations, quick=True)
     if rank == 0:
         print(json.dumps(out), flush=True)
+    ctx.close()
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
 
 
 def measure_batched(ctx, count: int):
@@ -353,10 +365,6 @@ def measure_direct(ctx):
     ctx.fock(D, direct=True)
     return {"molecule": "(H2O)64", "n_basis": n, "schwarz": 1e-12, "fock_ms": ctx.stat("fock"),
             "wall_ms": 1e3 * (time.perf_counter() - t)}
-    ctx.close()
-    if world > 1:
-        import torch.distributed as dist
-        dist.destroy_process_group()
 
 
 # ----------------------------------------------------------------------------------------------

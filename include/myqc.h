@@ -110,6 +110,25 @@ int mq_fock(mq_ctx *ctx, const double *Da, const double *Db, double *Ga, double 
 #define MQ_FOCK_DF32 1
 int mq_set_fock_precision(mq_ctx *ctx, int precision);
 
+/* Incremental Fock builds in mq_scf with stored integrals; no reference
+ * counterpart.  tau > 0: once the density of an iteration differs from the
+ * previous one by less than tau (max |D_k - D_(k-1)|), the build is
+ * G_k = G_(k-1) + G[D_k - D_(k-1)] with the increment digested in FP32 on the
+ * FP32 pipes; larger changes get full builds in the mq_set_fock_precision
+ * arithmetic.  The increment's error scales with its size: tau = 1e-6 keeps
+ * the converged energy within ~1e-9 Eh of full builds.  tau = 0 (default): full
+ * builds only.  MQ_EINVAL outside [0, 1e-3]. */
+int mq_set_fock_incremental(mq_ctx *ctx, double tau);
+
+/* Overlap for the split-precision transform; no reference counterpart.
+ * planes = 2 or 3 (MQ_PREC_SPLIT_BF16 / MQ_PREC_SPLIT_BF16X3): an mq_scf that
+ * ends with an eigensolve of the purified Fock matrix (opts.purify) cuts the
+ * stored XX into that many BF16 planes on a low-priority side stream while
+ * the eigensolve runs, and the next split mq_ao2mo_iajb / mq_mp2_* of the same
+ * XX starts from those slices.  Results are identical with and without it.
+ * 0 (default): off. */
+int mq_set_ao2mo_prefetch(mq_ctx *ctx, int planes);
+
 /* Allocation-free RHF Fock build.  No counterpart in the reference: it exists
  * for callers that cannot allocate device memory themselves (device arrays
  * owned by an OpenACC / OpenMP-offload runtime or a preallocated pool, code

@@ -97,6 +97,8 @@ def lib(path: str | None = None):
     L.mq_mlp_set_data.argtypes = [vp, ctypes.c_longlong, vp, vp, vp]
     L.mq_mlp_train_epoch.argtypes = [vp, vp, c_int, ctypes.c_float, ctypes.POINTER(c_double)]
     L.mq_set_fock_precision.argtypes = [vp, c_int]
+    L.mq_set_fock_incremental.argtypes = [vp, c_double]
+    L.mq_set_ao2mo_prefetch.argtypes = [vp, c_int]
     L.mq_batch_clear.argtypes = [vp]
     L.mq_batch_add.argtypes = [vp, c_int, vp, vp, vp, vp, vp, vp, c_int]
     L.mq_batch_info.argtypes = [vp, ip, vp]

@@ -15,6 +15,7 @@
 // MP2 (src/mp2/mp2.f90:79-232): E(AB) = sum_{ijab} (ia|jb)^2 / D and
 // E(AA) = sum_{i<j,a<b} [(ia|jb) - (ib|ja)]^2 / D, D = e_i + e_j - e_a - e_b,
 // reduced in a fixed order (per-block partials, then one block).
+#include "df32.cuh"
 #include "internal.h"
 
 namespace mq {
@@ -82,6 +83,61 @@ __global__ void mp2_partial_kernel(const double *__restrict__ Om, int no1, int n
   }
 }
 
+// The same pair sums over (ia|jb) from the split-precision transform, whose
+// values carry ~2^-24 relative error already: arithmetic on the FP32 pipes
+// (GB300's FP64 rate would make the FP64 divide the bottleneck).  Each
+// integral is split into float hi + lo (integer operations), squares are
+// hi^2 + 2 hi lo, the same-spin difference is (hi - hi') + (lo - lo'), the
+// denominators and reciprocals are FP32 (round to nearest: the per-term errors
+// are unbiased), the sum over b is FP32 and everything after it FP64.
+__global__ void mp2_partial_f32_kernel(const double *__restrict__ Om, int no1, int nv1, int no2, int nv2,
+                                       const double *__restrict__ eo1, const double *__restrict__ ev1,
+                                       const double *__restrict__ eo2, const double *__restrict__ ev2, int same_spin,
+                                       double *__restrict__ part) {
+  __shared__ double s_os[256], s_ss[256];
+  extern __shared__ float evf[];  // ev2 as floats
+  for (int b = threadIdx.x; b < nv2; b += blockDim.x) evf[b] = (float)ev2[b];
+  __syncthreads();
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long tot = (long long)no1 * nv1 * no2;
+  double os = 0.0, ss = 0.0;
+  if (idx < tot) {
+    const int i = (int)(idx % no1);
+    const int a = (int)((idx / no1) % nv1);
+    const int j = (int)(idx / ((long long)no1 * nv1));
+    const size_t sb = (size_t)no1 * nv1 * no2;
+    const float eija = (float)(eo1[i] + eo2[j] - ev1[a]);
+    const bool ssp = same_spin && i < j;
+    float fo = 0.f, fs = 0.f;
+    for (int b = 0; b < nv2; ++b) {
+      const float2 x = split_f64(__ldcs(Om + idx + sb * b));
+      const float inv = __frcp_rn(eija - evf[b]);
+      fo = fmaf(fmaf(2.f * x.x, x.y, x.x * x.x), inv, fo);
+      if (ssp && a < b) {
+        const float2 xp = split_f64(Om[i + (size_t)no1 * (b + (size_t)nv1 * j) + sb * a]);
+        const float yh = x.x - xp.x, yl = x.y - xp.y;
+        fs = fmaf(fmaf(2.f * yh, yl, yh * yh), inv, fs);
+      }
+    }
+    os = fo;
+    ss = fs;
+  }
+  s_os[threadIdx.x] = os;
+  s_ss[threadIdx.x] = ss;
+  __syncthreads();
+  for (int k = blockDim.x / 2; k > 0; k >>= 1) {
+    if (threadIdx.x < k) {
+      s_os[threadIdx.x] += s_os[threadIdx.x + k];
+      s_ss[threadIdx.x] += s_ss[threadIdx.x + k];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    part[2 * blockIdx.x] = s_os[0];
+    part[2 * blockIdx.x + 1] = s_ss[0];
+  }
+}
+
 __global__ void mp2_final_kernel(const double *part, int nblk, double *out) {
   __shared__ double s_os[1024], s_ss[1024];
   double os = 0.0, ss = 0.0;
@@ -113,7 +169,11 @@ int mp2_pair_sums(mq_ctx *c, const double *d_Om, int no1, int nv1, int no2, int 
   const int nblk = (int)((tot + tb - 1) / tb);
   double *part = (double *)buf(c, "mp2_partials", sizeof(double) * (2 * (size_t)nblk + 2));
   if (!part) return MQ_ENOMEM;
-  if (nblk > 0)
+  const bool f32 = d_Om == c->d_iajb && c->iajb_precision != MQ_PREC_FP64;  // split-precision (ia|jb)
+  if (nblk > 0 && f32)
+    mp2_partial_f32_kernel<<<nblk, tb, sizeof(float) * nv2, c->stream>>>(
+        d_Om, no1, nv1, no2, nv2, d_e1, d_e1 + no1, d_e2, d_e2 + no2, same_spin, part);
+  else if (nblk > 0)
     mp2_partial_kernel<<<nblk, tb, 0, c->stream>>>(d_Om, no1, nv1, no2, nv2, d_e1, d_e1 + no1, d_e2, d_e2 + no2,
                                                    same_spin, part);
   mp2_final_kernel<<<1, 1024, 0, c->stream>>>(part, nblk, part + 2 * (size_t)nblk);

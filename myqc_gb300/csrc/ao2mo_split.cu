@@ -461,6 +461,7 @@ static int ao2mo_slices(mq_ctx *c, const double *Ci, int no1, const double *Ca, 
   if (no1 > 256 || nv1 > 256 || no2 > 256 || nv2 > 256)
     return set_err(c, MQ_EINVAL, "split transform: orbital blocks above 256 are not supported");
   if (Kp > SLICE_KMAX) return set_err(c, MQ_EINVAL, "split transform: more than 340 basis functions");
+  MQ_TRY(join_side(c));  // a prefetch of the XX slices, before any buffer is touched
   const long long n2 = n * n, n3 = n2 * n;
   // A operand rows per step, and the FP32 intermediates [rows][Kp]
   const long long rX = n3, r1 = (long long)nv2 * n2, r2 = (long long)no2 * nv2 * n, r3 = (long long)nv1 * no2 * nv2;
@@ -487,8 +488,10 @@ static int ao2mo_slices(mq_ctx *c, const double *Ci, int no1, const double *Ca, 
   GemmArgs g{};
   g.err = err;
   // 1: XX(d,l,u,v) at d + n*((l,u,v)): rows (l,u,v), K = d -> Y1[b][(u,v)][l]
+  // (already sliced on the side stream when the SCF prefetched it)
   Sliced A{pa, rX * Kp, ea};
-  MQ_TRY(slice_rows<S>(c, c->d_XX, rX, (int)n, n, Kp, A));
+  if (c->xx_sliced != S) MQ_TRY(slice_rows<S>(c, c->d_XX, rX, (int)n, n, Kp, A));
+  c->xx_sliced = 0;  // step 2 overwrites the slices
   g.out_f64 = 0;
   g.out32 = y1;
   g.mdiv = n;
@@ -532,6 +535,53 @@ static int ao2mo_slices(mq_ctx *c, const double *Ci, int no1, const double *Ca, 
   MQ_CUDA(c, cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   MQ_CUDA(c, cudaStreamSynchronize(c->stream));
   if (h) return set_err(c, MQ_ETIMEOUT, "split GEMM pipeline wait timed out");
+  return MQ_OK;
+}
+
+int join_side(mq_ctx *c) {
+  if (!c->side_pending) return MQ_OK;
+  MQ_CUDA(c, cudaStreamWaitEvent(c->stream, c->ev_side, 0));
+  c->side_pending = 0;
+  return MQ_OK;
+}
+
+// The first step's A operand -- XX cut into S planes, rows (l,u,v), K = d --
+// depends on XX alone, so it can be formed before the orbitals exist: on the
+// side stream (lowest priority) while the main stream finishes the SCF.  The
+// buffers are the ones ao2mo_slices uses, at the sizes it asks for (the
+// largest A operand of the four steps is XX itself: n^3 rows).
+template <int S>
+static int preslice(mq_ctx *c) {
+  const long long n = c->nao;
+  const int Kp = (int)((n + 7) / 8 * 8);
+  if (Kp > SLICE_KMAX || !c->d_XX) return MQ_OK;  // the transform would reject it anyway
+  const long long rX = n * n * n;
+  bf16 *pa = (bf16 *)buf(c, "slice_a", S * rX * Kp * sizeof(bf16));
+  int *ea = (int *)buf(c, "slice_ea", rX * sizeof(int));
+  if (!pa || !ea) return MQ_ENOMEM;
+  if (!c->side) {
+    int lo = 0, hi = 0;
+    MQ_CUDA(c, cudaDeviceGetStreamPriorityRange(&lo, &hi));
+    MQ_CUDA(c, cudaStreamCreateWithPriority(&c->side, cudaStreamNonBlocking, lo));
+    MQ_CUDA(c, cudaEventCreateWithFlags(&c->ev_main, cudaEventDisableTiming));
+    MQ_CUDA(c, cudaEventCreateWithFlags(&c->ev_side, cudaEventDisableTiming));
+  }
+  MQ_CUDA(c, cudaEventRecord(c->ev_main, c->stream));
+  MQ_CUDA(c, cudaStreamWaitEvent(c->side, c->ev_main, 0));
+  cudaStream_t main = c->stream;
+  c->stream = c->side;  // slice_rows launches on c->stream
+  const int rc = slice_rows<S>(c, c->d_XX, rX, (int)n, n, Kp, Sliced{pa, rX * Kp, ea});
+  c->stream = main;
+  MQ_TRY(rc);
+  MQ_CUDA(c, cudaEventRecord(c->ev_side, c->side));
+  c->side_pending = 1;
+  c->xx_sliced = S;
+  return MQ_OK;
+}
+
+int ao2mo_preslice_xx(mq_ctx *c) {
+  if (c->ao2mo_prefetch == 3) return preslice<3>(c);
+  if (c->ao2mo_prefetch == 2) return preslice<2>(c);
   return MQ_OK;
 }
 

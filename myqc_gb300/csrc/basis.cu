@@ -114,6 +114,7 @@ void free_pairs(mq_ctx *c) {
   for (void *p : c->pair_allocs) cudaFree(p);
   c->pair_allocs.clear();
   c->pt = PairTable{};
+  c->schwarz_valid = 0;
 }
 
 // Shell pairs of one molecule, in class order (ss), (sp,s), (sp,sp), with

@@ -515,8 +515,8 @@ int batch_scf(mq_ctx *c, const mq_batch_opts *o, double *energy, int *iters, int
   // ---- one SCF iteration for all active molecules
   PairLaunch L{};
   L.XX = d_XX;
-  L.df32 = c->fock_df32;  // FP64: the densities themselves; double-float: split copies
-  L.DJ = L.df32 ? (const void *)d_DJ : (const void *)dD;
+  L.arith = c->fock_df32 ? FOCK_ARITH_DF32 : FOCK_ARITH_F64;  // FP64: the densities themselves; double-float: split copies
+  L.DJ = L.arith ? (const void *)d_DJ : (const void *)dD;
   L.DKa = L.DJ;
   L.tiles = d_tiles;
   L.row_first = d_rf;
@@ -530,7 +530,7 @@ int batch_scf(mq_ctx *c, const mq_batch_opts *o, double *energy, int *iters, int
   L.Qa = d_Q;
   L.Ka = dK;
   auto iteration = [&]() -> int {
-    if (L.df32) MQ_TRY(split_density(c, dD, nullptr, mat, d_DJ, d_DJ, nullptr, 0));
+    if (L.arith) MQ_TRY(split_density(c, dD, nullptr, mat, d_DJ, d_DJ, nullptr, 0));
     MQ_TRY(pair_digest(c, JC, false, L, dG, nullptr, false));
     batch_energy_kernel<<<M, BT, 0, c->stream>>>(d_md, d_active, dH, dG, dD, d_en, dF, d_Ek);
     const double *Fuse = dF;

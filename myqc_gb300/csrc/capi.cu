@@ -112,7 +112,9 @@ int mq_init(mq_ctx **ctx, int device) {
   mq_ctx *c = new mq_ctx();
   c->device = device;
   if (const char *e = getenv("MYQC_DGEMM")) c->dgemm_cublas = !strcmp(e, "cublas");
-  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+  int prio_lo = 0, prio_hi = 0;  // the main stream outranks the side stream's overlapping work
+  cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
+  if (cudaStreamCreateWithPriority(&c->stream, cudaStreamNonBlocking, prio_hi) != cudaSuccess) {
     delete c;
     return MQ_ECUDA;
   }
@@ -123,6 +125,7 @@ int mq_init(mq_ctx **ctx, int device) {
 int mq_free(mq_ctx *c) {
   if (!c) return MQ_OK;
   cudaSetDevice(c->device);
+  if (c->side) cudaStreamSynchronize(c->side);
   cudaStreamSynchronize(c->stream);
   free_pairs(c);
   batch_clear(c);
@@ -136,6 +139,9 @@ int mq_free(mq_ctx *c) {
   if (c->d_nuc) cudaFree(c->d_nuc);
   if (c->cublas) cublas_destroy(c->cublas);
   cudaStreamDestroy(c->stream);
+  if (c->side) cudaStreamDestroy(c->side);
+  if (c->ev_main) cudaEventDestroy(c->ev_main);
+  if (c->ev_side) cudaEventDestroy(c->ev_side);
   delete c;
   return MQ_OK;
 }
@@ -154,6 +160,8 @@ int mq_set_system(mq_ctx *c, int nnuc, const int *Z, const double *xyz, const do
   if (mode != MQ_MODE_REFERENCE && mode != MQ_MODE_TIGHT) return set_err(c, MQ_EINVAL, "bad mode");
   if (mode == MQ_MODE_REFERENCE && !ftab) return set_err(c, MQ_EINVAL, "reference mode needs the Ftab table");
   cudaSetDevice(c->device);
+  MQ_TRY(join_side(c));  // the side stream may still read the previous system's XX
+  c->xx_sliced = 0;
   c->have_system = 0;
   c->mode = mode;
   MQ_TRY(build_shells(c, nnuc, Z, xyz, bas, set, basinfo, setinfo));
@@ -191,11 +199,12 @@ int mq_set_system(mq_ctx *c, int nnuc, const int *Z, const double *xyz, const do
   MQ_CUDA(c, cudaMemcpy(c->d_nuc, nuc.data(), nuc.size() * sizeof(double), cudaMemcpyHostToDevice));
   // integrals of a previous system are stale
   c->slab_live_valid = 0;
+  c->schwarz_valid = 0;
   if (c->d_XX) cudaFree(c->d_XX);
   c->d_XX = nullptr;
   c->XX_elems = 0;
   c->have_system = 1;
-  if (c->schwarz_thr > 0) MQ_TRY(eri_schwarz(c));
+  if (c->schwarz_thr > 0) MQ_TRY(ensure_schwarz(c));
   return MQ_OK;
 }
 
@@ -209,7 +218,7 @@ int mq_norb(const mq_ctx *c, int *norb) {
 int mq_set_schwarz(mq_ctx *c, double threshold) {
   if (!c || threshold < 0) return MQ_EINVAL;
   c->schwarz_thr = threshold;
-  if (c->have_system && threshold > 0) return eri_schwarz(c);
+  if (c->have_system && threshold > 0) return ensure_schwarz(c);
   return MQ_OK;
 }
 
@@ -262,10 +271,12 @@ int mq_eri_upload(mq_ctx *c, const double *XX) {
   MQ_TRY(need_system(c));
   if (!XX) return set_err(c, MQ_EINVAL, "null input");
   cudaSetDevice(c->device);
+  MQ_TRY(join_side(c));
   MQ_TRY(ensure_xx(c));
   MQ_CUDA(c, cudaMemcpyAsync(c->d_XX, XX, c->XX_elems * sizeof(double), cudaMemcpyHostToDevice, c->stream));
   MQ_CUDA(c, cudaStreamSynchronize(c->stream));
   c->slab_live_valid = 0;  // any slab of the uploaded integrals may be nonzero
+  c->xx_sliced = 0;
   return MQ_OK;
 }
 
@@ -355,6 +366,7 @@ int mq_ao2mo_iajb(mq_ctx *c, const double *Ci, int no1, const double *Ca, int nv
   c->iajb_dims[1] = nv1;
   c->iajb_dims[2] = no2;
   c->iajb_dims[3] = nv2;
+  c->iajb_precision = precision;
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
@@ -509,6 +521,19 @@ int mq_set_fock_precision(mq_ctx *c, int precision) {
   return MQ_OK;
 }
 
+int mq_set_ao2mo_prefetch(mq_ctx *c, int planes) {
+  if (!c) return MQ_EINVAL;
+  if (planes != 0 && planes != 2 && planes != 3) return set_err(c, MQ_EINVAL, "prefetch planes must be 0, 2 or 3");
+  c->ao2mo_prefetch = planes;
+  return MQ_OK;
+}
+
+int mq_set_fock_incremental(mq_ctx *c, double tau) {
+  if (!c || !(tau >= 0.0) || tau > 1e-3) return c ? set_err(c, MQ_EINVAL, "incremental Fock threshold must be in [0, 1e-3]") : MQ_EINVAL;
+  c->fock_inc_tau = tau;
+  return MQ_OK;
+}
+
 int mq_batch_clear(mq_ctx *c) {
   if (!c) return MQ_EINVAL;
   return batch_clear(c);
@@ -614,6 +639,7 @@ int mq_stat(const mq_ctx *c, const char *key, double *value) {
   else if (!strcmp(key, "eig_jacobi")) *value = s.ms_eig_jacobi;
   else if (!strcmp(key, "eig_jacobi_sweeps")) *value = s.eig_jacobi_sweeps;
   else if (!strcmp(key, "fock_precision")) *value = c->fock_df32;
+  else if (!strcmp(key, "fock_inc_builds")) *value = s.fock_inc_builds;
   else if (!strcmp(key, "fock_kernel")) *value = s.ms_fock_kernel;
   else if (!strcmp(key, "fock_kernel_launches")) *value = s.fock_kernel_launches;
   else if (!strcmp(key, "tune_fock_ms")) *value = s.tune_fock_ms;

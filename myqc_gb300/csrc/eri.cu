@@ -709,8 +709,13 @@ int eri_schwarz(mq_ctx *c) {
     h.nq = np;
     MQ_TRY(launch_class<EPI_SCHWARZ>(c, h, cl, cl));
   }
+  c->schwarz_valid = 1;
   return MQ_OK;
 }
+
+// The bounds depend only on the system (geometry, basis, Boys mode): computed
+// once per mq_set_system, on the first call that needs them.
+int ensure_schwarz(mq_ctx *c) { return c->schwarz_valid ? MQ_OK : eri_schwarz(c); }
 
 // largest Schwarz bound (one CTA)
 __global__ void schwarz_max_kernel(const double *__restrict__ sch, int npairs, double *__restrict__ out) {
@@ -750,13 +755,15 @@ __global__ void slab_live_kernel(PairTable t, int n, double thr, const double *_
 
 int eri_full_device(mq_ctx *c, double *d_XX) {
   const size_t n = (size_t)c->nao;
+  MQ_TRY(join_side(c));  // a slicing of the previous XX may still read it
+  c->xx_sliced = 0;
   MQ_CUDA(c, cudaMemsetAsync(d_XX, 0, n * n * n * n * sizeof(double), c->stream));
   EriArgs g = base_args(c);
   g.XX = d_XX;
   g.thr = c->schwarz_thr;
   const bool mixed = c->eri_f32_tau > 0.0 && c->mode == MQ_MODE_TIGHT && c->d_boys_f32;
   if (mixed) g.boys_f = c->d_boys_f32;
-  if (g.thr > 0 || mixed) MQ_TRY(eri_schwarz(c));
+  if (g.thr > 0 || mixed) MQ_TRY(ensure_schwarz(c));
   unsigned long long *cnt = (unsigned long long *)buf(c, "eri_counters", 4 * sizeof(unsigned long long));
   if (!cnt) return MQ_ENOMEM;
   MQ_CUDA(c, cudaMemsetAsync(cnt, 0, 4 * sizeof(unsigned long long), c->stream));

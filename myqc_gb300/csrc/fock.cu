@@ -12,6 +12,7 @@
 // the CTA, and the chunk's partial K column goes to a scratch slice; a second
 // kernel sums the slices in a fixed order.  No atomics, deterministic.
 #include <algorithm>
+#include <type_traits>
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
@@ -34,6 +35,7 @@ struct ArithDF32 {
   typedef float2 Acc;
   __device__ static Acc zero() { return make_float2(0.f, 0.f); }
   __device__ static float2 load(const double *p) { return split_f64(__ldcs(p)); }
+  __device__ static float2 cvt(double x) { return split_f64(x); }
   __device__ static void fma(Acc &s, float2 x, Den d) { dfma(s, x, d); }
   __device__ static double val(Acc s) { return (double)s.x + (double)s.y; }
 };
@@ -42,9 +44,48 @@ struct ArithF64 {
   typedef double Acc;
   __device__ static Acc zero() { return 0.0; }
   __device__ static double load(const double *p) { return __ldcs(p); }
+  __device__ static double cvt(double x) { return x; }
   __device__ static void fma(Acc &s, double x, Den d) { s = ::fma(x, d, s); }
   __device__ static double val(Acc s) { return s; }
 };
+
+// ArithF32: single-precision products and row sums, for the increments
+// G[D_k - D_{k-1}] of an SCF whose density has almost stopped changing (the
+// error scales with the increment).  An integral becomes a float by
+// truncating its significand (integer operations; relative error < 2^-23,
+// values below 2^-126 flush to 0).
+struct ArithF32 {
+  typedef float Den;
+  typedef float Acc;
+  __device__ static Acc zero() { return 0.f; }
+  __device__ static float cvt(double x) {
+    const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+    const unsigned sign = hi & 0x80000000u;
+    const unsigned E = (hi >> 20) & 0x7ffu;
+    const unsigned hb = sign | (((hi & 0x7fffffffu) - 0x38000000u) << 3) | (lo >> 29);
+    return __uint_as_float(E > 896u ? hb : sign);
+  }
+  __device__ static float load(const double *p) { return cvt(__ldcs(p)); }
+  __device__ static void fma(Acc &s, float x, Den d) { s = fmaf(x, d, s); }
+  __device__ static double val(Acc s) { return (double)s; }
+};
+
+// FP32 density increments: DJ = triangle-weighted total (Da + Db) - (Dpa + Dpb),
+// DKa = Da - Dpa, DKb = Db - Dpb (UHF), differences formed in FP64
+__global__ void delta_density_f32_kernel(const double *__restrict__ Da, const double *__restrict__ Db,
+                                         const double *__restrict__ Dpa, const double *__restrict__ Dpb, size_t n2,
+                                         int tri_n, float *__restrict__ DJ, float *__restrict__ DKa,
+                                         float *__restrict__ DKb) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n2) return;
+  const double a = Da[i] - Dpa[i];
+  const double b = Db ? Db[i] - Dpb[i] : 0.0;
+  const size_t k = i % (size_t)tri_n, l = i / (size_t)tri_n;
+  const double wj = l < k ? 2.0 : (l == k ? 1.0 : 0.0);
+  DJ[i] = (float)(wj * (a + b));
+  DKa[i] = (float)a;
+  if (Db) DKb[i] = (float)b;
+}
 
 // FP64 density prepared for J: the lower-triangle weights of the total density
 // (2 D(k,l) for l < k, D(k,k), 0 above) for a system of order tri_n
@@ -172,7 +213,6 @@ __global__ void fock_combine_kernel(const double *__restrict__ J, const double *
 // deterministic, no atomics.  Thread t of T = blockDim.x owns rows k = t + T r,
 // r < R.
 constexpr int PAIR_MAX_THREADS = 256;
-
 // A tile is (i, j0, j1, molecule); the molecule's descriptor gives its order
 // and where its XX, matrices and Q live, so one launch serves one system or a
 // whole batch.  Tiles of molecules whose `active` flag is 0 do nothing.
@@ -227,42 +267,97 @@ __global__ void __launch_bounds__(PAIR_MAX_THREADS) fock_pair_kernel(
     }
   }
   // slabs known to be zero (every quartet screened out) are not read
-  bool lv[JC];
-  bool any = false;
+  // live slabs of the tile as a bit mask (kept in a register)
+  unsigned lvm = 0;
 #pragma unroll
-  for (int jj = 0; jj < JC; ++jj) {
-    lv[jj] = jj < nj && (!live || live[i + N * (j0 + jj)]);
-    any |= lv[jj];
-  }
+  for (int jj = 0; jj < JC; ++jj)
+    if (jj < nj && (!live || live[i + N * (j0 + jj)])) lvm |= 1u << jj;
   const double *S0 = XX + n2 * ((size_t)i + N * j0);
+  // FP64 (the reference's arithmetic, the plain path) and the largest orders
+  // (R = 4) interleave loads and arithmetic; the FP32-pipe arithmetics batch
+  // the loads of several columns (below).
+  constexpr bool BATCH = !std::is_same<P, ArithF64>::value && R <= 2;
+  if constexpr (!BATCH) {
 #pragma unroll 2
-  for (int l = 0; any && l < n; ++l) {
-    const Den di_a = dia[l];
-    const Den di_b = UHF ? dib[l] : dz;
-    Den dj[R];
+    for (int l = 0; lvm && l < n; ++l) {
+      const Den di_a = dia[l];
+      const Den di_b = UHF ? dib[l] : dz;
+      Den dj[R];
 #pragma unroll
-    for (int r = 0; r < R; ++r) {
-      const int k = tid + r * T;
-      dj[r] = k < n ? DJ[k + N * l] : dz;
+      for (int r = 0; r < R; ++r) {
+        const int k = tid + r * T;
+        dj[r] = k < n ? DJ[k + N * l] : dz;
+      }
+#pragma unroll
+      for (int jj = 0; jj < JC; ++jj) {
+        if (lvm >> jj & 1u) {
+          const Den dja_l = dja[jj * n + l];
+          const Den djb_l = UHF ? djb[jj * n + l] : dz;
+          const double *S = S0 + n2 * N * jj + N * l;
+#pragma unroll
+          for (int r = 0; r < R; ++r) {
+            const int k = tid + r * T;
+            if (k < n) {
+              const auto x = P::load(S + k);  // streamed once: keep it out of L2
+              // triangle weights are 0 for l > k: skip once l passes the warp's last row
+              if (!tri || l <= (tid | 31) + r * T) P::fma(aj[jj][r], x, dj[r]);
+              P::fma(aka[r], x, dja_l);
+              P::fma(aqa[jj][r], x, di_a);
+              if (UHF) {
+                P::fma(akb[r], x, djb_l);
+                P::fma(aqb[jj][r], x, di_b);
+              }
+            }
+          }
+        }
+      }
     }
+  } else {
+    // Batched loads: the operands of UB consecutive columns l -- XX(k, l, i, j)
+    // of the tile's live slabs and DJ(k, l) for the thread's rows k -- are all
+    // requested before any is used, so each thread keeps UB (JC + 1) R loads in
+    // flight instead of the few that the interleaved loop above exposes.
+    constexpr int UB = JC * R >= 4 ? 2 : (JC * R >= 2 ? 4 : 8);
+    for (int l0 = 0; lvm && l0 < n; l0 += UB) {
+      double xv[UB][JC][R];
+      Den dv[UB][R];
 #pragma unroll
-    for (int jj = 0; jj < JC; ++jj) {
-      if (lv[jj]) {
-        const Den dja_l = dja[jj * n + l];
-        const Den djb_l = UHF ? djb[jj * n + l] : dz;
-        const double *S = S0 + n2 * N * jj + N * l;
+      for (int u = 0; u < UB; ++u) {
+        const int l = l0 + u;
 #pragma unroll
         for (int r = 0; r < R; ++r) {
           const int k = tid + r * T;
-          if (k < n) {
-            const auto x = P::load(S + k);  // streamed once: keep it out of L2
-            // triangle weights are 0 for l > k: skip once l passes the warp's last row
-            if (!tri || l <= (tid | 31) + r * T) P::fma(aj[jj][r], x, dj[r]);
-            P::fma(aka[r], x, dja_l);
-            P::fma(aqa[jj][r], x, di_a);
-            if (UHF) {
-              P::fma(akb[r], x, djb_l);
-              P::fma(aqb[jj][r], x, di_b);
+          const bool ok = k < n && l < n;
+          dv[u][r] = ok ? DJ[k + N * l] : dz;
+#pragma unroll
+          for (int jj = 0; jj < JC; ++jj)
+            xv[u][jj][r] = ok && (lvm >> jj & 1u) ? __ldcs(S0 + n2 * N * jj + N * l + k) : 0.0;
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < UB; ++u) {
+        const int l = l0 + u;
+        if (l >= n) break;
+        const Den di_a = dia[l];
+        const Den di_b = UHF ? dib[l] : dz;
+#pragma unroll
+        for (int jj = 0; jj < JC; ++jj) {
+          if (lvm >> jj & 1u) {
+            const Den dja_l = dja[jj * n + l];
+            const Den djb_l = UHF ? djb[jj * n + l] : dz;
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+              const int k = tid + r * T;
+              if (k < n) {
+                const auto x = P::cvt(xv[u][jj][r]);
+                if (!tri || l <= (tid | 31) + r * T) P::fma(aj[jj][r], x, dv[u][r]);
+                P::fma(aka[r], x, dja_l);
+                P::fma(aqa[jj][r], x, di_a);
+                if (UHF) {
+                  P::fma(akb[r], x, djb_l);
+                  P::fma(aqb[jj][r], x, di_b);
+                }
+              }
             }
           }
         }
@@ -326,10 +421,11 @@ __global__ void fock_pair_assemble_kernel(const double *__restrict__ Kp, const d
   K[md.mat + idx] = s;
 }
 
-// G = J - f (K + K^T)/2 per molecule (blockIdx.y)
+// G = J - f (K + K^T)/2 per molecule (blockIdx.y), plus Gbase when given
+// (single system: an increment added to the previous G)
 __global__ void fock_pair_combine_kernel(const double *__restrict__ J, const double *__restrict__ K,
                                          const MolDesc *__restrict__ mols, const int *__restrict__ active, double f,
-                                         double *__restrict__ G) {
+                                         const double *__restrict__ Gbase, double *__restrict__ G) {
   const int m = blockIdx.y;
   if (active && !active[m]) return;
   const MolDesc md = mols[m];
@@ -337,11 +433,14 @@ __global__ void fock_pair_combine_kernel(const double *__restrict__ J, const dou
   const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= n2) return;
   const size_t tdx = (idx % N) * N + idx / N;
-  G[md.mat + idx] = J[md.mat + idx] - f * (0.5 * (K[md.mat + idx] + K[md.mat + tdx]));
+  const double g = J[md.mat + idx] - f * (0.5 * (K[md.mat + idx] + K[md.mat + tdx]));
+  G[md.mat + idx] = Gbase ? Gbase[md.mat + idx] + g : g;
 }
 
 template <class P, int R, int JC>
-static int launch_pair(mq_ctx *c, const PairLaunch &L, int threads, size_t smem, bool uhf) {
+static int launch_pair(mq_ctx *c, const PairLaunch &L, int threads, bool uhf) {
+  const size_t smem = sizeof(typename P::Den) * (size_t)(1 + JC) * L.nmax * (uhf ? 2 : 1);  // density columns
+  if (smem > 227u * 1024) return set_err(c, MQ_EINVAL, "Fock digestion: shared memory");
   typedef typename P::Den Den;
   const Den *DJ = (const Den *)L.DJ, *DKa = (const Den *)L.DKa, *DKb = (const Den *)L.DKb;
   if (uhf) {
@@ -359,20 +458,20 @@ static int launch_pair(mq_ctx *c, const PairLaunch &L, int threads, size_t smem,
 }
 
 template <class P, int R>
-static int launch_pair_jc(mq_ctx *c, int jc, const PairLaunch &L, int threads, size_t smem, bool uhf) {
+static int launch_pair_jc(mq_ctx *c, int jc, const PairLaunch &L, int threads, bool uhf) {
   switch (jc) {
-    case 1: return launch_pair<P, R, 1>(c, L, threads, smem, uhf);
-    case 2: return launch_pair<P, R, 2>(c, L, threads, smem, uhf);
-    default: return launch_pair<P, R, 4>(c, L, threads, smem, uhf);
+    case 1: return launch_pair<P, R, 1>(c, L, threads, uhf);
+    case 2: return launch_pair<P, R, 2>(c, L, threads, uhf);
+    default: return launch_pair<P, R, 4>(c, L, threads, uhf);
   }
 }
 
 template <class P>
-static int launch_pair_r(mq_ctx *c, int Rp, int jc, const PairLaunch &L, int threads, size_t smem, bool uhf) {
+static int launch_pair_r(mq_ctx *c, int Rp, int jc, const PairLaunch &L, int threads, bool uhf) {
   switch (Rp) {
-    case 1: return launch_pair_jc<P, 1>(c, jc, L, threads, smem, uhf);
-    case 2: return launch_pair_jc<P, 2>(c, jc, L, threads, smem, uhf);
-    default: return launch_pair_jc<P, 4>(c, jc, L, threads, smem, uhf);
+    case 1: return launch_pair_jc<P, 1>(c, jc, L, threads, uhf);
+    case 2: return launch_pair_jc<P, 2>(c, jc, L, threads, uhf);
+    default: return launch_pair_jc<P, 4>(c, jc, L, threads, uhf);
   }
 }
 
@@ -427,9 +526,10 @@ int pair_digest(mq_ctx *c, int JC, bool uhf, const PairLaunch &L, double *d_Ga, 
   const int T = std::min(PAIR_MAX_THREADS, (n + 31) / 32 * 32);
   const int R0 = (n + T - 1) / T;
   const int Rp = R0 <= 1 ? 1 : R0 <= 2 ? 2 : 4;
-  const size_t smem = 8 * (size_t)n * (1 + JC) * (uhf ? 2 : 1);  // float2 or double density columns
   if (timed) c->t_fock_kernel.start(c->stream);
-  MQ_TRY(L.df32 ? launch_pair_r<ArithDF32>(c, Rp, JC, L, T, smem, uhf) : launch_pair_r<ArithF64>(c, Rp, JC, L, T, smem, uhf));
+  if (L.arith == FOCK_ARITH_DF32) MQ_TRY(launch_pair_r<ArithDF32>(c, Rp, JC, L, T, uhf));
+  else if (L.arith == FOCK_ARITH_F32) MQ_TRY(launch_pair_r<ArithF32>(c, Rp, JC, L, T, uhf));
+  else MQ_TRY(launch_pair_r<ArithF64>(c, Rp, JC, L, T, uhf));
   if (timed) {
     c->t_fock_kernel.stop(c->stream);
     c->stats.fock_kernel_launches += 1;
@@ -440,16 +540,19 @@ int pair_digest(mq_ctx *c, int JC, bool uhf, const PairLaunch &L, double *d_Ga, 
   fock_pair_assemble_kernel<<<gb, tb, 0, c->stream>>>(L.Kpa, L.Qa, L.row_first, L.mols, L.active, L.nmax, L.Ka);
   if (uhf)
     fock_pair_assemble_kernel<<<gb, tb, 0, c->stream>>>(L.Kpb, L.Qb, L.row_first, L.mols, L.active, L.nmax, L.Kb);
-  fock_pair_combine_kernel<<<gb, tb, 0, c->stream>>>(L.J, L.Ka, L.mols, L.active, uhf ? 1.0 : 0.5, d_Ga);
-  if (uhf) fock_pair_combine_kernel<<<gb, tb, 0, c->stream>>>(L.J, L.Kb, L.mols, L.active, 1.0, d_Gb);
+  const size_t n2 = (size_t)n * n;
+  fock_pair_combine_kernel<<<gb, tb, 0, c->stream>>>(L.J, L.Ka, L.mols, L.active, uhf ? 1.0 : 0.5, L.Gbase, d_Ga);
+  if (uhf)
+    fock_pair_combine_kernel<<<gb, tb, 0, c->stream>>>(L.J, L.Kb, L.mols, L.active, 1.0,
+                                                       L.Gbase ? L.Gbase + n2 : nullptr, d_Gb);
   c->stats.launches += uhf ? 5 : 3;
   MQ_CUDA(c, cudaGetLastError());
   return MQ_OK;
 }
 
 // Scratch of the single system: J | K slices | Q | K.
-static int pair_build(mq_ctx *c, int JC, bool uhf, const void *DJ, const void *DKa, const void *DKb,
-                      double *d_Ga, double *d_Gb, bool timed = false) {
+static int pair_build(mq_ctx *c, int arith, int JC, bool uhf, const void *DJ, const void *DKa, const void *DKb,
+                      double *d_Ga, double *d_Gb, bool timed = false, const double *Gbase = nullptr) {
   const int n = c->nao;
   const size_t N = n, n2 = N * N;
   PairLaunch L{};
@@ -461,7 +564,8 @@ static int pair_build(mq_ctx *c, int JC, bool uhf, const void *DJ, const void *D
   L.XX = c->d_XX;
   L.tri = 1;
   L.live = c->slab_live_valid ? c->d_slab_live : nullptr;
-  L.df32 = c->fock_df32;
+  L.arith = arith;
+  L.Gbase = Gbase;
   L.DJ = DJ;
   L.DKa = DKa;
   L.DKb = DKb;
@@ -481,11 +585,11 @@ static int pair_build(mq_ctx *c, int JC, bool uhf, const void *DJ, const void *D
 // candidate computes the same G (the tile length only changes the summation
 // grouping, ~1e-13 relative), and the call's result comes from the chosen one.
 // MYQC_FOCK_JC=1|2|4 in the environment pins the choice instead.
-static int pair_choose_jc(mq_ctx *c, bool uhf, const void *DJ, const void *DKa, const void *DKb, double *d_Ga,
-                          double *d_Gb) {
+static int pair_choose_jc(mq_ctx *c, int arith, bool uhf, const void *DJ, const void *DKa, const void *DKb,
+                          double *d_Ga, double *d_Gb) {
   const int n = c->nao;
-  int &slot = c->fock_jc[uhf ? 1 : 0][c->fock_df32 ? 1 : 0];
-  int &slot_n = c->fock_jc_n[uhf ? 1 : 0][c->fock_df32 ? 1 : 0];
+  int &slot = c->fock_jc[uhf ? 1 : 0][arith];
+  int &slot_n = c->fock_jc_n[uhf ? 1 : 0][arith];
   if (slot_n == n && slot > 0) return slot;
   if (const char *e = getenv("MYQC_FOCK_JC")) {
     const int v = atoi(e);
@@ -500,10 +604,10 @@ static int pair_choose_jc(mq_ctx *c, bool uhf, const void *DJ, const void *DKa, 
   float best = 1e30f;
   int best_jc = 2;
   for (int jc : cand) {
-    if (pair_build(c, jc, uhf, DJ, DKa, DKb, d_Ga, d_Gb) != MQ_OK) continue;  // warm-up, tile table
+    if (pair_build(c, arith, jc, uhf, DJ, DKa, DKb, d_Ga, d_Gb) != MQ_OK) continue;  // warm-up, tile table
     cudaEventRecord(a, c->stream);
     bool ok = true;
-    for (int r = 0; r < 2 && ok; ++r) ok = pair_build(c, jc, uhf, DJ, DKa, DKb, d_Ga, d_Gb) == MQ_OK;
+    for (int r = 0; r < 2 && ok; ++r) ok = pair_build(c, arith, jc, uhf, DJ, DKa, DKb, d_Ga, d_Gb) == MQ_OK;
     cudaEventRecord(b, c->stream);
     cudaEventSynchronize(b);
     float ms = 0.f;
@@ -555,10 +659,36 @@ int fock_stored_device(mq_ctx *c, const double *d_Da, const double *d_Db, double
   const bool uhf = d_Db != nullptr;
   const void *DJ, *DKa, *DKb;
   MQ_TRY(fock_densities(c, n, d_Da, d_Db, &DJ, &DKa, &DKb));
-  const int JC = pair_choose_jc(c, uhf, DJ, DKa, DKb, d_Ga, d_Gb);
+  const int arith = c->fock_df32 ? FOCK_ARITH_DF32 : FOCK_ARITH_F64;
+  const int JC = pair_choose_jc(c, arith, uhf, DJ, DKa, DKb, d_Ga, d_Gb);
   c->stats.fock_jc = JC;
   c->t_fock_kernel.collect();  // a previous build's timing not yet collected by its caller
-  return pair_build(c, JC, uhf, DJ, DKa, DKb, d_Ga, d_Gb, true);
+  return pair_build(c, arith, JC, uhf, DJ, DKa, DKb, d_Ga, d_Gb, true);
+}
+
+// G = Gprev + G[D - Dprev], the increment digested in FP32 (J and K linear in
+// D).  On the first call for an order n the autotuner's candidate builds write
+// the bare increment to G before the final build overwrites it, so G must not
+// alias Gprev.
+int fock_stored_increment(mq_ctx *c, const double *d_Da, const double *d_Db, const double *d_Dpa,
+                          const double *d_Dpb, const double *d_Gpa, const double *d_Gpb, double *d_Ga, double *d_Gb) {
+  const int n = c->nao;
+  if (!c->d_XX) return set_err(c, MQ_ESTATE, "no integrals on the device (call mq_eri_store or mq_eri_upload)");
+  if (n > 4 * PAIR_MAX_THREADS) return set_err(c, MQ_EINVAL, "stored Fock build supports n <= 1024");
+  const bool uhf = d_Db != nullptr;
+  if (uhf && d_Gpb != d_Gpa + (size_t)n * n) return set_err(c, MQ_EINVAL, "increment: beta G must follow alpha G");
+  if (d_Ga == d_Gpa) return set_err(c, MQ_EINVAL, "increment: G must not alias the previous G");
+  const size_t n2 = (size_t)n * n;
+  float *d = (float *)buf(c, "fock_dinc", sizeof(float) * n2 * (uhf ? 3 : 2));
+  if (!d) return MQ_ENOMEM;
+  delta_density_f32_kernel<<<(unsigned)((n2 + 255) / 256), 256, 0, c->stream>>>(
+      d_Da, d_Db, d_Dpa, d_Dpb, n2, n, d, d + n2, uhf ? d + 2 * n2 : nullptr);
+  c->stats.launches += 1;
+  MQ_CUDA(c, cudaGetLastError());
+  const void *DJ = d, *DKa = d + n2, *DKb = uhf ? d + 2 * n2 : nullptr;
+  const int JC = pair_choose_jc(c, FOCK_ARITH_F32, uhf, DJ, DKa, DKb, d_Ga, d_Gb);
+  c->t_fock_kernel.collect();
+  return pair_build(c, FOCK_ARITH_F32, JC, uhf, DJ, DKa, DKb, d_Ga, d_Gb, true, d_Gpa);
 }
 
 // ---------------------------------------------------------------------------

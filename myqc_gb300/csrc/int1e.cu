@@ -43,11 +43,18 @@ __device__ __forceinline__ void axis_E(double PA, double PB, double i2p, double 
       }
 }
 
+// One warp per contracted shell pair: the 32 lanes split the nuclei of the
+// attraction integrals (nucleus cn on lane cn mod 32) and every lane contracts
+// its partial V with the Hermite coefficients; lane 0 adds the overlap and
+// kinetic terms, and a shuffle tree sums the lanes (fixed order).
+constexpr int INT1E_WARPS = 4;
+
 template <int LA, int LB>
-__global__ void __launch_bounds__(128) int1e_kernel(Int1eArgs g) {
+__global__ void __launch_bounds__(32 * INT1E_WARPS) int1e_kernel(Int1eArgs g) {
   constexpr int NA = LA ? 4 : 1, NB = LB ? 4 : 1, L = LA + LB, QREF = 3 * L;
-  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= g.np) return;
+  const int idx = blockIdx.x * INT1E_WARPS + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (idx >= g.np) return;  // warp-uniform
   const int P = g.pOff + idx;
   const PairTable &t = g.t;
   const double *nuc = g.nuc;
@@ -89,7 +96,7 @@ __global__ void __launch_bounds__(128) int1e_kernel(Int1eArgs g) {
       for (int y = 0; y <= L; ++y)
 #pragma unroll
         for (int z = 0; z <= L; ++z) V[x][y][z] = 0.0;
-    for (int cn = 0; cn < nnuc; ++cn) {
+    for (int cn = lane; cn < nnuc; cn += 32) {
       const double X = Px - nuc[4 * cn], Y = Py - nuc[4 * cn + 1], Z = Pz - nuc[4 * cn + 2];
       const double T = p * (X * X + Y * Y + Z * Z);
       double F[L + 1];
@@ -140,7 +147,8 @@ __global__ void __launch_bounds__(128) int1e_kernel(Int1eArgs g) {
         const int ax = a == 1, ay = a == 2, az = a == 3, bx = b == 1, by = b == 2, bz = b == 3;
         const double cf = c[2 * (a > 0) + (b > 0)];
         const double sx = Ex[ax][bx][0], sy = Ey[ay][by][0], sz = Ez[az][bz][0];
-        s[a][b] += cf * pp32 * sx * sy * sz;
+        const double own = lane == 0 ? 1.0 : 0.0;  // overlap and kinetic terms: lane 0 only
+        s[a][b] += own * cf * pp32 * sx * sy * sz;
         // kinetic: -1/2 sum_axis [nb(nb-1) E(na,nb-2) - 2b(2nb+1) E(na,nb) + 4b^2 E(na,nb+2)] * others
         auto kin = [&](const double (&E)[2][4][5], int na, int nb) {
           double v = -2.0 * bb * (2 * nb + 1) * E[na][nb][0] + 4.0 * bb * bb * E[na][nb + 2][0];
@@ -155,9 +163,19 @@ __global__ void __launch_bounds__(128) int1e_kernel(Int1eArgs g) {
           for (int y = 0; y <= ay + by; ++y)
 #pragma unroll
             for (int z = 0; z <= az + bz; ++z) v += Ex[ax][bx][x] * Ey[ay][by][y] * Ez[az][bz][z] * V[x][y][z];
-        h[a][b] += cf * (-0.5 * pp32 * tk + v);
+        h[a][b] += cf * (-0.5 * own * pp32 * tk + v);
       }
   }
+#pragma unroll
+  for (int a = 0; a < NA; ++a)
+#pragma unroll
+    for (int b = 0; b < NB; ++b)
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        s[a][b] += __shfl_xor_sync(0xffffffffu, s[a][b], o);
+        h[a][b] += __shfl_xor_sync(0xffffffffu, h[a][b], o);
+      }
+  if (lane != 0) return;
   const int A = t.shA[P], B = t.shB[P], i0 = t.aoA[P], j0 = t.aoB[P];
 #pragma unroll
   for (int a = 0; a < NA; ++a)
@@ -190,10 +208,10 @@ int int1e_batch_device(mq_ctx *c, const PairTable &t, const double *d_nuc, const
     g.pOff = t.class_off[cl];
     g.np = t.class_off[cl + 1] - g.pOff;
     if (!g.np) continue;
-    dim3 grid((g.np + 127) / 128);
-    if (cl == 0) int1e_kernel<0, 0><<<grid, 128, 0, c->stream>>>(g);
-    else if (cl == 1) int1e_kernel<1, 0><<<grid, 128, 0, c->stream>>>(g);
-    else int1e_kernel<1, 1><<<grid, 128, 0, c->stream>>>(g);
+    dim3 grid((g.np + INT1E_WARPS - 1) / INT1E_WARPS);
+    if (cl == 0) int1e_kernel<0, 0><<<grid, 32 * INT1E_WARPS, 0, c->stream>>>(g);
+    else if (cl == 1) int1e_kernel<1, 0><<<grid, 32 * INT1E_WARPS, 0, c->stream>>>(g);
+    else int1e_kernel<1, 1><<<grid, 32 * INT1E_WARPS, 0, c->stream>>>(g);
     c->stats.launches += 1;
     MQ_CUDA(c, cudaGetLastError());
   }
@@ -217,10 +235,10 @@ int int1e_device(mq_ctx *c, double *d_S, double *d_H) {
     g.pOff = c->pt.class_off[cl];
     g.np = c->pt.class_off[cl + 1] - g.pOff;
     if (!g.np) continue;
-    dim3 grid((g.np + 127) / 128);
-    if (cl == 0) int1e_kernel<0, 0><<<grid, 128, 0, c->stream>>>(g);
-    else if (cl == 1) int1e_kernel<1, 0><<<grid, 128, 0, c->stream>>>(g);
-    else int1e_kernel<1, 1><<<grid, 128, 0, c->stream>>>(g);
+    dim3 grid((g.np + INT1E_WARPS - 1) / INT1E_WARPS);
+    if (cl == 0) int1e_kernel<0, 0><<<grid, 32 * INT1E_WARPS, 0, c->stream>>>(g);
+    else if (cl == 1) int1e_kernel<1, 0><<<grid, 32 * INT1E_WARPS, 0, c->stream>>>(g);
+    else int1e_kernel<1, 1><<<grid, 32 * INT1E_WARPS, 0, c->stream>>>(g);
     c->stats.launches += 1;
     MQ_CUDA(c, cudaGetLastError());
   }

@@ -102,6 +102,7 @@ struct Stats {
   // phases' times, FP64 Jacobi sweeps
   double eig_f32_sweeps = 0, eig_f32_off = 0, ms_eig_f32 = 0, ms_eig_refine = 0, ms_eig_jacobi = 0;
   double eig_jacobi_sweeps = 0;
+  double fock_inc_builds = 0;  // FP32 incremental builds of the last SCF
 };
 
 // Event pair on the context's stream that adds its elapsed time to a counter
@@ -142,7 +143,16 @@ struct StageTimer {
 
 struct mq_ctx {
   int device = 0;
-  cudaStream_t stream = nullptr;
+  cudaStream_t stream = nullptr;  // the context's stream (highest priority)
+  // side stream (lowest priority) for work that overlaps the main stream: the
+  // slicing of XX for the split transform during the SCF's final eigensolve
+  // (mq_set_ao2mo_prefetch).  ev_side marks the end of the last side work;
+  // anything that rewrites XX or the slice buffers waits for it (join_side).
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_main = nullptr, ev_side = nullptr;
+  int side_pending = 0;
+  int ao2mo_prefetch = 0;  // planes (2, 3) to slice XX into ahead of the transform; 0: off
+  int xx_sliced = 0;       // the slice buffers hold XX cut into this many planes (0: not)
   void *cublas = nullptr;
   int dgemm_cublas = 0;  // MYQC_DGEMM=cublas: every FP64 product through cuBLAS (comparison runs)
   std::string err;
@@ -176,15 +186,20 @@ struct mq_ctx {
   // integrals of the last mq_eri_store with a threshold; null otherwise.
   unsigned char *d_slab_live = nullptr;
   int slab_live_valid = 0;
+  int schwarz_valid = 0;  // pt.schwarz holds the bounds of the current system
   unsigned long long *d_slab_live_count = nullptr;  // live slabs (i, j), both orders counted
   unsigned long long *d_eri_counters = nullptr;  // its quartet counters (device)  // the digestion kernel alone, collected at the caller's sync points
   mq::FockTiles fock_tiles[9];  // pair-slab tile tables, indexed by slabs per tile
-  int fock_jc[2][2] = {{0, 0}, {0, 0}}, fock_jc_n[2][2] = {{0, 0}, {0, 0}};  // autotuned tile length [uhf][df32]
+  int fock_jc[2][3] = {{0, 0, 0}, {0, 0, 0}}, fock_jc_n[2][3] = {{0, 0, 0}, {0, 0, 0}};  // tile length [uhf][arith]
   int fock_df32 = 0;  // digestion arithmetic: 0 FP64, 1 double-float (mq_set_fock_precision)
+  // mq_scf with stored integrals: once max|D_k - D_{k-1}| < fock_inc_tau, G_k =
+  // G_{k-1} + G[D_k - D_{k-1}] digested in FP32 (0: every build full; mq_set_fock_incremental)
+  double fock_inc_tau = 0.0;
   size_t XX_elems = 0;
   double *d_iajb = nullptr;  // last (ia|jb) block
   size_t iajb_elems = 0;
   int iajb_dims[4] = {0, 0, 0, 0};
+  int iajb_precision = 0;  // MQ_PREC_* of the transform that produced d_iajb
   // named device work buffers: each grows on demand and is reused across calls
   std::map<std::string, mq::DeviceBuf> bufs;
   mq::Stats stats;
@@ -220,13 +235,19 @@ struct PairLaunch {
   int ntiles, nmol, nmax;
   int tri;   // DJ carries lower-triangle weights: J sums over l <= k only
   const unsigned char *live;  // slab (i,j) may be nonzero (n x n, single system); null: every slab
-  int df32;  // densities are float pairs and the digestion double-float (else FP64 arrays)
+  int arith;  // FOCK_ARITH_*: FP64 arrays, float pairs (double-float), or floats (FP32 increments)
+  const double *Gbase;  // single system: G = Gbase + J - f K (null: G = J - f K)
   double *J, *Kpa, *Kpb, *Qa, *Qb, *Ka, *Kb;
 };
 // density operands of the digestion in the context's arithmetic (fock.cu)
 int fock_densities(mq_ctx *c, int n, const double *d_Da, const double *d_Db, const void **DJ, const void **DKa,
                    const void **DKb);
+enum { FOCK_ARITH_F64 = 0, FOCK_ARITH_DF32 = 1, FOCK_ARITH_F32 = 2 };
 int pair_digest(mq_ctx *c, int JC, bool uhf, const PairLaunch &L, double *d_Ga, double *d_Gb, bool timed);
+// G = Gprev + G[D - Dprev] for the stored integrals, digested in FP32 (the
+// incremental builds of mq_scf); RHF when the beta arguments are null
+int fock_stored_increment(mq_ctx *c, const double *d_Da, const double *d_Db, const double *d_Dpa,
+                          const double *d_Dpb, const double *d_Gpa, const double *d_Gpb, double *d_Ga, double *d_Gb);
 // densities as hi/lo float pairs: DJ from Da (+ Db), DKa from Da, DKb from Db;
 // tri_n > 0: DJ with lower-triangle weights for a system of order tri_n
 int split_density(mq_ctx *c, const double *Da, const double *Db, size_t n2, float2 *DJ, float2 *DKa, float2 *DKb,
@@ -261,6 +282,7 @@ void tight_boys_table(std::vector<double> &tab);  // TIGHT_NT x TIGHT_NM, row-ma
 // eri.cu
 int eri_full_device(mq_ctx *c, double *d_XX);
 int eri_schwarz(mq_ctx *c);
+int ensure_schwarz(mq_ctx *c);  // eri_schwarz unless the current system's bounds are there
 int fock_direct_device(mq_ctx *c, const double *d_Da, const double *d_Db, double *d_J, double *d_Ka, double *d_Kb);
 // G = sym(J) - f sym(K) from the direct kernel's half-sums (f = 1/2 RHF, 1 UHF)
 int direct_combine(mq_ctx *c, const double *J, const double *Ka, const double *Kb, double *Ga, double *Gb);
@@ -312,6 +334,11 @@ int mp2_pair_sums(mq_ctx *c, const double *d_Om, int no1, int nv1, int no2, int 
 // ao2mo_split.cu: split-BF16 tensor-core transform (tcgen05) with 2 or 3 operand planes
 int ao2mo_split_device(mq_ctx *c, const double *d_Ci, int no1, const double *d_Ca, int nv1, const double *d_Cj,
                        int no2, const double *d_Cb, int nv2, double *d_out, int planes);
+// XX cut into c->ao2mo_prefetch planes on the side stream, after the work queued
+// so far on the main stream; the next split transform of the same XX uses it
+int ao2mo_preslice_xx(mq_ctx *c);
+// the main stream waits for the side stream's last work (no-op when none is pending)
+int join_side(mq_ctx *c);
 
 // scf.cu
 int scf_device(mq_ctx *c, const double *S, const double *H, const mq_scf_opts *o, double *C, double *eps, double *D,

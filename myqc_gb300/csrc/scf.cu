@@ -227,7 +227,7 @@ int scf_device(mq_ctx *c, const double *S, const double *H, const mq_scf_opts *o
   if (!o->direct && !c->d_XX) return set_err(c, MQ_ESTATE, "no stored integrals for a conventional SCF");
 
   // device workspace
-  const size_t nmat = 8 + 6 * ns + (size_t)2 * ndiis * ns;
+  const size_t nmat = 8 + 8 * ns + (size_t)2 * ndiis * ns;
   double *w = (double *)buf(c, "scf_work", sizeof(double) * (n2 * nmat + 256 + n * ns + 16 * RED_BLOCKS));
   if (!w) return MQ_ENOMEM;
   double *dS = w, *dH = dS + n2, *dX = dH + n2, *dT1 = dX + n2, *dT2 = dT1 + n2, *dT3 = dT2 + n2;
@@ -240,7 +240,9 @@ int scf_device(mq_ctx *c, const double *S, const double *H, const mq_scf_opts *o
   double *dFp = dC + n2 * ns;      // ns (orthogonal-basis Fock / eigvec scratch)
   double *dFh = dFp + n2 * ns;     // DIIS Fock history ns * ndiis
   double *dEh = dFh + n2 * ns * ndiis;  // DIIS error history
-  double *dScal = dEh + n2 * ns * ndiis;  // 256 scalars
+  double *dGp = dEh + n2 * ns * ndiis;  // ns: G of the previous build (incremental builds)
+  double *dDp = dGp + n2 * ns;          // ns: the density it was built from
+  double *dScal = dDp + n2 * ns;        // 256 scalars
   double *dEps = dScal + 256;           // n * ns
   double *dRed = dEps + n * ns;         // reduction partials, 16 per CTA
   MQ_CUDA(c, cudaMemcpyAsync(dS, S, n2 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
@@ -366,6 +368,14 @@ int scf_device(mq_ctx *c, const double *S, const double *H, const mq_scf_opts *o
   int it = 0;
   std::vector<double> hist;
   const double *lastF = nullptr;
+  // incremental builds: once the density moves by less than fock_inc_tau
+  // (max |D_k - D_{k-1}|), G_k = G_{k-1} + G[D_k - D_{k-1}] with the increment
+  // digested in FP32; its error scales with the increment, so the converged
+  // energy stays within ~1e-9 Eh of the full builds'
+  const bool inc = !o->direct && c->fock_inc_tau > 0.0;
+  bool have_prev_g = false;
+  double last_maxdiff = INFINITY;
+  c->stats.fock_inc_builds = 0;
   for (; it < max_iter && !conv; ++it) {
     // G[D_k]
     t_fock.start(c->stream);
@@ -373,8 +383,17 @@ int scf_device(mq_ctx *c, const double *S, const double *H, const mq_scf_opts *o
       double *J = dT1, *Ka = dT2, *Kb = uhf ? dT3 : nullptr;
       MQ_TRY(fock_direct_device(c, dD, uhf ? dD + n2 : nullptr, J, Ka, Kb));
       MQ_TRY(direct_combine(c, J, Ka, Kb, dG, uhf ? dG + n2 : nullptr));
+    } else if (inc && have_prev_g && last_maxdiff < c->fock_inc_tau) {
+      MQ_TRY(fock_stored_increment(c, dD, uhf ? dD + n2 : nullptr, dDp, uhf ? dDp + n2 : nullptr, dGp,
+                                   uhf ? dGp + n2 : nullptr, dG, uhf ? dG + n2 : nullptr));
+      c->stats.fock_inc_builds += 1;
     } else {
       MQ_TRY(fock_stored_device(c, dD, uhf ? dD + n2 : nullptr, dG, uhf ? dG + n2 : nullptr));
+    }
+    if (inc) {
+      MQ_CUDA(c, cudaMemcpyAsync(dGp, dG, n2 * ns * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+      MQ_CUDA(c, cudaMemcpyAsync(dDp, dD, n2 * ns * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+      have_prev_g = true;
     }
     t_fock.stop(c->stream);
     for (int s = 0; s < ns; ++s) add_kernel<<<blocks(n2), 256, 0, c->stream>>>(dH, dG + n2 * s, dF + n2 * s, n2);
@@ -437,6 +456,7 @@ int scf_device(mq_ctx *c, const double *S, const double *H, const mq_scf_opts *o
     c->t_fock_kernel.collect();
     E = hs[0] + (uhf ? hs[2] : 0.0) + enuc;
     const double diff = o->conv_rms ? hs[9] : hs[8];
+    last_maxdiff = hs[8];  // max |D_{k+1} - D_k|: the next build's increment
     hist.push_back(E);
     hist.push_back(it > 0 ? diff : NAN);
     if (it > 0) conv = diff < thr;
@@ -448,6 +468,8 @@ int scf_device(mq_ctx *c, const double *S, const double *H, const mq_scf_opts *o
   // outputs: orbitals and eigenvalues of the last diagonalisation, D_k of the last iteration
   c->stats.ms_eig_final = 0;
   if (purify && lastF) {  // one eigensolve of the last iteration's Fock matrices for C and eps
+    // the transform's XX slices need no orbitals: form them beside the eigensolve
+    if (c->ao2mo_prefetch && !o->direct) MQ_TRY(ao2mo_preslice_xx(c));
     StageTimer t_eig;
     t_eig.start(c->stream);
     have_prev = false;

@@ -176,6 +176,14 @@ class Context:
         """_lib.FOCK_FP64 (default) or _lib.FOCK_DF32 (double-float digestion)."""
         self._check(self.L.mq_set_fock_precision(self.h, precision))
 
+    def set_fock_incremental(self, tau: float):
+        """FP32 incremental Fock builds in scf() once max|D_k - D_(k-1)| < tau (0: off)."""
+        self._check(self.L.mq_set_fock_incremental(self.h, float(tau)))
+
+    def set_ao2mo_prefetch(self, planes: int):
+        """Slice XX for the split transform (2 or 3 planes) during the purified SCF's final eigensolve (0: off)."""
+        self._check(self.L.mq_set_ao2mo_prefetch(self.h, int(planes)))
+
     def set_schwarz(self, thr: float):
         self._check(self.L.mq_set_schwarz(self.h, thr))
 

@@ -308,3 +308,33 @@ def test_schwarz_screened_integrals(ctx, basis_text):
     assert np.max(np.abs(XX[~kept])) < 1e-11
     assert nq > 0
     assert np.max(np.abs(Gd - G)) < 1e-9 * np.max(np.abs(G))
+
+
+@pytest.mark.parametrize("uhf", [False, True])
+def test_incremental_fock_builds(ctx, basis_text, uhf):
+    """FP32 incremental Fock builds (mq_set_fock_incremental) once the density
+    moves by less than 1e-6: same converged energy as full FP64 builds within
+    1e-9 Eh, same iteration count within 1, and some builds were incremental.
+    RHF on (H2O)8 (n = 56), UHF on its cation."""
+    from myqc_gb300 import FOCK_DF32, FOCK_FP64, MODE_TIGHT, molecules
+    sysm = molecules.water_cluster_system(8, 8.0, 11)
+    basis = formats.parse_mybasis_text(basis_text, sysm.atoms)
+    ctx.set_schwarz(0.0)
+    ctx.set_system(sysm, basis, None, MODE_TIGHT)
+    S, H = ctx.int1e()
+    ctx.eri_store()
+    na, nb = (sysm.nelcA, sysm.nelcB) if not uhf else (sysm.nelcA, sysm.nelcB - 1)
+    kw = dict(uhf=uhf, conv=1e-10, conv_rms=True, diis=8, max_iter=200)
+    ctx.set_fock_precision(FOCK_FP64)
+    ref = ctx.scf(S, H, na, nb, **kw)
+    try:
+        for prec in (FOCK_FP64, FOCK_DF32):
+            ctx.set_fock_precision(prec)
+            ctx.set_fock_incremental(1e-6)
+            r = ctx.scf(S, H, na, nb, **kw)
+            assert ctx.stat("fock_inc_builds") >= 2
+            assert abs(r.energy - ref.energy) < 1e-9, (prec, r.energy - ref.energy)
+            assert abs(r.iterations - ref.iterations) <= 1, (r.iterations, ref.iterations)
+    finally:
+        ctx.set_fock_incremental(0.0)
+        ctx.set_fock_precision(FOCK_FP64)

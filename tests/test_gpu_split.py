@@ -64,3 +64,31 @@ def test_split_rectangular_blocks(ctx, basis_text):
     for prec, tol, _ in MODES:
         got = ctx.ao2mo_iajb(Ci, Ca, Cj, Cb, prec)
         assert np.max(np.abs(got - ref)) < tol * np.max(np.abs(ref))
+
+
+def test_prefetched_slices_identical(ctx, basis_text):
+    """XX sliced on the side stream during the purified SCF's final eigensolve
+    (mq_set_ao2mo_prefetch) gives the same (ia|jb) and E(MBPT2), bit for bit,
+    as slicing it inside the transform; a second solve of another system with
+    the prefetch on still matches (the slices follow XX)."""
+    from myqc_gb300 import FOCK_FP64
+    for k, seed in ((4, 3), (6, 4)):
+        sysm = molecules.water_cluster_system(k, (27.0 * k) ** (1 / 3) + 1.0, seed)
+        basis = formats.parse_mybasis_text(basis_text, sysm.atoms)
+        ctx.set_fock_precision(FOCK_FP64)
+        ctx.set_system(sysm, basis, None, MODE_TIGHT)
+        S, H = ctx.int1e()
+        kw = dict(conv=1e-10, conv_rms=True, diis=8, purify=True)
+        ctx.eri_store()
+        ctx.set_ao2mo_prefetch(0)
+        r0 = ctx.scf(S, H, sysm.nelcA, sysm.nelcB, **kw)
+        e0 = ctx.mp2_rhf(r0.eig, sysm.nelcA, PREC_SPLIT_BF16X3, C=r0.C)
+        try:
+            ctx.set_ao2mo_prefetch(3)
+            r1 = ctx.scf(S, H, sysm.nelcA, sysm.nelcB, **kw)
+            e1 = ctx.mp2_rhf(r1.eig, sysm.nelcA, PREC_SPLIT_BF16X3, C=r1.C)
+        finally:
+            ctx.set_ao2mo_prefetch(0)
+        assert r1.energy == r0.energy
+        assert np.array_equal(r1.C, r0.C)
+        assert e1["E_MP2"] == e0["E_MP2"], (k, e1, e0)
