@@ -184,7 +184,7 @@ def run_ours(args):
 
     # ---- fast path, device-resident system (value)
     L0 = stat(ctx, "launches")
-    t_fock = t_eri = t_diag = t_ao2mo = t_fock_kernel = 0.0
+    t_fock = t_eri = t_diag = t_ao2mo = t_fock_kernel = t_mp2 = 0.0
     nq = nq32 = 0.0
     nfock = n_fock_kernel = n_inc = 0
     iters = []
@@ -207,6 +207,7 @@ def run_ours(args):
             live = stat(ctx, "live_slabs")
             t_diag += stat(ctx, "diag")
             t_ao2mo += stat(ctx, "ao2mo")
+            t_mp2 += stat(ctx, "mp2")
             iters.append(res.iterations)
         ev1.record()
         torch.cuda.nvtx.range_pop()
@@ -262,6 +263,8 @@ def run_ours(args):
         traffic = tr["traffic_over_algorithmic"] * alg_bytes
     except Exception:
         pass
+    rooflines = piece_rooflines(n, sysm.nelcA, t_eri / args.steps, nq / args.steps, t_ao2mo / args.steps,
+                                t_mp2 / args.steps, peaks)
     vals = [ms_value, ms_e2e]
     if world > 1:
         import torch.distributed as dist
@@ -298,9 +301,11 @@ def run_ours(args):
                      "live_slab_fraction": live,
                      "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
                      "traffic": traffic, "peak_source": "measured" if peaks else "fallback"},
+        "rooflines": rooflines,
         "clocks": clk.summary(),
         "breakdown_ms_per_solve": {"eri": t_eri / args.steps, "scf_fock": t_fock / args.steps,
-                                   "scf_diag": t_diag / args.steps, "ao2mo": t_ao2mo / args.steps},
+                                   "scf_diag": t_diag / args.steps, "ao2mo": t_ao2mo / args.steps,
+                                   "mp2_pair_sums": t_mp2 / args.steps},
         "scf_iterations": {"fast": float(np.mean(iters)), "plain": res_p.iterations,
                            "fast_used_learned_guess": bool(getattr(res, "learned_guess", False))},
         "plain_fp64": {"ms_per_solve": ms_plain, "solves_per_s": 1000.0 / ms_plain,
@@ -322,6 +327,36 @@ def run_ours(args):
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+
+
+def piece_rooflines(n, o, ms_eri, quartets, ms_ao2mo, ms_mp2, peaks):
+    """Each piece of the solve against the roofline that bounds it.
+    ERI: quartets/s, with the FP64 / FP32 pipe utilisation of the integral
+    kernels from an ncu capture (profiles/eri_pipes.json, measured on a smaller
+    cluster).  ao2mo: algorithmic FLOP 2(o n^4 + o v n^3 + o^2 v n^2 + o^2 v^2 n)
+    per second against the BF16 tensor peak, and the bytes of XX it must read
+    (8 n^4) per second against HBM.  MP2 pair sums: the 8 o^2 v^2 bytes of
+    (ia|jb) per second against HBM."""
+    v = n - o
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    tc = peaks.get("bf16_tflops", 1900.0)
+    out = {"peak_source": "measured" if peaks else "fallback"}
+    eri = {"quartets_per_s": quartets / (ms_eri * 1e-3) if ms_eri > 0 else None, "ms": ms_eri}
+    try:
+        eri.update(json.load(open(os.path.join(ROOT, "profiles", "eri_pipes.json"))))
+    except Exception:
+        pass
+    out["eri"] = eri
+    if ms_ao2mo > 0:
+        fl = 2.0 * (o * n ** 4 + o * v * n ** 3 + o * o * v * n * n + o * o * v * v * n)
+        tf = fl / (ms_ao2mo * 1e-3) / 1e12
+        gbs = 8.0 * n ** 4 / (ms_ao2mo * 1e-3) / 1e9
+        out["ao2mo"] = {"ms": ms_ao2mo, "algorithmic_flop": fl, "achieved_tflops": tf, "tensor_peak_tflops": tc,
+                        "tensor_frac": tf / tc, "xx_read_gbs": gbs, "hbm_frac": gbs / hbm}
+    if ms_mp2 > 0:
+        gbs = 8.0 * o * o * v * v / (ms_mp2 * 1e-3) / 1e9
+        out["mp2"] = {"ms": ms_mp2, "achieved_gbs": gbs, "hbm_frac": gbs / hbm}
+    return out
 
 
 def measure_batched(ctx, count: int):

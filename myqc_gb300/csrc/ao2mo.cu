@@ -170,6 +170,10 @@ int mp2_pair_sums(mq_ctx *c, const double *d_Om, int no1, int nv1, int no2, int 
   double *part = (double *)buf(c, "mp2_partials", sizeof(double) * (2 * (size_t)nblk + 2));
   if (!part) return MQ_ENOMEM;
   const bool f32 = d_Om == c->d_iajb && c->iajb_precision != MQ_PREC_FP64;  // split-precision (ia|jb)
+  cudaEvent_t e0, e1;  // the pair-sum kernels alone (stat "mp2")
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventRecord(e0, c->stream);
   if (nblk > 0 && f32)
     mp2_partial_f32_kernel<<<nblk, tb, sizeof(float) * nv2, c->stream>>>(
         d_Om, no1, nv1, no2, nv2, d_e1, d_e1 + no1, d_e2, d_e2 + no2, same_spin, part);
@@ -177,10 +181,20 @@ int mp2_pair_sums(mq_ctx *c, const double *d_Om, int no1, int nv1, int no2, int 
     mp2_partial_kernel<<<nblk, tb, 0, c->stream>>>(d_Om, no1, nv1, no2, nv2, d_e1, d_e1 + no1, d_e2, d_e2 + no2,
                                                    same_spin, part);
   mp2_final_kernel<<<1, 1024, 0, c->stream>>>(part, nblk, part + 2 * (size_t)nblk);
+  cudaEventRecord(e1, c->stream);
   c->stats.launches += 2;
-  MQ_CUDA(c, cudaGetLastError());
-  MQ_CUDA(c, cudaMemcpyAsync(sums, part + 2 * (size_t)nblk, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
-  MQ_CUDA(c, cudaStreamSynchronize(c->stream));
+  const cudaError_t le = cudaGetLastError();
+  const cudaError_t ce = cudaMemcpyAsync(sums, part + 2 * (size_t)nblk, 2 * sizeof(double), cudaMemcpyDeviceToHost,
+                                         c->stream);
+  const cudaError_t se = cudaStreamSynchronize(c->stream);
+  float ms = 0.f;
+  if (se == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  MQ_CUDA(c, le);
+  MQ_CUDA(c, ce);
+  MQ_CUDA(c, se);
+  c->stats.ms_mp2 = ms;
   return MQ_OK;
 }
 
