@@ -23,7 +23,7 @@ namespace mq {
 int ao2mo_device(mq_ctx *c, const double *Ci, int no1, const double *Ca, int nv1, const double *Cj, int no2,
                  const double *Cb, int nv2, int precision, double *d_out) {
   const long long n = c->nao;
-  if (!c->d_XX) return set_err(c, MQ_ESTATE, "no integrals on the device");
+  if (!c->xx_valid) return set_err(c, MQ_ESTATE, "no integrals on the device");
   if (no1 == 0 || nv1 == 0 || no2 == 0 || nv2 == 0) return MQ_OK;  // empty block (e.g. no beta electrons)
   if (precision != MQ_PREC_FP64)
     return ao2mo_split_device(c, Ci, no1, Ca, nv1, Cj, no2, Cb, nv2, d_out, precision == MQ_PREC_SPLIT_BF16X3 ? 3 : 2);

@@ -554,7 +554,7 @@ template <int S>
 static int preslice(mq_ctx *c) {
   const long long n = c->nao;
   const int Kp = (int)((n + 7) / 8 * 8);
-  if (Kp > SLICE_KMAX || !c->d_XX) return MQ_OK;  // the transform would reject it anyway
+  if (Kp > SLICE_KMAX || !c->xx_valid) return MQ_OK;  // the transform would reject it anyway
   const long long rX = n * n * n;
   bf16 *pa = (bf16 *)buf(c, "slice_a", S * rX * Kp * sizeof(bf16));
   int *ea = (int *)buf(c, "slice_ea", rX * sizeof(int));

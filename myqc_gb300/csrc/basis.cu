@@ -3,7 +3,9 @@
 // accurate Boys table used in MQ_MODE_TIGHT.
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <map>
+#include <mutex>
 #include <type_traits>
 
 #include "internal.h"
@@ -222,36 +224,17 @@ void append_pairs_class(HostPairs &dst, const HostPairs &src, int cl, int mol) {
   }
 }
 
-int upload_pairs(mq_ctx *c, const HostPairs &h, std::vector<void *> &allocs, PairTable &t) {
+// All arrays of the table in one device block (256-byte aligned pieces),
+// staged through one pinned host buffer and one copy.  allocs != null: a new
+// block recorded there (batches); null: the context's reusable "pair_table"
+// buffer, after the work queued on the stream (which may read the previous
+// table) has finished.
+int upload_pairs(mq_ctx *c, const HostPairs &h, std::vector<void *> *allocs, PairTable &t) {
   t = PairTable{};
   for (int k = 0; k < 4; ++k) t.class_off[k] = h.class_off[k];
   t.npairs = (int)h.shA.size();
   t.npp = (int)h.p.size();
-  auto up = [&](auto *&dst, const auto &src) -> int {
-    using T = typename std::decay<decltype(src)>::type::value_type;
-    dst = nullptr;
-    const size_t bytes = std::max<size_t>(1, src.size()) * sizeof(T);
-    if (cudaMalloc((void **)&dst, bytes) != cudaSuccess) return set_err(c, MQ_ENOMEM, "cudaMalloc pair table");
-    allocs.push_back(dst);
-    if (!src.empty()) MQ_CUDA(c, cudaMemcpy(dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice));
-    return MQ_OK;
-  };
-  MQ_TRY(up(t.shA, h.shA));
-  MQ_TRY(up(t.shB, h.shB));
-  MQ_TRY(up(t.pp_off, h.off));
-  MQ_TRY(up(t.aoA, h.aoA));
-  MQ_TRY(up(t.aoB, h.aoB));
-  MQ_TRY(up(t.mol, h.mol));
   std::vector<double> ones(h.shA.size(), 1.0e300);
-  MQ_TRY(up(t.schwarz, ones));
-  MQ_TRY(up(t.p, h.p));
-  MQ_TRY(up(t.inv2p, h.inv2p));
-  MQ_TRY(up(t.beta, h.beta));
-  MQ_TRY(up(t.Px, h.Px)); MQ_TRY(up(t.Py, h.Py)); MQ_TRY(up(t.Pz, h.Pz));
-  MQ_TRY(up(t.PAx, h.PAx)); MQ_TRY(up(t.PAy, h.PAy)); MQ_TRY(up(t.PAz, h.PAz));
-  MQ_TRY(up(t.PBx, h.PBx)); MQ_TRY(up(t.PBy, h.PBy)); MQ_TRY(up(t.PBz, h.PBz));
-  MQ_TRY(up(t.K, h.K));
-  MQ_TRY(up(t.c4, h.c4));
   std::vector<float4> pf(4 * h.p.size());
   for (size_t i = 0; i < h.p.size(); ++i) {
     pf[4 * i] = make_float4((float)h.p[i], (float)h.inv2p[i], (float)h.K[i], (float)h.Px[i]);
@@ -260,7 +243,58 @@ int upload_pairs(mq_ctx *c, const HostPairs &h, std::vector<void *> &allocs, Pai
     pf[4 * i + 3] = make_float4((float)h.c4[4 * i], (float)h.c4[4 * i + 1], (float)h.c4[4 * i + 2],
                                 (float)h.c4[4 * i + 3]);
   }
-  MQ_TRY(up(t.pf, pf));
+  struct Item {
+    void **dst;
+    const void *src;
+    size_t bytes, off;
+  };
+  std::vector<Item> items;
+  size_t total = 0;
+  auto add = [&](auto *&dst, const auto &src) {
+    using T = typename std::decay<decltype(src)>::type::value_type;
+    const size_t bytes = src.size() * sizeof(T);
+    items.push_back({(void **)&dst, (const void *)src.data(), bytes, total});
+    total += (std::max<size_t>(bytes, 1) + 255) / 256 * 256;
+  };
+  add(t.shA, h.shA);
+  add(t.shB, h.shB);
+  add(t.pp_off, h.off);
+  add(t.aoA, h.aoA);
+  add(t.aoB, h.aoB);
+  add(t.mol, h.mol);
+  add(t.schwarz, ones);
+  add(t.p, h.p);
+  add(t.inv2p, h.inv2p);
+  add(t.beta, h.beta);
+  add(t.Px, h.Px); add(t.Py, h.Py); add(t.Pz, h.Pz);
+  add(t.PAx, h.PAx); add(t.PAy, h.PAy); add(t.PAz, h.PAz);
+  add(t.PBx, h.PBx); add(t.PBy, h.PBy); add(t.PBz, h.PBz);
+  add(t.K, h.K);
+  add(t.c4, h.c4);
+  add(t.pf, pf);
+  char *dev = nullptr;
+  MQ_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (allocs) {
+    if (cudaMalloc((void **)&dev, total) != cudaSuccess) return set_err(c, MQ_ENOMEM, "cudaMalloc pair table");
+    allocs->push_back(dev);
+  } else {
+    dev = (char *)buf(c, "pair_table", total);
+    if (!dev) return MQ_ENOMEM;
+  }
+  if (c->pin_bytes < total) {
+    if (c->pin) cudaFreeHost(c->pin);
+    c->pin = nullptr;
+    c->pin_bytes = 0;
+    MQ_CUDA(c, cudaHostAlloc(&c->pin, total, cudaHostAllocDefault));
+    c->pin_bytes = total;
+  }
+  char *st = (char *)c->pin;
+  for (const Item &it : items) {
+    if (it.bytes) memcpy(st + it.off, it.src, it.bytes);
+    *it.dst = dev + it.off;
+  }
+  MQ_CUDA(c, cudaMemcpyAsync(dev, st, total, cudaMemcpyHostToDevice, c->stream));
+  MQ_CUDA(c, cudaStreamSynchronize(c->stream));  // the staging buffer is reused by the next upload
   return MQ_OK;
 }
 
@@ -268,7 +302,7 @@ int build_pairs(mq_ctx *c) {
   free_pairs(c);
   HostPairs h;
   pairs_host(c->shells, c->xyz, h);
-  MQ_TRY(upload_pairs(c, h, c->pair_allocs, c->pt));
+  MQ_TRY(upload_pairs(c, h, nullptr, c->pt));
   c->pair_class_count = {h.class_off[1] - h.class_off[0], h.class_off[2] - h.class_off[1],
                          h.class_off[3] - h.class_off[2]};
   return MQ_OK;
@@ -277,7 +311,17 @@ int build_pairs(mq_ctx *c) {
 // F_m(T) for T = 0.0, 0.1, ..., 36.0 and m = 0..12 by the power series
 //   F_m(T) = e^-T sum_k (2T)^k / ((2m+1)(2m+3)...(2m+2k+1))
 // at m = 12 in long double, then downward recursion F_m = (2T F_{m+1} + e^-T)/(2m+1).
+// The table is a constant: computed once per process (the long-double series
+// is slow where long double is a software type, as on aarch64).
+static void tight_boys_compute(std::vector<double> &tab);
 void tight_boys_table(std::vector<double> &tab) {
+  static std::once_flag once;
+  static std::vector<double> cached;
+  std::call_once(once, [] { tight_boys_compute(cached); });
+  tab = cached;
+}
+
+static void tight_boys_compute(std::vector<double> &tab) {
   tab.assign((size_t)TIGHT_NT * TIGHT_NM, 0.0);
   for (int it = 0; it < TIGHT_NT; ++it) {
     long double T = it / 10.0L;

@@ -447,7 +447,7 @@ int batch_scf(mq_ctx *c, const mq_batch_opts *o, double *energy, int *iters, int
   }
   free_batch_pairs(c);
   PairTable bpt;
-  MQ_TRY(upload_pairs(c, bh, c->batch_allocs, bpt));
+  MQ_TRY(upload_pairs(c, bh, &c->batch_allocs, bpt));
   MolDesc *d_md = upload_vec(c, "batch_mols", md);
   double *d_nuc = upload_vec(c, "batch_nuc", nuc);
   double *d_en = upload_vec(c, "batch_enuc", en);

@@ -138,6 +138,7 @@ int mq_free(mq_ctx *c) {
   if (c->d_boys) cudaFree(c->d_boys);
   if (c->d_nuc) cudaFree(c->d_nuc);
   if (c->cublas) cublas_destroy(c->cublas);
+  if (c->pin) cudaFreeHost(c->pin);
   cudaStreamDestroy(c->stream);
   if (c->side) cudaStreamDestroy(c->side);
   if (c->ev_main) cudaEventDestroy(c->ev_main);
@@ -166,43 +167,49 @@ int mq_set_system(mq_ctx *c, int nnuc, const int *Z, const double *xyz, const do
   c->mode = mode;
   MQ_TRY(build_shells(c, nnuc, Z, xyz, bas, set, basinfo, setinfo));
   MQ_TRY(build_pairs(c));
-  // Boys table (+ its grid values Tk/10, as the reference computes them)
-  std::vector<double> tab;
-  if (mode == MQ_MODE_REFERENCE) {
-    tab.assign(ftab, ftab + FTAB_NT * FTAB_NM);
-    for (int k = 0; k < FTAB_NT; ++k) tab.push_back(k / 10.0);
-  } else {
-    tight_boys_table(tab);
-    for (int k = 0; k < TIGHT_NT; ++k) tab.push_back(k / 10.0);
+  // Boys table (+ its grid values Tk/10, as the reference computes them); the
+  // tight table is a constant and stays on the device once uploaded
+  if (mode == MQ_MODE_REFERENCE || c->boys_loaded != MQ_MODE_TIGHT) {
+    std::vector<double> tab;
+    if (mode == MQ_MODE_REFERENCE) {
+      tab.assign(ftab, ftab + FTAB_NT * FTAB_NM);
+      for (int k = 0; k < FTAB_NT; ++k) tab.push_back(k / 10.0);
+    } else {
+      tight_boys_table(tab);
+      for (int k = 0; k < TIGHT_NT; ++k) tab.push_back(k / 10.0);
+    }
+    c->boys_loaded = -1;
+    if (c->d_boys) cudaFree(c->d_boys);
+    c->d_boys = nullptr;
+    if (c->d_boys_f32) cudaFree(c->d_boys_f32);
+    c->d_boys_f32 = nullptr;
+    if (mode == MQ_MODE_TIGHT) {  // single-precision copy for the mixed-precision integral pass
+      std::vector<float> tf(tab.begin(), tab.end());
+      MQ_CUDA(c, cudaMalloc((void **)&c->d_boys_f32, tf.size() * sizeof(float)));
+      MQ_CUDA(c, cudaMemcpy(c->d_boys_f32, tf.data(), tf.size() * sizeof(float), cudaMemcpyHostToDevice));
+    }
+    MQ_CUDA(c, cudaMalloc((void **)&c->d_boys, tab.size() * sizeof(double)));
+    MQ_CUDA(c, cudaMemcpy(c->d_boys, tab.data(), tab.size() * sizeof(double), cudaMemcpyHostToDevice));
+    c->boys_loaded = mode;
   }
-  if (c->d_boys) cudaFree(c->d_boys);
-  c->d_boys = nullptr;
-  if (c->d_boys_f32) cudaFree(c->d_boys_f32);
-  c->d_boys_f32 = nullptr;
-  if (mode == MQ_MODE_TIGHT) {  // single-precision copy for the mixed-precision integral pass
-    std::vector<float> tf(tab.begin(), tab.end());
-    MQ_CUDA(c, cudaMalloc((void **)&c->d_boys_f32, tf.size() * sizeof(float)));
-    MQ_CUDA(c, cudaMemcpy(c->d_boys_f32, tf.data(), tf.size() * sizeof(float), cudaMemcpyHostToDevice));
-  } else {
-    c->eri_f32_tau = 0.0;
-  }
-  MQ_CUDA(c, cudaMalloc((void **)&c->d_boys, tab.size() * sizeof(double)));
-  MQ_CUDA(c, cudaMemcpy(c->d_boys, tab.data(), tab.size() * sizeof(double), cudaMemcpyHostToDevice));
+  if (mode != MQ_MODE_TIGHT) c->eri_f32_tau = 0.0;
   std::vector<double> nuc(4 * (size_t)nnuc);
   for (int a = 0; a < nnuc; ++a) {
     for (int k = 0; k < 3; ++k) nuc[4 * a + k] = c->xyz[3 * a + k];
     nuc[4 * a + 3] = Z[a];
   }
-  if (c->d_nuc) cudaFree(c->d_nuc);
-  c->d_nuc = nullptr;
-  MQ_CUDA(c, cudaMalloc((void **)&c->d_nuc, nuc.size() * sizeof(double)));
+  if (nnuc > c->nuc_cap) {
+    if (c->d_nuc) cudaFree(c->d_nuc);
+    c->d_nuc = nullptr;
+    c->nuc_cap = 0;
+    MQ_CUDA(c, cudaMalloc((void **)&c->d_nuc, nuc.size() * sizeof(double)));
+    c->nuc_cap = nnuc;
+  }
   MQ_CUDA(c, cudaMemcpy(c->d_nuc, nuc.data(), nuc.size() * sizeof(double), cudaMemcpyHostToDevice));
   // integrals of a previous system are stale
   c->slab_live_valid = 0;
   c->schwarz_valid = 0;
-  if (c->d_XX) cudaFree(c->d_XX);
-  c->d_XX = nullptr;
-  c->XX_elems = 0;
+  c->xx_valid = 0;  // the allocation stays for the next mq_eri_store of the same order
   c->have_system = 1;
   if (c->schwarz_thr > 0) MQ_TRY(ensure_schwarz(c));
   return MQ_OK;
@@ -248,6 +255,7 @@ int mq_int1e(mq_ctx *c, double *S, double *H) {
 int mq_eri_store(mq_ctx *c) {
   MQ_TRY(need_system(c));
   cudaSetDevice(c->device);
+  MQ_TRY(join_side(c));
   MQ_TRY(ensure_xx(c));
   // queued on the context's stream; the call returns without waiting (later
   // calls on the context order after it)
@@ -256,6 +264,7 @@ int mq_eri_store(mq_ctx *c) {
   c->t_eri.start(c->stream);
   const int rc = eri_full_device(c, c->d_XX);
   c->t_eri.stop(c->stream);
+  c->xx_valid = rc == MQ_OK;
   return rc;
 }
 
@@ -277,6 +286,7 @@ int mq_eri_upload(mq_ctx *c, const double *XX) {
   MQ_CUDA(c, cudaStreamSynchronize(c->stream));
   c->slab_live_valid = 0;  // any slab of the uploaded integrals may be nonzero
   c->xx_sliced = 0;
+  c->xx_valid = 1;
   return MQ_OK;
 }
 

@@ -654,7 +654,7 @@ int fock_densities(mq_ctx *c, int n, const double *d_Da, const double *d_Db, con
 
 int fock_stored_device(mq_ctx *c, const double *d_Da, const double *d_Db, double *d_Ga, double *d_Gb) {
   const int n = c->nao;
-  if (!c->d_XX) return set_err(c, MQ_ESTATE, "no integrals on the device (call mq_eri_store or mq_eri_upload)");
+  if (!c->xx_valid) return set_err(c, MQ_ESTATE, "no integrals on the device (call mq_eri_store or mq_eri_upload)");
   if (n > 4 * PAIR_MAX_THREADS) return set_err(c, MQ_EINVAL, "stored Fock build supports n <= 1024");
   const bool uhf = d_Db != nullptr;
   const void *DJ, *DKa, *DKb;
@@ -673,7 +673,7 @@ int fock_stored_device(mq_ctx *c, const double *d_Da, const double *d_Db, double
 int fock_stored_increment(mq_ctx *c, const double *d_Da, const double *d_Db, const double *d_Dpa,
                           const double *d_Dpb, const double *d_Gpa, const double *d_Gpb, double *d_Ga, double *d_Gb) {
   const int n = c->nao;
-  if (!c->d_XX) return set_err(c, MQ_ESTATE, "no integrals on the device (call mq_eri_store or mq_eri_upload)");
+  if (!c->xx_valid) return set_err(c, MQ_ESTATE, "no integrals on the device (call mq_eri_store or mq_eri_upload)");
   if (n > 4 * PAIR_MAX_THREADS) return set_err(c, MQ_EINVAL, "stored Fock build supports n <= 1024");
   const bool uhf = d_Db != nullptr;
   if (uhf && d_Gpb != d_Gpa + (size_t)n * n) return set_err(c, MQ_EINVAL, "increment: beta G must follow alpha G");

@@ -172,7 +172,12 @@ struct mq_ctx {
   double *d_nuc = nullptr;   // nnuc x 4: x, y, z, Z
   mq::PairTable pt{};
   std::vector<void *> pair_allocs;
-  double *d_XX = nullptr;    // n^4 full integral array
+  void *pin = nullptr;  // pinned staging buffer of the pair-table uploads
+  size_t pin_bytes = 0;
+  int boys_loaded = -1;  // mode whose Boys table d_boys holds (-1: none; reference tables are always reloaded)
+  int nuc_cap = 0;       // nuclei d_nuc has room for
+  double *d_XX = nullptr;    // n^4 full integral array (kept allocated across systems of the same order)
+  int xx_valid = 0;          // d_XX holds the current system's integrals (mq_eri_store / mq_eri_upload)
   // batch of independent closed-shell molecules (mq_batch_*)
   std::vector<mq::BatchMol> bmols;
   std::vector<void *> batch_allocs;  // batch pair table
@@ -275,7 +280,7 @@ int build_shells(mq_ctx *c, int nnuc, const int *Z, const double *xyz, const dou
 int build_pairs(mq_ctx *c);
 void pairs_host(const std::vector<HostShell> &shells, const std::vector<double> &xyz, HostPairs &h);
 void append_pairs_class(HostPairs &dst, const HostPairs &src, int cl, int mol);
-int upload_pairs(mq_ctx *c, const HostPairs &h, std::vector<void *> &allocs, PairTable &t);
+int upload_pairs(mq_ctx *c, const HostPairs &h, std::vector<void *> *allocs, PairTable &t);
 void free_pairs(mq_ctx *c);
 void tight_boys_table(std::vector<double> &tab);  // TIGHT_NT x TIGHT_NM, row-major [T][m]
 

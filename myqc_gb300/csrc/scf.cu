@@ -224,7 +224,7 @@ int scf_device(mq_ctx *c, const double *S, const double *H, const mq_scf_opts *o
   const double occf = uhf ? 1.0 : 2.0;
   if (!uhf && o->nalpha != o->nbeta) return set_err(c, MQ_EINVAL, "RHF needs nalpha == nbeta");
   if (nocc[0] > n || nocc[1] > n || nocc[0] < 0 || nocc[1] < 0) return set_err(c, MQ_EINVAL, "bad occupation");
-  if (!o->direct && !c->d_XX) return set_err(c, MQ_ESTATE, "no stored integrals for a conventional SCF");
+  if (!o->direct && !c->xx_valid) return set_err(c, MQ_ESTATE, "no stored integrals for a conventional SCF");
 
   // device workspace
   const size_t nmat = 8 + 8 * ns + (size_t)2 * ndiis * ns;
