@@ -80,6 +80,13 @@ int mq_set_eri_mixed(mq_ctx *ctx, double tau);
  * Replaces proc1e (src/integrals/int1e.f90:132-280). */
 int mq_int1e(mq_ctx *ctx, double *S, double *H);
 
+/* Dipole integrals Px(c, u, v) = <u| r_c |v> about the origin (bohr), c = x, y, z,
+ * written as three n x n column-major matrices one after the other (the order of
+ * the reference's Pxuv file); replaces proc1p (src/integrals/int1p.f90:150-300).
+ * The dipole moment of cphf_dipole_rhf (src/props/cphf.f90:80-131) is then
+ * mu_c = -sum_uv D(u,v) Px(c,v,u) + sum_A Z_A R_A,c on the host. */
+int mq_int1p(mq_ctx *ctx, double *Px);
+
 /* Full two-electron integral array XX(i,j,g,h) at i+n*(j+n*(g+n*h)), all 8
  * permutations filled, into a host buffer of n^4 doubles.  Replaces proc2e +
  * fillsym (src/integrals/int2e.f90:78-351,540-613).  Also leaves the array

@@ -72,6 +72,7 @@ def lib(path: str | None = None):
     L.mq_set_schwarz.argtypes = [vp, c_double]
     L.mq_set_eri_mixed.argtypes = [vp, c_double]
     L.mq_int1e.argtypes = [vp, dp, dp]
+    L.mq_int1p.argtypes = [vp, vp]
     L.mq_eri_full.argtypes = [vp, dp]
     L.mq_eri_store.argtypes = [vp]
     L.mq_eri_upload.argtypes = [vp, dp]

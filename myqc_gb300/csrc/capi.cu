@@ -252,6 +252,19 @@ int mq_int1e(mq_ctx *c, double *S, double *H) {
   return MQ_OK;
 }
 
+int mq_int1p(mq_ctx *c, double *Px) {
+  MQ_TRY(need_system(c));
+  if (!Px) return set_err(c, MQ_EINVAL, "null output");
+  cudaSetDevice(c->device);
+  const size_t n2 = (size_t)c->nao * c->nao;
+  double *d = (double *)buf(c, "int1p_out", 3 * n2 * sizeof(double));
+  if (!d) return MQ_ENOMEM;
+  MQ_TRY(int1p_device(c, d));
+  MQ_CUDA(c, cudaMemcpyAsync(Px, d, 3 * n2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  MQ_CUDA(c, cudaStreamSynchronize(c->stream));
+  return MQ_OK;
+}
+
 int mq_eri_store(mq_ctx *c) {
   MQ_TRY(need_system(c));
   cudaSetDevice(c->device);

@@ -190,6 +190,80 @@ __global__ void __launch_bounds__(32 * INT1E_WARPS) int1e_kernel(Int1eArgs g) {
     }
 }
 
+// Dipole integrals about the origin, the property integrals of int1p
+// (src/integrals/int1p.f90:150-300): <a| r_c |b> per primitive pair is
+// K_ab c_a c_b (pi/p)^(3/2) E^{ab}_0 of the two other axes times
+// (E^{ab}_1 + P_c E^{ab}_0) of axis c.  One thread per contracted shell pair;
+// Px holds the x, y, z matrices one after the other (column-major n x n).
+template <int LA, int LB>
+__global__ void __launch_bounds__(128) dipole_kernel(PairTable t, int pOff, int np, int n, int mode,
+                                                     double *__restrict__ Px) {
+  constexpr int NA = LA ? 4 : 1, NB = LB ? 4 : 1;
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= np) return;
+  const int P = pOff + idx;
+  const double pi = mode == MQ_MODE_REFERENCE ? PI_REF : PI_TRUE;
+  double d[3][NA][NB];
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+#pragma unroll
+    for (int a = 0; a < NA; ++a)
+#pragma unroll
+      for (int b = 0; b < NB; ++b) d[c][a][b] = 0.0;
+  for (int ip = t.pp_off[P]; ip < t.pp_off[P + 1]; ++ip) {
+    const double p = t.p[ip], i2p = t.inv2p[ip];
+    double E[3][2][4][5];
+    axis_E(t.PAx[ip], t.PBx[ip], i2p, E[0]);
+    axis_E(t.PAy[ip], t.PBy[ip], i2p, E[1]);
+    axis_E(t.PAz[ip], t.PBz[ip], i2p, E[2]);
+    const double Pc[3] = {t.Px[ip], t.Py[ip], t.Pz[ip]};
+    const double pp32 = pow(pi / p, 1.5);
+#pragma unroll
+    for (int a = 0; a < NA; ++a)
+#pragma unroll
+      for (int b = 0; b < NB; ++b) {
+        const int la[3] = {a == 1, a == 2, a == 3}, lb[3] = {b == 1, b == 2, b == 3};
+        const double cf = t.c4[4 * ip + 2 * (a > 0) + (b > 0)] * pp32;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          const int o1 = (c + 1) % 3, o2 = (c + 2) % 3;
+          const double e0 = E[c][la[c]][lb[c]][0], e1 = E[c][la[c]][lb[c]][1];
+          d[c][a][b] += cf * E[o1][la[o1]][lb[o1]][0] * E[o2][la[o2]][lb[o2]][0] * (e1 + Pc[c] * e0);
+        }
+      }
+  }
+  const int A = t.shA[P], B = t.shB[P], i0 = t.aoA[P], j0 = t.aoB[P];
+  const size_t N = n, n2 = N * N;
+#pragma unroll
+  for (int a = 0; a < NA; ++a)
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+      const int i = i0 + a, j = j0 + b;
+      if (A == B && i < j) continue;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        Px[n2 * c + i + N * j] = d[c][a][b];
+        Px[n2 * c + j + N * i] = d[c][a][b];
+      }
+    }
+}
+
+int int1p_device(mq_ctx *c, double *d_Px) {
+  const size_t n = c->nao;
+  MQ_CUDA(c, cudaMemsetAsync(d_Px, 0, 3 * n * n * sizeof(double), c->stream));
+  for (int cl = 0; cl < 3; ++cl) {
+    const int pOff = c->pt.class_off[cl], np = c->pt.class_off[cl + 1] - pOff;
+    if (!np) continue;
+    const dim3 grid((np + 127) / 128);
+    if (cl == 0) dipole_kernel<0, 0><<<grid, 128, 0, c->stream>>>(c->pt, pOff, np, (int)n, c->mode, d_Px);
+    else if (cl == 1) dipole_kernel<1, 0><<<grid, 128, 0, c->stream>>>(c->pt, pOff, np, (int)n, c->mode, d_Px);
+    else dipole_kernel<1, 1><<<grid, 128, 0, c->stream>>>(c->pt, pOff, np, (int)n, c->mode, d_Px);
+    c->stats.launches += 1;
+    MQ_CUDA(c, cudaGetLastError());
+  }
+  return MQ_OK;
+}
+
 // Batch: S and H of every molecule of the batch table into the packed n x n
 // arrays (offset MolDesc::mat), one launch per pair class for all molecules.
 int int1e_batch_device(mq_ctx *c, const PairTable &t, const double *d_nuc, const MolDesc *d_mols, size_t mat_total,

@@ -294,6 +294,7 @@ int direct_combine(mq_ctx *c, const double *J, const double *Ka, const double *K
 
 // int1e.cu
 int int1e_device(mq_ctx *c, double *d_S, double *d_H);
+int int1p_device(mq_ctx *c, double *d_Px);  // dipole integrals, 3 n x n (x, y, z)
 
 // fock.cu
 int fock_stored_device(mq_ctx *c, const double *d_Da, const double *d_Db, double *d_Ga, double *d_Gb);

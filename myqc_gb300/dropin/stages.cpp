@@ -1,5 +1,6 @@
 // stages.cpp -- drop-in replacements of the reference's stage executables
-// int1e, int2e, scf, ao2mo and mp2, computing through libmyqc.
+// int1e, int2e, scf, ao2mo and mp2 (and the property stages int1p, cphf and
+// props), computing through libmyqc.
 //
 // One binary; the stage is the name it is invoked by (symlinks int1e, int2e,
 // scf, ao2mo, mp2) or its first argument.  Like the reference's programs they
@@ -12,7 +13,10 @@
 //   Suv, Huv                    text (int1e)
 //   XX                          gfortran unformatted record, n^4 doubles (int2e)
 //   Cui, eig, MOLDEN            text (scf); Cui is also read as a guess
-//   ijab_AA, ijab_AB, ijab_BB   one unformatted record per (i, j) pair (ao2mo)
+//   Da, Dold                    one unformatted record per spin (scf)
+//   Pxuv                        text, dipole integrals x, y, z (int1p; read by cphf)
+//   ijab_AA, ijab_AB, ijab_BB   one unformatted record per (i, j) pair (ao2mo, MP2)
+//   ajib_AA/AB/BB, ajbi_AA/BB   one unformatted record per (j, b) pair (ao2mo, UHF CIS)
 // A failure prints a message, creates the file `error` (the reference's
 // signal to its driver, src/myQC/myQC.f90:30) and exits with status 1; a
 // stage started while `error` exists stops at once, as the reference does.
@@ -21,6 +25,7 @@
 // selects the split-BF16 tensor-core transform in ao2mo.
 #include <sys/stat.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -455,7 +460,91 @@ int stage_scf() {
   write_text("Cui", cm, n2);
   write_text("eig", em, (size_t)n);
   write_molden(e, b, n, C, eps, uhf);
+  // the density files of the reference's loop (dens.f90 writes Da, scf.f90
+  // keeps Dold): one unformatted record per spin; both hold the last
+  // iteration's density here, converged to the SCF threshold
+  for (const char *fn : {"Da", "Dold"}) {
+    std::ofstream f(fn, std::ios::binary | std::ios::trunc);
+    if (!f) fail(std::string("cannot write ") + fn);
+    for (int s2 = 0; s2 < ns; ++s2) write_record(f, D.data() + s2 * n2, n2 * sizeof(double));
+  }
   return 0;
+}
+
+// int1p (src/integrals/int1p.f90): dipole integrals into Pxuv (text, the x, y, z
+// matrices in turn); an existing Pxuv is kept, as the reference keeps it
+int stage_int1p() {
+  std::printf(" int1p called\n               STARTING PROPERTY INTEGRALS\n"
+              " ------------------------------------------------------------\n");
+  Env e = read_env();
+  if (exists("Pxuv")) {
+    std::printf(" Reading Dipole integrals from Pxuv\n");
+    return 0;
+  }
+  Basis b = build_basis(e.Z);
+  Lib L;
+  const int n = set_system(L, e, b);
+  const size_t n2 = (size_t)n * n;
+  std::vector<double> P(3 * n2);
+  L.check(mq_int1p(L.ctx, P.data()), "int1p");
+  write_text("Pxuv", {P.data(), P.data() + n2, P.data() + 2 * n2}, n2);
+  std::printf(" Dipole moment integrals written to Pxuv\n");
+  return 0;
+}
+
+// cphf (src/props/cphf.f90:80-131): the RHF dipole moment from Pxuv and Da,
+// mu_c = -sum_uv D(u,v) Px(c,v,u) + sum_A Z_A R_A,c
+int stage_cphf() {
+  std::printf("\n cphf called\n\n");
+  Env e = read_env();
+  const bool uhf = e.options.size() > 3 && e.options[3] == 1;
+  if (uhf) {
+    std::printf(" Sorry, only RHF CPHF equations are coded\n");
+    return 0;
+  }
+  std::vector<double> bi = numbers("basinfo");
+  if (bi.size() < 2) fail("basinfo: too short");
+  const size_t n = (size_t)bi[1], n2 = n * n;
+  std::vector<double> P = numbers("Pxuv");
+  if (P.size() < 3 * n2) fail("Pxuv: too short");
+  auto recs = read_records("Da");
+  if (recs.empty() || recs[0].size() != n2 * sizeof(double)) fail("Da: bad record");
+  const double *D = (const double *)recs[0].data();
+  double mu[3];
+  for (int c = 0; c < 3; ++c) {
+    double t = 0.0;
+    for (size_t u = 0; u < n; ++u)
+      for (size_t v = 0; v < n; ++v) t -= D[u + n * v] * P[c * n2 + v + n * u];
+    for (int a = 0; a < e.nnuc; ++a) t += e.Z[a] * e.xyz[a + (size_t)e.nnuc * c];
+    mu[c] = t;
+  }
+  std::printf("                 Dipole Moments                \n ----------------------------------------------\n"
+              "        X              Y              Z        \n%15.6f%15.6f%15.6f\n"
+              " ----------------------------------------------\n",
+              mu[0], mu[1], mu[2]);
+  return 0;
+}
+
+// props (src/props/props.f90): first- or second-order properties of an SCF
+// (options(1) = 0) run int1p then cphf
+int stage_props() {
+  std::printf("\n               STARTING PROPERTY CALCULATIONS\n"
+              " ------------------------------------------------------------\n props called\n\n");
+  Env e = read_env();
+  const int order = e.options.size() > 16 ? e.options[16] : 0;
+  const int calc = e.options.size() > 1 ? e.options[1] : 0;
+  if (order == 0) {
+    std::printf(" Property order   :  none\n");
+    return 0;
+  }
+  std::printf(" Property order   :  %s\n", order == 1 ? "first" : "second");
+  if (calc != 0) {
+    std::printf(" Sorry, only cphf properties for RHF available\n");
+    return 0;
+  }
+  std::printf(" Property method  :  cphf\n");
+  if (const int rc = stage_int1p()) return rc;
+  return stage_cphf();
 }
 
 int precision_from_env() {
@@ -481,6 +570,49 @@ void write_ijab(const char *path, const std::vector<double> &Om, int no1, int nv
     }
 }
 
+// The UHF CIS integral blocks of slow_ao2mo_CIS_UHF (src/ao2mo/ao2mo.f90:919-1227):
+// Om(x1,x2,x3,x4) = sum (uv|ld) C1(u,x1) C2(v,x2) C3(l,x3) C4(d,x4), x1 fastest,
+// one record per (j, b) with the (i, a) block, a fastest:
+//   ajib_AA, ajib_AB, ajib_BB   Om(a,i,j,b) over the blocks (vrt, occ, occ, vrt)
+//   ajbi_AA, ajbi_BB            Om(a,b,j,i) over the blocks (vrt, vrt, occ, occ)
+void cis_blocks(Lib &L, const double *CA, const double *CB, int n, int noA, int noB, int prec) {
+  struct Blk {
+    const char *file;
+    const double *c1, *c3;  // alpha/beta coefficients of the first two and the last two indices
+    int o1, o3;
+    bool ajbi;
+  };
+  const Blk blocks[5] = {{"ajib_AA", CA, CA, noA, noA, false}, {"ajbi_AA", CA, CA, noA, noA, true},
+                         {"ajib_AB", CA, CB, noA, noB, false}, {"ajib_BB", CB, CB, noB, noB, false},
+                         {"ajbi_BB", CB, CB, noB, noB, true}};
+  for (const Blk &k : blocks) {
+    const int v1 = n - k.o1, v3 = n - k.o3;
+    const double *occ1 = k.c1, *vrt1 = k.c1 + (size_t)n * k.o1, *occ3 = k.c3, *vrt3 = k.c3 + (size_t)n * k.o3;
+    std::vector<double> Om((size_t)v1 * (k.ajbi ? v1 : k.o1) * k.o3 * (k.ajbi ? k.o3 : v3));
+    if (!k.ajbi)
+      L.check(mq_ao2mo_iajb(L.ctx, vrt1, v1, occ1, k.o1, occ3, k.o3, vrt3, v3, prec, Om.data()), "ao2mo");
+    else
+      L.check(mq_ao2mo_iajb(L.ctx, vrt1, v1, vrt1, v1, occ3, k.o3, occ3, k.o3, prec, Om.data()), "ao2mo");
+    std::printf(" Writing to %s\n", k.file);
+    std::ofstream f(k.file, std::ios::binary | std::ios::trunc);
+    if (!f) fail(std::string("cannot write ") + k.file);
+    std::vector<double> rec((size_t)k.o1 * v1);
+    const int nj = k.o3, nb = k.ajbi ? v1 : v3;
+    for (int j = 0; j < nj; ++j)
+      for (int b = 0; b < nb; ++b) {
+        if (!k.ajbi) {  // Om(:, :, j, b) is one contiguous (a, i) block
+          const double *src = Om.data() + (size_t)v1 * k.o1 * (j + (size_t)k.o3 * b);
+          std::copy(src, src + rec.size(), rec.begin());
+        } else {  // Om(a, b, j, i) gathered over i, a
+          for (int i = 0; i < k.o1; ++i)
+            for (int a = 0; a < v1; ++a)
+              rec[a + (size_t)v1 * i] = Om[a + (size_t)v1 * (b + (size_t)v1 * (j + (size_t)k.o3 * i))];
+        }
+        write_record(f, rec.data(), rec.size() * sizeof(double));
+      }
+  }
+}
+
 int stage_ao2mo() {
   std::printf("\n                STARTING AO TRANSFORM\n ------------------------------------------------------------\n");
   std::printf(" ao2mo called\n\n Starting AO to MO integral transform\n");
@@ -496,6 +628,18 @@ int stage_ao2mo() {
   std::vector<double> C = numbers("Cui");
   if (C.size() < (uhf ? 2 : 1) * n2) fail("Cui: too short");
   const int prec = precision_from_env();
+  // transform type as ao2mo.f90 chooses it: MP2 (options(1) = 1), SCF CIS
+  // (options(13) = 1, options(1) = 0, UHF only), else an error
+  const int calc = e.options.size() > 1 ? e.options[1] : 0;
+  const int excite = e.options.size() > 13 ? e.options[13] : 0;
+  if (calc != 1) {
+    if (excite == 1 && calc == 0) {
+      if (!uhf) fail("Sorry, only UHF CIS is coded");
+      cis_blocks(L, C.data(), C.data() + n2, n, e.nelcA, e.nelcB, prec);
+      return 0;
+    }
+    fail("Sorry, that transform type has not been coded yet");
+  }
   struct Blk {
     const char *file;
     const double *c1, *c2;
@@ -574,9 +718,13 @@ int main(int argc, char **argv) {
   std::string name = argv[0];
   const size_t slash = name.find_last_of('/');
   if (slash != std::string::npos) name = name.substr(slash + 1);
-  if (name != "int1e" && name != "int2e" && name != "scf" && name != "ao2mo" && name != "mp2") {
+  static const char *const stages[] = {"int1e", "int2e", "scf", "ao2mo", "mp2", "int1p", "cphf", "props"};
+  bool known = false;
+  for (const char *st : stages) known = known || name == st;
+  if (!known) {
     if (argc < 2) {
-      std::fprintf(stderr, "usage: %s int1e|int2e|scf|ao2mo|mp2 (or invoke through a link of that name)\n", argv[0]);
+      std::fprintf(stderr, "usage: %s int1e|int2e|scf|ao2mo|mp2|int1p|cphf|props (or through a link of that name)\n",
+                   argv[0]);
       return 2;
     }
     name = argv[1];
@@ -587,6 +735,9 @@ int main(int argc, char **argv) {
   if (name == "scf") return stage_scf();
   if (name == "ao2mo") return stage_ao2mo();
   if (name == "mp2") return stage_mp2();
+  if (name == "int1p") return stage_int1p();
+  if (name == "cphf") return stage_cphf();
+  if (name == "props") return stage_props();
   std::fprintf(stderr, "unknown stage %s\n", name.c_str());
   return 2;
 }

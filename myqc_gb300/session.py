@@ -199,6 +199,13 @@ class Context:
         self._check(self.L.mq_int1e(self.h, ptr(S), ptr(H)))
         return S, H
 
+    def int1p(self) -> np.ndarray:
+        """Dipole integrals (3, n, n): <u| x |v>, <u| y |v>, <u| z |v> about the origin."""
+        n = self.n
+        P = np.zeros(3 * n * n)
+        self._check(self.L.mq_int1p(self.h, ptr(P)))
+        return np.stack([P[c * n * n:(c + 1) * n * n].reshape(n, n, order="F") for c in range(3)])
+
     def eri_full(self) -> np.ndarray:
         n = self.n
         XX = np.zeros((n, n, n, n), order="F")

@@ -438,6 +438,51 @@ int orc_int1e(int nset, int setl, int ops, int norb, const double *bas, const do
 }
 
 /* ------------------------------------------------------------------ */
+/* Dipole integrals <u| r_c |v> about the origin, int1p.f90 proc1p/dipole
+ * (src/integrals/int1p.f90:150-300): every set pair (a, b) with EIJ >= 1e-14,
+ * E_0 and E_1 of getcoef_dipole (auxilary.f90:649-696; the standard Hermite
+ * table), P_c = EIJ (pi/p)^(3/2) c_a c_b N_a N_b E^y_0 E^z_0 (E^x_1 + P_x E^x_0)
+ * for c = x and likewise for y, z.  Both pi constants of int1p are default-real
+ * literals, so mode 0 uses the float-valued pi in both.  Px: 3 n x n matrices
+ * (x, y, z), column-major. */
+int orc_int1p(int nset, int setl, int ops, int norb, const double *bas, const double *set, const int *basinfo,
+              const int *setinfo, int nnuc, const int *atoms, const double *xyz, int mode, double *Px) {
+  sys_t S = {nset, setl, ops, norb, bas, set, basinfo, setinfo, xyz, nnuc, atoms, NULL, mode};
+  const sys_t *s = &S;
+  const int n = norb;
+  const double pi = pi_of(mode);
+  for (int i = 0; i < 3 * n * n; ++i) Px[i] = 0.0;
+  for (int a = 0; a < nset; ++a)
+    for (int b = 0; b < nset; ++b) {
+      pair_t pr;
+      ecoef_t E;
+      const double aa = set[a], bb = set[b];
+      make_pair(s, a, b, 0, &pr, &E);
+      if (pr.EIJ < 1.0e-14) { free_pair(&pr); continue; } /* int1p.f90 EIJ screen */
+      const double p = pr.p, EIJ = pr.EIJ;
+      for (int i = 0; i < set_nao(s, a); ++i) {
+        int oa = set_ao(s, a, i), la[3];
+        ao_lmn(s, oa, la);
+        for (int j = 0; j < set_nao(s, b); ++j) {
+          int ob = set_ao(s, b, j), lb[3];
+          ao_lmn(s, ob, lb);
+          const double w = EIJ * pow(pi / p, 3.0 / 2.0) * bas[a * ops + i] * bas[b * ops + j] *
+                           gtoD(ao_l(s, oa), aa, pi) * gtoD(ao_l(s, ob), bb, pi);
+          for (int c = 0; c < 3; ++c) {
+            const int o1 = (c + 1) % 3, o2 = (c + 2) % 3;
+            double t = w * eget(&E, o1 < o2 ? o1 : o2, 0, la[o1 < o2 ? o1 : o2], lb[o1 < o2 ? o1 : o2]) *
+                       eget(&E, o1 < o2 ? o2 : o1, 0, la[o1 < o2 ? o2 : o1], lb[o1 < o2 ? o2 : o1]);
+            t = t * (eget(&E, c, 1, la[c], lb[c]) + pr.P[c] * eget(&E, c, 0, la[c], lb[c]));
+            Px[(size_t)c * n * n + oa + (size_t)n * ob] += t;
+          }
+        }
+      }
+      free_pair(&pr);
+    }
+  return 0;
+}
+
+/* ------------------------------------------------------------------ */
 /* dens.f90:115-124 (RHF, factor 2) and :213-228 (UHF) */
 void orc_density(int n, int nocc, const double *C, double factor, double *D) {
   for (int v = 0; v < n; ++v)

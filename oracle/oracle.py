@@ -65,6 +65,7 @@ def lib():
         L.orc_boys.argtypes = [c_int, c_double, c_int, dp, dp]
         L.orc_int2e.argtypes = [c_int, c_int, c_int, c_int, dp, dp, ip, ip, c_int, dp, dp, c_int, dp]
         L.orc_int1e.argtypes = [c_int, c_int, c_int, c_int, dp, dp, ip, ip, c_int, ip, dp, dp, c_int, dp, dp]
+        L.orc_int1p.argtypes = [c_int, c_int, c_int, c_int, dp, dp, ip, ip, c_int, ip, dp, c_int, dp]
         L.orc_density.argtypes = [c_int, c_int, dp, c_double, dp]
         L.orc_fock_rhf.argtypes = [c_int, dp, dp, dp]
         L.orc_fock_uhf.argtypes = [c_int, dp, dp, dp, dp, dp]
@@ -335,6 +336,26 @@ def int1e(mol: Molecule, basis: Basis, ftab: np.ndarray, mode: int = 0):
     return S.reshape(n, n, order="F"), H.reshape(n, n, order="F")
 
 
+def int1p(mol: Molecule, basis: Basis, mode: int = 0) -> np.ndarray:
+    """Dipole integrals Px[c] = <u| r_c |v>, c = x, y, z (int1p.f90 proc1p), (3, n, n)."""
+    n = basis.norb
+    Px = np.zeros(3 * n * n)
+    rc = lib().orc_int1p(basis.nset, basis.setl, basis.ops, n, basis.bas, basis.set, basis.basinfo,
+                         basis.setinfo, len(mol.atoms), np.ascontiguousarray(mol.atoms, dtype=np.int32),
+                         _xyz_colmajor(mol), mode, Px)
+    if rc != 0:
+        raise RuntimeError("int1p failed")
+    return np.stack([Px[c * n * n:(c + 1) * n * n].reshape(n, n, order="F") for c in range(3)])
+
+
+def dipole_moment(Px: np.ndarray, D: np.ndarray, mol: Molecule) -> np.ndarray:
+    """cphf_dipole_rhf (src/props/cphf.f90:80-131): mu_c = -sum_uv D(u,v) Px(c,v,u)
+    + sum_A Z_A R_A,c, with D the total density (Da) and R in bohr."""
+    mu = -np.einsum("uv,cvu->c", D, Px)
+    xyz = np.asarray(mol.xyz, dtype=float).reshape(len(mol.atoms), 3)
+    return mu + np.einsum("a,ac->c", np.asarray(mol.atoms, dtype=float), xyz)
+
+
 def _f(a):
     return np.ascontiguousarray(np.asarray(a, dtype=np.float64).reshape(-1, order="F"))
 
@@ -460,6 +481,27 @@ def ao2mo(XX: np.ndarray, Ci, Ca, Cj, Cb) -> np.ndarray:
     if rc != 0:
         raise MemoryError("ao2mo")
     return Om.reshape(no1, nv1, no2, nv2, order="F")
+
+
+def cis_records(XX: np.ndarray, CA: np.ndarray, CB: np.ndarray, noA: int, noB: int) -> dict:
+    """The UHF CIS integral files of slow_ao2mo_CIS_UHF (src/ao2mo/ao2mo.f90:919-1227)
+    as lists of records: ajib_AA/AB/BB hold Om(a,i,j,b) = (ai|jb) over the blocks
+    (vrt, occ, occ, vrt) (:955-996, :1040-1075, :1077-1113), ajbi_AA/BB hold
+    Om(a,b,j,i) over (vrt, vrt, occ, occ) (:1001-1036, :1115-1153); one record per
+    (j, b), j outer, with the (i, a) block, a fastest."""
+    out = {}
+    for name, C1, C3, o1, o3, ajbi in (("ajib_AA", CA, CA, noA, noA, False), ("ajbi_AA", CA, CA, noA, noA, True),
+                                       ("ajib_AB", CA, CB, noA, noB, False), ("ajib_BB", CB, CB, noB, noB, False),
+                                       ("ajbi_BB", CB, CB, noB, noB, True)):
+        occ1, vrt1, occ3, vrt3 = C1[:, :o1], C1[:, o1:], C3[:, :o3], C3[:, o3:]
+        if not ajbi:
+            Om = ao2mo(XX, vrt1, occ1, occ3, vrt3)       # Om[a, i, j, b]
+            recs = [Om[:, :, j, b].flatten(order="F") for j in range(o3) for b in range(vrt3.shape[1])]
+        else:
+            Om = ao2mo(XX, vrt1, vrt1, occ3, occ3)       # Om[a, b, j, i]
+            recs = [Om[:, b, j, :].flatten(order="F") for j in range(o3) for b in range(vrt1.shape[1])]
+        out[name] = recs
+    return out
 
 
 def mp2_rhf(eig: np.ndarray, Om: np.ndarray):

@@ -59,3 +59,66 @@ def test_stage_chain(tmp_path, ftab, basis_text, name):
     (tmp_path / "error").write_text("")
     r = subprocess.run([os.path.join(BINDIR, "scf")], cwd=str(tmp_path), capture_output=True, text=True)
     assert r.returncode == 0 and "STARTING SCF" not in r.stdout
+
+
+def test_cis_blocks(tmp_path, ftab, basis_text):
+    """UHF CIS integral files of the ao2mo stage (EXCITE= CIS, CALC= SCF) on the
+    reference's OH example: every record of ajib_AA, ajbi_AA, ajib_AB, ajib_BB
+    and ajbi_BB against the oracle's restatement of slow_ao2mo_CIS_UHF, applied
+    to the XX and Cui files the earlier stages wrote (the orbitals' signs are
+    the scf stage's own).  A CIS request on an RHF reference fails as the
+    reference does."""
+    zt = open(golden("zmat", "OH.ZMAT")).read()
+    sysm = formats.parse_zmat_text(zt)
+    assert sysm.options[13] == 1 and sysm.options[1] == 0 and sysm.options[3] == 1
+    sysm.options[8] = 10
+    formats.write_env(sysm, str(tmp_path))
+    shutil.copy(golden("mybasis"), tmp_path / "mybasis")
+    shutil.copy(golden("Ftab"), tmp_path / "Ftab")
+    for s in ("int1e", "int2e", "scf", "ao2mo"):
+        _run(s, str(tmp_path))
+    n = int(formats.read_text_numbers(str(tmp_path / "basinfo"))[1])
+    XX = np.frombuffer(formats.read_records(str(tmp_path / "XX"))[0], "<f8").reshape((n,) * 4, order="F")
+    C = formats.read_text_numbers(str(tmp_path / "Cui"))
+    CA, CB = C[:n * n].reshape(n, n, order="F"), C[n * n:2 * n * n].reshape(n, n, order="F")
+    ref = O.cis_records(XX, CA, CB, sysm.nelcA, sysm.nelcB)
+    for name, recs in ref.items():
+        got = formats.read_records(str(tmp_path / name))
+        assert len(got) == len(recs), name
+        for g, r in zip(got, recs):
+            g = np.frombuffer(g, "<f8")
+            assert g.shape == r.shape and np.max(np.abs(g - r)) < 1e-12, name
+    # RHF reference: the reference's ao2mo stops with an error
+    sysm.options[3] = 0
+    formats.write_env(sysm, str(tmp_path))
+    r = subprocess.run([os.path.join(BINDIR, "ao2mo")], cwd=str(tmp_path), capture_output=True, text=True)
+    assert r.returncode != 0 and (tmp_path / "error").exists()
+
+
+def test_props_dipole(tmp_path, ftab, basis_text):
+    """PROP= first on an SCF of HF: the props stage (int1p, then cphf) after int1e,
+    int2e and scf prints the dipole moment of cphf_dipole_rhf, computed from the
+    Pxuv and Da files; it matches the oracle's dipole integrals contracted with
+    the oracle's SCF density (1e-8), and Pxuv matches the oracle's integrals."""
+    zt = open(golden("zmat", "HF.ZMAT")).read()
+    sysm = formats.parse_zmat_text(zt)
+    sysm.options[8] = 10
+    sysm.options[1] = 0
+    sysm.options[16] = 1
+    formats.write_env(sysm, str(tmp_path))
+    shutil.copy(golden("mybasis"), tmp_path / "mybasis")
+    shutil.copy(golden("Ftab"), tmp_path / "Ftab")
+    out = "".join(_run(s, str(tmp_path)) for s in ("int1e", "int2e", "scf", "props"))
+    ref = O.run_job(zt, basis_text, ftab, 0, conv_exp=10)
+    mol = ref["mol"]
+    P = O.int1p(mol, ref["basis"], 0)
+    n = P.shape[1]
+    Pf = formats.read_text_numbers(str(tmp_path / "Pxuv"))
+    assert np.max(np.abs(Pf.reshape(3, n * n) - P.reshape(3, n, n).transpose(0, 2, 1).reshape(3, n * n))) < 1e-11
+    mu = O.dipole_moment(P, O.density(ref["scf"].C, mol.nelcA, 2.0), mol)
+    m = re.search(r"X\s+Y\s+Z\s*\n\s*(-?\d+\.\d+)\s+(-?\d+\.\d+)\s+(-?\d+\.\d+)", out)
+    assert m, out[-1500:]
+    got = np.array([float(g) for g in m.groups()])
+    assert np.max(np.abs(got - mu)) < 2e-6, (got, mu)  # printed with 6 decimals (F15.6)
+    Da = np.frombuffer(formats.read_records(str(tmp_path / "Da"))[0], "<f8").reshape(n, n, order="F")
+    assert np.max(np.abs(O.dipole_moment(P, Da, mol) - mu)) < 1e-8

@@ -41,6 +41,9 @@ def test_integrals(ctx, ftab, basis_text, name, mode):
     So, Ho = O.int1e(mol, ob, ftab, mode)
     assert np.max(np.abs(S - So)) < 1e-11
     assert np.max(np.abs(H - Ho)) < 1e-10
+    # dipole integrals (int1p)
+    P = ctx.int1p()
+    assert np.max(np.abs(P - O.int1p(mol, ob, mode))) < 1e-11
     XX = ctx.eri_full()
     XXo = O.int2e(mol, ob, ftab, mode)
     assert np.max(np.abs(XX - XXo)) < 1e-10

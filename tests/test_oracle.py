@@ -115,3 +115,54 @@ def test_bf16_rounding():
     assert r[0] == 1.0 and r[1] == 1.0  # halfway between 1 and 1 + 2^-7: ties to even
     assert r[2] == 1.0 + 2 ** -7  # 1.5 BF16 ulp above 1 rounds up to the even neighbour
     assert abs(r[3] + 3.140625) < 1e-12 and r[4] == 0.0
+
+
+def test_cis_records_layout(ftab, basis_text):
+    """The oracle's UHF CIS integral files (slow_ao2mo_CIS_UHF) on the reference's
+    OH example: record counts and lengths per file, (ai|jb) symmetric under
+    (ai) <-> (jb) in the same-spin files, and the ajbi records equal to
+    (ab|ji) assembled from the oracle's own transform."""
+    zt = open(golden("zmat", "OH.ZMAT")).read()
+    ref = O.run_job(zt, basis_text, ftab, 0, conv_exp=8)
+    mol, XX, C = ref["mol"], ref["XX"], ref["scf"].C
+    n, noA, noB = XX.shape[0], mol.nelcA, mol.nelcB
+    nvA, nvB = n - noA, n - noB
+    r = O.cis_records(XX, C[0], C[1], noA, noB)
+    shapes = {"ajib_AA": (noA * nvA, noA * nvA), "ajbi_AA": (noA * nvA, noA * nvA),
+              "ajib_AB": (noB * nvB, noA * nvA), "ajib_BB": (noB * nvB, noB * nvB), "ajbi_BB": (noB * nvB, noB * nvB)}
+    for name, (nrec, ln) in shapes.items():
+        assert len(r[name]) == nrec and all(v.shape == (ln,) for v in r[name]), name
+    for name, no, nv in (("ajib_AA", noA, nvA), ("ajib_BB", noB, nvB)):
+        M = np.array(r[name]).reshape(no, nv, no, nv)        # [j, b, i, a]
+        assert np.max(np.abs(M - M.transpose(2, 3, 0, 1))) < 1e-13
+    vrt, occ = C[0][:, noA:], C[0][:, :noA]
+    Om = O.ao2mo(XX, vrt, vrt, occ, occ)                     # Om[a, b, j, i] = (ab|ji)
+    rec = r["ajbi_AA"][noA * nvA - 1]                         # j = noA-1, b = nvA-1
+    assert np.allclose(rec, Om[:, nvA - 1, noA - 1, :].flatten(order="F"), rtol=0, atol=1e-15)
+
+
+def test_dipole_integrals(ftab, basis_text):
+    """The oracle's restatement of int1p (dipole integrals) and cphf_dipole_rhf:
+    Px symmetric; moving every centre by t moves the integrals by t S exactly as
+    x -> x + t does; the dipole of a neutral molecule does not depend on the
+    origin; CO2 and H2 (centrosymmetric, centred by the parser) have none."""
+    for name in ("HF", "CO2", "H2"):
+        zt = open(golden("zmat", name + ".ZMAT")).read()
+        ref = O.run_job(zt, basis_text, ftab, 0, conv_exp=10)
+        mol, basis = ref["mol"], ref["basis"]
+        P = O.int1p(mol, basis, 0)
+        assert np.max(np.abs(P - P.transpose(0, 2, 1))) < 1e-15
+        D = O.density(ref["scf"].C, mol.nelcA, 2.0)
+        mu = O.dipole_moment(P, D, mol)
+        t = np.array([0.3, -1.1, 0.7])
+        moved = O.Molecule(atoms=mol.atoms, xyz=np.asarray(mol.xyz) + t, nelcA=mol.nelcA, nelcB=mol.nelcB,
+                           options=mol.options)
+        P2 = O.int1p(moved, basis, 0)
+        S = ref["S"]
+        for c in range(3):
+            assert np.max(np.abs(P2[c] - (P[c] + t[c] * S))) < 1e-12
+        assert np.max(np.abs(O.dipole_moment(P2, D, moved) - mu)) < 1e-10
+        if name in ("CO2", "H2"):
+            assert np.max(np.abs(mu)) < 1e-10
+        else:
+            assert abs(mu[2]) > 0.1
