@@ -20,10 +20,13 @@
 // The four steps use the integral symmetry (uv|ld) = (dl|uv) = (vu|ld) so that
 // XX itself is the first step's K-major A and each epilogue writes the next
 // step's A with coalesced stores:
-//   1  Y1[b][(l,u,v)]   = sum_d XX(d,l,u,v) Cb(d,b)       A1 rows (l,u,v), K = d
-//   2  Y2[j,b][(u,v)]   = sum_l Y1[b][(l,u,v)] Cj(l,j)     A2 rows (u,v),   K = l
+//   1  Y1[b][(l,p)]     = sum_d XX(d,l,u,v) Cb(d,b)       A1 rows (l,p),   K = d
+//   2  Y2[j,b][p]       = sum_l Y1[b][(l,p)] Cj(l,j)       A2 rows p,       K = l
 //   3  Y3[a,j,b][v]     = sum_u Y2[j,b][(u,v)] Ca(u,a)     A3 rows v,       K = u
 //   4  Om(i,a,j,b)      = sum_v Y3[a,j,b][v] Ci(v,i)       A4 rows (a,j,b), K = v
+// where p runs over the AO pairs u <= v only ((uv|ld) = (vu|ld)): steps 1 and
+// 2 do half the rows, and step 3's slicing reads (u,v) and (v,u) from the same
+// packed element of Y2.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
@@ -323,22 +326,53 @@ __device__ __forceinline__ void load_chunk(const T *__restrict__ x, int k0, int 
   }
 }
 
-template <int S, class T, int H>
+// Where row r of a sliced operand comes from (RowSrc):
+//   ROW_PLAIN  in + r * ld;
+//   ROW_PAIRS  rows (l, p) of XX restricted to the pairs p = (u <= v): source row
+//              l + n (u + n v) of XX (rows of n values), l = r mod n;
+//   ROW_SYMM   row (v, jb) of the pair-packed Y2: element u is
+//              in[jb * npairs + pidx(min(u, v), max(u, v))], pidx(u, v) = u + v (v + 1) / 2.
+enum { ROW_PLAIN = 0, ROW_PAIRS = 1, ROW_SYMM = 2 };
+struct RowSrc {
+  const int2 *pairs;  // (u, v) of each pair p, u <= v
+  long long n, npairs;
+};
+
+template <int S, class T, int H, int MODE>
 __global__ void __launch_bounds__(256, 4) slice_rows_kernel(const T *__restrict__ in, long long rows, int kvalid,
                                                          long long ld, int Kp, long long plane, bf16 *__restrict__ out,
-                                                         int *__restrict__ e, int vec) {
+                                                         int *__restrict__ e, int vec, RowSrc rs) {
   const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
   const int lane = threadIdx.x & 31;
   const int nchunk = Kp >> 3;
   for (long long r = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); r < rows; r += warps) {
     const T *x = in + r * ld;
+    long long jb = 0;
+    int vrow = 0;
+    if (MODE == ROW_PAIRS) {
+      const long long pidx = r / rs.n;
+      const int2 uv = rs.pairs[pidx];
+      x = in + ((r - pidx * rs.n) + rs.n * (uv.x + rs.n * (long long)uv.y)) * ld;
+    } else if (MODE == ROW_SYMM) {
+      jb = r / rs.n;
+      vrow = (int)(r - jb * rs.n);
+      x = in + jb * rs.npairs;
+    }
     T v[H][8];
     int emax = 0;
 #pragma unroll
     for (int h = 0; h < H; ++h) {
       const int c = lane + 32 * h;
       if (c < nchunk) {
-        load_chunk(x, 8 * c, kvalid, vec != 0, v[h]);
+        if (MODE == ROW_SYMM) {
+#pragma unroll
+          for (int j = 0; j < 8; ++j) {
+            const int u = 8 * c + j, lo = min(u, vrow), hi = max(u, vrow);
+            v[h][j] = u < kvalid ? __ldg(x + lo + (long long)hi * (hi + 1) / 2) : (T)0;
+          }
+        } else {
+          load_chunk(x, 8 * c, kvalid, vec != 0, v[h]);
+        }
 #pragma unroll
         for (int j = 0; j < 8; ++j) emax = max(emax, exp_field(v[h][j]));
       }
@@ -435,22 +469,40 @@ static int slice_gemm(mq_ctx *c, Sliced A, long long M, int batch, long long a_b
   return sync_check(c, "slice_gemm");
 }
 
-template <int S, class T>
-static int slice_rows(mq_ctx *c, const T *in, long long rows, int kvalid, long long ld, int Kp, Sliced o) {
+template <int S, int MODE = ROW_PLAIN, class T>
+static int slice_rows(mq_ctx *c, const T *in, long long rows, int kvalid, long long ld, int Kp, Sliced o,
+                      RowSrc rs = RowSrc{nullptr, 1, 0}) {
   if (Kp % 8 || Kp > 512) return set_err(c, MQ_EINVAL, "slice_rows: Kp must be a multiple of 8 up to 512");
   const int tb = 256;
   const long long blocks = std::max<long long>(1, std::min<long long>((rows + 7) / 8, 1 << 20));
   const int per16 = 16 / (int)sizeof(T);
-  const int vec = ((uintptr_t)in % 16 == 0) && (ld % per16 == 0) && (kvalid % per16 == 0);
+  const int vec = MODE != ROW_SYMM && ((uintptr_t)in % 16 == 0) && (ld % per16 == 0) && (kvalid % per16 == 0);
   if (Kp <= 256)
-    slice_rows_kernel<S, T, 1><<<(unsigned)blocks, tb, 0, c->stream>>>(in, rows, kvalid, ld, Kp, o.plane, o.base, o.e,
-                                                                       vec);
+    slice_rows_kernel<S, T, 1, MODE><<<(unsigned)blocks, tb, 0, c->stream>>>(in, rows, kvalid, ld, Kp, o.plane,
+                                                                             o.base, o.e, vec, rs);
   else
-    slice_rows_kernel<S, T, 2><<<(unsigned)blocks, tb, 0, c->stream>>>(in, rows, kvalid, ld, Kp, o.plane, o.base, o.e,
-                                                                       vec);
+    slice_rows_kernel<S, T, 2, MODE><<<(unsigned)blocks, tb, 0, c->stream>>>(in, rows, kvalid, ld, Kp, o.plane,
+                                                                             o.base, o.e, vec, rs);
   c->stats.launches += 1;
   MQ_CUDA(c, cudaGetLastError());
   return sync_check(c, "slice_rows");
+}
+
+// (u, v) of every AO pair u <= v at p = u + v (v + 1) / 2
+__global__ void pair_table_kernel(int n, int2 *__restrict__ pairs) {
+  const int u = blockIdx.x * blockDim.x + threadIdx.x, v = blockIdx.y;
+  if (u <= v && v < n) pairs[u + (long long)v * (v + 1) / 2] = make_int2(u, v);
+}
+
+static int pair_table(mq_ctx *c, int n, const int2 **out) {
+  const long long np = (long long)n * (n + 1) / 2;
+  int2 *d = (int2 *)buf(c, "ao2mo_pairs", np * sizeof(int2));
+  if (!d) return MQ_ENOMEM;
+  pair_table_kernel<<<dim3((n + 127) / 128, n), 128, 0, c->stream>>>(n, d);
+  c->stats.launches += 1;
+  MQ_CUDA(c, cudaGetLastError());
+  *out = d;
+  return MQ_OK;
 }
 
 template <int S>
@@ -487,32 +539,40 @@ static int ao2mo_slices(mq_ctx *c, const double *Ci, int no1, const double *Ca, 
   MQ_TRY(slice_rows<S>(c, Cb, nv2, (int)n, n, Kp, Bb));
   GemmArgs g{};
   g.err = err;
-  // 1: XX(d,l,u,v) at d + n*((l,u,v)): rows (l,u,v), K = d -> Y1[b][(u,v)][l]
+  // (uv|ld) = (vu|ld): the first two steps run over the AO pairs p = (u <= v)
+  // only, half of the rows; the third reads (u, v) and (v, u) from the same
+  // packed element.
+  const long long np = n * (n + 1) / 2, rXp = n * np;
+  const int2 *pairs = nullptr;
+  MQ_TRY(pair_table(c, (int)n, &pairs));
+  const RowSrc rs{pairs, n, np};
+  // 1: XX(d,l,u,v) at d + n*((l,u,v)): rows (l,p), K = d -> Y1[b][p][l]
   // (already sliced on the side stream when the SCF prefetched it)
   Sliced A{pa, rX * Kp, ea};
-  if (c->xx_sliced != S) MQ_TRY(slice_rows<S>(c, c->d_XX, rX, (int)n, n, Kp, A));
+  if (c->xx_sliced != S) MQ_TRY((slice_rows<S, ROW_PAIRS>(c, c->d_XX, rXp, (int)n, n, Kp, A, rs)));
   c->xx_sliced = 0;  // step 2 overwrites the slices
   g.out_f64 = 0;
   g.out32 = y1;
   g.mdiv = n;
   g.s_m0 = 1;
   g.s_m1 = Kp;
-  g.s_n = n2 * Kp;
+  g.s_n = np * Kp;
   g.s_b = 0;
-  MQ_TRY(slice_gemm<S>(c, A, rX, 1, 0, Bb, nv2, Kp, g));
-  // 2: batch b; rows m = u + n*v, K = l -> Y2[j,b][v][u]
-  A = Sliced{pa, r1 * Kp, ea};
-  MQ_TRY(slice_rows<S>(c, y1, r1, (int)n, Kp, Kp, A));
+  MQ_TRY(slice_gemm<S>(c, A, rXp, 1, 0, Bb, nv2, Kp, g));
+  // 2: batch b; rows p, K = l -> Y2[j,b][p] (packed pairs)
+  const long long r1p = (long long)nv2 * np;
+  A = Sliced{pa, r1p * Kp, ea};
+  MQ_TRY(slice_rows<S>(c, y1, r1p, (int)n, Kp, Kp, A));
   g.out32 = y2;
-  g.mdiv = n;
+  g.mdiv = 1ll << 62;
   g.s_m0 = 1;
-  g.s_m1 = Kp;
-  g.s_n = n * Kp;
-  g.s_b = (long long)no2 * n * Kp;
-  MQ_TRY(slice_gemm<S>(c, A, n2, nv2, n2 * Kp, Bj, no2, Kp, g));
-  // 3: batch (j + no2*b); rows v, K = u -> Y3[a + nv1*(j + no2*b)][v]
+  g.s_m1 = 0;
+  g.s_n = np;
+  g.s_b = (long long)no2 * np;
+  MQ_TRY(slice_gemm<S>(c, A, np, nv2, np * Kp, Bj, no2, Kp, g));
+  // 3: batch (j + no2*b); rows v, K = u (gathered from the packed pairs) -> Y3[a + nv1*(j + no2*b)][v]
   A = Sliced{pa, r2 * Kp, ea};
-  MQ_TRY(slice_rows<S>(c, y2, r2, (int)n, Kp, Kp, A));
+  MQ_TRY((slice_rows<S, ROW_SYMM>(c, y2, r2, (int)n, 0, Kp, A, rs)));
   g.out32 = y1;  // Y1 is dead
   g.mdiv = 1ll << 62;
   g.s_m0 = 1;
@@ -566,11 +626,15 @@ static int preslice(mq_ctx *c) {
     MQ_CUDA(c, cudaEventCreateWithFlags(&c->ev_main, cudaEventDisableTiming));
     MQ_CUDA(c, cudaEventCreateWithFlags(&c->ev_side, cudaEventDisableTiming));
   }
+  const long long np = n * (n + 1) / 2;
+  const int2 *pairs = nullptr;
+  MQ_TRY(pair_table(c, (int)n, &pairs));  // on the main stream, before the event below
   MQ_CUDA(c, cudaEventRecord(c->ev_main, c->stream));
   MQ_CUDA(c, cudaStreamWaitEvent(c->side, c->ev_main, 0));
   cudaStream_t main = c->stream;
   c->stream = c->side;  // slice_rows launches on c->stream
-  const int rc = slice_rows<S>(c, c->d_XX, rX, (int)n, n, Kp, Sliced{pa, rX * Kp, ea});
+  const int rc = slice_rows<S, ROW_PAIRS>(c, c->d_XX, n * np, (int)n, n, Kp, Sliced{pa, rX * Kp, ea},
+                                          RowSrc{pairs, n, np});
   c->stream = main;
   MQ_TRY(rc);
   MQ_CUDA(c, cudaEventRecord(c->ev_side, c->side));

@@ -77,8 +77,9 @@ def test_cis_blocks(tmp_path, ftab, basis_text):
     shutil.copy(golden("Ftab"), tmp_path / "Ftab")
     for s in ("int1e", "int2e", "scf", "ao2mo"):
         _run(s, str(tmp_path))
-    n = int(formats.read_text_numbers(str(tmp_path / "basinfo"))[1])
-    XX = np.frombuffer(formats.read_records(str(tmp_path / "XX"))[0], "<f8").reshape((n,) * 4, order="F")
+    XX = np.frombuffer(formats.read_records(str(tmp_path / "XX"))[0], "<f8")
+    n = int(round(XX.size ** 0.25))
+    XX = XX.reshape((n,) * 4, order="F")
     C = formats.read_text_numbers(str(tmp_path / "Cui"))
     CA, CB = C[:n * n].reshape(n, n, order="F"), C[n * n:2 * n * n].reshape(n, n, order="F")
     ref = O.cis_records(XX, CA, CB, sysm.nelcA, sysm.nelcB)
