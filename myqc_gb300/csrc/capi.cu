@@ -112,9 +112,12 @@ int mq_init(mq_ctx **ctx, int device) {
   mq_ctx *c = new mq_ctx();
   c->device = device;
   if (const char *e = getenv("MYQC_DGEMM")) c->dgemm_cublas = !strcmp(e, "cublas");
-  int prio_lo = 0, prio_hi = 0;  // the main stream outranks the side stream's overlapping work
+  // priorities (lower is higher): the aux stream's short network passes, then
+  // the main stream, then the side stream's overlapping slicing
+  int prio_lo = 0, prio_hi = 0;
   cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
-  if (cudaStreamCreateWithPriority(&c->stream, cudaStreamNonBlocking, prio_hi) != cudaSuccess) {
+  const int prio_main = prio_hi < prio_lo ? prio_hi + 1 : prio_hi;
+  if (cudaStreamCreateWithPriority(&c->stream, cudaStreamNonBlocking, prio_main) != cudaSuccess) {
     delete c;
     return MQ_ECUDA;
   }
@@ -126,6 +129,7 @@ int mq_free(mq_ctx *c) {
   if (!c) return MQ_OK;
   cudaSetDevice(c->device);
   if (c->side) cudaStreamSynchronize(c->side);
+  if (c->aux) cudaStreamSynchronize(c->aux);
   cudaStreamSynchronize(c->stream);
   free_pairs(c);
   batch_clear(c);
@@ -141,6 +145,9 @@ int mq_free(mq_ctx *c) {
   if (c->pin) cudaFreeHost(c->pin);
   cudaStreamDestroy(c->stream);
   if (c->side) cudaStreamDestroy(c->side);
+  if (c->aux) cudaStreamDestroy(c->aux);
+  if (c->ev_params) cudaEventDestroy(c->ev_params);
+  if (c->ev_early) cudaEventDestroy(c->ev_early);
   if (c->ev_main) cudaEventDestroy(c->ev_main);
   if (c->ev_side) cudaEventDestroy(c->ev_side);
   delete c;
@@ -663,6 +670,7 @@ int mq_stat(const mq_ctx *c, const char *key, double *value) {
   else if (!strcmp(key, "eig_jacobi_sweeps")) *value = s.eig_jacobi_sweeps;
   else if (!strcmp(key, "fock_precision")) *value = c->fock_df32;
   else if (!strcmp(key, "fock_inc_builds")) *value = s.fock_inc_builds;
+  else if (!strcmp(key, "eig_early")) *value = s.eig_early;
   else if (!strcmp(key, "fock_kernel")) *value = s.ms_fock_kernel;
   else if (!strcmp(key, "fock_kernel_launches")) *value = s.fock_kernel_launches;
   else if (!strcmp(key, "tune_fock_ms")) *value = s.tune_fock_ms;

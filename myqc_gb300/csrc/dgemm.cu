@@ -115,7 +115,10 @@ int dgemm_small(mq_ctx *c, char ta, char tb, int m, int n, int k, double alpha, 
   splits = (k + kchunk - 1) / kchunk;
   double *W = nullptr;
   if (splits > 1) {
-    W = (double *)buf(c, "dgemm_split", (size_t)splits * m * n * sizeof(double));
+    // products queued on the aux stream (an eigensolve overlapping the SCF)
+    // keep their own partial sums
+    W = (double *)buf(c, c->aux && c->stream == c->aux ? "dgemm_split_aux" : "dgemm_split",
+                      (size_t)splits * m * n * sizeof(double));
     if (!W) return MQ_ENOMEM;
   }
   const dim3 grid(tiles, splits);

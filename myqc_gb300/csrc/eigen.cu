@@ -315,19 +315,22 @@ __global__ void __launch_bounds__(RF_THREADS) first_order_kernel(int n, const do
   }
 }
 
-int syev_large_cold(mq_ctx *c, int n, double *d_A, double *d_w, double *d_V) {
-  if (n > CJ_MAX || n <= JAC_SMEM_MAX) return syev_large_device(c, n, d_A, nullptr, d_w, d_V);
+int syev_large_cold(mq_ctx *c, int n, double *d_A, double *d_w, double *d_V, bool async) {
+  if (n > CJ_MAX || n <= JAC_SMEM_MAX) return syev_large_device(c, n, d_A, nullptr, d_w, d_V, async);
   const size_t n2 = (size_t)n * n;
   double *ws = (double *)buf(c, "eig_refine", 3 * n2 * sizeof(double) + 64);
   if (!ws) return MQ_ENOMEM;
   double *G = ws, *T = ws + n2, *E = ws + 2 * n2;
   int *info = (int *)(ws + 3 * n2);
-  StageTimer t1, t2, t3;
-  t1.start(c->stream);
-  if (jacobi_cluster_f32(c, n, d_A, d_V, info) != MQ_OK) return syev_large_device(c, n, d_A, nullptr, d_w, d_V);
+  StageTimer t1, t2, t3;  // not used by an async solve (they would need a synchronisation)
+  if (!async) t1.start(c->stream);
+  if (jacobi_cluster_f32(c, n, d_A, d_V, info) != MQ_OK)
+    return syev_large_device(c, n, d_A, nullptr, d_w, d_V, async);
   MQ_CUDA(c, cudaGetLastError());
-  t1.stop(c->stream);
-  t2.start(c->stream);
+  if (!async) {
+    t1.stop(c->stream);
+    t2.start(c->stream);
+  }
   double *X = d_V;
   auto bjorck = [&]() -> int {  // X <- X (3 I - X^T X) / 2
     MQ_TRY(gemm(c, 'T', 'N', n, n, n, 1.0, X, n, X, n, 0.0, G, n));
@@ -354,6 +357,7 @@ int syev_large_cold(mq_ctx *c, int n, double *d_A, double *d_w, double *d_V) {
   MQ_TRY(gemm(c, 'N', 'N', n, n, n, 1.0, d_A, n, X, n, 0.0, T, n));
   MQ_TRY(gemm(c, 'T', 'N', n, n, n, 1.0, X, n, T, n, 0.0, d_A, n));
   MQ_CUDA(c, cudaGetLastError());
+  if (async) return syev_large_device(c, n, d_A, d_V, d_w, d_V, true);
   t2.stop(c->stream);
   t3.start(c->stream);
   MQ_TRY(syev_large_device(c, n, d_A, d_V, d_w, d_V));

@@ -103,6 +103,7 @@ struct Stats {
   double eig_f32_sweeps = 0, eig_f32_off = 0, ms_eig_f32 = 0, ms_eig_refine = 0, ms_eig_jacobi = 0;
   double eig_jacobi_sweeps = 0;
   double fock_inc_builds = 0;  // FP32 incremental builds of the last SCF
+  double eig_early = 0;        // 1: the last SCF's final eigensolve started from its early eigensolve
 };
 
 // Event pair on the context's stream that adds its elapsed time to a counter
@@ -151,6 +152,12 @@ struct mq_ctx {
   cudaStream_t side = nullptr;
   cudaEvent_t ev_main = nullptr, ev_side = nullptr;
   int side_pending = 0;
+  // aux stream (highest priority) for the learned guess's network forward
+  // pass, so that it does not queue behind the integral pass on the main
+  // stream; ev_params marks the last write of the network's parameters
+  cudaStream_t aux = nullptr;
+  cudaEvent_t ev_params = nullptr;
+  cudaEvent_t ev_early = nullptr;  // the SCF's early eigensolve on the aux stream
   int ao2mo_prefetch = 0;  // planes (2, 3) to slice XX into ahead of the transform; 0: off
   int xx_sliced = 0;       // the slice buffers hold XX cut into this many planes (0: not)
   void *cublas = nullptr;
@@ -304,10 +311,16 @@ constexpr int JAC_SMEM_MAX = 110;  // largest order whose A and V (2 n^2 doubles
 int syev_batched_device(mq_ctx *c, int n, int batch, double *d_A, double *d_w, double *d_V);
 // one matrix of order n > JAC_SMEM_MAX on all SMs; d_V0 (optional) are start
 // vectors and d_A must then already be V0^T A V0
-int syev_large_device(mq_ctx *c, int n, double *d_A, const double *d_V0, double *d_w, double *d_V);
+int syev_large_device(mq_ctx *c, int n, double *d_A, const double *d_V0, double *d_w, double *d_V,
+                      bool async = false);
+// after an async syev_large_device/cold solve has finished: its status (0 ok,
+// MQ_ETIMEOUT, MQ_ENOCONV), read from the solver's workspace on c->stream
+int syev_large_status(mq_ctx *c);
 // one matrix of order n > JAC_SMEM_MAX without start vectors: FP32 Jacobi on a
 // thread-block cluster, FP64 refinement, then syev_large_device (eigen.cu)
-int syev_large_cold(mq_ctx *c, int n, double *d_A, double *d_w, double *d_V);
+// async: queue everything on c->stream and return without reading anything
+// back (no host synchronisation); syev_large_status then gives the outcome
+int syev_large_cold(mq_ctx *c, int n, double *d_A, double *d_w, double *d_V, bool async = false);
 // small FP64 products on all SMs (dgemm.cu); gemm() takes them when they fit
 bool dgemm_small_fits(int m, int n, int k);
 int dgemm_small(mq_ctx *c, char ta, char tb, int m, int n, int k, double alpha, const double *A, int lda,

@@ -219,7 +219,7 @@ __global__ void set_identity_kernel(double *V, int n) {
 
 // One large matrix: A (n x n, device, overwritten), optional start vectors V0
 // (A must then already be V0^T A V0), eigenvalues w, eigenvectors Vout.
-int syev_large_device(mq_ctx *c, int n, double *d_A, const double *d_V0, double *d_w, double *d_V) {
+int syev_large_device(mq_ctx *c, int n, double *d_A, const double *d_V0, double *d_w, double *d_V, bool async) {
   const size_t n2 = (size_t)n * n;
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
@@ -246,9 +246,17 @@ int syev_large_device(mq_ctx *c, int n, double *d_A, const double *d_V0, double 
   MQ_CUDA(c, cudaLaunchCooperativeKernel((void *)jacobi_grid_kernel, dim3(nblocks), dim3(JG_THREADS), args, 0,
                                          c->stream));
   c->stats.launches += 2;
+  if (async) return MQ_OK;
+  return syev_large_status(c);
+}
+
+int syev_large_status(mq_ctx *c) {
+  auto it = c->bufs.find("jacobi_grid");
+  if (it == c->bufs.end() || !it->second.ptr) return MQ_OK;  // no grid solve ran
+  const char *ws = (const char *)it->second.ptr;
   int h = 0, sw = 0;
-  MQ_CUDA(c, cudaMemcpyAsync(&h, gs.err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-  MQ_CUDA(c, cudaMemcpyAsync(&sw, info, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  MQ_CUDA(c, cudaMemcpyAsync(&h, ws + 128, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  MQ_CUDA(c, cudaMemcpyAsync(&sw, ws + 192, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   MQ_CUDA(c, cudaStreamSynchronize(c->stream));
   c->stats.eig_jacobi_sweeps = sw;
   if (h == 2) return set_err(c, MQ_ETIMEOUT, "Jacobi grid barrier timed out");

@@ -409,6 +409,8 @@ struct Mlp {
 
 static Mlp *mlp_of(mq_ctx *c) { return (Mlp *)c->mlp; }
 
+static int mark_params(mq_ctx *c);
+
 int mlp_init(mq_ctx *c, int nin, int width, int nout) {
   if (nin <= 0 || width <= 0 || nout <= 0 || width > 256 || nout > 256 || nin % 8)
     return set_err(c, MQ_EINVAL, "MLP sizes: width and nout <= 256, nin a multiple of 8");
@@ -447,7 +449,7 @@ int mlp_init(mq_ctx *c, int nin, int width, int nout) {
     m->Wt[l] = q;
     q += (size_t)m->d[l] * m->kp[l + 1];
   }
-  return MQ_OK;
+  return mark_params(c);  // the zeroed parameters
 }
 
 int mlp_param_count(mq_ctx *c) {
@@ -472,7 +474,7 @@ int mlp_set_params(mq_ctx *c, const float *h) {
   }
   c->stats.launches += 3;
   MQ_CUDA(c, cudaGetLastError());
-  return MQ_OK;
+  return mark_params(c);
 }
 
 int mlp_get_params(mq_ctx *c, float *h) {
@@ -670,10 +672,15 @@ static int upload_x(mq_ctx *c, Mlp *m, const float *X, int rows, Acts &a) {
   return MQ_OK;
 }
 
-int mlp_forward(mq_ctx *c, int rows, const float *X, float *Y) {
-  Mlp *m = mlp_of(c);
-  if (!m) return set_err(c, MQ_ESTATE, "no MLP (mq_mlp_init)");
-  if (rows <= 0) return MQ_OK;
+// Parameters written on the main stream: later forward passes on the aux
+// stream start after this point, not after the main stream's later work.
+static int mark_params(mq_ctx *c) {
+  if (!c->ev_params) MQ_CUDA(c, cudaEventCreateWithFlags(&c->ev_params, cudaEventDisableTiming));
+  MQ_CUDA(c, cudaEventRecord(c->ev_params, c->stream));
+  return MQ_OK;
+}
+
+static int forward_on_stream(mq_ctx *c, Mlp *m, int rows, const float *X, float *Y) {
   Acts a;
   MQ_TRY(acts_alloc(c, m, rows, a));
   MQ_TRY(upload_x(c, m, X, rows, a));
@@ -681,6 +688,28 @@ int mlp_forward(mq_ctx *c, int rows, const float *X, float *Y) {
   MQ_CUDA(c, cudaMemcpyAsync(Y, a.out, (size_t)rows * m->d[3] * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
   MQ_CUDA(c, cudaStreamSynchronize(c->stream));
   return MQ_OK;
+}
+
+// The forward pass runs on the aux stream (highest priority), ordered after
+// the last parameter write only: a guess evaluated while the integral pass is
+// queued on the main stream returns without waiting for it.  The network's
+// activation buffers are used by this call alone, which returns synchronised.
+int mlp_forward(mq_ctx *c, int rows, const float *X, float *Y) {
+  Mlp *m = mlp_of(c);
+  if (!m) return set_err(c, MQ_ESTATE, "no MLP (mq_mlp_init)");
+  if (rows <= 0) return MQ_OK;
+  if (!c->aux) {
+    int lo = 0, hi = 0;
+    MQ_CUDA(c, cudaDeviceGetStreamPriorityRange(&lo, &hi));
+    MQ_CUDA(c, cudaStreamCreateWithPriority(&c->aux, cudaStreamNonBlocking, hi));
+  }
+  if (!c->ev_params) MQ_TRY(mark_params(c));
+  MQ_CUDA(c, cudaStreamWaitEvent(c->aux, c->ev_params, 0));
+  cudaStream_t main = c->stream;
+  c->stream = c->aux;
+  const int rc = forward_on_stream(c, m, rows, X, Y);
+  c->stream = main;
+  return rc;
 }
 
 int mlp_grad(mq_ctx *c, int rows, const float *X, const float *T, const float *Wl, float *grads, double *loss) {
@@ -770,7 +799,7 @@ int mlp_train_epoch(mq_ctx *c, const int *perm, int batch, float lr, double *los
   }
   MQ_CUDA(c, cudaStreamSynchronize(c->stream));
   *loss = nb ? total / nb : 0.0;
-  return MQ_OK;
+  return mark_params(c);
 }
 
 void mlp_free(mq_ctx *c) {

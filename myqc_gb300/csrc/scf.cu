@@ -308,6 +308,57 @@ int scf_device(mq_ctx *c, const double *S, const double *H, const mq_scf_opts *o
   // stalls (degenerate frontier levels) falls back to the eigensolver, cold
   // started: the warm-start vectors in dU/dW are overwritten by its scratch.
   const bool purify = o->purify != 0;
+  // Early eigensolve (purification, RHF, JAC_SMEM_MAX < n): once the density
+  // changes by less than EARLY_EIG_RMS, the cold eigensolve of that
+  // iteration's Fock matrix is queued on the aux stream and overlaps the
+  // remaining iterations; the final eigensolve then starts from its vectors
+  // (a few FP64 Jacobi sweeps) instead of cold.  Its own buffers: the Fock
+  // copy, X^T F X, the vectors, the eigenvalues, a GEMM temporary.
+  constexpr double EARLY_EIG_RMS = 1e-5;
+  bool early = false;  // queued, not yet joined
+  double *dFe = nullptr, *dAe = nullptr, *dUe = nullptr, *dTe = nullptr, *dEe = nullptr;
+  auto join_early = [&](bool use) -> int {  // the main stream after the early solve; its vectors into dU when use
+    if (!early) return MQ_OK;
+    early = false;
+    MQ_CUDA(c, cudaStreamWaitEvent(c->stream, c->ev_early, 0));
+    cudaStream_t main = c->stream;
+    c->stream = c->aux;
+    const int st = syev_large_status(c);  // synchronises the aux stream
+    c->stream = main;
+    if (!use || st != MQ_OK) return MQ_OK;  // a failed early solve only costs the warm start
+    MQ_CUDA(c, cudaMemcpyAsync(dU, dUe, n2 * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+    have_prev = true;
+    c->stats.eig_early = 1;
+    return MQ_OK;
+  };
+  auto launch_early = [&](const double *Fm) -> int {
+    double *e = (double *)buf(c, "scf_early", sizeof(double) * (4 * n2 + n));
+    if (!e) return MQ_ENOMEM;
+    dFe = e;
+    dAe = e + n2;
+    dUe = e + 2 * n2;
+    dTe = e + 3 * n2;
+    dEe = e + 4 * n2;
+    if (!c->aux) {
+      int lo = 0, hi = 0;
+      MQ_CUDA(c, cudaDeviceGetStreamPriorityRange(&lo, &hi));
+      MQ_CUDA(c, cudaStreamCreateWithPriority(&c->aux, cudaStreamNonBlocking, hi));
+    }
+    if (!c->ev_early) MQ_CUDA(c, cudaEventCreateWithFlags(&c->ev_early, cudaEventDisableTiming));
+    MQ_CUDA(c, cudaMemcpyAsync(dFe, Fm, n2 * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+    MQ_CUDA(c, cudaEventRecord(c->ev_early, c->stream));
+    MQ_CUDA(c, cudaStreamWaitEvent(c->aux, c->ev_early, 0));
+    cudaStream_t main = c->stream;
+    c->stream = c->aux;
+    int rc = gemm(c, 'T', 'N', n, n, n, 1.0, dX, n, dFe, n, 0.0, dTe, n);
+    if (rc == MQ_OK) rc = gemm(c, 'N', 'N', n, n, n, 1.0, dTe, n, dX, n, 0.0, dAe, n);
+    if (rc == MQ_OK) rc = syev_large_cold(c, n, dAe, dEe, dUe, true);
+    if (rc == MQ_OK) rc = cuda_check(c, cudaEventRecord(c->ev_early, c->aux), "cudaEventRecord");
+    c->stream = main;
+    MQ_TRY(rc);
+    early = true;
+    return MQ_OK;
+  };
   auto density_step = [&](const double *Fm, double *Dout) -> int {
     if (purify) {
       bool ok = true;
@@ -326,6 +377,7 @@ int scf_device(mq_ctx *c, const double *S, const double *H, const mq_scf_opts *o
         MQ_TRY(gemm(c, 'N', 'N', n, n, n, occf, dT1, n, dX, n, 0.0, Dout + n2 * s, n));
       }
       if (ok) return MQ_OK;
+      MQ_TRY(join_early(false));  // the eigensolver's buffers are the early solve's too
       have_prev = false;
     }
     MQ_TRY(diagonalize(Fm));
@@ -374,8 +426,10 @@ int scf_device(mq_ctx *c, const double *S, const double *H, const mq_scf_opts *o
   // energy stays within ~1e-9 Eh of the full builds'
   const bool inc = !o->direct && c->fock_inc_tau > 0.0;
   bool have_prev_g = false;
-  double last_maxdiff = INFINITY;
+  double last_maxdiff = INFINITY, prev_rms = INFINITY;
+  bool early_done = false;
   c->stats.fock_inc_builds = 0;
+  c->stats.eig_early = 0;
   for (; it < max_iter && !conv; ++it) {
     // G[D_k]
     t_fock.start(c->stream);
@@ -441,6 +495,10 @@ int scf_device(mq_ctx *c, const double *S, const double *H, const mq_scf_opts *o
       }
       head = (head + 1) % ndiis;
     }
+    if (purify && !uhf && !early_done && n > JAC_SMEM_MAX && prev_rms < EARLY_EIG_RMS) {
+      MQ_TRY(launch_early(Fdiag));
+      early_done = true;
+    }
     t_diag.start(c->stream);
     MQ_TRY(density_step(Fdiag, dDn));
     t_diag.stop(c->stream);
@@ -457,6 +515,7 @@ int scf_device(mq_ctx *c, const double *S, const double *H, const mq_scf_opts *o
     E = hs[0] + (uhf ? hs[2] : 0.0) + enuc;
     const double diff = o->conv_rms ? hs[9] : hs[8];
     last_maxdiff = hs[8];  // max |D_{k+1} - D_k|: the next build's increment
+    prev_rms = hs[9];
     hist.push_back(E);
     hist.push_back(it > 0 ? diff : NAN);
     if (it > 0) conv = diff < thr;
@@ -473,6 +532,7 @@ int scf_device(mq_ctx *c, const double *S, const double *H, const mq_scf_opts *o
     StageTimer t_eig;
     t_eig.start(c->stream);
     have_prev = false;
+    MQ_TRY(join_early(true));  // warm start from the early eigensolve when there was one
     MQ_TRY(diagonalize(lastF));
     c->stats.diag_calls += 1;
     for (int s = 0; s < ns; ++s)
@@ -481,6 +541,7 @@ int scf_device(mq_ctx *c, const double *S, const double *H, const mq_scf_opts *o
     t_eig.collect_sync();
     c->stats.ms_eig_final = t_eig.total;
   }
+  MQ_TRY(join_early(false));  // (an SCF that ended without a final eigensolve)
   MQ_CUDA(c, cudaMemcpyAsync(C, dC, n2 * ns * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   MQ_CUDA(c, cudaMemcpyAsync(eps, dEps, (size_t)n * ns * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   if (D) MQ_CUDA(c, cudaMemcpyAsync(D, dD, n2 * ns * sizeof(double), cudaMemcpyDeviceToHost, c->stream));

@@ -341,3 +341,28 @@ def test_incremental_fock_builds(ctx, basis_text, uhf):
     finally:
         ctx.set_fock_incremental(0.0)
         ctx.set_fock_precision(FOCK_FP64)
+
+
+def test_purification_early_eigensolve(ctx, basis_text):
+    """(H2O)16 (n = 112, above the single-CTA Jacobi size): with purification the
+    cold eigensolve of a Fock matrix near convergence runs on a second stream
+    while the SCF finishes, and the final eigensolve starts from its vectors.
+    Energy, orbital energies and density match the eigensolver SCF; MP2 from
+    the final orbitals matches too."""
+    from myqc_gb300 import MODE_TIGHT, PREC_FP64, molecules
+    sysm = molecules.water_cluster_system(16, 7.6, 3)
+    basis = formats.parse_mybasis_text(basis_text, sysm.atoms)
+    ctx.set_schwarz(0.0)
+    ctx.set_system(sysm, basis, None, MODE_TIGHT)
+    S, H = ctx.int1e()
+    ctx.eri_store()
+    kw = dict(conv=1e-10, conv_rms=True, diis=8)
+    a = ctx.scf(S, H, sysm.nelcA, sysm.nelcB, **kw)
+    b = ctx.scf(S, H, sysm.nelcA, sysm.nelcB, purify=True, **kw)
+    assert ctx.stat("eig_early") == 1
+    assert abs(a.energy - b.energy) < 1e-10
+    assert np.max(np.abs(np.asarray(a.eig) - np.asarray(b.eig))) < 1e-8
+    assert np.max(np.abs(a.D - b.D)) < 1e-8
+    ea = ctx.mp2_rhf(a.eig, sysm.nelcA, PREC_FP64, C=a.C)["E_MP2"]
+    eb = ctx.mp2_rhf(b.eig, sysm.nelcA, PREC_FP64, C=b.C)["E_MP2"]
+    assert abs(ea - eb) < 1e-9, (ea, eb)
