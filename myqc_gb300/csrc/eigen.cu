@@ -315,22 +315,16 @@ __global__ void __launch_bounds__(RF_THREADS) first_order_kernel(int n, const do
   }
 }
 
-int syev_large_cold(mq_ctx *c, int n, double *d_A, double *d_w, double *d_V, bool async) {
-  if (n > CJ_MAX || n <= JAC_SMEM_MAX) return syev_large_device(c, n, d_A, nullptr, d_w, d_V, async);
+// Steps 2 and 3 from start vectors d_V that nearly diagonalise d_A (the FP32
+// cluster solve's, or a previous solve's): orthonormalise, two first-order
+// corrections, FP64 Jacobi cleanup.  d_A keeps the matrix until the last step.
+static int refine_from(mq_ctx *c, int n, double *d_A, double *d_w, double *d_V, bool async, StageTimer *t2,
+                       StageTimer *t3) {
   const size_t n2 = (size_t)n * n;
   double *ws = (double *)buf(c, "eig_refine", 3 * n2 * sizeof(double) + 64);
   if (!ws) return MQ_ENOMEM;
   double *G = ws, *T = ws + n2, *E = ws + 2 * n2;
-  int *info = (int *)(ws + 3 * n2);
-  StageTimer t1, t2, t3;  // not used by an async solve (they would need a synchronisation)
-  if (!async) t1.start(c->stream);
-  if (jacobi_cluster_f32(c, n, d_A, d_V, info) != MQ_OK)
-    return syev_large_device(c, n, d_A, nullptr, d_w, d_V, async);
-  MQ_CUDA(c, cudaGetLastError());
-  if (!async) {
-    t1.stop(c->stream);
-    t2.start(c->stream);
-  }
+  if (t2) t2->start(c->stream);
   double *X = d_V;
   auto bjorck = [&]() -> int {  // X <- X (3 I - X^T X) / 2
     MQ_TRY(gemm(c, 'T', 'N', n, n, n, 1.0, X, n, X, n, 0.0, G, n));
@@ -357,11 +351,38 @@ int syev_large_cold(mq_ctx *c, int n, double *d_A, double *d_w, double *d_V, boo
   MQ_TRY(gemm(c, 'N', 'N', n, n, n, 1.0, d_A, n, X, n, 0.0, T, n));
   MQ_TRY(gemm(c, 'T', 'N', n, n, n, 1.0, X, n, T, n, 0.0, d_A, n));
   MQ_CUDA(c, cudaGetLastError());
-  if (async) return syev_large_device(c, n, d_A, d_V, d_w, d_V, true);
-  t2.stop(c->stream);
-  t3.start(c->stream);
-  MQ_TRY(syev_large_device(c, n, d_A, d_V, d_w, d_V));
-  t3.stop(c->stream);
+  if (t2) t2->stop(c->stream);
+  if (t3) t3->start(c->stream);
+  MQ_TRY(syev_large_device(c, n, d_A, d_V, d_w, d_V, async));
+  if (t3) t3->stop(c->stream);
+  return MQ_OK;
+}
+
+int syev_large_warm(mq_ctx *c, int n, double *d_A, double *d_w, double *d_V) {
+  if (n > CJ_MAX || n <= JAC_SMEM_MAX) {  // the grid Jacobi from the start vectors: A <- V^T A V first
+    double *T = (double *)buf(c, "eig_warm", (size_t)n * n * sizeof(double));
+    if (!T) return MQ_ENOMEM;
+    MQ_TRY(gemm(c, 'T', 'N', n, n, n, 1.0, d_V, n, d_A, n, 0.0, T, n));
+    MQ_TRY(gemm(c, 'N', 'N', n, n, n, 1.0, T, n, d_V, n, 0.0, d_A, n));
+    return syev_large_device(c, n, d_A, d_V, d_w, d_V);
+  }
+  return refine_from(c, n, d_A, d_w, d_V, false, nullptr, nullptr);
+}
+
+int syev_large_cold(mq_ctx *c, int n, double *d_A, double *d_w, double *d_V, bool async) {
+  if (n > CJ_MAX || n <= JAC_SMEM_MAX) return syev_large_device(c, n, d_A, nullptr, d_w, d_V, async);
+  const size_t n2 = (size_t)n * n;
+  double *ws = (double *)buf(c, "eig_refine", 3 * n2 * sizeof(double) + 64);
+  if (!ws) return MQ_ENOMEM;
+  int *info = (int *)(ws + 3 * n2);
+  StageTimer t1, t2, t3;  // not used by an async solve (they would need a synchronisation)
+  if (!async) t1.start(c->stream);
+  if (jacobi_cluster_f32(c, n, d_A, d_V, info) != MQ_OK)
+    return syev_large_device(c, n, d_A, nullptr, d_w, d_V, async);
+  MQ_CUDA(c, cudaGetLastError());
+  if (async) return refine_from(c, n, d_A, d_w, d_V, true, nullptr, nullptr);
+  t1.stop(c->stream);
+  MQ_TRY(refine_from(c, n, d_A, d_w, d_V, false, &t2, &t3));
   int h[2] = {0, 0};
   MQ_CUDA(c, cudaMemcpyAsync(h, info, 2 * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   MQ_CUDA(c, cudaStreamSynchronize(c->stream));

@@ -321,6 +321,9 @@ int syev_large_status(mq_ctx *c);
 // async: queue everything on c->stream and return without reading anything
 // back (no host synchronisation); syev_large_status then gives the outcome
 int syev_large_cold(mq_ctx *c, int n, double *d_A, double *d_w, double *d_V, bool async = false);
+// from start vectors d_V of a nearby matrix: FP64 refinement by GEMMs (first-order
+// rotations of the separated pairs), then the FP64 Jacobi cleanup (eigen.cu)
+int syev_large_warm(mq_ctx *c, int n, double *d_A, double *d_w, double *d_V);
 // small FP64 products on all SMs (dgemm.cu); gemm() takes them when they fit
 bool dgemm_small_fits(int m, int n, int k);
 int dgemm_small(mq_ctx *c, char ta, char tb, int m, int n, int k, double alpha, const double *A, int lda,

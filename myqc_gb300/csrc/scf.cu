@@ -273,6 +273,7 @@ int scf_device(mq_ctx *c, const double *S, const double *H, const mq_scf_opts *o
   // orders start the Jacobi sweeps from the previous iteration's vectors:
   // A0 = U^T F' U is nearly diagonal once the SCF settles, so few sweeps remain.
   bool have_prev = false;
+  bool refine_prev = false;  // dU holds vectors of an earlier SCF iteration's Fock matrix (the early eigensolve)
   auto diagonalize = [&](const double *Fm) -> int {
     for (int s = 0; s < ns; ++s) {
       MQ_TRY(gemm(c, 'T', 'N', n, n, n, 1.0, dX, n, Fm + n2 * s, n, 0.0, dT1, n));
@@ -283,6 +284,10 @@ int scf_device(mq_ctx *c, const double *S, const double *H, const mq_scf_opts *o
     } else {
       for (int s = 0; s < ns; ++s) {
         double *A = dFp + n2 * s, *U = dU + n2 * s;
+        if (refine_prev) {  // start vectors of an earlier Fock matrix: refine, then the Jacobi cleanup
+          MQ_TRY(syev_large_warm(c, n, A, dEps + (size_t)n * s, U));
+          continue;
+        }
         if (have_prev) {
           MQ_TRY(gemm(c, 'T', 'N', n, n, n, 1.0, U, n, A, n, 0.0, dT1, n));
           MQ_TRY(gemm(c, 'N', 'N', n, n, n, 1.0, dT1, n, U, n, 0.0, A, n));
@@ -293,6 +298,7 @@ int scf_device(mq_ctx *c, const double *S, const double *H, const mq_scf_opts *o
           MQ_TRY(syev_large_cold(c, n, A, dEps + (size_t)n * s, U));
       }
       have_prev = true;
+      refine_prev = false;
     }
     return MQ_OK;
   };
@@ -328,6 +334,7 @@ int scf_device(mq_ctx *c, const double *S, const double *H, const mq_scf_opts *o
     if (!use || st != MQ_OK) return MQ_OK;  // a failed early solve only costs the warm start
     MQ_CUDA(c, cudaMemcpyAsync(dU, dUe, n2 * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
     have_prev = true;
+    refine_prev = true;
     c->stats.eig_early = 1;
     return MQ_OK;
   };
@@ -353,7 +360,10 @@ int scf_device(mq_ctx *c, const double *S, const double *H, const mq_scf_opts *o
     int rc = gemm(c, 'T', 'N', n, n, n, 1.0, dX, n, dFe, n, 0.0, dTe, n);
     if (rc == MQ_OK) rc = gemm(c, 'N', 'N', n, n, n, 1.0, dTe, n, dX, n, 0.0, dAe, n);
     if (rc == MQ_OK) rc = syev_large_cold(c, n, dAe, dEe, dUe, true);
-    if (rc == MQ_OK) rc = cuda_check(c, cudaEventRecord(c->ev_early, c->aux), "cudaEventRecord");
+    if (rc == MQ_OK) {
+      const cudaError_t e = cudaEventRecord(c->ev_early, c->aux);
+      if (e != cudaSuccess) rc = cuda_check(c, e, "cudaEventRecord (early eigensolve)");
+    }
     c->stream = main;
     MQ_TRY(rc);
     early = true;
