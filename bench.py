@@ -227,7 +227,10 @@ def run_ours(args):
     e1.record()
     barrier()
     ms_e2e = e0.elapsed_time(e1) / args.steps
-    # ---- plain FP64 path (reference-style Roothaan, FP64 transform), one solve
+    # ---- plain FP64 path (reference-style Roothaan, FP64 transform): one
+    # untimed solve (its first-use allocations and the FP64 tile autotuning),
+    # then one timed solve
+    solve(ctx, sysm, basis, False, False)
     barrier()
     p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     p0.record()
