@@ -107,10 +107,11 @@ MODEL = os.path.join(ROOT, "myqc_gb300", "data", "guess_mlp.npz")
 SCHWARZ = 1e-12  # fast arm: contracted quartets with a Schwarz bound below this are skipped
 # fast arm: quartets with a Schwarz bound below this in FP32, and FP32 incremental
 # Fock builds once max|D_k - D_(k-1)| is below FOCK_INC_TAU.  Measured on the
-# (H2O)32 solve: SCF energy within 5e-11 Eh of the plain FP64 arm, E(MBPT2)
-# within 0.1 uEh; (1e-4, 1e-4) moves it to 2e-10 Eh for ~2 ms more.
+# (H2O)32 solve: SCF energy within 1.3e-11 Eh of the plain FP64 arm, E(MBPT2)
+# within 0.1 uEh (8 of 12 builds incremental); an ERI threshold of 1e-4 would
+# move the SCF energy to 4e-10 Eh for 1 ms.
 ERI_F32_TAU = 3e-5
-FOCK_INC_TAU = 1e-5
+FOCK_INC_TAU = 1e-3
 AO2MO_PREFETCH = 3  # fast arm: XX cut into 3 BF16 planes beside the SCF's final eigensolve
 _learned = {}
 
@@ -128,7 +129,7 @@ def solve(ctx, sysm, basis, fast: bool, set_system: bool):
     (core guess when the prediction fails its checks or the SCF does not
     converge from it), Schwarz screening at 1e-12, quartets with a bound below
     3e-5 in FP32, the double-float Fock digestion with FP32 incremental builds
-    once the density moves by less than 1e-5, densities by purification (one
+    once the density moves by less than 1e-3, densities by purification (one
     eigensolve at the end, with the XX slices of the transform formed beside
     it) and split-precision MP2; plain: the core-Hamiltonian guess, the
     eigensolver every iteration and the FP64 transform.  Both use DIIS(8)
