@@ -24,6 +24,8 @@
 
 namespace mq {
 
+static inline bool cuda_ok(cudaError_t e) { return e == cudaSuccess; }
+
 __global__ void add_kernel(const double *a, const double *b, double *c, size_t n) {
   size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) c[i] = a[i] + b[i];
@@ -245,18 +247,35 @@ int scf_device(mq_ctx *c, const double *S, const double *H, const mq_scf_opts *o
   double *dScal = dDp + n2 * ns;        // 256 scalars
   double *dEps = dScal + 256;           // n * ns
   double *dRed = dEps + n * ns;         // reduction partials, 16 per CTA
-  MQ_CUDA(c, cudaMemcpyAsync(dS, S, n2 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
-  MQ_CUDA(c, cudaMemcpyAsync(dH, H, n2 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
-
   // X = S^-1/2: Newton-Schulz (GEMMs only) with purification, else (and as its
-  // fallback) the eigendecomposition S = U s U^T
+  // fallback) the eigendecomposition S = U s U^T.  Newton-Schulz needs S alone:
+  // it runs on the aux stream, so that it does not wait for work queued on
+  // the main stream before this call (an integral pass), and the main stream
+  // waits for it before any use of S, X or its scratch.
   bool have_x = false;
   if (o->purify) {
+    if (!c->aux) {
+      int lo = 0, hi = 0;
+      MQ_CUDA(c, cudaDeviceGetStreamPriorityRange(&lo, &hi));
+      MQ_CUDA(c, cudaStreamCreateWithPriority(&c->aux, cudaStreamNonBlocking, hi));
+    }
+    if (!c->ev_early) MQ_CUDA(c, cudaEventCreateWithFlags(&c->ev_early, cudaEventDisableTiming));
+    cudaStream_t main = c->stream;
+    c->stream = c->aux;
     int ns_steps = 0;
-    const int rc = inv_sqrt_ns(c, n, dS, dX, dT1, dScal + 128, &ns_steps);  // scratch dT1..dW (5 n^2)
+    int rc = cuda_ok(cudaMemcpyAsync(dS, S, n2 * sizeof(double), cudaMemcpyHostToDevice, c->stream))
+                 ? inv_sqrt_ns(c, n, dS, dX, dT1, dScal + 128, &ns_steps)  // scratch dT1..dW (5 n^2)
+                 : set_err(c, MQ_ECUDA, "S upload");
+    const bool rec = cudaEventRecord(c->ev_early, c->stream) == cudaSuccess;
+    c->stream = main;
+    if (rec) MQ_CUDA(c, cudaStreamWaitEvent(c->stream, c->ev_early, 0));
+    else MQ_CUDA(c, cudaStreamSynchronize(c->aux));
     if (rc != MQ_OK && rc != MQ_ENOCONV) return rc;
     have_x = rc == MQ_OK;
+  } else {
+    MQ_CUDA(c, cudaMemcpyAsync(dS, S, n2 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
   }
+  MQ_CUDA(c, cudaMemcpyAsync(dH, H, n2 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
   if (!have_x) {
     MQ_CUDA(c, cudaMemcpyAsync(dT1, dS, n2 * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
     MQ_TRY(syev_batched_device(c, n, 1, dT1, dEps, dU));
