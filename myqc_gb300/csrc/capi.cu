@@ -551,6 +551,16 @@ int mq_set_fock_precision(mq_ctx *c, int precision) {
   return MQ_OK;
 }
 
+int ensure_aux(mq_ctx *c) {
+  if (!c->aux) {
+    int lo = 0, hi = 0;
+    MQ_CUDA(c, cudaDeviceGetStreamPriorityRange(&lo, &hi));
+    MQ_CUDA(c, cudaStreamCreateWithPriority(&c->aux, cudaStreamNonBlocking, hi));
+  }
+  if (!c->ev_early) MQ_CUDA(c, cudaEventCreateWithFlags(&c->ev_early, cudaEventDisableTiming));
+  return MQ_OK;
+}
+
 int mq_set_ao2mo_prefetch(mq_ctx *c, int planes) {
   if (!c) return MQ_EINVAL;
   if (planes != 0 && planes != 2 && planes != 3) return set_err(c, MQ_EINVAL, "prefetch planes must be 0, 2 or 3");

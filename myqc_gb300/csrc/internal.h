@@ -359,6 +359,8 @@ int ao2mo_split_device(mq_ctx *c, const double *d_Ci, int no1, const double *d_C
 // XX cut into c->ao2mo_prefetch planes on the side stream, after the work queued
 // so far on the main stream; the next split transform of the same XX uses it
 int ao2mo_preslice_xx(mq_ctx *c);
+// the aux stream (highest priority) and the event of its SCF hand-overs, created on first use
+int ensure_aux(mq_ctx *c);
 // the main stream waits for the side stream's last work (no-op when none is pending)
 int join_side(mq_ctx *c);
 

@@ -698,11 +698,7 @@ int mlp_forward(mq_ctx *c, int rows, const float *X, float *Y) {
   Mlp *m = mlp_of(c);
   if (!m) return set_err(c, MQ_ESTATE, "no MLP (mq_mlp_init)");
   if (rows <= 0) return MQ_OK;
-  if (!c->aux) {
-    int lo = 0, hi = 0;
-    MQ_CUDA(c, cudaDeviceGetStreamPriorityRange(&lo, &hi));
-    MQ_CUDA(c, cudaStreamCreateWithPriority(&c->aux, cudaStreamNonBlocking, hi));
-  }
+  MQ_TRY(ensure_aux(c));
   if (!c->ev_params) MQ_TRY(mark_params(c));
   MQ_CUDA(c, cudaStreamWaitEvent(c->aux, c->ev_params, 0));
   cudaStream_t main = c->stream;

@@ -254,12 +254,7 @@ int scf_device(mq_ctx *c, const double *S, const double *H, const mq_scf_opts *o
   // waits for it before any use of S, X or its scratch.
   bool have_x = false;
   if (o->purify) {
-    if (!c->aux) {
-      int lo = 0, hi = 0;
-      MQ_CUDA(c, cudaDeviceGetStreamPriorityRange(&lo, &hi));
-      MQ_CUDA(c, cudaStreamCreateWithPriority(&c->aux, cudaStreamNonBlocking, hi));
-    }
-    if (!c->ev_early) MQ_CUDA(c, cudaEventCreateWithFlags(&c->ev_early, cudaEventDisableTiming));
+    MQ_TRY(ensure_aux(c));
     cudaStream_t main = c->stream;
     c->stream = c->aux;
     int ns_steps = 0;
@@ -365,12 +360,7 @@ int scf_device(mq_ctx *c, const double *S, const double *H, const mq_scf_opts *o
     dUe = e + 2 * n2;
     dTe = e + 3 * n2;
     dEe = e + 4 * n2;
-    if (!c->aux) {
-      int lo = 0, hi = 0;
-      MQ_CUDA(c, cudaDeviceGetStreamPriorityRange(&lo, &hi));
-      MQ_CUDA(c, cudaStreamCreateWithPriority(&c->aux, cudaStreamNonBlocking, hi));
-    }
-    if (!c->ev_early) MQ_CUDA(c, cudaEventCreateWithFlags(&c->ev_early, cudaEventDisableTiming));
+    MQ_TRY(ensure_aux(c));
     MQ_CUDA(c, cudaMemcpyAsync(dFe, Fm, n2 * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
     MQ_CUDA(c, cudaEventRecord(c->ev_early, c->stream));
     MQ_CUDA(c, cudaStreamWaitEvent(c->aux, c->ev_early, 0));
