@@ -551,7 +551,7 @@ int mq_set_fock_precision(mq_ctx *c, int precision) {
   return MQ_OK;
 }
 
-int ensure_aux(mq_ctx *c) {
+int mq::ensure_aux(mq_ctx *c) {
   if (!c->aux) {
     int lo = 0, hi = 0;
     MQ_CUDA(c, cudaDeviceGetStreamPriorityRange(&lo, &hi));
