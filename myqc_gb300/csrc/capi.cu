@@ -91,6 +91,16 @@ static int ensure_xx(mq_ctx *c) {
   return MQ_OK;
 }
 
+int ensure_aux(mq_ctx *c) {
+  if (!c->aux) {
+    int lo = 0, hi = 0;
+    MQ_CUDA(c, cudaDeviceGetStreamPriorityRange(&lo, &hi));
+    MQ_CUDA(c, cudaStreamCreateWithPriority(&c->aux, cudaStreamNonBlocking, hi));
+  }
+  if (!c->ev_early) MQ_CUDA(c, cudaEventCreateWithFlags(&c->ev_early, cudaEventDisableTiming));
+  return MQ_OK;
+}
+
 }  // namespace mq
 
 using namespace mq;
@@ -548,16 +558,6 @@ int mq_set_fock_precision(mq_ctx *c, int precision) {
   if (!c) return MQ_EINVAL;
   if (precision != MQ_FOCK_FP64 && precision != MQ_FOCK_DF32) return set_err(c, MQ_EINVAL, "bad Fock precision");
   c->fock_df32 = precision == MQ_FOCK_DF32;
-  return MQ_OK;
-}
-
-int mq::ensure_aux(mq_ctx *c) {
-  if (!c->aux) {
-    int lo = 0, hi = 0;
-    MQ_CUDA(c, cudaDeviceGetStreamPriorityRange(&lo, &hi));
-    MQ_CUDA(c, cudaStreamCreateWithPriority(&c->aux, cudaStreamNonBlocking, hi));
-  }
-  if (!c->ev_early) MQ_CUDA(c, cudaEventCreateWithFlags(&c->ev_early, cudaEventDisableTiming));
   return MQ_OK;
 }
 
