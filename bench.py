@@ -20,6 +20,8 @@ molecule (replicas, no collective); rank 0 prints.
 from __future__ import annotations
 
 import argparse
+import atexit
+import datetime
 import json
 import os
 import subprocess
@@ -44,9 +46,12 @@ def env_rank():
 
 
 class ClockSampler:
-    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+    """nvidia-smi samples of SM clock and throttle reasons.  The sampler starts
+    before the warm-up (its start-up, which touches the driver, stays out of the
+    timed region); `window` marks the timed region and `summary` keeps the
+    samples taken inside it."""
 
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
@@ -58,6 +63,11 @@ class ClockSampler:
         import tempfile
         folder = os.environ.get("MYQC_CLOCKS_DIR", tempfile.gettempdir())
         self.path = os.path.join(folder, f"clocks_bench_{os.getpid()}.csv")
+        self.t0 = self.t1 = None
+
+    def window(self, t0, t1):
+        """Host datetimes bracketing the timed region."""
+        self.t0, self.t1 = t0, t1
 
     def __enter__(self):
         try:
@@ -66,33 +76,37 @@ class ClockSampler:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
                                           "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
                                          stderr=subprocess.DEVNULL)
+            atexit.register(self.__exit__)  # the sampler never outlives the bench
         except Exception:
             self.proc = None
         return self
 
     def __exit__(self, *a):
-        if self.proc:
+        if self.proc and self.proc.poll() is None:
             self.proc.terminate()
             self.proc.wait()
+        if self.proc and not self.f.closed:
             self.f.close()
 
     def summary(self):
         if not self.proc:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
         rows = [r.split(",") for r in open(self.path).read().strip().split("\n") if r.strip()]
-        sm, mx, reasons = [], None, set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        parsed = []
         for r in rows:
             try:
-                sm.append(float(r[1]))
-                mx = float(r[2])
-                for k, v in zip(names, r[5:9]):
-                    if v.strip().lower() == "active":
-                        reasons.add(k)
+                ts = datetime.datetime.strptime(r[0].strip(), "%Y/%m/%d %H:%M:%S.%f")
+                parsed.append((ts, float(r[2]), float(r[3]), [v.strip().lower() for v in r[6:10]]))
             except (ValueError, IndexError):
                 pass
-        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
-                "samples": len(sm)}
+        inside = [p for p in parsed if self.t0 is None or (self.t0 <= p[0] <= self.t1)]
+        if not inside and parsed and self.t0 is not None:  # a region shorter than the sampling period
+            inside = [min(parsed, key=lambda p: abs((p[0] - self.t0).total_seconds()))]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = {k for p in inside for k, v in zip(names, p[3]) if v == "active"}
+        sm = [p[1] for p in inside]
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": inside[-1][2] if inside else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
 
 
 def load_workload(seed: int):
@@ -177,7 +191,8 @@ def run_ours(args):
     from myqc_gb300 import MODE_TIGHT
     ctx.set_system(sysm, basis, None, MODE_TIGHT)
     n = ctx.n
-    # warm-up (untimed)
+    # clock sampling starts before the warm-up; the warm-up is untimed
+    clk = ClockSampler(dev).__enter__()
     for _ in range(args.warmup):
         res, mp2, prec = solve(ctx, sysm, basis, True, True)
 
@@ -195,28 +210,30 @@ def run_ours(args):
     iters = []
     barrier()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(dev) as clk:
-        # NVTX range "timed": `ncu --nvtx --nvtx-include "timed/"` lists exactly these kernels
-        torch.cuda.nvtx.range_push("timed")
-        ev0.record()
-        for _ in range(args.steps):
-            res, mp2, prec = solve(ctx, sysm, basis, True, False)
-            t_fock += stat(ctx, "fock")
-            nfock += stat(ctx, "fock_calls")
-            t_fock_kernel += stat(ctx, "fock_kernel")
-            n_inc += stat(ctx, "fock_inc_builds")
-            n_fock_kernel += stat(ctx, "fock_kernel_launches")
-            t_eri += stat(ctx, "eri")
-            nq32 += stat(ctx, "quartets_f32")
-            nq += stat(ctx, "quartets")
-            live = stat(ctx, "live_slabs")
-            t_diag += stat(ctx, "diag")
-            t_ao2mo += stat(ctx, "ao2mo")
-            t_mp2 += stat(ctx, "mp2")
-            iters.append(res.iterations)
-        ev1.record()
-        torch.cuda.nvtx.range_pop()
-        barrier()
+    w0 = datetime.datetime.now()
+    # NVTX range "timed": `ncu --nvtx --nvtx-include "timed/"` lists exactly these kernels
+    torch.cuda.nvtx.range_push("timed")
+    ev0.record()
+    for _ in range(args.steps):
+        res, mp2, prec = solve(ctx, sysm, basis, True, False)
+        t_fock += stat(ctx, "fock")
+        nfock += stat(ctx, "fock_calls")
+        t_fock_kernel += stat(ctx, "fock_kernel")
+        n_inc += stat(ctx, "fock_inc_builds")
+        n_fock_kernel += stat(ctx, "fock_kernel_launches")
+        t_eri += stat(ctx, "eri")
+        nq32 += stat(ctx, "quartets_f32")
+        nq += stat(ctx, "quartets")
+        live = stat(ctx, "live_slabs")
+        t_diag += stat(ctx, "diag")
+        t_ao2mo += stat(ctx, "ao2mo")
+        t_mp2 += stat(ctx, "mp2")
+        iters.append(res.iterations)
+    ev1.record()
+    torch.cuda.nvtx.range_pop()
+    barrier()
+    clk.window(w0, datetime.datetime.now())
+    clk.__exit__()
     ms_value = ev0.elapsed_time(ev1) / args.steps
     launches = int(stat(ctx, "launches") - L0)
     # ---- fast path through the full public API with host buffers (e2e)
@@ -526,7 +543,7 @@ def main():
     global NMOL, BOX
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=8)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--seed", type=int, default=0)
