@@ -547,10 +547,37 @@ __global__ void quartet_pack_kernel(const long long *__restrict__ part, const in
   for (int k = threadIdx.x; k < counts[b]; k += blockDim.x) list[offs[b] + k] = part[(size_t)b * block + k];
 }
 
+// Schwarz bounds need only the diagonal integrals (ab|ab) of a shell pair: one
+// thread per pair and diagonal function pair S = (a, b), a single integral each
+template <int LA, int LB, int S>
+__device__ __forceinline__ void schwarz_diag(const EriArgs &g, int P, size_t n, double *XX) {
+  constexpr int NB = nfun(LB), a = S / NB, b = S % NB;
+  if constexpr (a < nfun(LA))
+    quartet<LA, LB, LA, LB, a, a + 1, b, b + 1, a, a + 1, b, b + 1, EPI_SCHWARZ, double>(g, P, P, n, XX);
+}
+
 template <int LA, int LB, int LC, int LD, int EPI, class RT = double>
 __global__ void __launch_bounds__(128) eri_kernel(EriArgs g) {
   constexpr int NA = nfun(LA), NB = nfun(LB);
   constexpr int NOUT = NA * NB * nfun(LC) * nfun(LD);
+  if constexpr (EPI == EPI_SCHWARZ) {  // diagonal classes only (LC = LA, LD = LB)
+    constexpr int NDIAG = NA * NB;
+    const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int split = (int)(warp % NDIAG);
+    const long long q = (warp / NDIAG) * 32 + (threadIdx.x & 31);
+    int P, Q, m;
+    if (!decode(g, q, P, Q, m)) return;
+    const size_t n = (size_t)g.n;
+    switch (split) {
+#define MQ_DIAG(s) \
+  case s: schwarz_diag<LA, LB, s>(g, P, n, g.XX); break;
+      MQ_DIAG(0) MQ_DIAG(1) MQ_DIAG(2) MQ_DIAG(3) MQ_DIAG(4) MQ_DIAG(5) MQ_DIAG(6) MQ_DIAG(7)
+      MQ_DIAG(8) MQ_DIAG(9) MQ_DIAG(10) MQ_DIAG(11) MQ_DIAG(12) MQ_DIAG(13) MQ_DIAG(14)
+      default: schwarz_diag<LA, LB, 15>(g, P, n, g.XX); break;
+#undef MQ_DIAG
+    }
+    return;
+  }
   constexpr int NSPLIT = NOUT <= 16 ? 1 : (NOUT <= 64 ? 4 : 16);
   const long long gtid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long warp = gtid >> 5;
@@ -594,7 +621,8 @@ static int nsplit_of(int cP, int cQ) {
 
 template <int EPI, class RT = double>
 static int launch_class(mq_ctx *c, EriArgs g, int cP, int cQ) {
-  const int nsplit = nsplit_of(cP, cQ);
+  // Schwarz: one warp slot per diagonal function pair (ab|ab) of the class
+  const int nsplit = EPI == EPI_SCHWARZ ? (cP == 0 ? 1 : cP == 1 ? 4 : 16) : nsplit_of(cP, cQ);
   const long long warps = (g.nq + 31) / 32 * nsplit;
   const long long threads = warps * 32;
   const int block = 128;
