@@ -121,10 +121,11 @@ MODEL = os.path.join(ROOT, "myqc_gb300", "data", "guess_mlp.npz")
 SCHWARZ = 1e-12  # fast arm: contracted quartets with a Schwarz bound below this are skipped
 # fast arm: quartets with a Schwarz bound below this in FP32, and FP32 incremental
 # Fock builds once max|D_k - D_(k-1)| is below FOCK_INC_TAU.  Measured on the
-# (H2O)32 solve: SCF energy within 1.3e-11 Eh of the plain FP64 arm, E(MBPT2)
-# within 0.1 uEh (8 of 12 builds incremental); an ERI threshold of 1e-4 would
-# move the SCF energy to 4e-10 Eh for 1 ms.
-ERI_F32_TAU = 3e-5
+# (H2O)32 solve (8 of 12 builds incremental), SCF energy error vs the plain FP64
+# arm and integral-pass time by ERI threshold: 3e-5: 1.3e-11 Eh, 21.3 ms;
+# 1e-4: 4.1e-10 Eh, 20.7 ms; 3e-4: 5.2e-10 Eh, 18.7 ms; 1e-3: 3.4e-9 Eh, 18.0 ms;
+# 3e-3: 9.6e-9 Eh, 16.9 ms.  E(MBPT2) stays within 0.11 uEh throughout.
+ERI_F32_TAU = 1e-3
 FOCK_INC_TAU = 1e-3
 AO2MO_PREFETCH = 3  # fast arm: XX cut into 3 BF16 planes beside the SCF's final eigensolve
 _learned = {}
@@ -142,7 +143,7 @@ def solve(ctx, sysm, basis, fast: bool, set_system: bool):
     """One solve through the public API.  fast: the learned initial density
     (core guess when the prediction fails its checks or the SCF does not
     converge from it), Schwarz screening at 1e-12, quartets with a bound below
-    3e-5 in FP32, the double-float Fock digestion with FP32 incremental builds
+    1e-3 in FP32, the double-float Fock digestion with FP32 incremental builds
     once the density moves by less than 1e-3, densities by purification (one
     eigensolve at the end, with the XX slices of the transform formed beside
     it) and split-precision MP2; plain: the core-Hamiltonian guess, the
@@ -540,13 +541,15 @@ def run_reference(args):
 
 
 def main():
-    global NMOL, BOX
+    global NMOL, BOX, ERI_F32_TAU
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=8)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--eri-f32-tau", type=float, default=ERI_F32_TAU,
+                    help="Schwarz bound below which quartets run in FP32 (fast arm)")
     ap.add_argument("--plain-iters", type=int, default=30,
                     help="SCF iterations assumed for the reference CPU extrapolation")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
@@ -557,6 +560,7 @@ def main():
     ap.add_argument("--box", type=float, default=BOX, help="cube side in Angstrom")
     args = ap.parse_args()
     NMOL, BOX = args.nmol, args.box
+    ERI_F32_TAU = args.eri_f32_tau
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

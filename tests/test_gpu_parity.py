@@ -108,7 +108,7 @@ def test_syev_batched(ctx):
 
 def test_eri_mixed_precision(ctx, basis_text):
     """Quartets with a Schwarz bound below tau computed in FP32: every integral
-    of (H2O)8 within 1e-6 tau of the FP64 pass (tau = 1e-4 and 1e-6), the
+    of (H2O)8 within 1e-6 tau of the FP64 pass (tau = 1e-3, 1e-4 and 1e-6), the
     FP32 share counted, and FP64 again once tau is 0."""
     from myqc_gb300 import MODE_TIGHT, molecules
     sysm = molecules.water_cluster_system(8, 7.0, 3)
@@ -119,7 +119,7 @@ def test_eri_mixed_precision(ctx, basis_text):
         ctx.set_eri_mixed(0.0)
         X64 = ctx.eri_full()
         assert ctx.stat("quartets_f32") == 0
-        for tau in (1e-4, 1e-6):
+        for tau in (1e-3, 1e-4, 1e-6):
             ctx.set_eri_mixed(tau)
             Xm = ctx.eri_full()
             nf = ctx.stat("quartets_f32")
