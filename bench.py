@@ -121,12 +121,14 @@ MODEL = os.path.join(ROOT, "myqc_gb300", "data", "guess_mlp.npz")
 SCHWARZ = 1e-12  # fast arm: contracted quartets with a Schwarz bound below this are skipped
 # fast arm: quartets with a Schwarz bound below this in FP32, and FP32 incremental
 # Fock builds once max|D_k - D_(k-1)| is below FOCK_INC_TAU.  Measured on the
-# (H2O)32 solve (8 of 12 builds incremental), SCF energy error vs the plain FP64
-# arm and integral-pass time by ERI threshold: 3e-5: 1.3e-11 Eh, 21.3 ms;
+# (H2O)32 solve, SCF energy error vs the plain FP64 arm and integral-pass time by
+# ERI threshold (Fock increments below 1e-3): 3e-5: 1.3e-11 Eh, 21.3 ms;
 # 1e-4: 4.1e-10 Eh, 20.7 ms; 3e-4: 5.2e-10 Eh, 18.7 ms; 1e-3: 3.4e-9 Eh, 18.0 ms;
-# 3e-3: 9.6e-9 Eh, 16.9 ms.  E(MBPT2) stays within 0.11 uEh throughout.
+# 3e-3: 9.6e-9 Eh, 16.9 ms.  By Fock threshold (ERI 1e-3): 1e-3: 8 of 12 builds
+# incremental, 3.4e-9 Eh, Fock 16.5 ms; 3e-3: 9, 4.2e-9 Eh, 15.5 ms; 1e-2: 10,
+# 1.0e-8 Eh, 14.6 ms.  E(MBPT2) stays within 0.11 uEh throughout.
 ERI_F32_TAU = 1e-3
-FOCK_INC_TAU = 1e-3
+FOCK_INC_TAU = 1e-2
 AO2MO_PREFETCH = 3  # fast arm: XX cut into 3 BF16 planes beside the SCF's final eigensolve
 _learned = {}
 
@@ -144,7 +146,7 @@ def solve(ctx, sysm, basis, fast: bool, set_system: bool):
     (core guess when the prediction fails its checks or the SCF does not
     converge from it), Schwarz screening at 1e-12, quartets with a bound below
     1e-3 in FP32, the double-float Fock digestion with FP32 incremental builds
-    once the density moves by less than 1e-3, densities by purification (one
+    once the density moves by less than 1e-2, densities by purification (one
     eigensolve at the end, with the XX slices of the transform formed beside
     it) and split-precision MP2; plain: the core-Hamiltonian guess, the
     eigensolver every iteration and the FP64 transform.  Both use DIIS(8)
@@ -541,7 +543,7 @@ def run_reference(args):
 
 
 def main():
-    global NMOL, BOX, ERI_F32_TAU
+    global NMOL, BOX, ERI_F32_TAU, FOCK_INC_TAU
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=8)
@@ -550,6 +552,8 @@ def main():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--eri-f32-tau", type=float, default=ERI_F32_TAU,
                     help="Schwarz bound below which quartets run in FP32 (fast arm)")
+    ap.add_argument("--fock-inc-tau", type=float, default=FOCK_INC_TAU,
+                    help="max|dD| below which Fock builds are FP32 increments (fast arm)")
     ap.add_argument("--plain-iters", type=int, default=30,
                     help="SCF iterations assumed for the reference CPU extrapolation")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
@@ -561,6 +565,7 @@ def main():
     args = ap.parse_args()
     NMOL, BOX = args.nmol, args.box
     ERI_F32_TAU = args.eri_f32_tau
+    FOCK_INC_TAU = args.fock_inc_tau
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

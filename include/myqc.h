@@ -122,9 +122,9 @@ int mq_set_fock_precision(mq_ctx *ctx, int precision);
  * previous one by less than tau (max |D_k - D_(k-1)|), the build is
  * G_k = G_(k-1) + G[D_k - D_(k-1)] with the increment digested in FP32 on the
  * FP32 pipes; larger changes get full builds in the mq_set_fock_precision
- * arithmetic.  The increment's error scales with its size: tau = 1e-6 keeps
- * the converged energy within ~1e-9 Eh of full builds.  tau = 0 (default): full
- * builds only.  MQ_EINVAL outside [0, 1e-3]. */
+ * arithmetic.  The increment's error scales with its size: on (H2O)8 the
+ * converged energy stays within 1e-9 Eh of full builds for tau up to 1e-2.
+ * tau = 0 (default): full builds only.  MQ_EINVAL outside [0, 1e-2]. */
 int mq_set_fock_incremental(mq_ctx *ctx, double tau);
 
 /* Overlap for the split-precision transform; no reference counterpart.

@@ -569,7 +569,7 @@ int mq_set_ao2mo_prefetch(mq_ctx *c, int planes) {
 }
 
 int mq_set_fock_incremental(mq_ctx *c, double tau) {
-  if (!c || !(tau >= 0.0) || tau > 1e-3) return c ? set_err(c, MQ_EINVAL, "incremental Fock threshold must be in [0, 1e-3]") : MQ_EINVAL;
+  if (!c || !(tau >= 0.0) || tau > 1e-2) return c ? set_err(c, MQ_EINVAL, "incremental Fock threshold must be in [0, 1e-2]") : MQ_EINVAL;
   c->fock_inc_tau = tau;
   return MQ_OK;
 }
