@@ -1,5 +1,6 @@
-// eri.cu -- FP64 two-electron repulsion integrals over contracted s/sp shell
-// quartets (McMurchie-Davidson), with three epilogues:
+// eri.cu -- two-electron repulsion integrals over contracted s/sp shell
+// quartets (McMurchie-Davidson), in FP64, or in FP32 for quartets whose
+// Schwarz bound is below the context's threshold, with three epilogues:
 //   EPI_XX      scatter each unique integral to its 8 places in the full
 //               XX(i,j,g,h) array (replaces proc2e + fillsym,
 //               src/integrals/int2e.f90:78-351,540-613);
@@ -22,8 +23,11 @@
 // one (bra class, ket class) combination, so every thread of a launch runs the
 // same fully unrolled register code.  Quartets with more than 16 integrals
 // ((sp sp|sp s): 64, (sp sp|sp sp): 256) are split over 4 or 16 threads by
-// bra function; the split index is constant per warp (warp w serves split
-// w % nsplit for 32 consecutive quartets), so no lane diverges.
+// ket function c or ket pair (c, d), each thread forming the whole bra; the
+// split index is constant per warp (warp w serves split w % nsplit for 32
+// consecutive quartets), so no lane diverges.  The Schwarz launches split a
+// diagonal quartet (P|P) the same way into one thread per diagonal integral
+// (ab|ab).
 #include <algorithm>
 #include <string>
 #include <vector>
