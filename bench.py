@@ -542,8 +542,7 @@ def run_reference(args):
     print(json.dumps(out), flush=True)
 
 
-def main():
-    global NMOL, BOX, ERI_F32_TAU, FOCK_INC_TAU
+def parse_args(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=8)
@@ -562,12 +561,22 @@ def main():
     ap.add_argument("--batch-count", type=int, default=4096)
     ap.add_argument("--nmol", type=int, default=NMOL, help="water molecules in the cluster")
     ap.add_argument("--box", type=float, default=BOX, help="cube side in Angstrom")
-    args = ap.parse_args()
+    args = ap.parse_args(argv)
+    if not (0.0 <= args.fock_inc_tau <= 1e-2):
+        ap.error("--fock-inc-tau must be in [0, 1e-2] (the library's accepted range)")
+    if not args.eri_f32_tau >= 0.0:
+        ap.error("--eri-f32-tau must be >= 0")
+    if args.warmup < 3:
+        args.warmup = 3
+    return args
+
+
+def main():
+    global NMOL, BOX, ERI_F32_TAU, FOCK_INC_TAU
+    args = parse_args()
     NMOL, BOX = args.nmol, args.box
     ERI_F32_TAU = args.eri_f32_tau
     FOCK_INC_TAU = args.fock_inc_tau
-    if args.warmup < 3:
-        args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
     else:

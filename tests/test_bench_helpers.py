@@ -52,3 +52,35 @@ def test_clock_sampler_keeps_the_timed_window():
         assert c.summary()["samples"] == 1
     finally:
         os.remove(c.path)
+
+
+def test_threshold_flags():
+    a = bench.parse_args([])
+    assert a.eri_f32_tau == bench.ERI_F32_TAU and a.fock_inc_tau == bench.FOCK_INC_TAU
+    assert 0.0 <= bench.FOCK_INC_TAU <= 1e-2 and bench.ERI_F32_TAU >= 0.0
+    a = bench.parse_args(["--eri-f32-tau", "3e-5", "--fock-inc-tau", "1e-3", "--warmup", "1"])
+    assert (a.eri_f32_tau, a.fock_inc_tau, a.warmup) == (3e-5, 1e-3, 3)  # at least 3 warm-up steps
+    for bad in (["--fock-inc-tau", "0.02"], ["--fock-inc-tau", "-1e-3"], ["--eri-f32-tau", "-1"]):
+        try:
+            bench.parse_args(bad)
+        except SystemExit as e:
+            assert e.code == 2
+        else:
+            raise AssertionError(bad)
+
+
+def test_cpu_extrapolation_by_loop_counts():
+    """A sample of the cluster itself extrapolates to its own times (x iterations
+    for the Fock digestion); one of half the waters scales by the loop counts."""
+    nm = bench.NMOL
+    t = {"int1e": 1.0, "int2e": 2.0, "fock": 3.0, "ao2mo": 4.0, "mp2": 5.0}
+    s = {"n": 7 * nm, "nset": 12 * nm, "nnuc": 3 * nm, "no": 5 * nm, "t": t}
+    r = bench._extrapolate(s, 25)
+    assert r == {"int1e": 1.0, "int2e": 2.0, "scf": 75.0, "ao2mo": 4.0, "mp2": 5.0}
+    h = nm // 2
+    s = {"n": 7 * h, "nset": 12 * h, "nnuc": 3 * h, "no": 5 * h, "t": t}
+    r = bench._extrapolate(s, 1)
+    f = nm / h
+    expect = {"int1e": f ** 3, "int2e": 2.0 * f ** 4, "scf": 3.0 * f ** 4, "ao2mo": 4.0 * f ** 5,
+              "mp2": 5.0 * f ** 4}
+    assert all(abs(r[k] - v) <= 1e-12 * v for k, v in expect.items()), r
