@@ -177,7 +177,8 @@ class Context:
         self._check(self.L.mq_set_fock_precision(self.h, precision))
 
     def set_fock_incremental(self, tau: float):
-        """FP32 incremental Fock builds in scf() once max|D_k - D_(k-1)| < tau (0: off)."""
+        """FP32 incremental Fock builds in scf() once max|D_k - D_(k-1)| < tau
+        (0: off; tau in [0, 1e-2], else MyQCError)."""
         self._check(self.L.mq_set_fock_incremental(self.h, float(tau)))
 
     def set_ao2mo_prefetch(self, planes: int):
