@@ -87,6 +87,25 @@ def test_mp2_sum_identity(ftab, basis_text):
     assert abs(E - r["mp2"]["E_MP2"]) < 1e-12
 
 
+def test_uhf_restatements_reduce_to_rhf(ftab, basis_text):
+    """Closed-shell limit of the UHF restatements: UHFI2G with Da = Db = D/2
+    gives RHFI2G's G for both spins, and mp2_uhf with identical spin blocks
+    gives mp2_rhf's E(MBPT2) (E(AA) = E(BB), both equal to mp2_rhf's E(AA))."""
+    r = _run("CO2", ftab, basis_text, conv_exp=9)
+    res, XX, no = r["scf"], r["XX"], r["mol"].nelcA
+    D = res.D
+    Ga, Gb = O.fock_uhf(XX, 0.5 * D, 0.5 * D)
+    G = O.fock_rhf(XX, D)
+    assert np.allclose(Ga, G, atol=1e-12) and np.allclose(Gb, G, atol=1e-12)
+    C, e = res.C, res.eig
+    Om = O.ao2mo(XX, C[:, :no], C[:, no:], C[:, :no], C[:, no:])
+    rh = O.mp2_rhf(e, Om)
+    uh = O.mp2_uhf(e, e, Om, Om, Om)
+    assert abs(uh["E_AA"] - uh["E_BB"]) < 1e-15
+    assert abs(uh["E_AA"] - rh["E_AA"]) < 1e-13 and abs(uh["E_AB"] - rh["E_AB"]) < 1e-13
+    assert abs(uh["E_MP2"] - rh["E_MP2"]) < 1e-12
+
+
 def test_mlp_oracle_gradient_finite_differences():
     """The MLP oracle's analytic gradient (float64, no BF16 rounding) against
     central differences."""
