@@ -10,8 +10,8 @@
  * (one caller thread at a time), like the reference's programs.
  *
  * Each declaration names the reference routine it replaces (file:line in
- * jhthorpe/myQC).  A Fortran host binds them through iso_c_binding; the
- * interface block is in INTEGRATION.md.
+ * jhthorpe/myQC).  A Fortran host binds them through iso_c_binding with the
+ * interface module include/myqc_gpu.f90.
  */
 #ifndef MYQC_H
 #define MYQC_H
@@ -48,6 +48,11 @@ int mq_last_error(const mq_ctx *ctx, char *buf, int len);
 
 /* Library version string, e.g. "myqc-gb300 0.1 sm_103a". */
 const char *mq_version(void);
+
+/* FP64 fused multiply-add rate of the context's GPU in TFLOP/s, measured by a
+ * short kernel of independent FP64 fma chains.  No counterpart in the
+ * reference: the denominator of the FP64-bound kernels' roofline. */
+int mq_probe_fp64(mq_ctx *ctx, double *tflops);
 
 /* Define the molecule and basis.  Replaces getenv (src/myQC/env.f90:16-74)
  * plus buildBasis (src/myQC/basis.f90:23-226) plus the Ftab read
@@ -93,8 +98,22 @@ int mq_int1p(mq_ctx *ctx, double *Px);
  * resident on the device for mq_fock / mq_ao2mo_iajb. */
 int mq_eri_full(mq_ctx *ctx, double *XX);
 
-/* As mq_eri_full but keeps the array on the device only (no host copy). */
+/* As mq_eri_full but keeps the integrals on the device only (no host copy),
+ * in the storage mq_set_eri_storage selected. */
 int mq_eri_store(mq_ctx *ctx);
+
+/* Device storage of mq_eri_store (no counterpart in the reference, which
+ * writes the full XX file, src/integrals/int2e.f90:540-613):
+ *   MQ_STORE_FULL (default): the n^4 array XX(i,j,g,h), every permutation;
+ *   MQ_STORE_QUARTETS: each contracted shell quartet that passes the Schwarz
+ *     screen (threshold > 0 required at mq_eri_store) stored once as one
+ *     block; the RHF Fock build digests it directly (six FP64 multiply-adds
+ *     per unique integral), and consumers of the full array (UHF builds, the
+ *     four-index transform, mq_eri_full) get it filled from the store on
+ *     first use. */
+#define MQ_STORE_FULL 0
+#define MQ_STORE_QUARTETS 1
+int mq_set_eri_storage(mq_ctx *ctx, int storage);
 
 /* Upload an existing XX (n^4 doubles, the int2e file payload) to the device,
  * e.g. when a drop-in scf reads the reference's XX file. */

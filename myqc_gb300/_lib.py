@@ -20,6 +20,7 @@ MQ_OK, MQ_EINVAL, MQ_ENOMEM, MQ_ECUDA, MQ_ETIMEOUT, MQ_ENOCONV, MQ_ESTATE = rang
 MODE_REFERENCE, MODE_TIGHT = 0, 1
 PREC_FP64, PREC_SPLIT_BF16, PREC_SPLIT_BF16X3 = 0, 1, 2
 FOCK_FP64, FOCK_DF32 = 0, 1
+STORE_FULL, STORE_QUARTETS = 0, 1
 _NAMES = {0: "MQ_OK", 1: "MQ_EINVAL", 2: "MQ_ENOMEM", 3: "MQ_ECUDA", 4: "MQ_ETIMEOUT", 5: "MQ_ENOCONV",
           6: "MQ_ESTATE"}
 
@@ -71,6 +72,8 @@ def lib(path: str | None = None):
     L.mq_norb.argtypes = [vp, ip]
     L.mq_set_schwarz.argtypes = [vp, c_double]
     L.mq_set_eri_mixed.argtypes = [vp, c_double]
+    L.mq_set_eri_storage.argtypes = [vp, c_int]
+    L.mq_probe_fp64.argtypes = [vp, ctypes.POINTER(ctypes.c_double)]
     L.mq_int1e.argtypes = [vp, dp, dp]
     L.mq_int1p.argtypes = [vp, vp]
     L.mq_eri_full.argtypes = [vp, dp]

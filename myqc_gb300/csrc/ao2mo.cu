@@ -23,10 +23,14 @@ namespace mq {
 int ao2mo_device(mq_ctx *c, const double *Ci, int no1, const double *Ca, int nv1, const double *Cj, int no2,
                  const double *Cb, int nv2, int precision, double *d_out) {
   const long long n = c->nao;
-  if (!c->xx_valid) return set_err(c, MQ_ESTATE, "no integrals on the device");
   if (no1 == 0 || nv1 == 0 || no2 == 0 || nv2 == 0) return MQ_OK;  // empty block (e.g. no beta electrons)
+  const int planes = precision == MQ_PREC_SPLIT_BF16X3 ? 3 : 2;
+  if (!c->xx_valid && !(precision != MQ_PREC_FP64 && c->xx_sliced == planes)) {
+    MQ_TRY(ensure_xx_full(c));  // from the quartet store, if that is what mq_eri_store kept
+  }
+  if (precision == MQ_PREC_FP64) MQ_TRY(join_side(c));
   if (precision != MQ_PREC_FP64)
-    return ao2mo_split_device(c, Ci, no1, Ca, nv1, Cj, no2, Cb, nv2, d_out, precision == MQ_PREC_SPLIT_BF16X3 ? 3 : 2);
+    return ao2mo_split_device(c, Ci, no1, Ca, nv1, Cj, no2, Cb, nv2, d_out, planes);
   const size_t y1 = (size_t)(n * n * n) * nv2, y2 = (size_t)(n * n) * no2 * nv2, y3 = (size_t)n * nv1 * no2 * nv2;
   double *Y1 = (double *)buf(c, "ao2mo_y1", sizeof(double) * std::max(y1, y3));
   double *Y2 = (double *)buf(c, "ao2mo_y2", sizeof(double) * y2);

@@ -614,7 +614,7 @@ template <int S>
 static int preslice(mq_ctx *c) {
   const long long n = c->nao;
   const int Kp = (int)((n + 7) / 8 * 8);
-  if (Kp > SLICE_KMAX || !c->xx_valid) return MQ_OK;  // the transform would reject it anyway
+  if (Kp > SLICE_KMAX || (!c->xx_valid && !c->qs.valid)) return MQ_OK;  // the transform would reject it anyway
   const long long rX = n * n * n;
   bf16 *pa = (bf16 *)buf(c, "slice_a", S * rX * Kp * sizeof(bf16));
   int *ea = (int *)buf(c, "slice_ea", rX * sizeof(int));
@@ -632,9 +632,10 @@ static int preslice(mq_ctx *c) {
   MQ_CUDA(c, cudaEventRecord(c->ev_main, c->stream));
   MQ_CUDA(c, cudaStreamWaitEvent(c->side, c->ev_main, 0));
   cudaStream_t main = c->stream;
-  c->stream = c->side;  // slice_rows launches on c->stream
-  const int rc = slice_rows<S, ROW_PAIRS>(c, c->d_XX, n * np, (int)n, n, Kp, Sliced{pa, rX * Kp, ea},
-                                          RowSrc{pairs, n, np});
+  c->stream = c->side;  // the fill from the quartet store and slice_rows launch on c->stream
+  int rc = ensure_xx_full(c);
+  if (rc == MQ_OK)
+    rc = slice_rows<S, ROW_PAIRS>(c, c->d_XX, n * np, (int)n, n, Kp, Sliced{pa, rX * Kp, ea}, RowSrc{pairs, n, np});
   c->stream = main;
   MQ_TRY(rc);
   MQ_CUDA(c, cudaEventRecord(c->ev_side, c->side));

@@ -305,6 +305,12 @@ int build_pairs(mq_ctx *c) {
   MQ_TRY(upload_pairs(c, h, nullptr, c->pt));
   c->pair_class_count = {h.class_off[1] - h.class_off[0], h.class_off[2] - h.class_off[1],
                          h.class_off[3] - h.class_off[2]};
+  c->hp_shA = h.shA;
+  c->hp_shB = h.shB;
+  c->hp_aoA = h.aoA;
+  c->hp_aoB = h.aoB;
+  for (int k = 0; k < 4; ++k) c->hp_class_off[k] = h.class_off[k];
+  c->qs.valid = 0;
   return MQ_OK;
 }
 

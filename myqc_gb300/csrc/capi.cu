@@ -77,7 +77,7 @@ static double *to_dev(mq_ctx *c, const char *name, const double *h, size_t count
   return d;
 }
 
-static int ensure_xx(mq_ctx *c) {
+int ensure_xx_alloc(mq_ctx *c) {
   const size_t n = c->nao, n4 = n * n * n * n;
   if (c->d_XX && c->XX_elems == n4) return MQ_OK;
   if (c->d_XX) cudaFree(c->d_XX);
@@ -88,6 +88,17 @@ static int ensure_xx(mq_ctx *c) {
     return set_err(c, MQ_ENOMEM, "cannot allocate the n^4 integral array on the device");
   }
   c->XX_elems = n4;
+  return MQ_OK;
+}
+
+// The full n^4 array of the current system: already there, or filled from the
+// quartet store (on c->stream).
+int ensure_xx_full(mq_ctx *c) {
+  if (c->xx_valid) return MQ_OK;
+  if (!c->qs.valid) return set_err(c, MQ_ESTATE, "no integrals on the device (call mq_eri_store or mq_eri_upload)");
+  MQ_TRY(ensure_xx_alloc(c));
+  MQ_TRY(qstore_expand(c, c->d_XX));
+  c->xx_valid = 1;
   return MQ_OK;
 }
 
@@ -227,6 +238,7 @@ int mq_set_system(mq_ctx *c, int nnuc, const int *Z, const double *xyz, const do
   c->slab_live_valid = 0;
   c->schwarz_valid = 0;
   c->xx_valid = 0;  // the allocation stays for the next mq_eri_store of the same order
+  c->qs.valid = 0;
   c->have_system = 1;
   if (c->schwarz_thr > 0) MQ_TRY(ensure_schwarz(c));
   return MQ_OK;
@@ -242,7 +254,10 @@ int mq_norb(const mq_ctx *c, int *norb) {
 int mq_set_schwarz(mq_ctx *c, double threshold) {
   if (!c || threshold < 0) return MQ_EINVAL;
   c->schwarz_thr = threshold;
-  if (c->have_system && threshold > 0) return ensure_schwarz(c);
+  if (c->have_system && threshold > 0) {  // bounds of the current system, recomputed
+    c->schwarz_valid = 0;
+    return ensure_schwarz(c);
+  }
   return MQ_OK;
 }
 
@@ -282,11 +297,8 @@ int mq_int1p(mq_ctx *c, double *Px) {
   return MQ_OK;
 }
 
-int mq_eri_store(mq_ctx *c) {
-  MQ_TRY(need_system(c));
-  cudaSetDevice(c->device);
-  MQ_TRY(join_side(c));
-  MQ_TRY(ensure_xx(c));
+static int eri_store_full(mq_ctx *c) {
+  MQ_TRY(ensure_xx_alloc(c));
   // queued on the context's stream; the call returns without waiting (later
   // calls on the context order after it)
   c->t_eri.collect_sync();
@@ -298,9 +310,40 @@ int mq_eri_store(mq_ctx *c) {
   return rc;
 }
 
+int mq_eri_store(mq_ctx *c) {
+  MQ_TRY(need_system(c));
+  cudaSetDevice(c->device);
+  MQ_TRY(join_side(c));
+  c->qs.valid = 0;
+  c->xx_valid = 0;
+  c->xx_sliced = 0;
+  c->slab_live_valid = 0;
+  if (c->eri_storage != MQ_STORE_QUARTETS) return eri_store_full(c);
+  if (!(c->schwarz_thr > 0.0))
+    return set_err(c, MQ_EINVAL, "MQ_STORE_QUARTETS needs a Schwarz threshold > 0 (mq_set_schwarz)");
+  if (c->eri_f32_tau > 0.0) return set_err(c, MQ_EINVAL, "MQ_STORE_QUARTETS stores FP64 integrals only");
+  c->t_eri.collect_sync();
+  c->t_eri.total = 0;
+  c->t_eri.start(c->stream);
+  const int rc = qstore_build(c);
+  c->t_eri.stop(c->stream);
+  return rc;
+}
+
+int mq_set_eri_storage(mq_ctx *c, int storage) {
+  if (!c || (storage != MQ_STORE_FULL && storage != MQ_STORE_QUARTETS)) return MQ_EINVAL;
+  c->eri_storage = storage;
+  return MQ_OK;
+}
+
 int mq_eri_full(mq_ctx *c, double *XX) {
   if (!XX) return set_err(c, MQ_EINVAL, "null output");
-  MQ_TRY(mq_eri_store(c));
+  MQ_TRY(need_system(c));
+  cudaSetDevice(c->device);
+  MQ_TRY(join_side(c));
+  c->qs.valid = 0;
+  c->xx_sliced = 0;
+  MQ_TRY(eri_store_full(c));
   MQ_CUDA(c, cudaMemcpyAsync(XX, c->d_XX, c->XX_elems * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   MQ_CUDA(c, cudaStreamSynchronize(c->stream));
   return MQ_OK;
@@ -311,12 +354,13 @@ int mq_eri_upload(mq_ctx *c, const double *XX) {
   if (!XX) return set_err(c, MQ_EINVAL, "null input");
   cudaSetDevice(c->device);
   MQ_TRY(join_side(c));
-  MQ_TRY(ensure_xx(c));
+  MQ_TRY(ensure_xx_alloc(c));
   MQ_CUDA(c, cudaMemcpyAsync(c->d_XX, XX, c->XX_elems * sizeof(double), cudaMemcpyHostToDevice, c->stream));
   MQ_CUDA(c, cudaStreamSynchronize(c->stream));
   c->slab_live_valid = 0;  // any slab of the uploaded integrals may be nonzero
   c->xx_sliced = 0;
   c->xx_valid = 1;
+  c->qs.valid = 0;
   return MQ_OK;
 }
 
@@ -658,6 +702,9 @@ int mq_stat(const mq_ctx *c, const char *key, double *value) {
   if (!strcmp(key, "eri")) {
     mut->t_eri.collect_sync();
     *value = c->t_eri.total;
+  } else if (!strcmp(key, "eri_kernel")) {  // quartet store: the integral kernels alone (0 otherwise)
+    mut->t_eri_kernel.collect_sync();
+    *value = c->qs.valid ? c->t_eri_kernel.total : 0.0;
   }
   else if (!strcmp(key, "fock")) *value = s.ms_fock;
   else if (!strcmp(key, "diag")) *value = s.ms_diag;
@@ -698,6 +745,9 @@ int mq_stat(const mq_ctx *c, const char *key, double *value) {
     *value = (double)(f32 ? h[prim ? 3 : 2] : h[prim ? 1 : 0] + h[prim ? 3 : 2]);
   }
   else if (!strcmp(key, "eri_f32_tau")) *value = c->eri_f32_tau;
+  else if (!strcmp(key, "store_unique")) *value = c->qs.valid ? c->qs.unique : 0.0;
+  else if (!strcmp(key, "store_quartets")) *value = c->qs.valid ? c->qs.quartets : 0.0;
+  else if (!strcmp(key, "store_bytes")) *value = c->qs.valid ? 8.0 * (double)c->qs.X_elems : 0.0;
   else if (!strcmp(key, "live_slabs")) {  // fraction of XX slabs the digestion reads (1: all)
     unsigned long long h = 0;
     if (c->slab_live_valid && c->d_slab_live_count) {

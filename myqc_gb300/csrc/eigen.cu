@@ -319,7 +319,7 @@ __global__ void __launch_bounds__(RF_THREADS) first_order_kernel(int n, const do
 // cluster solve's, or a previous solve's): orthonormalise, two first-order
 // corrections, FP64 Jacobi cleanup.  d_A keeps the matrix until the last step.
 static int refine_from(mq_ctx *c, int n, double *d_A, double *d_w, double *d_V, bool async, StageTimer *t2,
-                       StageTimer *t3) {
+                       StageTimer *t3, bool jacobi = true) {
   const size_t n2 = (size_t)n * n;
   double *ws = (double *)buf(c, "eig_refine", 3 * n2 * sizeof(double) + 64);
   if (!ws) return MQ_ENOMEM;
@@ -347,6 +347,11 @@ static int refine_from(mq_ctx *c, int n, double *d_A, double *d_w, double *d_V, 
     MQ_TRY(bjorck());
     MQ_TRY(bjorck());
   }
+  if (!jacobi) {  // start vectors only: A is left as it was
+    MQ_CUDA(c, cudaGetLastError());
+    if (t2) t2->stop(c->stream);
+    return MQ_OK;
+  }
   // B = X^T A X replaces A; the FP64 Jacobi rotates from X
   MQ_TRY(gemm(c, 'N', 'N', n, n, n, 1.0, d_A, n, X, n, 0.0, T, n));
   MQ_TRY(gemm(c, 'T', 'N', n, n, n, 1.0, X, n, T, n, 0.0, d_A, n));
@@ -367,6 +372,15 @@ int syev_large_warm(mq_ctx *c, int n, double *d_A, double *d_w, double *d_V) {
     return syev_large_device(c, n, d_A, d_V, d_w, d_V);
   }
   return refine_from(c, n, d_A, d_w, d_V, false, nullptr, nullptr);
+}
+
+int syev_large_start(mq_ctx *c, int n, const double *d_A, double *d_V) {
+  if (n > CJ_MAX || n <= JAC_SMEM_MAX) return set_err(c, MQ_EINVAL, "start vectors: order outside the cluster range");
+  const size_t n2 = (size_t)n * n;
+  double *ws = (double *)buf(c, "eig_refine", 3 * n2 * sizeof(double) + 64);
+  if (!ws) return MQ_ENOMEM;
+  MQ_TRY(jacobi_cluster_f32(c, n, d_A, d_V, (int *)(ws + 3 * n2)));
+  return refine_from(c, n, const_cast<double *>(d_A), nullptr, d_V, true, nullptr, nullptr, false);
 }
 
 int syev_large_cold(mq_ctx *c, int n, double *d_A, double *d_w, double *d_V, bool async) {

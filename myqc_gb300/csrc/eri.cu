@@ -6,7 +6,10 @@
 //               src/integrals/int2e.f90:78-351,540-613);
 //   EPI_SCHWARZ sqrt(max |(ab|ab)|) per shell pair (Schwarz bounds);
 //   EPI_FOCK    digest each unique integral straight into J and K (direct SCF;
-//               the reference digests the stored XX in RHFI2G/UHFI2G).
+//               the reference digests the stored XX in RHFI2G/UHFI2G);
+//   EPI_STORE   write each surviving quartet's integral block once, contiguous,
+//               into the quartet store (qstore.cu), which the sparse Fock
+//               digestion reads instead of the n^4 array.
 //
 // Integral formula (the reference's clmnew, int2e.f90:618-726):
 //   (ab|cd) = sum_prim  2 pi^5/2 / (p q sqrt(p+q)) *
@@ -32,12 +35,14 @@
 #include <string>
 #include <vector>
 
+// the EPI_STORE epilogue returns before the element loop of the other epilogues
+#pragma nv_diag_suppress 128
 #include "boys.cuh"
 #include "internal.h"
 
 namespace mq {
 
-enum { EPI_XX = 0, EPI_SCHWARZ = 1, EPI_FOCK = 2 };
+enum { EPI_XX = 0, EPI_SCHWARZ = 1, EPI_FOCK = 2, EPI_STORE = 3 };
 
 struct EriArgs {
   PairTable t;
@@ -69,6 +74,14 @@ struct EriArgs {
   // inline); nq is then only the bound the grid is sized for
   const long long *list;
   const long long *list_n;
+  // quartet store (EPI_STORE): the launch covers the staircase of one class
+  // combination -- bra rank r holds the ket ranks s < len_r, quartet index
+  // q in [st_off[r], st_off[r+1]) -- with ranks mapped to pairs by permP /
+  // permQ; block q of the launch goes to store + q * (integrals per quartet)
+  const long long *st_off;
+  int st_n;
+  const int *permP, *permQ;
+  double *store;
 };
 
 __host__ __device__ constexpr int fl(int f, int axis) { return f == axis + 1 ? 1 : 0; }  // f: 0 s, 1 px, 2 py, 3 pz
@@ -382,6 +395,19 @@ __device__ __forceinline__ void quartet(const EriArgs &g, int P, int Q, size_t n
       atomicAdd(g.counters + 1, (unsigned long long)np_w);
     }
   }
+  if constexpr (EPI == EPI_STORE) {  // the whole block (this thread's share), layout ((a NB + b) NC + c) ND + d
+    constexpr int NB_ = nfun(LB), NC_ = nfun(LC), ND_ = nfun(LD);
+#pragma unroll
+    for (int a = A0; a < A1; ++a)
+#pragma unroll
+      for (int b = B0; b < B1; ++b)
+#pragma unroll
+        for (int c = C0; c < C1; ++c)
+#pragma unroll
+          for (int d = D0; d < D1; ++d)
+            XXout[((a * NB_ + b) * NC_ + c) * ND_ + d] = (double)acc[a - A0][b - B0][c - C0][d - D0];
+    return;
+  }
 #pragma unroll
   for (int a = A0; a < A1; ++a)
 #pragma unroll
@@ -442,6 +468,18 @@ __device__ __forceinline__ void quartet(const EriArgs &g, int P, int Q, size_t n
 // one system); returns false past the end
 __device__ __forceinline__ bool decode(const EriArgs &g, long long q, int &P, int &Q, int &m) {
   if (q >= g.nq) return false;
+  if (g.st_off) {  // largest r with st_off[r] <= q
+    int lo = 0, hi = g.st_n - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (g.st_off[mid] <= q) lo = mid;
+      else hi = mid - 1;
+    }
+    m = 0;
+    P = g.permP[lo];
+    Q = g.permQ[(int)(q - g.st_off[lo])];
+    return true;
+  }
   const bool listed = g.list != nullptr;
   if (listed) {
     if (q >= *g.list_n) return false;
@@ -596,6 +634,7 @@ __global__ void __launch_bounds__(128) eri_kernel(EriArgs g) {
     n = (size_t)g.mols[m].n;
     XX += g.mols[m].xx;
   }
+  if constexpr (EPI == EPI_STORE) XX = g.store + q * NOUT;
   constexpr int NC = nfun(LC), ND = nfun(LD);
   if (NSPLIT == 1) {
     quartet<LA, LB, LC, LD, 0, NA, 0, NB, 0, NC, 0, ND, EPI, RT>(g, P, Q, n, XX);
@@ -644,7 +683,8 @@ static int launch_class(mq_ctx *c, EriArgs g, int cP, int cQ) {
 #undef MQ_LAUNCH
   c->stats.launches += 1;
   MQ_CUDA(c, cudaGetLastError());
-  return sync_check(c, EPI == EPI_SCHWARZ ? "eri_schwarz" : (EPI == EPI_XX ? "eri_xx" : "eri_fock"));
+  return sync_check(c, EPI == EPI_SCHWARZ ? "eri_schwarz"
+                       : (EPI == EPI_XX ? "eri_xx" : (EPI == EPI_STORE ? "eri_store" : "eri_fock")));
 }
 
 static EriArgs base_args(mq_ctx *c) {
@@ -819,6 +859,31 @@ int eri_full_device(mq_ctx *c, double *d_XX) {
     c->d_slab_live_count = lc;
     c->slab_live_valid = 1;
   }
+  return MQ_OK;
+}
+
+// The quartet store's integral blocks: one launch per class combination over
+// its staircase of surviving quartets (qstore.cu builds the tables first).
+int eri_store_quartets(mq_ctx *c) {
+  QStore &qs = c->qs;
+  unsigned long long *cnt = (unsigned long long *)buf(c, "eri_counters", 4 * sizeof(unsigned long long));
+  if (!cnt) return MQ_ENOMEM;
+  MQ_CUDA(c, cudaMemsetAsync(cnt, 0, 4 * sizeof(unsigned long long), c->stream));
+  EriArgs g = base_args(c);
+  g.counters = cnt;
+  for (int k = 0; k < 6; ++k) {
+    const QCombo &cb = qs.combo[k];
+    if (cb.total == 0) continue;
+    EriArgs h = g;
+    h.nq = cb.total;
+    h.st_off = cb.off;
+    h.st_n = cb.nP;
+    h.permP = qs.perm + qs.cls_off[cb.cP];
+    h.permQ = qs.perm + qs.cls_off[cb.cQ];
+    h.store = qs.X + cb.base;
+    MQ_TRY(launch_class<EPI_STORE>(c, h, cb.cP, cb.cQ));
+  }
+  c->d_eri_counters = cnt;
   return MQ_OK;
 }
 

@@ -654,9 +654,18 @@ int fock_densities(mq_ctx *c, int n, const double *d_Da, const double *d_Db, con
 
 int fock_stored_device(mq_ctx *c, const double *d_Da, const double *d_Db, double *d_Ga, double *d_Gb) {
   const int n = c->nao;
-  if (!c->xx_valid) return set_err(c, MQ_ESTATE, "no integrals on the device (call mq_eri_store or mq_eri_upload)");
-  if (n > 4 * PAIR_MAX_THREADS) return set_err(c, MQ_EINVAL, "stored Fock build supports n <= 1024");
   const bool uhf = d_Db != nullptr;
+  if (c->qs.valid && !uhf && !c->fock_df32) {  // RHF, FP64: digest the quartet store itself
+    c->t_fock_kernel.collect();
+    c->t_fock_kernel.start(c->stream);
+    const int rc = qstore_fock_rhf(c, d_Da, d_Ga);
+    c->t_fock_kernel.stop(c->stream);
+    c->stats.fock_kernel_launches += 1;
+    return rc;
+  }
+  MQ_TRY(ensure_xx_full(c));
+  MQ_TRY(join_side(c));
+  if (n > 4 * PAIR_MAX_THREADS) return set_err(c, MQ_EINVAL, "stored Fock build supports n <= 1024");
   const void *DJ, *DKa, *DKb;
   MQ_TRY(fock_densities(c, n, d_Da, d_Db, &DJ, &DKa, &DKb));
   const int arith = c->fock_df32 ? FOCK_ARITH_DF32 : FOCK_ARITH_F64;
@@ -673,7 +682,8 @@ int fock_stored_device(mq_ctx *c, const double *d_Da, const double *d_Db, double
 int fock_stored_increment(mq_ctx *c, const double *d_Da, const double *d_Db, const double *d_Dpa,
                           const double *d_Dpb, const double *d_Gpa, const double *d_Gpb, double *d_Ga, double *d_Gb) {
   const int n = c->nao;
-  if (!c->xx_valid) return set_err(c, MQ_ESTATE, "no integrals on the device (call mq_eri_store or mq_eri_upload)");
+  MQ_TRY(ensure_xx_full(c));
+  MQ_TRY(join_side(c));
   if (n > 4 * PAIR_MAX_THREADS) return set_err(c, MQ_EINVAL, "stored Fock build supports n <= 1024");
   const bool uhf = d_Db != nullptr;
   if (uhf && d_Gpb != d_Gpa + (size_t)n * n) return set_err(c, MQ_EINVAL, "increment: beta G must follow alpha G");

@@ -90,6 +90,41 @@ struct MolDesc {
   int row_first, pad;
 };
 
+// Quartet store: every contracted shell quartet that survives the Schwarz
+// screen, its integral block written once (qstore.cu).  The pairs of each
+// class are ranked by Schwarz bound, descending; for a class combination
+// (bra class cP >= ket class cQ) the surviving ket ranks of bra rank r are
+// then a prefix s < len_r ("staircase": len_r = m_r, or min(m_r, r + 1) when
+// cP == cQ, with m_r = #{s : bound_P(r) bound_Q(s) >= threshold}).
+struct QCombo {
+  int cP = 0, cQ = 0, tri = 0, nout = 0;  // classes, same class, integrals per quartet
+  int nP = 0, nQ = 0;                     // ranks in the bra and ket class
+  long long total = 0;                    // quartets
+  long long base = 0;                     // offset (doubles) of the combination's blocks in the store
+  long long *off = nullptr;               // device: nP + 1 quartet offsets by bra rank
+  int *len = nullptr;                     // device: nP staircase lengths
+  int *rcol = nullptr;                    // device: per ket rank s, R_s = #{r : m_r > s}
+};
+struct QStore {
+  int valid = 0;        // the store holds the current system's integrals
+  double thr = 0.0;     // Schwarz threshold it was built with
+  int ncls[3] = {0, 0, 0}, cls_off[3] = {0, 0, 0};
+  int *perm = nullptr;  // device: class offset + rank -> pair index
+  QCombo combo[6];      // index cP (cP + 1) / 2 + cQ
+  double *X = nullptr;  // device: the integral blocks
+  size_t X_elems = 0;
+  // digestion tables (device), built with the store
+  int nthr = 0, nsp_pad = 0;  // row-pass threads: sp shells, padded to 32 (nsp_pad), then s shells, padded
+  int *thr_shell = nullptr;   // row-pass thread -> shell (-1: idle)
+  int *lst_off = nullptr;     // [(3 classes x 2 roles) x (nshell + 1)] offsets into lst
+  int *lst = nullptr;         // ranks in class cQ of the pairs whose role-th shell is s, ascending
+  int *ksh_off = nullptr;     // [nshell + 1] offsets into ksh
+  int2 *ksh = nullptr;        // (pair, row offset of the shell in the pair's partial K rows)
+  int *shell_ao0 = nullptr;   // [nshell] first AO of each shell
+  double quartets = 0;        // quartets stored
+  double unique = 0;          // canonical unique integrals stored (the digestion's 6 FMAs each)
+};
+
 struct Stats {
   double ms_eri = 0, ms_fock = 0, ms_diag = 0, ms_ao2mo = 0, ms_mp2 = 0, ms_scf = 0;
   double fock_calls = 0, diag_calls = 0, scf_iters = 0, purify_steps = 0, fock_jc = 0, tune_fock_ms = 0;
@@ -192,6 +227,7 @@ struct mq_ctx {
   void *mlp = nullptr;               // the learned guess's network (mlp.cu)
   mq::StageTimer t_fock_kernel;
   mq::StageTimer t_eri;                       // the last integral pass, collected when asked for
+  mq::StageTimer t_eri_kernel;                // its integral kernels alone (quartet store)
   // live[i + n j] = 0 when every integral of slab XX(:,:,i,j) was screened out
   // (Schwarz bound of the slab's shell pair times the largest bound below the
   // threshold): the slab is zero and the digestion skips it.  Valid for the
@@ -200,6 +236,13 @@ struct mq_ctx {
   int slab_live_valid = 0;
   int schwarz_valid = 0;  // pt.schwarz holds the bounds of the current system
   unsigned long long *d_slab_live_count = nullptr;  // live slabs (i, j), both orders counted
+  // integral storage of mq_eri_store: 0 the full n^4 array (the reference's
+  // XX layout), 1 the quartet store (Schwarz threshold > 0, RHF digestion;
+  // the n^4 array is filled from it when a consumer needs it)
+  int eri_storage = 0;
+  mq::QStore qs;
+  std::vector<int> hp_shA, hp_shB, hp_aoA, hp_aoB;  // host copy of the pair table's shells and AO offsets
+  int hp_class_off[4] = {0, 0, 0, 0};
   unsigned long long *d_eri_counters = nullptr;  // its quartet counters (device)  // the digestion kernel alone, collected at the caller's sync points
   mq::FockTiles fock_tiles[9];  // pair-slab tile tables, indexed by slabs per tile
   int fock_jc[2][3] = {{0, 0, 0}, {0, 0, 0}}, fock_jc_n[2][3] = {{0, 0, 0}, {0, 0, 0}};  // tile length [uhf][arith]
@@ -293,6 +336,17 @@ void tight_boys_table(std::vector<double> &tab);  // TIGHT_NT x TIGHT_NM, row-ma
 
 // eri.cu
 int eri_full_device(mq_ctx *c, double *d_XX);
+// integral blocks of every combination of the quartet store (tables built)
+int eri_store_quartets(mq_ctx *c);
+// qstore.cu: rank the pairs, build the staircase and digestion tables, compute
+// the integral blocks; RHF G from the store; the n^4 array filled from it
+int qstore_build(mq_ctx *c);
+int qstore_fock_rhf(mq_ctx *c, const double *d_D, double *d_G);
+int qstore_expand(mq_ctx *c, double *d_XX);
+// the full n^4 array of the current system: computed (full storage) or filled
+// from the quartet store
+int ensure_xx_full(mq_ctx *c);
+int ensure_xx_alloc(mq_ctx *c);  // the n^4 device array of the current order (capi.cu)
 int eri_schwarz(mq_ctx *c);
 int ensure_schwarz(mq_ctx *c);  // eri_schwarz unless the current system's bounds are there
 int fock_direct_device(mq_ctx *c, const double *d_Da, const double *d_Db, double *d_J, double *d_Ka, double *d_Kb);
@@ -324,6 +378,10 @@ int syev_large_cold(mq_ctx *c, int n, double *d_A, double *d_w, double *d_V, boo
 // from start vectors d_V of a nearby matrix: FP64 refinement by GEMMs (first-order
 // rotations of the separated pairs), then the FP64 Jacobi cleanup (eigen.cu)
 int syev_large_warm(mq_ctx *c, int n, double *d_A, double *d_w, double *d_V);
+// start vectors d_V of a matrix of order JAC_SMEM_MAX < n <= 512 for a later
+// syev_large_warm: FP32 cluster Jacobi and the FP64 first-order refinement,
+// queued on c->stream with no grid-wide barrier and nothing read back (eigen.cu)
+int syev_large_start(mq_ctx *c, int n, const double *d_A, double *d_V);
 // small FP64 products on all SMs (dgemm.cu); gemm() takes them when they fit
 bool dgemm_small_fits(int m, int n, int k);
 int dgemm_small(mq_ctx *c, char ta, char tb, int m, int n, int k, double alpha, const double *A, int lda,

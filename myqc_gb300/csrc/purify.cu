@@ -19,6 +19,7 @@
 // to the eigensolver for that iteration.
 #include <algorithm>
 #include <cmath>
+#include <type_traits>
 #include <vector>
 
 #include "df32.cuh"
@@ -146,10 +147,12 @@ __global__ void identity_kernel(double *__restrict__ A, int n) {
 // ---- All TC2 steps in one cooperative launch (n <= PUR_PERSIST_MAX).
 // CTA b owns the lower-triangle 16x16 tiles b, b + grid, ... of X^2.  X is
 // symmetric, so (X^2)_ij = sum_k X_ki X_kj: the tile's 16 + 16 columns are
-// staged in shared memory as double-float pairs and each thread forms one
-// element in double-float arithmetic on the FP32 pipes (FP64 issues at a small
-// fraction of the FP32 rate here); X itself, the selection and the traces stay
-// FP64.  The selection
+// staged in shared memory and each thread forms one element.  F64 = true
+// (the default): FP64 products and sums.  F64 = false (contexts whose Fock
+// digestion is double-float, mq_set_fock_precision(MQ_FOCK_DF32)): the columns
+// as double-float pairs and the products and sums in double-float on the FP32
+// pipes, which issue many times faster than FP64 on this GPU.  X itself, the
+// selection and the traces are FP64 either way.  The selection
 // needs tr X and tr X^2 of the matrix being squared; tr X^2 = ||X||_F^2, so
 // both come from per-tile partial sums that the previous step wrote with X
 // itself (double-buffered by step parity), and a step is: read the partials,
@@ -180,11 +183,16 @@ __device__ __forceinline__ void tile_partials(double tr, double sq, double *red,
   }
 }
 
+template <bool F64>
 __global__ void __launch_bounds__(256) purify_persist_kernel(int n, double nocc, double *X0,
                                                              double *X1, double *part,
                                                              double *__restrict__ err, int *__restrict__ info,
                                                              GridSync gs) {
-  extern __shared__ float2 cols[];  // [2][16][ld] as double-float pairs, ld = n | 1: a warp's 16 columns hit 16 bank pairs
+  // [2][16][ld] doubles or double-float pairs (8 bytes either way), ld = n | 1:
+  // a warp's 16 columns hit 16 bank pairs
+  typedef typename std::conditional<F64, double, float2>::type Col;
+  extern __shared__ __align__(16) unsigned char cols_raw[];
+  Col *cols = (Col *)cols_raw;
   __shared__ double red[32];
   const int nt = (n + PUR_TILE - 1) / PUR_TILE, ntiles = nt * (nt + 1) / 2;
   const int tid = threadIdx.x, ti = tid % PUR_TILE, tj = tid / PUR_TILE;
@@ -230,7 +238,7 @@ __global__ void __launch_bounds__(256) purify_persist_kernel(int n, double nocc,
       // loads rows e, e + 32, .. (8 loads in flight per batch), no division
       for (int cc = tid >> 5; cc < 2 * PUR_TILE; cc += blockDim.x >> 5) {
         const int col = cc < PUR_TILE ? I * PUR_TILE + cc : J * PUR_TILE + cc - PUR_TILE;
-        float2 *dst = cols + (size_t)cc * ld;
+        Col *dst = cols + (size_t)cc * ld;
         const double *src = X + N * col;
         for (int r0 = tid & 31; r0 < n; r0 += 8 * 32) {
           double v[8];
@@ -242,26 +250,43 @@ __global__ void __launch_bounds__(256) purify_persist_kernel(int n, double nocc,
 #pragma unroll
           for (int u = 0; u < 8; ++u) {
             const int r = r0 + 32 * u;
-            if (r < n) dst[r] = split_f64(v[u]);
+            if (r < n) {
+              if constexpr (F64) dst[r] = v[u];
+              else dst[r] = split_f64(v[u]);
+            }
           }
         }
       }
       __syncthreads();
       const int i = I * PUR_TILE + ti, j = J * PUR_TILE + tj;
       const double xij = (i < n && j < n) ? X[i + N * j] : 0.0;
-      const float2 *ci = cols + (size_t)ti * ld, *cj = cols + (size_t)(PUR_TILE + tj) * ld;
-      // (X^2)_ij in double-float on the FP32 pipes (about 2^-48 relative per
-      // product), four interleaved sums
-      float2 t0 = make_float2(0.f, 0.f), t1 = t0, t2 = t0, t3 = t0;
-      int r = 0;
-      for (; r + 3 < n; r += 4) {
-        dfma(t0, ci[r], cj[r]);
-        dfma(t1, ci[r + 1], cj[r + 1]);
-        dfma(t2, ci[r + 2], cj[r + 2]);
-        dfma(t3, ci[r + 3], cj[r + 3]);
+      const Col *ci = cols + (size_t)ti * ld, *cj = cols + (size_t)(PUR_TILE + tj) * ld;
+      double t;
+      if constexpr (F64) {  // (X^2)_ij in FP64, four interleaved sums
+        double t0 = 0.0, t1 = 0.0, t2 = 0.0, t3 = 0.0;
+        int r = 0;
+        for (; r + 3 < n; r += 4) {
+          t0 = fma(ci[r], cj[r], t0);
+          t1 = fma(ci[r + 1], cj[r + 1], t1);
+          t2 = fma(ci[r + 2], cj[r + 2], t2);
+          t3 = fma(ci[r + 3], cj[r + 3], t3);
+        }
+        for (; r < n; ++r) t0 = fma(ci[r], cj[r], t0);
+        t = (t0 + t1) + (t2 + t3);
+      } else {
+        // (X^2)_ij in double-float on the FP32 pipes (about 2^-48 relative per
+        // product), four interleaved sums
+        float2 t0 = make_float2(0.f, 0.f), t1 = t0, t2 = t0, t3 = t0;
+        int r = 0;
+        for (; r + 3 < n; r += 4) {
+          dfma(t0, ci[r], cj[r]);
+          dfma(t1, ci[r + 1], cj[r + 1]);
+          dfma(t2, ci[r + 2], cj[r + 2]);
+          dfma(t3, ci[r + 3], cj[r + 3]);
+        }
+        for (; r < n; ++r) dfma(t0, ci[r], cj[r]);
+        t = (df_val(t0) + df_val(t1)) + (df_val(t2) + df_val(t3));
       }
-      for (; r < n; ++r) dfma(t0, ci[r], cj[r]);
-      const double t = (df_val(t0) + df_val(t1)) + (df_val(t2) + df_val(t3));
       double ptr = 0.0, psq = 0.0;
       if (i < n && j < n) {
         const double y = square ? t : 2.0 * xij - t;
@@ -283,24 +308,25 @@ __global__ void __launch_bounds__(256) purify_persist_kernel(int n, double nocc,
 static int purify_persistent(mq_ctx *c, int n, int nocc, double *d_P, double *d_W, double *d_err, int *steps) {
   const size_t n2 = (size_t)n * n;
   const int nt = (n + PUR_TILE - 1) / PUR_TILE, ntiles = nt * (nt + 1) / 2;
-  const size_t smem = (size_t)2 * PUR_TILE * (n | 1) * sizeof(float2);
+  const size_t smem = (size_t)2 * PUR_TILE * (n | 1) * sizeof(double);
+  const void *kfn = c->fock_df32 ? (const void *)purify_persist_kernel<false> : (const void *)purify_persist_kernel<true>;
   char *ws = (char *)buf(c, "purify_persist", 256 + 64 + sizeof(double) * 4 * ntiles);
   if (!ws) return MQ_ENOMEM;
   GridSync gs{(unsigned *)ws, (unsigned *)(ws + 64), (int *)(ws + 128)};
   int *info = (int *)(ws + 192);
   double *part = (double *)(ws + 320);
   MQ_CUDA(c, cudaMemsetAsync(ws, 0, 320, c->stream));
-  MQ_CUDA(c, cudaFuncSetAttribute(purify_persist_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  MQ_CUDA(c, cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int sms = 0, per_sm = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
-  MQ_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, purify_persist_kernel, 256, smem));
+  MQ_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, 256, smem));
   if (per_sm < 1) return set_err(c, MQ_EINVAL, "purification kernel does not fit on an SM");
   // one tile per CTA where the tiles allow; every CTA must be resident
   int grid = std::min(ntiles, sms * per_sm);
   double *X0 = d_P, *X1 = d_W;
   double noccd = (double)nocc;
   void *args[] = {&n, &noccd, &X0, &X1, &part, &d_err, &info, &gs};
-  MQ_CUDA(c, cudaLaunchCooperativeKernel((void *)purify_persist_kernel, dim3(grid), dim3(256), args, smem,
+  MQ_CUDA(c, cudaLaunchCooperativeKernel(kfn, dim3(grid), dim3(256), args, smem,
                                          c->stream));
   c->stats.launches += 1;
   int h[2] = {0, 0}, berr = 0;

@@ -226,7 +226,8 @@ int scf_device(mq_ctx *c, const double *S, const double *H, const mq_scf_opts *o
   const double occf = uhf ? 1.0 : 2.0;
   if (!uhf && o->nalpha != o->nbeta) return set_err(c, MQ_EINVAL, "RHF needs nalpha == nbeta");
   if (nocc[0] > n || nocc[1] > n || nocc[0] < 0 || nocc[1] < 0) return set_err(c, MQ_EINVAL, "bad occupation");
-  if (!o->direct && !c->xx_valid) return set_err(c, MQ_ESTATE, "no stored integrals for a conventional SCF");
+  if (!o->direct && !c->xx_valid && !c->qs.valid)
+    return set_err(c, MQ_ESTATE, "no stored integrals for a conventional SCF");
 
   // device workspace
   const size_t nmat = 8 + 8 * ns + (size_t)2 * ndiis * ns;
@@ -337,15 +338,12 @@ int scf_device(mq_ctx *c, const double *S, const double *H, const mq_scf_opts *o
   constexpr double EARLY_EIG_RMS = 1e-5;
   bool early = false;  // queued, not yet joined
   double *dFe = nullptr, *dAe = nullptr, *dUe = nullptr, *dTe = nullptr, *dEe = nullptr;
+  bool early_vectors = false;  // the early solve queued start vectors into dUe
   auto join_early = [&](bool use) -> int {  // the main stream after the early solve; its vectors into dU when use
     if (!early) return MQ_OK;
     early = false;
     MQ_CUDA(c, cudaStreamWaitEvent(c->stream, c->ev_early, 0));
-    cudaStream_t main = c->stream;
-    c->stream = c->aux;
-    const int st = syev_large_status(c);  // synchronises the aux stream
-    c->stream = main;
-    if (!use || st != MQ_OK) return MQ_OK;  // a failed early solve only costs the warm start
+    if (!use || !early_vectors) return MQ_OK;
     MQ_CUDA(c, cudaMemcpyAsync(dU, dUe, n2 * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
     have_prev = true;
     refine_prev = true;
@@ -368,14 +366,22 @@ int scf_device(mq_ctx *c, const double *S, const double *H, const mq_scf_opts *o
     c->stream = c->aux;
     int rc = gemm(c, 'T', 'N', n, n, n, 1.0, dX, n, dFe, n, 0.0, dTe, n);
     if (rc == MQ_OK) rc = gemm(c, 'N', 'N', n, n, n, 1.0, dTe, n, dX, n, 0.0, dAe, n);
-    if (rc == MQ_OK) rc = syev_large_cold(c, n, dAe, dEe, dUe, true);
+    // start vectors only: the grid-barrier FP64 Jacobi of the final solve
+    // runs on the main stream after the iterations, never beside another
+    // cooperatively launched kernel (the purification)
+    bool started = false;
     if (rc == MQ_OK) {
-      const cudaError_t e = cudaEventRecord(c->ev_early, c->aux);
-      if (e != cudaSuccess) rc = cuda_check(c, e, "cudaEventRecord (early eigensolve)");
+      rc = syev_large_start(c, n, dAe, dUe);
+      started = rc == MQ_OK;
+      if (rc == MQ_EINVAL) rc = MQ_OK;  // an order without the cluster solver: no warm start
     }
+    // the event marks the end of whatever was queued on the aux stream
+    const cudaError_t ev = cudaEventRecord(c->ev_early, c->aux);
+    if (rc == MQ_OK && ev != cudaSuccess) rc = cuda_check(c, ev, "cudaEventRecord (early eigensolve)");
     c->stream = main;
     MQ_TRY(rc);
     early = true;
+    early_vectors = started;
     return MQ_OK;
   };
   auto density_step = [&](const double *Fm, double *Dout) -> int {

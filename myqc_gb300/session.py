@@ -188,6 +188,11 @@ class Context:
     def set_schwarz(self, thr: float):
         self._check(self.L.mq_set_schwarz(self.h, thr))
 
+    def set_eri_storage(self, storage: int):
+        """_lib.STORE_FULL (the n^4 array, default) or _lib.STORE_QUARTETS (each
+        screened shell quartet once; needs a Schwarz threshold > 0)."""
+        self._check(self.L.mq_set_eri_storage(self.h, int(storage)))
+
     def set_eri_mixed(self, tau: float):
         """Quartets with a Schwarz bound below tau in FP32 (tight mode; 0: all FP64)."""
         self._check(self.L.mq_set_eri_mixed(self.h, float(tau)))
@@ -318,6 +323,12 @@ class Context:
         C = np.zeros((n, n), order="F")
         self._check(self.L.mq_sygv(self.h, n, ptr(F_), ptr(S_), ptr(w), ptr(C)))
         return w, C
+
+    def probe_fp64(self) -> float:
+        """FP64 fma rate of this GPU in TFLOP/s (a short measuring kernel)."""
+        v = ctypes.c_double()
+        self._check(self.L.mq_probe_fp64(self.h, ctypes.byref(v)))
+        return v.value
 
     def stat(self, key: str) -> float:
         v = ctypes.c_double()

@@ -7,21 +7,40 @@ import os
 import bench
 
 
+def _per(**kw):
+    base = {k: 0.0 for k in ("fock", "fock_calls", "fock_kernel", "fock_kernel_launches", "eri", "eri_kernel",
+                             "quartets", "quartets_f32", "prim_quartets", "diag", "ao2mo", "mp2", "fock_inc_builds",
+                             "store_unique", "store_bytes")}
+    base.update(kw)
+    return base
+
+
 def test_piece_rooflines_arithmetic():
     n, o = 224, 160
     v = n - o
     peaks = {"hbm_gbs": 6000.0, "bf16_tflops": 2000.0}
-    r = bench.piece_rooflines(n, o, ms_eri=20.0, quartets=4e6, ms_ao2mo=10.0, ms_mp2=0.5, peaks=peaks)
-    assert r["peak_source"] == "measured"
+    per = _per(eri=25.0, eri_kernel=20.0, quartets=4e6, prim_quartets=1e8, ao2mo=10.0, mp2=0.5, fock_kernel=12.0,
+               fock_kernel_launches=12.0, store_unique=5e7, store_bytes=4e8)
+    r = bench.piece_rooflines(n, o, per, peaks, 1.25)
+    assert r["peak_source"] == "measured" and r["fp64_peak_tflops"] == 1.25
     assert abs(r["eri"]["quartets_per_s"] - 2e8) < 1.0
+    # digestion: 6 fma (12 FP64 flops) per unique integral per build of 1 ms
+    assert abs(r["fock"]["achieved_tflops"] - 12.0 * 5e7 / 1e-3 / 1e12) < 1e-9
+    assert abs(r["fock"]["frac"] - r["fock"]["achieved_tflops"] / 1.25) < 1e-12
+    assert abs(r["fock"]["store_gbs"] - 4e8 / 1e-3 / 1e9) < 1e-9
     fl = 2.0 * (o * n ** 4 + o * v * n ** 3 + o * o * v * n * n + o * o * v * v * n)
     assert abs(r["ao2mo"]["algorithmic_flop"] - fl) < 1.0
     assert abs(r["ao2mo"]["achieved_tflops"] - fl / 1e-2 / 1e12) < 1e-9
     assert abs(r["ao2mo"]["hbm_frac"] - 8.0 * n ** 4 / 1e-2 / 1e9 / 6000.0) < 1e-12
     assert abs(r["mp2"]["achieved_gbs"] - 8.0 * o * o * v * v / 5e-4 / 1e9) < 1e-6
+    if "achieved_tflops" in r["eri"]:  # with the committed FP64 count per primitive quartet
+        f = r["eri"]["fp64_flop_per_prim_quartet"]
+        assert abs(r["eri"]["achieved_tflops"] - 1e8 * f / 2e-2 / 1e12) < 1e-9
+        top = bench.dominant_roofline(r)
+        assert top["bound"] == "fp64" and top["achieved"] == r["eri"]["achieved_tflops"]
     # no timings: no entries, and fallback peaks without a peaks file
-    r = bench.piece_rooflines(n, o, 0.0, 0.0, 0.0, 0.0, {})
-    assert r["peak_source"] == "fallback" and "ao2mo" not in r and "mp2" not in r
+    r = bench.piece_rooflines(n, o, _per(), {}, 1.25)
+    assert r["peak_source"] == "fallback" and "ao2mo" not in r and "mp2" not in r and "fock" not in r
 
 
 class _Done:
@@ -69,18 +88,17 @@ def test_threshold_flags():
             raise AssertionError(bad)
 
 
-def test_cpu_extrapolation_by_loop_counts():
-    """A sample of the cluster itself extrapolates to its own times (x iterations
-    for the Fock digestion); one of half the waters scales by the loop counts."""
+def test_cpu_fit_and_extrapolation():
+    """Stage times that grow as N^k in the cluster size N are fitted with
+    exponent k and extrapolated exactly; the SCF is iterations x (digestion +
+    one DSYGV)."""
     nm = bench.NMOL
-    t = {"int1e": 1.0, "int2e": 2.0, "fock": 3.0, "ao2mo": 4.0, "mp2": 5.0}
-    s = {"n": 7 * nm, "nset": 12 * nm, "nnuc": 3 * nm, "no": 5 * nm, "t": t}
-    r = bench._extrapolate(s, 25)
-    assert r == {"int1e": 1.0, "int2e": 2.0, "scf": 75.0, "ao2mo": 4.0, "mp2": 5.0}
-    h = nm // 2
-    s = {"n": 7 * h, "nset": 12 * h, "nnuc": 3 * h, "no": 5 * h, "t": t}
-    r = bench._extrapolate(s, 1)
-    f = nm / h
-    expect = {"int1e": f ** 3, "int2e": 2.0 * f ** 4, "scf": 3.0 * f ** 4, "ao2mo": 4.0 * f ** 5,
-              "mp2": 5.0 * f ** 4}
-    assert all(abs(r[k] - v) <= 1e-12 * v for k, v in expect.items()), r
+    pts = []
+    for N in (3, 4, 5, 6):
+        pts.append({"nmol": N, "t": {"int1e": 1e-3 * N ** 2, "int2e": 1e-4 * N ** 3.5, "fock": 1e-5 * N ** 4,
+                                     "ao2mo": 1e-6 * N ** 5, "mp2": 1e-7 * N ** 4}})
+    fit, ext = bench.fit_and_extrapolate(pts, 10, 0.02)
+    assert abs(fit["int2e"]["exponent"] - 3.5) < 1e-9 and abs(fit["ao2mo"]["exponent"] - 5.0) < 1e-9
+    expect = {"int1e": 1e-3 * nm ** 2, "int2e": 1e-4 * nm ** 3.5, "scf": 10 * (1e-5 * nm ** 4 + 0.02),
+              "ao2mo": 1e-6 * nm ** 5, "mp2": 1e-7 * nm ** 4}
+    assert all(abs(ext[k] - v) <= 1e-9 * v for k, v in expect.items()), ext

@@ -81,11 +81,11 @@ def test_header_symbols_exported():
 
 
 def test_fortran_module_binds_every_entry_point():
-    """The Fortran interface module of INTEGRATION.md has one BIND(C) interface
-    per function include/myqc.h declares, and no other."""
+    """The Fortran interface module include/myqc_gpu.f90 has one BIND(C)
+    interface per function include/myqc.h declares, and no other."""
     import re
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-    text = open(os.path.join(root, "INTEGRATION.md")).read()
+    text = open(os.path.join(root, "include", "myqc_gpu.f90")).read()
     module = text[text.index("MODULE myqc_gpu"):text.index("END MODULE")]
     bound = set(re.findall(r"FUNCTION (mq_\w+)\(", module))
     assert bound == set(_lib.header_symbols()), (set(_lib.header_symbols()) ^ bound)
