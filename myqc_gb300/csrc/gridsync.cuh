@@ -3,7 +3,8 @@
 // bounded: after BARRIER_SPIN_LIMIT polls it raises err = 2 and returns false,
 // and every CTA that sees a raised flag leaves its wait too, so a kernel whose
 // barrier fails ends instead of hanging.  Words: count, gen, err (zeroed
-// before the launch, on separate 64-byte lines).
+// before the launch, on separate 64-byte lines); on a timeout err[1..3] hold
+// the arrivals counted, the CTA that gave up and the barrier generation.
 #pragma once
 
 namespace mq {
@@ -30,6 +31,10 @@ __device__ __forceinline__ bool grid_barrier(const GridSync &gs, unsigned nblock
       long long it = 0;
       while (*genv == g) {
         if (++it > BARRIER_SPIN_LIMIT) {
+          // record where the wait gave up: arrivals seen, this CTA, generation
+          gs.err[1] = (int)*(volatile unsigned *)gs.count;
+          gs.err[2] = (int)blockIdx.x;
+          gs.err[3] = (int)g;
           atomicExch(gs.err, 2);
           break;
         }

@@ -114,10 +114,13 @@ struct QStore {
   double *X = nullptr;  // device: the integral blocks
   size_t X_elems = 0;
   // digestion tables (device), built with the store
-  int nthr = 0, nsp_pad = 0;  // row-pass threads: sp shells, padded to 32 (nsp_pad), then s shells, padded
+  int nthr = 0, nsp_pad = 0;  // row-pass threads: sp-shell AOs, padded to 32 (nsp_pad), then s AOs, padded
   int *thr_shell = nullptr;   // row-pass thread -> shell (-1: idle)
+  int *thr_ao = nullptr;      // row-pass thread -> its AO column
+  int4 *rinfo = nullptr;      // by class offset + rank: pair, A | B << 16, i0 | j0 << 16
   int *lst_off = nullptr;     // [(3 classes x 2 roles) x (nshell + 1)] offsets into lst
-  int *lst = nullptr;         // ranks in class cQ of the pairs whose role-th shell is s, ascending
+  int4 *lst = nullptr;        // pairs of class cQ whose role-th shell is s, by ascending rank:
+                              // (rank, pair, C | D << 16, k0 | l0 << 16)
   int *ksh_off = nullptr;     // [nshell + 1] offsets into ksh
   int2 *ksh = nullptr;        // (pair, row offset of the shell in the pair's partial K rows)
   int *shell_ao0 = nullptr;   // [nshell] first AO of each shell

@@ -12,6 +12,8 @@
 // below tol * ||A||_F; the result is sorted ascending.
 #include <cublas_v2.h>
 
+#include <string>
+
 #include "internal.h"
 #include "gridsync.cuh"
 #include "jacobi.cuh"
@@ -243,6 +245,9 @@ int syev_large_device(mq_ctx *c, int n, double *d_A, const double *d_V0, double 
   double tol = 1e-14;  // ||offdiag||_F / ||A||_F at stop; eigenvalue error ~ tol^2 ||A|| / gap
   int *info = (int *)(ws + 192);
   void *args[] = {&n, &d_A, &V, &d_w, &d_V, &part, &gs, &max_sweeps, &tol, &info};
+  // every CTA of a grid-barrier kernel must be resident at once: nothing of
+  // the side stream (the transform's XX slicing) runs beside it
+  if (c->stream != c->side) MQ_TRY(join_side(c));
   MQ_CUDA(c, cudaLaunchCooperativeKernel((void *)jacobi_grid_kernel, dim3(nblocks), dim3(JG_THREADS), args, 0,
                                          c->stream));
   c->stats.launches += 2;
@@ -254,13 +259,16 @@ int syev_large_status(mq_ctx *c) {
   auto it = c->bufs.find("jacobi_grid");
   if (it == c->bufs.end() || !it->second.ptr) return MQ_OK;  // no grid solve ran
   const char *ws = (const char *)it->second.ptr;
-  int h = 0, sw = 0;
-  MQ_CUDA(c, cudaMemcpyAsync(&h, ws + 128, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  int h[4] = {0, 0, 0, 0}, sw = 0;
+  MQ_CUDA(c, cudaMemcpyAsync(h, ws + 128, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
   MQ_CUDA(c, cudaMemcpyAsync(&sw, ws + 192, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   MQ_CUDA(c, cudaStreamSynchronize(c->stream));
   c->stats.eig_jacobi_sweeps = sw;
-  if (h == 2) return set_err(c, MQ_ETIMEOUT, "Jacobi grid barrier timed out");
-  if (h == 1) return set_err(c, MQ_ENOCONV, "Jacobi eigensolver did not converge");
+  if (h[0] == 2)
+    return set_err(c, MQ_ETIMEOUT, "Jacobi grid barrier timed out (" + std::to_string(h[1]) + " arrivals counted, CTA " +
+                                       std::to_string(h[2]) + ", barrier " + std::to_string(h[3]) + ", sweeps " +
+                                       std::to_string(sw) + ")");
+  if (h[0] == 1) return set_err(c, MQ_ENOCONV, "Jacobi eigensolver did not converge");
   return MQ_OK;
 }
 

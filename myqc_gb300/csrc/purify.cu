@@ -19,6 +19,7 @@
 // to the eigensolver for that iteration.
 #include <algorithm>
 #include <cmath>
+#include <string>
 #include <type_traits>
 #include <vector>
 
@@ -329,11 +330,14 @@ static int purify_persistent(mq_ctx *c, int n, int nocc, double *d_P, double *d_
   MQ_CUDA(c, cudaLaunchCooperativeKernel(kfn, dim3(grid), dim3(256), args, smem,
                                          c->stream));
   c->stats.launches += 1;
-  int h[2] = {0, 0}, berr = 0;
+  int h[2] = {0, 0}, berr[4] = {0, 0, 0, 0};
   MQ_CUDA(c, cudaMemcpyAsync(h, info, 2 * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-  MQ_CUDA(c, cudaMemcpyAsync(&berr, gs.err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  MQ_CUDA(c, cudaMemcpyAsync(berr, gs.err, sizeof(berr), cudaMemcpyDeviceToHost, c->stream));
   MQ_CUDA(c, cudaStreamSynchronize(c->stream));
-  if (berr) return set_err(c, MQ_ETIMEOUT, "purification grid barrier timed out");
+  if (berr[0])
+    return set_err(c, MQ_ETIMEOUT, "purification grid barrier timed out (" + std::to_string(berr[1]) +
+                                       " arrivals counted of " + std::to_string(grid) + ", CTA " +
+                                       std::to_string(berr[2]) + ", barrier " + std::to_string(berr[3]) + ")");
   *steps = h[0];
   if (!h[1]) return set_err(c, MQ_ENOCONV, "purification did not converge (no gap at the Fermi level?)");
   if (h[0] & 1) MQ_CUDA(c, cudaMemcpyAsync(d_P, d_W, n2 * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));

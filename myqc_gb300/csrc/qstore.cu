@@ -49,7 +49,10 @@ __host__ __device__ constexpr int nfa(int cls) { return cls >= 1 ? 4 : 1; }
 __host__ __device__ constexpr int nfb(int cls) { return cls == 2 ? 4 : 1; }
 __host__ __device__ constexpr int combo_index(int cP, int cQ) { return cP * (cP + 1) / 2 + cQ; }
 
-constexpr int QS_THREADS = 256;
+constexpr int QS_THREADS = 256;      // row pass: AO columns (x shares) per CTA
+constexpr int QS_COL_THREADS = 256;  // column pass
+constexpr int QS_SHARES[3] = {1, 2, 4};  // row-pass CTAs per bra pair, by bra class
+constexpr int QS_MAX_SHARES = 4;
 
 // rank of each pair of one class by Schwarz bound, descending (ties: pair
 // index); the bounds are >= 0, so their bit patterns order like the values
@@ -77,7 +80,11 @@ struct QsArgs {
   const int *rcol[6];
   const int *thr_shell;
   int nthr, nsp_pad;
-  const int *lst_off, *lst;
+  const int *lst_off;
+  const int4 *lst;
+  const int4 *rinfo;  // by class offset + rank: pair, A | B << 16, i0 | j0 << 16
+  const int *thr_ao;
+  int nshare[3];  // row-pass shares (CTAs per bra pair) by bra class
   const int2 *ksh;
   const int *ksh_off;
   const int *shell_ao0;
@@ -89,86 +96,88 @@ struct QsArgs {
   double *Jh, *Kh;
 };
 
-// canonical-element weight of (i,j,k,l) in a degenerate block (0: not canonical)
+// canonical-element weight of (i,j,k,l) in a degenerate block (0: not
+// canonical; else 1/2 for each of i = j, k = l, (i,j) = (k,l)), from integer
+// tests and one table entry
 __device__ __forceinline__ double canon_weight(int A, int B, int C, int Dsh, int P, int Q, int i, int j, int k, int l,
-                                               size_t n) {
-  if (A == B && i < j) return 0.0;
-  if (C == Dsh && k < l) return 0.0;
-  if (P == Q && (size_t)i * n + j < (size_t)k * n + l) return 0.0;
-  double w = 1.0;
-  if (i == j) w *= 0.5;
-  if (k == l) w *= 0.5;
-  if (i == k && j == l) w *= 0.5;
-  return w;
+                                               int n) {
+  const bool zero = (A == B && i < j) || (C == Dsh && k < l) || (P == Q && i * n + j < k * n + l);
+  const int h = (i == j) + (k == l) + (i == k && j == l);
+  return zero ? 0.0 : (h == 0 ? 1.0 : (h == 1 ? 0.5 : (h == 2 ? 0.25 : 0.125)));
 }
 
-// One role of a row-pass thread: the kets Q of class CQ whose ROLE-th shell
-// (0: first, 1: second) is the thread's shell -- ranks from lst[lo, hi),
-// ascending -- up to the staircase length of bra rank r.
+// The contribution of one ket block to a row-pass thread's column f.  DEGEN:
+// the block has A = B, C = D or P = Q, and its elements carry the canonical
+// weights (an integer test per element; the general blocks need none).
+template <int NA, int NB, int NC, int ND, int ROLE, bool DEGEN>
+__device__ __forceinline__ void row_block(const double *__restrict__ Xb, const double *__restrict__ D, size_t n,
+                                          int A, int B, int C, int Dsh, int P, int Q, int i0, int j0, int k0, int l0,
+                                          int f, double (&KA)[4], double (&KB)[4], double (&Jr)[4][4]) {
+  if (ROLE == 0) {  // column k = k0 + f: Kh[i,k] += x D[j,l], Kh[j,k] += x D[i,l], Jh[i,j] += x D[k,l]
+#pragma unroll 1
+    for (int d = 0; d < ND; ++d) {
+      double Dbd[NB], Dad[NA];
+#pragma unroll
+      for (int b = 0; b < NB; ++b) Dbd[b] = D[(j0 + b) + n * (l0 + d)];
+#pragma unroll
+      for (int a = 0; a < NA; ++a) Dad[a] = D[(i0 + a) + n * (l0 + d)];
+      const double Dcd = D[(k0 + f) + n * (l0 + d)];
+#pragma unroll
+      for (int a = 0; a < NA; ++a)
+#pragma unroll
+        for (int b = 0; b < NB; ++b) {
+          double x = Xb[((a * NB + b) * NC + f) * ND + d];
+          if (DEGEN) x *= canon_weight(A, B, C, Dsh, P, Q, i0 + a, j0 + b, k0 + f, l0 + d, (int)n);
+          KA[a] = fma(x, Dbd[b], KA[a]);
+          KB[b] = fma(x, Dad[a], KB[b]);
+          Jr[a][b] = fma(x, Dcd, Jr[a][b]);
+        }
+    }
+  } else {  // column l = l0 + f: Kh[i,l] += x D[j,k], Kh[j,l] += x D[i,k]
+#pragma unroll 1
+    for (int c = 0; c < NC; ++c) {
+      double Dbc[NB], Dac[NA];
+#pragma unroll
+      for (int b = 0; b < NB; ++b) Dbc[b] = D[(j0 + b) + n * (k0 + c)];
+#pragma unroll
+      for (int a = 0; a < NA; ++a) Dac[a] = D[(i0 + a) + n * (k0 + c)];
+#pragma unroll
+      for (int a = 0; a < NA; ++a)
+#pragma unroll
+        for (int b = 0; b < NB; ++b) {
+          double x = Xb[((a * NB + b) * NC + c) * ND + f];
+          if (DEGEN) x *= canon_weight(A, B, C, Dsh, P, Q, i0 + a, j0 + b, k0 + c, l0 + f, (int)n);
+          KA[a] = fma(x, Dbc[b], KA[a]);
+          KB[b] = fma(x, Dac[a], KB[b]);
+        }
+    }
+  }
+}
+
+// One role of a row-pass thread, which owns AO column f of shell s: the kets
+// Q of class CQ whose ROLE-th shell (0: first, 1: second) is s -- ranks from
+// lst[lo, hi), ascending, every S-th from lo + k (the column's S threads
+// share the list) -- up to the staircase length of bra rank r.
 template <int CP, int CQ, int ROLE>
-__device__ __forceinline__ void row_role(const QsArgs &g, int r, int P, int A, int B, int i0, int j0, int lo, int hi,
-                                         double (&KA)[4][4], double (&KB)[4][4], double (&Jr)[4][4]) {
+__device__ __forceinline__ void row_role(const QsArgs &g, int r, int P, int A, int B, int i0, int j0, int f, int lo,
+                                         int hi, int k, int S, double (&KA)[4], double (&KB)[4], double (&Jr)[4][4]) {
   constexpr int NA = nfa(CP), NB = nfb(CP), NC = nfa(CQ), ND = nfb(CQ);
   constexpr int NOUT = NA * NB * NC * ND;
   constexpr int K = combo_index(CP, CQ);
   const int lenr = g.len[K][r];
   const double *Xc = g.X + g.base[K] + (size_t)g.off[K][r] * NOUT;
-  const int *permQ = g.perm + g.cls_off[CQ];
   const size_t n = g.n;
   const double *D = g.D;
-  for (int e = lo; e < hi; ++e) {
-    const int t = g.lst[e];
-    if (t >= lenr) break;  // ranks ascend: the rest lie beyond the staircase
-    const int Q = permQ[t];
-    const int C = g.shA[Q], Dsh = g.shB[Q], k0 = g.aoA[Q], l0 = g.aoB[Q];
-    const double *Xb = Xc + (size_t)t * NOUT;
-    const bool degen = (A == B) || (C == Dsh) || (P == Q);
-    if (ROLE == 0) {
-      // Kh[i,k] += x D[j,l], Kh[j,k] += x D[i,l], Jh[i,j] += x D[k,l]
-#pragma unroll
-      for (int d = 0; d < ND; ++d) {
-        double Dbd[NB], Dad[NA], Dcd[NC];
-#pragma unroll
-        for (int b = 0; b < NB; ++b) Dbd[b] = D[(j0 + b) + n * (l0 + d)];
-#pragma unroll
-        for (int a = 0; a < NA; ++a) Dad[a] = D[(i0 + a) + n * (l0 + d)];
-#pragma unroll
-        for (int c = 0; c < NC; ++c) Dcd[c] = D[(k0 + c) + n * (l0 + d)];
-#pragma unroll
-        for (int a = 0; a < NA; ++a)
-#pragma unroll
-          for (int b = 0; b < NB; ++b)
-#pragma unroll
-            for (int c = 0; c < NC; ++c) {
-              double x = Xb[((a * NB + b) * NC + c) * ND + d];
-              if (degen) x *= canon_weight(A, B, C, Dsh, P, Q, i0 + a, j0 + b, k0 + c, l0 + d, n);
-              KA[a][c] = fma(x, Dbd[b], KA[a][c]);
-              KB[b][c] = fma(x, Dad[a], KB[b][c]);
-              Jr[a][b] = fma(x, Dcd[c], Jr[a][b]);
-            }
-      }
-    } else {
-      // Kh[i,l] += x D[j,k], Kh[j,l] += x D[i,k]
-#pragma unroll
-      for (int c = 0; c < NC; ++c) {
-        double Dbc[NB], Dac[NA];
-#pragma unroll
-        for (int b = 0; b < NB; ++b) Dbc[b] = D[(j0 + b) + n * (k0 + c)];
-#pragma unroll
-        for (int a = 0; a < NA; ++a) Dac[a] = D[(i0 + a) + n * (k0 + c)];
-#pragma unroll
-        for (int a = 0; a < NA; ++a)
-#pragma unroll
-          for (int b = 0; b < NB; ++b)
-#pragma unroll
-            for (int d = 0; d < ND; ++d) {
-              double x = Xb[((a * NB + b) * NC + c) * ND + d];
-              if (degen) x *= canon_weight(A, B, C, Dsh, P, Q, i0 + a, j0 + b, k0 + c, l0 + d, n);
-              KA[a][d] = fma(x, Dbc[b], KA[a][d]);
-              KB[b][d] = fma(x, Dac[a], KB[b][d]);
-            }
-      }
-    }
+#pragma unroll 1
+  for (int e = lo + k; e < hi; e += S) {
+    const int4 q = g.lst[e];  // rank, pair, shells C | D << 16, AOs k0 | l0 << 16
+    if (q.x >= lenr) break;   // ranks ascend: the rest lie beyond the staircase
+    const int Q = q.y, C = q.z & 0xffff, Dsh = q.z >> 16, k0 = q.w & 0xffff, l0 = q.w >> 16;
+    const double *Xb = Xc + (size_t)q.x * NOUT;
+    if ((A == B) || (C == Dsh) || (P == Q))
+      row_block<NA, NB, NC, ND, ROLE, true>(Xb, D, n, A, B, C, Dsh, P, Q, i0, j0, k0, l0, f, KA, KB, Jr);
+    else
+      row_block<NA, NB, NC, ND, ROLE, false>(Xb, D, n, A, B, C, Dsh, P, Q, i0, j0, k0, l0, f, KA, KB, Jr);
   }
 }
 
@@ -179,14 +188,48 @@ __device__ __forceinline__ void list_range(const QsArgs &g, int s, int &lo, int 
   hi = o[s + 1];
 }
 
-// Row pass for the bra pairs of class CP: CTA = bra rank, thread = shell
-// (sp shells first, padded to whole warps, then s shells: warps never mix the
-// two code paths).
+// All roles of the row-pass thread of column slot t (shell s), list share k of S.
+template <int CP>
+__device__ __forceinline__ void row_column(const QsArgs &g, int r, int P, int A, int B, int i0, int j0, int t, int k,
+                                           int S, double (&KA)[4], double (&KB)[4], double (&Jr)[4][4]) {
+  const int s = g.thr_shell[t];
+  if (s < 0) return;
+  const int f = g.thr_ao[t] - g.shell_ao0[s];
+  int lo, hi;
+  if (t < g.nsp_pad) {  // sp-shell AOs (uniform per warp)
+    if constexpr (CP >= 1) {
+      list_range<1, 0>(g, s, lo, hi);
+      row_role<CP, 1, 0>(g, r, P, A, B, i0, j0, f, lo, hi, k, S, KA, KB, Jr);
+    }
+    if constexpr (CP >= 2) {
+      list_range<2, 0>(g, s, lo, hi);
+      row_role<CP, 2, 0>(g, r, P, A, B, i0, j0, f, lo, hi, k, S, KA, KB, Jr);
+      list_range<2, 1>(g, s, lo, hi);
+      row_role<CP, 2, 1>(g, r, P, A, B, i0, j0, f, lo, hi, k, S, KA, KB, Jr);
+    }
+  } else {
+    list_range<0, 0>(g, s, lo, hi);
+    row_role<CP, 0, 0>(g, r, P, A, B, i0, j0, 0, lo, hi, k, S, KA, KB, Jr);
+    list_range<0, 1>(g, s, lo, hi);
+    row_role<CP, 0, 1>(g, r, P, A, B, i0, j0, 0, lo, hi, k, S, KA, KB, Jr);
+    if constexpr (CP >= 1) {
+      list_range<1, 1>(g, s, lo, hi);
+      row_role<CP, 1, 1>(g, r, P, A, B, i0, j0, 0, lo, hi, k, S, KA, KB, Jr);
+    }
+  }
+}
+
+// Row pass for the bra pairs of class CP: CTA (bra rank, share k of S), thread
+// = one AO column (the four AOs of each sp shell first, padded to whole
+// warps, then the s shells: warps never mix the two code paths).  Share k
+// takes every S-th ket of each list; its partial rows and row part of Jh go to
+// its own slice (the assembly adds the S slices in order), so the result does
+// not depend on timing.
 template <int CP>
 __global__ void __launch_bounds__(QS_THREADS) qs_row_kernel(QsArgs g) {
   constexpr int NA = nfa(CP), NB = nfb(CP);
   __shared__ double red[QS_THREADS / 32][NA * NB];
-  const int r = blockIdx.x;
+  const int r = blockIdx.x, k = blockIdx.y, S = gridDim.y;
   const int P = g.perm[g.cls_off[CP] + r];
   const int A = g.shA[P], B = g.shB[P], i0 = g.aoA[P], j0 = g.aoB[P];
   const size_t n = g.n;
@@ -195,46 +238,16 @@ __global__ void __launch_bounds__(QS_THREADS) qs_row_kernel(QsArgs g) {
   for (int a = 0; a < 4; ++a)
 #pragma unroll
     for (int b = 0; b < 4; ++b) Jr[a][b] = 0.0;
+  double *kp0 = g.Kpart + ((size_t)k * g.npairs + P) * 8 * n;
   for (int t = threadIdx.x; t < g.nthr; t += blockDim.x) {
-    const int s = g.thr_shell[t];
-    if (s < 0) continue;
-    const bool sp = t < g.nsp_pad;  // uniform per warp
-    double KA[4][4], KB[4][4];
+    double KA[4] = {0.0, 0.0, 0.0, 0.0}, KB[4] = {0.0, 0.0, 0.0, 0.0};
+    row_column<CP>(g, r, P, A, B, i0, j0, t, k, S, KA, KB, Jr);
+    if (g.thr_shell[t] < 0) continue;
+    double *kp = kp0 + g.thr_ao[t];  // this column of P's partial rows: A's rows, then B's
 #pragma unroll
-    for (int a = 0; a < 4; ++a)
+    for (int a = 0; a < NA; ++a) kp[(size_t)a * n] = KA[a];
 #pragma unroll
-      for (int f = 0; f < 4; ++f) KA[a][f] = KB[a][f] = 0.0;
-    int lo, hi;
-    if (sp) {
-      if constexpr (CP >= 1) {
-        list_range<1, 0>(g, s, lo, hi);
-        row_role<CP, 1, 0>(g, r, P, A, B, i0, j0, lo, hi, KA, KB, Jr);
-      }
-      if constexpr (CP >= 2) {
-        list_range<2, 0>(g, s, lo, hi);
-        row_role<CP, 2, 0>(g, r, P, A, B, i0, j0, lo, hi, KA, KB, Jr);
-        list_range<2, 1>(g, s, lo, hi);
-        row_role<CP, 2, 1>(g, r, P, A, B, i0, j0, lo, hi, KA, KB, Jr);
-      }
-    } else {
-      list_range<0, 0>(g, s, lo, hi);
-      row_role<CP, 0, 0>(g, r, P, A, B, i0, j0, lo, hi, KA, KB, Jr);
-      list_range<0, 1>(g, s, lo, hi);
-      row_role<CP, 0, 1>(g, r, P, A, B, i0, j0, lo, hi, KA, KB, Jr);
-      if constexpr (CP >= 1) {
-        list_range<1, 1>(g, s, lo, hi);
-        row_role<CP, 1, 1>(g, r, P, A, B, i0, j0, lo, hi, KA, KB, Jr);
-      }
-    }
-    // this thread's columns of P's partial rows: A's rows, then B's
-    const int ns = sp ? 4 : 1, c0 = g.shell_ao0[s];
-    double *kp = g.Kpart + (size_t)P * 8 * n;
-#pragma unroll
-    for (int a = 0; a < NA; ++a)
-      for (int f = 0; f < ns; ++f) kp[(size_t)a * n + c0 + f] = KA[a][f];
-#pragma unroll
-    for (int b = 0; b < NB; ++b)
-      for (int f = 0; f < ns; ++f) kp[(size_t)(NA + b) * n + c0 + f] = KB[b][f];
+    for (int b = 0; b < NB; ++b) kp[(size_t)(NA + b) * n] = KB[b];
   }
   // row part of Jh over P's block: warp sums, then the warps in order
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -250,8 +263,8 @@ __global__ void __launch_bounds__(QS_THREADS) qs_row_kernel(QsArgs g) {
   __syncthreads();
   if (threadIdx.x < NA * NB) {
     double v = 0.0;
-    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) v += red[k][threadIdx.x];
-    g.Jrow[(size_t)P * 16 + threadIdx.x] = v;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) v += red[q][threadIdx.x];
+    g.Jrow[((size_t)k * g.npairs + P) * 16 + threadIdx.x] = v;
   }
 }
 
@@ -264,12 +277,11 @@ __device__ __forceinline__ void col_combo(const QsArgs &g, int s, int Q, int C, 
   constexpr int NOUT = NA * NB * NC * ND;
   constexpr int K = combo_index(CP, CQ);
   const int r0 = CP == CQ ? s : 0, r1 = g.rcol[K][s];
-  const int *permP = g.perm + g.cls_off[CP];
   const size_t n = g.n;
   const double *D = g.D;
   for (int r = r0 + (int)threadIdx.x; r < r1; r += blockDim.x) {
-    const int P = permP[r];
-    const int A = g.shA[P], B = g.shB[P], i0 = g.aoA[P], j0 = g.aoB[P];
+    const int4 pi = g.rinfo[g.cls_off[CP] + r];  // pair, A | B << 16, i0 | j0 << 16
+    const int P = pi.x, A = pi.y & 0xffff, B = pi.y >> 16, i0 = pi.z & 0xffff, j0 = pi.z >> 16;
     const double *Xb = g.X + g.base[K] + ((size_t)g.off[K][r] + s) * NOUT;
     const bool degen = (A == B) || (C == Dsh) || (P == Q);
     double Dab[NA][NB];
@@ -286,16 +298,16 @@ __device__ __forceinline__ void col_combo(const QsArgs &g, int s, int Q, int C, 
 #pragma unroll
           for (int d = 0; d < ND; ++d) {
             double x = Xb[((a * NB + b) * NC + c) * ND + d];
-            if (degen) x *= canon_weight(A, B, C, Dsh, P, Q, i0 + a, j0 + b, k0 + c, l0 + d, n);
+            if (degen) x *= canon_weight(A, B, C, Dsh, P, Q, i0 + a, j0 + b, k0 + c, l0 + d, (int)n);
             Jc[c][d] = fma(x, Dab[a][b], Jc[c][d]);
           }
   }
 }
 
 template <int CQ>
-__global__ void __launch_bounds__(QS_THREADS) qs_col_kernel(QsArgs g) {
+__global__ void __launch_bounds__(QS_COL_THREADS) qs_col_kernel(QsArgs g) {
   constexpr int NC = nfa(CQ), ND = nfb(CQ);
-  __shared__ double red[QS_THREADS / 32][NC * ND];
+  __shared__ double red[QS_COL_THREADS / 32][NC * ND];
   const int s = blockIdx.x;
   const int Q = g.perm[g.cls_off[CQ] + s];
   const int C = g.shA[Q], Dsh = g.shB[Q], k0 = g.aoA[Q], l0 = g.aoB[Q];
@@ -333,12 +345,14 @@ __global__ void qs_khat_kernel(QsArgs g) {
   const int ns = (S + 1 < g.nshell ? g.shell_ao0[S + 1] : g.n) - a0;
   const size_t n = g.n;
   const int e0 = g.ksh_off[S], e1 = g.ksh_off[S + 1];
-  for (int idx = threadIdx.x; idx < ns * g.n; idx += blockDim.x) {
+  for (int idx = blockIdx.y * blockDim.x + threadIdx.x; idx < ns * g.n; idx += gridDim.y * blockDim.x) {
     const int a = idx / g.n, col = idx % g.n;
     double v = 0.0;
     for (int e = e0; e < e1; ++e) {
       const int2 pr = g.ksh[e];
-      v += g.Kpart[(size_t)pr.x * 8 * n + (size_t)(pr.y + a) * n + col];
+      const int cls = pr.x >= g.cls_off[2] ? 2 : (pr.x >= g.cls_off[1] ? 1 : 0);
+      for (int k = 0; k < g.nshare[cls]; ++k)
+        v += g.Kpart[((size_t)k * g.npairs + pr.x) * 8 * n + (size_t)(pr.y + a) * n + col];
     }
     g.Kh[(a0 + a) + n * col] = 2.0 * v;
   }
@@ -352,8 +366,11 @@ __global__ void qs_jhat_kernel(QsArgs g) {
   const int NA = nfa(cls), NB = nfb(cls), i0 = g.aoA[P], j0 = g.aoB[P];
   const size_t n = g.n;
   for (int a = 0; a < NA; ++a)
-    for (int b = 0; b < NB; ++b)
-      g.Jh[(i0 + a) + n * (j0 + b)] = 4.0 * (g.Jrow[(size_t)P * 16 + a * NB + b] + g.Jcol[(size_t)P * 16 + a * NB + b]);
+    for (int b = 0; b < NB; ++b) {
+      double v = 0.0;
+      for (int k = 0; k < g.nshare[cls]; ++k) v += g.Jrow[((size_t)k * g.npairs + P) * 16 + a * NB + b];
+      g.Jh[(i0 + a) + n * (j0 + b)] = 4.0 * (v + g.Jcol[(size_t)P * 16 + a * NB + b]);
+    }
 }
 
 // G = (Jh + Jh^T)/2 - f (Kh + Kh^T)/2
@@ -519,33 +536,47 @@ int qstore_build(mq_ctx *c) {
       o_len[k] = blob.add(len.data(), len.size());
       o_rcol[k] = blob.add(rcol.data(), rcol.size());
     }
-  // row-pass threads: sp shells (padded to a warp multiple), then s shells
-  std::vector<int> thr_shell;
-  int nsp = 0;
+  // row-pass threads, one per AO column: the four AOs of each sp shell
+  // (padded to a warp multiple), then the s shells' AOs (padded)
+  std::vector<int> thr_shell, thr_ao;
   for (int s = 0; s < nsh; ++s)
-    if (c->shells[s].type == 1) {
-      thr_shell.push_back(s);
-      ++nsp;
-    }
-  while (thr_shell.size() % 32) thr_shell.push_back(-1);
+    if (c->shells[s].type == 1)
+      for (int f = 0; f < 4; ++f) {
+        thr_shell.push_back(s);
+        thr_ao.push_back(c->shells[s].ao0 + f);
+      }
+  while (thr_shell.size() % 32) {
+    thr_shell.push_back(-1);
+    thr_ao.push_back(0);
+  }
   const int nsp_pad = (int)thr_shell.size();
   for (int s = 0; s < nsh; ++s)
-    if (c->shells[s].type == 0) thr_shell.push_back(s);
-  while (thr_shell.size() % 32) thr_shell.push_back(-1);
-  // per (ket class, role, shell): the ranks of the pairs whose role-th shell is s
-  std::vector<int> lst_off(6 * (nsh + 1), 0), lst;
+    if (c->shells[s].type == 0) {
+      thr_shell.push_back(s);
+      thr_ao.push_back(c->shells[s].ao0);
+    }
+  while (thr_shell.size() % 32) {
+    thr_shell.push_back(-1);
+    thr_ao.push_back(0);
+  }
+  if (nsh > 0xffff || n > 0xffff) return set_err(c, MQ_EINVAL, "quartet store: more than 65535 shells or AOs");
+  // per (ket class, role, shell): the pairs whose role-th shell is s, by
+  // ascending rank, packed (rank, pair, C | D << 16, k0 | l0 << 16)
+  std::vector<int> lst_off(6 * (nsh + 1), 0);
+  std::vector<int4> lst;
   {
-    std::vector<std::vector<int>> l(6 * nsh);
+    std::vector<std::vector<int4>> l(6 * nsh);
     for (int cl = 0; cl < 3; ++cl)
       for (int t = 0; t < qs.ncls[cl]; ++t) {
         const int p = perm[co[cl] + t];
-        l[(cl * 2 + 0) * nsh + c->hp_shA[p]].push_back(t);
-        l[(cl * 2 + 1) * nsh + c->hp_shB[p]].push_back(t);
+        const int4 e = make_int4(t, p, c->hp_shA[p] | (c->hp_shB[p] << 16), c->hp_aoA[p] | (c->hp_aoB[p] << 16));
+        l[(cl * 2 + 0) * nsh + c->hp_shA[p]].push_back(e);
+        l[(cl * 2 + 1) * nsh + c->hp_shB[p]].push_back(e);
       }
     for (int g = 0; g < 6; ++g)
       for (int s = 0; s < nsh; ++s) {
         lst_off[g * (nsh + 1) + s] = (int)lst.size();
-        for (int t : l[g * nsh + s]) lst.push_back(t);
+        for (const int4 &e : l[g * nsh + s]) lst.push_back(e);
         lst_off[g * (nsh + 1) + s + 1] = (int)lst.size();
       }
   }
@@ -569,7 +600,14 @@ int qstore_build(mq_ctx *c) {
   for (int s = 0; s < nsh; ++s) ao0[s] = c->shells[s].ao0;
   for (int s = 1; s < nsh; ++s)
     if (ao0[s] <= ao0[s - 1]) return set_err(c, MQ_EINVAL, "shell AOs out of order");
+  std::vector<int4> rinfo(np);
+  for (int k = 0; k < np; ++k) {
+    const int p = perm[k];
+    rinfo[k] = make_int4(p, c->hp_shA[p] | (c->hp_shB[p] << 16), c->hp_aoA[p] | (c->hp_aoB[p] << 16), 0);
+  }
+  const size_t o_ri = blob.add(rinfo.data(), rinfo.size());
   const size_t o_thr = blob.add(thr_shell.data(), thr_shell.size());
+  const size_t o_tao = blob.add(thr_ao.data(), thr_ao.size());
   const size_t o_lo = blob.add(lst_off.data(), lst_off.size());
   const size_t o_l = blob.add(lst.data(), lst.size());
   const size_t o_ko = blob.add(ksh_off.data(), ksh_off.size());
@@ -587,7 +625,9 @@ int qstore_build(mq_ctx *c) {
   qs.nsp_pad = nsp_pad;
   qs.thr_shell = (int *)(d + o_thr);
   qs.lst_off = (int *)(d + o_lo);
-  qs.lst = (int *)(d + o_l);
+  qs.lst = (int4 *)(d + o_l);
+  qs.thr_ao = (int *)(d + o_tao);
+  qs.rinfo = (int4 *)(d + o_ri);
   qs.ksh_off = (int *)(d + o_ko);
   qs.ksh = (int2 *)(d + o_k);
   qs.shell_ao0 = (int *)(d + o_ao);
@@ -630,6 +670,8 @@ static QsArgs qs_args(mq_ctx *c) {
   g.nsp_pad = qs.nsp_pad;
   g.lst_off = qs.lst_off;
   g.lst = qs.lst;
+  g.thr_ao = qs.thr_ao;
+  g.rinfo = qs.rinfo;
   g.ksh = qs.ksh;
   g.ksh_off = qs.ksh_off;
   g.shell_ao0 = qs.shell_ao0;
@@ -644,26 +686,32 @@ int qstore_fock_rhf(mq_ctx *c, const double *d_D, double *d_G) {
   if (!qs.valid) return set_err(c, MQ_ESTATE, "no quartet store");
   const int n = c->nao, np = c->pt.npairs;
   const size_t N = n, n2 = N * N;
-  double *w = (double *)buf(c, "qstore_fock", sizeof(double) * ((size_t)np * 8 * N + (size_t)np * 32 + 2 * n2));
+  const size_t SH = QS_MAX_SHARES;
+  double *w = (double *)buf(c, "qstore_fock",
+                            sizeof(double) * (SH * np * 8 * N + SH * np * 16 + (size_t)np * 16 + 2 * n2));
   if (!w) return MQ_ENOMEM;
   QsArgs g = qs_args(c);
   g.D = d_D;
   g.Kpart = w;
-  g.Jrow = w + (size_t)np * 8 * N;
-  g.Jcol = g.Jrow + (size_t)np * 16;
+  g.Jrow = w + SH * np * 8 * N;
+  g.Jcol = g.Jrow + SH * np * 16;
   g.Jh = g.Jcol + (size_t)np * 16;
   g.Kh = g.Jh + n2;
   // pairs that are no bra (or no ket) of any stored quartet still get their
   // partial rows and J parts written (as zeros) by their own CTAs
   MQ_CUDA(c, cudaMemsetAsync(g.Jh, 0, sizeof(double) * n2, c->stream));
-  const int rt = std::min(QS_THREADS, qs.nthr);  // one thread per shell where they fit
-  if (qs.ncls[0]) qs_row_kernel<0><<<qs.ncls[0], rt, 0, c->stream>>>(g);
-  if (qs.ncls[1]) qs_row_kernel<1><<<qs.ncls[1], rt, 0, c->stream>>>(g);
-  if (qs.ncls[2]) qs_row_kernel<2><<<qs.ncls[2], rt, 0, c->stream>>>(g);
-  if (qs.ncls[0]) qs_col_kernel<0><<<qs.ncls[0], QS_THREADS, 0, c->stream>>>(g);
-  if (qs.ncls[1]) qs_col_kernel<1><<<qs.ncls[1], QS_THREADS, 0, c->stream>>>(g);
-  if (qs.ncls[2]) qs_col_kernel<2><<<qs.ncls[2], QS_THREADS, 0, c->stream>>>(g);
-  qs_khat_kernel<<<c->nshell, QS_THREADS, 0, c->stream>>>(g);
+  // shares per bra pair: the (sp,sp) and (sp,s) bras have the longest rows
+  g.nshare[0] = QS_SHARES[0];
+  g.nshare[1] = QS_SHARES[1];
+  g.nshare[2] = QS_SHARES[2];
+  const int rt = std::min(QS_THREADS, qs.nthr);
+  if (qs.ncls[0]) qs_row_kernel<0><<<dim3(qs.ncls[0], g.nshare[0]), rt, 0, c->stream>>>(g);
+  if (qs.ncls[1]) qs_row_kernel<1><<<dim3(qs.ncls[1], g.nshare[1]), rt, 0, c->stream>>>(g);
+  if (qs.ncls[2]) qs_row_kernel<2><<<dim3(qs.ncls[2], g.nshare[2]), rt, 0, c->stream>>>(g);
+  if (qs.ncls[0]) qs_col_kernel<0><<<qs.ncls[0], QS_COL_THREADS, 0, c->stream>>>(g);
+  if (qs.ncls[1]) qs_col_kernel<1><<<qs.ncls[1], QS_COL_THREADS, 0, c->stream>>>(g);
+  if (qs.ncls[2]) qs_col_kernel<2><<<qs.ncls[2], QS_COL_THREADS, 0, c->stream>>>(g);
+  qs_khat_kernel<<<dim3(c->nshell, (4 * n + QS_COL_THREADS - 1) / QS_COL_THREADS), QS_COL_THREADS, 0, c->stream>>>(g);
   qs_jhat_kernel<<<(np + 127) / 128, 128, 0, c->stream>>>(g);
   qs_combine_kernel<<<(unsigned)((n2 + 255) / 256), 256, 0, c->stream>>>(g.Jh, g.Kh, n, 0.5, d_G);
   c->stats.launches += 9;
