@@ -111,6 +111,14 @@ int mq_eri_store(mq_ctx *ctx);
  *     per unique integral), and consumers of the full array (UHF builds, the
  *     four-index transform, mq_eri_full) get it filled from the store on
  *     first use. */
+/* This process's share of one molecule's Fock builds when several processes
+ * (one GPU each) split it: the quartet store and the direct RHF build keep
+ * only the shell quartets whose bra shell pair index is part mod nparts, so
+ * mq_fock / mq_fock_direct return that share's part of G; the sum over the
+ * parts (one all-reduce of n x n doubles) is the full G.  No counterpart in
+ * the reference (one process, src/I2G/RHFI2G.f90:80-90).  (0, 1): no split. */
+int mq_set_partition(mq_ctx *ctx, int part, int nparts);
+
 #define MQ_STORE_FULL 0
 #define MQ_STORE_QUARTETS 1
 int mq_set_eri_storage(mq_ctx *ctx, int storage);

@@ -61,6 +61,9 @@ MODULE myqc_gpu
     INTEGER(c_int) FUNCTION mq_probe_fp64(ctx, tflops) BIND(C)
       IMPORT; TYPE(c_ptr), VALUE :: ctx; REAL(c_double) :: tflops
     END FUNCTION
+    INTEGER(c_int) FUNCTION mq_set_partition(ctx, part, nparts) BIND(C)
+      IMPORT; TYPE(c_ptr), VALUE :: ctx; INTEGER(c_int), VALUE :: part, nparts
+    END FUNCTION
     INTEGER(c_int) FUNCTION mq_set_eri_storage(ctx, storage) BIND(C)
       IMPORT; TYPE(c_ptr), VALUE :: ctx; INTEGER(c_int), VALUE :: storage   ! MQ_STORE_FULL / MQ_STORE_QUARTETS
     END FUNCTION

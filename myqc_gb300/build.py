@@ -64,7 +64,7 @@ def build(force: bool = False, verbose: bool = False, extra=()) -> str:
             list(ex.map(lambda s: _compile(s, extra), todo))
     objs = [os.path.join(BUILD, s.replace(".cu", ".o")) for s in srcs]
     if force or todo or _stale(LIB, objs):
-        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcublas"]
+        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stderr}")

@@ -311,6 +311,7 @@ int build_pairs(mq_ctx *c) {
   c->hp_aoB = h.aoB;
   for (int k = 0; k < 4; ++k) c->hp_class_off[k] = h.class_off[k];
   c->qs.valid = 0;
+  c->qs.tables_valid = 0;
   return MQ_OK;
 }
 

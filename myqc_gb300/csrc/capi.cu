@@ -132,7 +132,6 @@ int mq_init(mq_ctx **ctx, int device) {
   if (cudaSetDevice(device) != cudaSuccess) return MQ_ECUDA;
   mq_ctx *c = new mq_ctx();
   c->device = device;
-  if (const char *e = getenv("MYQC_DGEMM")) c->dgemm_cublas = !strcmp(e, "cublas");
   // priorities (lower is higher): the aux stream's short network passes, then
   // the main stream, then the side stream's overlapping slicing
   int prio_lo = 0, prio_hi = 0;
@@ -162,7 +161,6 @@ int mq_free(mq_ctx *c) {
   if (c->d_boys_f32) cudaFree(c->d_boys_f32);
   if (c->d_boys) cudaFree(c->d_boys);
   if (c->d_nuc) cudaFree(c->d_nuc);
-  if (c->cublas) cublas_destroy(c->cublas);
   if (c->pin) cudaFreeHost(c->pin);
   cudaStreamDestroy(c->stream);
   if (c->side) cudaStreamDestroy(c->side);
@@ -254,6 +252,8 @@ int mq_norb(const mq_ctx *c, int *norb) {
 int mq_set_schwarz(mq_ctx *c, double threshold) {
   if (!c || threshold < 0) return MQ_EINVAL;
   c->schwarz_thr = threshold;
+  c->qs.valid = 0;
+  c->qs.tables_valid = 0;
   if (c->have_system && threshold > 0) {  // bounds of the current system, recomputed
     c->schwarz_valid = 0;
     return ensure_schwarz(c);
@@ -318,7 +318,10 @@ int mq_eri_store(mq_ctx *c) {
   c->xx_valid = 0;
   c->xx_sliced = 0;
   c->slab_live_valid = 0;
-  if (c->eri_storage != MQ_STORE_QUARTETS) return eri_store_full(c);
+  if (c->eri_storage != MQ_STORE_QUARTETS) {
+    if (c->nparts > 1) return set_err(c, MQ_EINVAL, "a partition of the quartets needs MQ_STORE_QUARTETS");
+    return eri_store_full(c);
+  }
   if (!(c->schwarz_thr > 0.0))
     return set_err(c, MQ_EINVAL, "MQ_STORE_QUARTETS needs a Schwarz threshold > 0 (mq_set_schwarz)");
   if (c->eri_f32_tau > 0.0) return set_err(c, MQ_EINVAL, "MQ_STORE_QUARTETS stores FP64 integrals only");
@@ -328,6 +331,15 @@ int mq_eri_store(mq_ctx *c) {
   const int rc = qstore_build(c);
   c->t_eri.stop(c->stream);
   return rc;
+}
+
+int mq_set_partition(mq_ctx *c, int part, int nparts) {
+  if (!c || nparts < 1 || part < 0 || part >= nparts) return MQ_EINVAL;
+  c->part = part;
+  c->nparts = nparts;
+  c->qs.valid = 0;
+  c->qs.tables_valid = 0;
+  return MQ_OK;
 }
 
 int mq_set_eri_storage(mq_ctx *c, int storage) {
@@ -383,7 +395,11 @@ static int fock_common(mq_ctx *c, const double *Da, const double *Db, double *Ga
   c->t_fock_kernel.total = 0;
   c->stats.fock_kernel_launches = 0;
   int rc;
-  if (direct) {
+  if (direct && !Db && !c->fock_df32) {  // RHF: integral blocks recomputed into the store, digested from it
+    rc = fock_direct_store_rhf(c, dD, dG);
+  } else if (c->nparts > 1 && (Db || c->fock_df32)) {
+    rc = set_err(c, MQ_EINVAL, "a partition of the quartets serves RHF FP64 builds only");
+  } else if (direct) {
     double *J = dG + n2 * ns, *Ka = J + n2, *Kb = Db ? Ka + n2 : nullptr;
     rc = fock_direct_device(c, dD, Db ? dD + n2 : nullptr, J, Ka, Kb);
     if (rc == MQ_OK) rc = direct_combine(c, J, Ka, Kb, dG, Db ? dG + n2 : nullptr);

@@ -107,6 +107,7 @@ struct QCombo {
 };
 struct QStore {
   int valid = 0;        // the store holds the current system's integrals
+  int tables_valid = 0; // ranking, staircase and digestion tables of the current system and thr
   double thr = 0.0;     // Schwarz threshold it was built with
   int ncls[3] = {0, 0, 0}, cls_off[3] = {0, 0, 0};
   int *perm = nullptr;  // device: class offset + rank -> pair index
@@ -198,8 +199,6 @@ struct mq_ctx {
   cudaEvent_t ev_early = nullptr;  // the SCF's early eigensolve on the aux stream
   int ao2mo_prefetch = 0;  // planes (2, 3) to slice XX into ahead of the transform; 0: off
   int xx_sliced = 0;       // the slice buffers hold XX cut into this many planes (0: not)
-  void *cublas = nullptr;
-  int dgemm_cublas = 0;  // MYQC_DGEMM=cublas: every FP64 product through cuBLAS (comparison runs)
   std::string err;
   // system
   int have_system = 0;
@@ -243,6 +242,9 @@ struct mq_ctx {
   // XX layout), 1 the quartet store (Schwarz threshold > 0, RHF digestion;
   // the n^4 array is filled from it when a consumer needs it)
   int eri_storage = 0;
+  // this process's share of a single molecule's quartets (mq_set_partition):
+  // the quartet-store rows whose bra pair index is part mod nparts
+  int part = 0, nparts = 1;
   mq::QStore qs;
   std::vector<int> hp_shA, hp_shB, hp_aoA, hp_aoB;  // host copy of the pair table's shells and AO offsets
   int hp_class_off[4] = {0, 0, 0, 0};
@@ -346,6 +348,9 @@ int eri_store_quartets(mq_ctx *c);
 int qstore_build(mq_ctx *c);
 int qstore_fock_rhf(mq_ctx *c, const double *d_D, double *d_G);
 int qstore_expand(mq_ctx *c, double *d_XX);
+// direct RHF G (no integrals kept between builds): the store's integral blocks
+// recomputed, then digested like a stored build (atomic-free, deterministic)
+int fock_direct_store_rhf(mq_ctx *c, const double *d_D, double *d_G);
 // the full n^4 array of the current system: computed (full storage) or filled
 // from the quartet store
 int ensure_xx_full(mq_ctx *c);
@@ -389,6 +394,10 @@ int syev_large_start(mq_ctx *c, int n, const double *d_A, double *d_V);
 bool dgemm_small_fits(int m, int n, int k);
 int dgemm_small(mq_ctx *c, char ta, char tb, int m, int n, int k, double alpha, const double *A, int lda,
                 const double *B, int ldb, double beta, double *C, int ldc);
+// any FP64 product, batched over blockIdx.z with strides sA, sB, sC (dgemm.cu)
+int dgemm_batched(mq_ctx *c, char ta, char tb, int m, int n, int k, double alpha, const double *A, int lda,
+                  long long sA, const double *B, int ldb, long long sB, double beta, double *C, int ldc,
+                  long long sC, int batch);
 int gemm(mq_ctx *c, char ta, char tb, int m, int n, int k, double alpha, const double *A, int lda, const double *B,
          int ldb, double beta, double *C, int ldc);
 int gemm_strided_batched(mq_ctx *c, char ta, char tb, int m, int n, int k, double alpha, const double *A, int lda,
@@ -404,7 +413,6 @@ int purify_projector(mq_ctx *c, int n, int nocc, const double *d_Fp, double *d_P
 // X = S^-1/2 by the coupled Newton-Schulz iteration (w: 5 n^2 doubles of
 // scratch, d_err: >= 101 doubles); MQ_ENOCONV when it does not settle
 int inv_sqrt_ns(mq_ctx *c, int n, const double *d_S, double *d_X, double *w, double *d_err, int *steps);
-void cublas_destroy(void *handle);
 
 // ao2mo.cu
 int ao2mo_device(mq_ctx *c, const double *d_Ci, int no1, const double *d_Ca, int nv1, const double *d_Cj, int no2,

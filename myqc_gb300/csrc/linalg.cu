@@ -10,7 +10,6 @@
 // eigenvectors live in shared memory when 2 n^2 doubles fit, else in a
 // global workspace.  Converges when the off-diagonal Frobenius norm falls
 // below tol * ||A||_F; the result is sorted ascending.
-#include <cublas_v2.h>
 
 #include <string>
 
@@ -302,53 +301,21 @@ int syev_batched_device(mq_ctx *c, int n, int batch, double *d_A, double *d_w, d
   return MQ_OK;
 }
 
-static cublasHandle_t handle(mq_ctx *c) {
-  if (!c->cublas) {
-    cublasHandle_t h;
-    if (cublasCreate(&h) != CUBLAS_STATUS_SUCCESS) return nullptr;
-    c->cublas = h;
-  }
-  cublasHandle_t h = (cublasHandle_t)c->cublas;
-  cublasSetStream(h, c->stream);
-  return h;
-}
-
-void cublas_destroy(void *h) { cublasDestroy((cublasHandle_t)h); }
-
-static cublasOperation_t op(char t) { return (t == 'T' || t == 't') ? CUBLAS_OP_T : CUBLAS_OP_N; }
-
 int gemm(mq_ctx *c, char ta, char tb, int m, int n, int k, double alpha, const double *A, int lda, const double *B,
          int ldb, double beta, double *C, int ldc) {
-  if (dgemm_small_fits(m, n, k) && !c->dgemm_cublas)
-    return dgemm_small(c, ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
-  cublasHandle_t h = handle(c);
-  if (!h) return set_err(c, MQ_ECUDA, "cublasCreate failed");
-  if (cublasDgemm(h, op(ta), op(tb), m, n, k, &alpha, A, lda, B, ldb, &beta, C, ldc) != CUBLAS_STATUS_SUCCESS)
-    return set_err(c, MQ_ECUDA, "cublasDgemm failed");
-  c->stats.lib_launches += 1;
-  return MQ_OK;
+  return dgemm_batched(c, ta, tb, m, n, k, alpha, A, lda, 0, B, ldb, 0, beta, C, ldc, 0, 1);
 }
 
-// lower triangle of C = alpha A A^T + beta C (n x n, A n x k); the upper triangle is not written
+// lower triangle of C = alpha A A^T + beta C (n x n, A n x k); the product
+// forms the whole of C (the upper triangle gets the same values)
 int syrk_lower(mq_ctx *c, int n, int k, double alpha, const double *A, int lda, double beta, double *C, int ldc) {
-  cublasHandle_t h = handle(c);
-  if (!h) return set_err(c, MQ_ECUDA, "cublasCreate failed");
-  if (cublasDsyrk(h, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, n, k, &alpha, A, lda, &beta, C, ldc) != CUBLAS_STATUS_SUCCESS)
-    return set_err(c, MQ_ECUDA, "cublasDsyrk failed");
-  c->stats.lib_launches += 1;
-  return MQ_OK;
+  return dgemm_batched(c, 'N', 'T', n, n, k, alpha, A, lda, 0, A, lda, 0, beta, C, ldc, 0, 1);
 }
 
 int gemm_strided_batched(mq_ctx *c, char ta, char tb, int m, int n, int k, double alpha, const double *A, int lda,
                          long long sA, const double *B, int ldb, long long sB, double beta, double *C, int ldc,
                          long long sC, int batch) {
-  cublasHandle_t h = handle(c);
-  if (!h) return set_err(c, MQ_ECUDA, "cublasCreate failed");
-  if (cublasDgemmStridedBatched(h, op(ta), op(tb), m, n, k, &alpha, A, lda, sA, B, ldb, sB, &beta, C, ldc, sC,
-                                batch) != CUBLAS_STATUS_SUCCESS)
-    return set_err(c, MQ_ECUDA, "cublasDgemmStridedBatched failed");
-  c->stats.lib_launches += 1;
-  return MQ_OK;
+  return dgemm_batched(c, ta, tb, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, batch);
 }
 
 // D = factor * C(:, 0:nocc-1) C(:, 0:nocc-1)^T, the sums of dens.f90:115-124

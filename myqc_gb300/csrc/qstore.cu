@@ -282,6 +282,7 @@ __device__ __forceinline__ void col_combo(const QsArgs &g, int s, int Q, int C, 
   for (int r = r0 + (int)threadIdx.x; r < r1; r += blockDim.x) {
     const int4 pi = g.rinfo[g.cls_off[CP] + r];  // pair, A | B << 16, i0 | j0 << 16
     const int P = pi.x, A = pi.y & 0xffff, B = pi.y >> 16, i0 = pi.z & 0xffff, j0 = pi.z >> 16;
+    if (s >= g.len[K][r]) continue;  // a row another partition holds
     const double *Xb = g.X + g.base[K] + ((size_t)g.off[K][r] + s) * NOUT;
     const bool degen = (A == B) || (C == Dsh) || (P == Q);
     double Dab[NA][NB];
@@ -435,12 +436,17 @@ struct Blob {
   }
 };
 
+int qstore_integrals(mq_ctx *c);
+
+// The staircase, digestion tables and store allocation of the current system
+// and threshold (rebuilt when either changes), then the integral blocks.
 int qstore_build(mq_ctx *c) {
   QStore &qs = c->qs;
   qs.valid = 0;
   const double thr = c->schwarz_thr;
-  if (!(thr > 0.0)) return set_err(c, MQ_EINVAL, "the quartet store needs a Schwarz threshold > 0");
+  if (!(thr >= 0.0)) return set_err(c, MQ_EINVAL, "the quartet store needs a Schwarz threshold >= 0");
   MQ_TRY(ensure_schwarz(c));
+  if (qs.tables_valid && qs.thr == thr) return qstore_integrals(c);
   const int np = c->pt.npairs, nsh = c->nshell, n = c->nao;
   const int *co = c->hp_class_off;
   if ((int)c->hp_shA.size() != np) return set_err(c, MQ_ESTATE, "pair table host copy missing");
@@ -491,6 +497,9 @@ int qstore_build(mq_ctx *c) {
         }
         m[r] = lo;
         len[r] = cb.tri ? std::min(lo, r + 1) : lo;
+        // a partition of the quartets over processes: this one keeps the
+        // rows whose bra pair index falls to it
+        if (c->nparts > 1 && perm[co[cP] + r] % c->nparts != c->part) len[r] = 0;
         off[r + 1] = off[r] + len[r];
       }
       for (int s = 0; s < cb.nQ; ++s) {  // first r with m_r <= s
@@ -640,13 +649,24 @@ int qstore_build(mq_ctx *c) {
   (void)n;
   // (a copy from pageable host memory returns once the data is staged, so
   // the blob may go; the integral launches queue behind it)
+  qs.tables_valid = 1;
+  return qstore_integrals(c);
+}
+
+// the integral blocks of the store (tables built), timed on their own
+int qstore_integrals(mq_ctx *c) {
   c->t_eri_kernel.collect_sync();
   c->t_eri_kernel.total = 0;
   c->t_eri_kernel.start(c->stream);
   MQ_TRY(eri_store_quartets(c));
   c->t_eri_kernel.stop(c->stream);
-  qs.valid = 1;
+  c->qs.valid = 1;
   return MQ_OK;
+}
+
+int fock_direct_store_rhf(mq_ctx *c, const double *d_D, double *d_G) {
+  MQ_TRY(qstore_build(c));
+  return qstore_fock_rhf(c, d_D, d_G);
 }
 
 static QsArgs qs_args(mq_ctx *c) {

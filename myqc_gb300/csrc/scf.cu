@@ -226,6 +226,9 @@ int scf_device(mq_ctx *c, const double *S, const double *H, const mq_scf_opts *o
   const double occf = uhf ? 1.0 : 2.0;
   if (!uhf && o->nalpha != o->nbeta) return set_err(c, MQ_EINVAL, "RHF needs nalpha == nbeta");
   if (nocc[0] > n || nocc[1] > n || nocc[0] < 0 || nocc[1] < 0) return set_err(c, MQ_EINVAL, "bad occupation");
+  if (c->nparts > 1)
+    return set_err(c, MQ_EINVAL, "a molecule split over processes iterates on the host (one all-reduce of G per "
+                                 "iteration); mq_scf needs mq_set_partition(ctx, 0, 1)");
   if (!o->direct && !c->xx_valid && !c->qs.valid)
     return set_err(c, MQ_ESTATE, "no stored integrals for a conventional SCF");
 
@@ -458,7 +461,12 @@ int scf_device(mq_ctx *c, const double *S, const double *H, const mq_scf_opts *o
   for (; it < max_iter && !conv; ++it) {
     // G[D_k]
     t_fock.start(c->stream);
-    if (o->direct) {
+    if (o->direct && !uhf && !c->fock_df32) {  // RHF: integral blocks recomputed into the store, digested from it
+      c->t_fock_kernel.start(c->stream);
+      MQ_TRY(fock_direct_store_rhf(c, dD, dG));
+      c->t_fock_kernel.stop(c->stream);
+      c->stats.fock_kernel_launches += 1;
+    } else if (o->direct) {
       double *J = dT1, *Ka = dT2, *Kb = uhf ? dT3 : nullptr;
       MQ_TRY(fock_direct_device(c, dD, uhf ? dD + n2 : nullptr, J, Ka, Kb));
       MQ_TRY(direct_combine(c, J, Ka, Kb, dG, uhf ? dG + n2 : nullptr));

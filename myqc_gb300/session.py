@@ -193,6 +193,12 @@ class Context:
         screened shell quartet once; needs a Schwarz threshold > 0)."""
         self._check(self.L.mq_set_eri_storage(self.h, int(storage)))
 
+    def set_partition(self, part: int, nparts: int):
+        """Keep only this process's share (part of nparts) of the molecule's
+        shell quartets in RHF Fock builds from the quartet store or direct;
+        the parts' G matrices sum to the full G."""
+        self._check(self.L.mq_set_partition(self.h, int(part), int(nparts)))
+
     def set_eri_mixed(self, tau: float):
         """Quartets with a Schwarz bound below tau in FP32 (tight mode; 0: all FP64)."""
         self._check(self.L.mq_set_eri_mixed(self.h, float(tau)))

@@ -102,3 +102,12 @@ def test_cpu_fit_and_extrapolation():
     expect = {"int1e": 1e-3 * nm ** 2, "int2e": 1e-4 * nm ** 3.5, "scf": 10 * (1e-5 * nm ** 4 + 0.02),
               "ao2mo": 1e-6 * nm ** 5, "mp2": 1e-7 * nm ** 4}
     assert all(abs(ext[k] - v) <= 1e-9 * v for k, v in expect.items()), ext
+
+
+def test_cpu_digestion_from_the_large_order_point():
+    pts = [{"nmol": N, "t": {"int1e": 1.0, "int2e": 1.0, "fock": 1e-5 * N ** 5, "ao2mo": 1.0, "mp2": 1.0}}
+           for N in (3, 4, 5, 6)]
+    nm = bench.NMOL
+    fit, ext = bench.fit_and_extrapolate(pts, 2, 0.5, (84, 0.4))
+    assert abs(ext["scf"] - 2 * (0.4 * (7.0 * nm / 84) ** 4 + 0.5)) < 1e-9
+    assert fit["fock"]["large_order_point_s"] == [84, 0.4]

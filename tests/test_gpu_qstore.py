@@ -104,3 +104,51 @@ def test_store_needs_a_threshold(qctx, basis_text):
     qctx.set_eri_storage(STORE_QUARTETS)
     with pytest.raises(MyQCError):
         qctx.eri_store()
+
+
+@pytest.mark.parametrize("thr", [0.0, 1e-12])
+def test_direct_build_through_the_store(qctx, basis_text, thr):
+    """The direct RHF build (no integrals kept between builds) recomputes the
+    store's blocks and digests them: no atomics, so two builds agree bit for
+    bit, and they agree with the stored full-array build."""
+    sysm, basis = _system("water5", basis_text)
+    qctx.set_system(sysm, basis, None, MODE_TIGHT)
+    qctx.set_schwarz(thr)
+    D = _density(qctx.n, 4)
+    G1 = qctx.fock(D, direct=True)
+    G2 = qctx.fock(D, direct=True)
+    assert np.array_equal(G1, G2)
+    qctx.set_eri_storage(STORE_FULL)
+    qctx.eri_store()
+    Gf = qctx.fock(D)
+    assert np.max(np.abs(G1 - Gf)) < 1e-12 * max(1.0, np.max(np.abs(Gf)))
+
+
+@pytest.mark.parametrize("direct", [False, True])
+def test_partitions_sum_to_the_full_fock(qctx, basis_text, direct):
+    """A molecule split over processes: each part of the quartet store (or of
+    the direct build) gives its share of G, and the shares sum to the whole
+    G -- here the three parts run one after the other on one GPU."""
+    from myqc_gb300 import MyQCError
+    sysm, basis = _system("water5", basis_text)
+    qctx.set_system(sysm, basis, None, MODE_TIGHT)
+    qctx.set_schwarz(1e-12)
+    qctx.set_eri_storage(STORE_QUARTETS)
+    D = _density(qctx.n, 6)
+    if not direct:
+        qctx.eri_store()
+    G = qctx.fock(D, direct=direct)
+    parts = []
+    try:
+        for k in range(3):
+            qctx.set_partition(k, 3)
+            if not direct:
+                qctx.eri_store()
+            parts.append(qctx.fock(D, direct=direct))
+        with pytest.raises(MyQCError):  # the SCF of a split molecule iterates on the host
+            S, H = qctx.int1e()
+            qctx.scf(S, H, sysm.nelcA, sysm.nelcB, conv=1e-8, diis=8, max_iter=5)
+    finally:
+        qctx.set_partition(0, 1)
+    assert all(np.max(np.abs(p)) > 0 for p in parts)
+    assert np.max(np.abs(sum(parts) - G)) < 1e-12 * max(1.0, np.max(np.abs(G)))
