@@ -365,7 +365,12 @@ int purify_projector(mq_ctx *c, int n, int nocc, const double *d_Fp, double *d_P
   MQ_TRY(gershgorin(c, d_Fp, n, 1, d_err + PUR_MAX_STEPS));  // [lo, hi] after the step errors
   purify_build_kernel<<<gb, 256, 0, c->stream>>>(d_Fp, n, d_err + PUR_MAX_STEPS, X);
   c->stats.launches += 1;
-  if (n <= PUR_PERSIST_MAX) return purify_persistent(c, n, nocc, d_P, d_W, d_err, steps);
+  // the one-launch form waits at grid-wide barriers, so it runs only when
+  // nothing else is in flight beside it (no slicing of the transform's
+  // operands on the side stream); otherwise one product and one update
+  // launch per step
+  if (c->side_pending && cudaEventQuery(c->ev_side) == cudaSuccess) MQ_TRY(join_side(c));  // it has finished
+  if (n <= PUR_PERSIST_MAX && !c->side_pending) return purify_persistent(c, n, nocc, d_P, d_W, d_err, steps);
   std::vector<double> e(MAX_STEPS);
   int k = 0, settled_at = -1;
   while (k < MAX_STEPS) {

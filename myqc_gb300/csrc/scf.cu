@@ -458,6 +458,10 @@ int scf_device(mq_ctx *c, const double *S, const double *H, const mq_scf_opts *o
   bool early_done = false;
   c->stats.fock_inc_builds = 0;
   c->stats.eig_early = 0;
+  // with the quartet store the n^4 array the transform slices is filled from
+  // the store: both run on the side stream from here on, memory-bound work
+  // beside the FP64-bound iterations
+  if (purify && c->ao2mo_prefetch && !o->direct && c->qs.valid && !c->xx_sliced) MQ_TRY(ao2mo_preslice_xx(c));
   for (; it < max_iter && !conv; ++it) {
     // G[D_k]
     t_fock.start(c->stream);
@@ -561,7 +565,7 @@ int scf_device(mq_ctx *c, const double *S, const double *H, const mq_scf_opts *o
   c->stats.ms_eig_final = 0;
   if (purify && lastF) {  // one eigensolve of the last iteration's Fock matrices for C and eps
     // the transform's XX slices need no orbitals: form them beside the eigensolve
-    if (c->ao2mo_prefetch && !o->direct) MQ_TRY(ao2mo_preslice_xx(c));
+    if (c->ao2mo_prefetch && !o->direct && !c->xx_sliced) MQ_TRY(ao2mo_preslice_xx(c));
     StageTimer t_eig;
     t_eig.start(c->stream);
     have_prev = false;
