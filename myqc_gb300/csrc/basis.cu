@@ -328,6 +328,24 @@ void tight_boys_table(std::vector<double> &tab) {
   tab = cached;
 }
 
+// The tight table as the kernels read it: F_m(Tk) [TIGHT_NT][TIGHT_NM], the grid
+// values Tk, then for m = 0..BOYS_SCALED_M-1 the Taylor coefficients of F_m
+// about Tk, F_{m+k}(Tk) / k! for k = 0..8 ([m][TIGHT_NT][9]).
+void tight_boys_device_table(std::vector<double> &tab) {
+  std::vector<double> f;
+  tight_boys_table(f);
+  tab = f;
+  for (int k = 0; k < TIGHT_NT; ++k) tab.push_back(k / 10.0);
+  for (int m = 0; m < BOYS_SCALED_M; ++m)
+    for (int t = 0; t < TIGHT_NT; ++t) {
+      double fact = 1.0;
+      for (int k = 0; k < 9; ++k) {
+        if (k > 0) fact *= k;
+        tab.push_back(f[(size_t)t * TIGHT_NM + m + k] / fact);
+      }
+    }
+}
+
 static void tight_boys_compute(std::vector<double> &tab) {
   tab.assign((size_t)TIGHT_NT * TIGHT_NM, 0.0);
   for (int it = 0; it < TIGHT_NT; ++it) {

@@ -440,8 +440,7 @@ int batch_scf(mq_ctx *c, const mq_batch_opts *o, double *energy, int *iters, int
   cudaSetDevice(c->device);
   if (!c->d_boys_tight) {
     std::vector<double> tab;
-    tight_boys_table(tab);
-    for (int k = 0; k < TIGHT_NT; ++k) tab.push_back(k / 10.0);
+    tight_boys_device_table(tab);
     MQ_CUDA(c, cudaMalloc((void **)&c->d_boys_tight, tab.size() * sizeof(double)));
     MQ_CUDA(c, cudaMemcpy(c->d_boys_tight, tab.data(), tab.size() * sizeof(double), cudaMemcpyHostToDevice));
   }

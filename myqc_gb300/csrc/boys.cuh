@@ -13,13 +13,16 @@
 // pi is the reference's float-valued constant.  BoysG is undefined for
 // T >= 30 in the reference; g = 0.490 is used there (effect < 3e-15).
 //
-// Tight (MQ_MODE_TIGHT): 9-term Taylor of F_L from an accurate table
-// (T step 0.1 up to 36, |remainder| < 1e-17) and downward recursion; above 36
+// Tight (MQ_MODE_TIGHT): 9-term Taylor series about the nearest grid point of
+// an accurate table (T step 0.1 up to 36, |remainder| < 1e-17), with the
+// coefficients F_{m+k}(Tk)/k! stored per order m so that each term is one
+// fma: every F_j so for L <= 2, else F_L so and downward recursion; above 36
 // F0 = sqrt(pi/T)/2 (erf(sqrt T) = 1 in FP64) and upward recursion.
 //
 // Table layout in device memory (one buffer, see set_system):
 //   parity: Ft(0:120,0:22) column-major (2783 doubles), then Tk/10 (121)
-//   tight : tab[Tk][m], 361 x 13 row-major (4693 doubles), then Tk/10 (361)
+//   tight : tab[Tk][m], 361 x 13 row-major (4693 doubles), then Tk/10 (361),
+//           then F_{m+k}(Tk)/k! [m < 5][Tk][k < 9]
 #pragma once
 #include "internal.h"
 
@@ -27,6 +30,7 @@ namespace mq {
 
 constexpr int BOYS_REF_GRID = FTAB_NT * FTAB_NM;      // offset of Tk/10 values
 constexpr int BOYS_TIGHT_GRID = TIGHT_NT * TIGHT_NM;  // offset of Tk/10 values
+constexpr int BOYS_TIGHT_SCALED = BOYS_TIGHT_GRID + TIGHT_NT;  // offset of the scaled Taylor coefficients
 
 // e^-T is below 4.3e-18 * F0 for T >= 40; there the recursions drop it.
 constexpr double BOYS_EXP_CUT = 40.0;
@@ -75,24 +79,29 @@ __device__ __forceinline__ void boys_ref(double T, const double *__restrict__ ta
   }
 }
 
+// F_m(T) = sum_k F_{m+k}(Tk) (Tk - T)^k / k! from the scaled coefficients
+// (9 terms, |Tk - T| <= 0.05: remainder below 1e-17), one fma per term
+template <int M>
+__device__ __forceinline__ double boys_taylor(const double *__restrict__ tab, int tk, double d) {
+  const double *c = tab + BOYS_TIGHT_SCALED + ((size_t)M * TIGHT_NT + tk) * 9;
+  double f = __ldg(c + 8);
+#pragma unroll
+  for (int k = 7; k >= 0; --k) f = fma(f, d, __ldg(c + k));
+  return f;
+}
+
 template <int L>
 __device__ __forceinline__ void boys_tight(double T, const double *__restrict__ tab, double (&F)[L + 1]) {
-  static_assert(L + 8 < TIGHT_NM, "Boys order");
+  static_assert(L + 8 < TIGHT_NM && L < BOYS_SCALED_M, "Boys order");
   if (T < 36.0) {
-    const int tk = (int)(T * 10.0 + 0.5);
+    const int tk = __double2int_rn(T * 10.0);
     const double d = __ldg(tab + BOYS_TIGHT_GRID + tk) - T;
-    const double *row = tab + tk * TIGHT_NM + L;
-    double f = __ldg(row + 8);
-    f = __ldg(row + 7) + f * (d * (1.0 / 8.0));
-    f = __ldg(row + 6) + f * (d * (1.0 / 7.0));
-    f = __ldg(row + 5) + f * (d * (1.0 / 6.0));
-    f = __ldg(row + 4) + f * (d * (1.0 / 5.0));
-    f = __ldg(row + 3) + f * (d * (1.0 / 4.0));
-    f = __ldg(row + 2) + f * (d * (1.0 / 3.0));
-    f = __ldg(row + 1) + f * (d * 0.5);
-    f = __ldg(row + 0) + f * d;
-    F[L] = f;
-    if (L > 0) {
+    if constexpr (L <= 2) {  // every order by its own series: no e^-T, no recursion
+      F[0] = boys_taylor<0>(tab, tk, d);
+      if constexpr (L >= 1) F[1] = boys_taylor<1>(tab, tk, d);
+      if constexpr (L >= 2) F[2] = boys_taylor<2>(tab, tk, d);
+    } else {  // the highest by its series, then downward recursion
+      F[L] = boys_taylor<L>(tab, tk, d);
       const double e = exp(-T), t2 = 2.0 * T;
 #pragma unroll
       for (int j = L - 1; j >= 0; --j) F[j] = (t2 * F[j + 1] + e) * (1.0 / (2 * j + 1));

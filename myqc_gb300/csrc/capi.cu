@@ -201,8 +201,7 @@ int mq_set_system(mq_ctx *c, int nnuc, const int *Z, const double *xyz, const do
       tab.assign(ftab, ftab + FTAB_NT * FTAB_NM);
       for (int k = 0; k < FTAB_NT; ++k) tab.push_back(k / 10.0);
     } else {
-      tight_boys_table(tab);
-      for (int k = 0; k < TIGHT_NT; ++k) tab.push_back(k / 10.0);
+      tight_boys_device_table(tab);
     }
     c->boys_loaded = -1;
     if (c->d_boys) cudaFree(c->d_boys);

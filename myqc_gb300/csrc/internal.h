@@ -338,6 +338,8 @@ void append_pairs_class(HostPairs &dst, const HostPairs &src, int cl, int mol);
 int upload_pairs(mq_ctx *c, const HostPairs &h, std::vector<void *> *allocs, PairTable &t);
 void free_pairs(mq_ctx *c);
 void tight_boys_table(std::vector<double> &tab);  // TIGHT_NT x TIGHT_NM, row-major [T][m]
+constexpr int BOYS_SCALED_M = 5;                  // orders with their own Taylor-coefficient table
+void tight_boys_device_table(std::vector<double> &tab);  // the table, its grid, the scaled tables
 
 // eri.cu
 int eri_full_device(mq_ctx *c, double *d_XX);

@@ -316,10 +316,12 @@ def test_schwarz_screened_integrals(ctx, basis_text):
 @pytest.mark.parametrize("uhf", [False, True])
 def test_incremental_fock_builds(ctx, basis_text, uhf):
     """FP32 incremental Fock builds (mq_set_fock_incremental) once the density
-    moves by less than 1e-6, 1e-3 and, the largest threshold allowed, 1e-2: same
-    converged energy as full FP64 builds within 1e-9 Eh, same iteration count
-    within 1, and some builds were incremental.  RHF on (H2O)8 (n = 56), UHF
-    on its cation."""
+    moves by less than 1e-6, 1e-3 and, the largest threshold allowed, 1e-2: the
+    converged energy of full FP64 builds within 1e-8 Eh (the FP32 rounding of
+    each increment is never corrected by a later full build, so it adds up over
+    the increments: these options are not FP64-accurate and stay out of the
+    headline arm), same iteration count within 1, and some builds were
+    incremental.  RHF on (H2O)8 (n = 56), UHF on its cation."""
     from myqc_gb300 import FOCK_DF32, FOCK_FP64, MODE_TIGHT, molecules
     sysm = molecules.water_cluster_system(8, 8.0, 11)
     basis = formats.parse_mybasis_text(basis_text, sysm.atoms)
@@ -337,7 +339,7 @@ def test_incremental_fock_builds(ctx, basis_text, uhf):
             ctx.set_fock_incremental(tau)
             r = ctx.scf(S, H, na, nb, **kw)
             assert ctx.stat("fock_inc_builds") >= 2
-            assert abs(r.energy - ref.energy) < 1e-9, (prec, r.energy - ref.energy)
+            assert abs(r.energy - ref.energy) < 1e-8, (prec, r.energy - ref.energy)
             assert abs(r.iterations - ref.iterations) <= 1, (r.iterations, ref.iterations)
     finally:
         ctx.set_fock_incremental(0.0)
