@@ -25,9 +25,10 @@ int ao2mo_device(mq_ctx *c, const double *Ci, int no1, const double *Ca, int nv1
   const long long n = c->nao;
   if (no1 == 0 || nv1 == 0 || no2 == 0 || nv2 == 0) return MQ_OK;  // empty block (e.g. no beta electrons)
   const int planes = precision == MQ_PREC_SPLIT_BF16X3 ? 3 : 2;
-  if (!c->xx_valid && !(precision != MQ_PREC_FP64 && c->xx_sliced == planes)) {
-    MQ_TRY(ensure_xx_full(c));  // from the quartet store, if that is what mq_eri_store kept
-  }
+  // the FP64 transform reads the n^4 array (filled from the quartet store if
+  // that is what mq_eri_store kept); the split one slices from either
+  if (precision == MQ_PREC_FP64) MQ_TRY(ensure_xx_full(c));
+  else if (!c->xx_valid && !c->qs.valid) return set_err(c, MQ_ESTATE, "no integrals on the device");
   if (precision == MQ_PREC_FP64) MQ_TRY(join_side(c));
   if (precision != MQ_PREC_FP64)
     return ao2mo_split_device(c, Ci, no1, Ca, nv1, Cj, no2, Cb, nv2, d_out, planes);

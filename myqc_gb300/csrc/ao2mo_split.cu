@@ -332,11 +332,63 @@ __device__ __forceinline__ void load_chunk(const T *__restrict__ x, int k0, int 
 //              l + n (u + n v) of XX (rows of n values), l = r mod n;
 //   ROW_SYMM   row (v, jb) of the pair-packed Y2: element u is
 //              in[jb * npairs + pidx(min(u, v), max(u, v))], pidx(u, v) = u + v (v + 1) / 2.
-enum { ROW_PLAIN = 0, ROW_PAIRS = 1, ROW_SYMM = 2 };
+//   ROW_STORE  as ROW_PAIRS, each value (d l|u v) looked up in the quartet store
+//              (no n^4 array): the canonical element of its shell quartet, zero
+//              when the quartet was screened out -- the value the full array
+//              filled from the store holds.
+enum { ROW_PLAIN = 0, ROW_PAIRS = 1, ROW_SYMM = 2, ROW_STORE = 3 };
+struct StoreView {
+  const double *X;
+  const int4 *pinfo;  // [S1 * nsh + S2]: pair, class, rank, bit 0: stored as (S2, S1), bit 1: S1 = S2
+  const int *ao_shell, *ao0;
+  const long long *off[6];
+  const int *len[6];
+  long long base[6];
+  int nsh;
+};
 struct RowSrc {
   const int2 *pairs;  // (u, v) of each pair p, u <= v
   long long n, npairs;
+  StoreView sv;  // ROW_STORE
 };
+
+__host__ __device__ constexpr int sv_nfa(int cls) { return cls >= 1 ? 4 : 1; }
+__host__ __device__ constexpr int sv_nfb(int cls) { return cls == 2 ? 4 : 1; }
+
+// (d l|u v) from the quartet store
+__device__ __forceinline__ double store_value(const StoreView &sv, int d, int l, int u, int v, int n) {
+  const int D = sv.ao_shell[d], Ls = sv.ao_shell[l], U = sv.ao_shell[u], V = sv.ao_shell[v];
+  const int4 e1 = sv.pinfo[D * sv.nsh + Ls], e2 = sv.pinfo[U * sv.nsh + V];
+  // stored orientation: first-shell AO i, second-shell AO j, function indices
+  int i1 = (e1.w & 1) ? l : d, j1 = (e1.w & 1) ? d : l, i2 = (e2.w & 1) ? v : u, j2 = (e2.w & 1) ? u : v;
+  if ((e1.w & 2) && i1 < j1) {  // A = B: the canonical element has i >= j
+    const int t = i1;
+    i1 = j1;
+    j1 = t;
+  }
+  if ((e2.w & 2) && i2 < j2) {
+    const int t = i2;
+    i2 = j2;
+    j2 = t;
+  }
+  const bool first_bra = e1.y > e2.y || (e1.y == e2.y && e1.z >= e2.z);
+  const int4 eb = first_bra ? e1 : e2, ek = first_bra ? e2 : e1;
+  int ia = first_bra ? i1 : i2, ja = first_bra ? j1 : j2, ka = first_bra ? i2 : i1, la = first_bra ? j2 : j1;
+  const int K = eb.y * (eb.y + 1) / 2 + ek.y;
+  if (ek.z >= sv.len[K][eb.z]) return 0.0;  // screened out
+  if (eb.x == ek.x && (long long)ia * n + ja < (long long)ka * n + la) {  // P = Q: ij >= kl
+    int t = ia;
+    ia = ka;
+    ka = t;
+    t = ja;
+    ja = la;
+    la = t;
+  }
+  const int NB = sv_nfb(eb.y), NC = sv_nfa(ek.y), ND = sv_nfb(ek.y), NOUT = sv_nfa(eb.y) * NB * NC * ND;
+  const int fa = ia - sv.ao0[sv.ao_shell[ia]], fb = ja - sv.ao0[sv.ao_shell[ja]];
+  const int fc = ka - sv.ao0[sv.ao_shell[ka]], fd = la - sv.ao0[sv.ao_shell[la]];
+  return __ldg(sv.X + sv.base[K] + (sv.off[K][eb.z] + ek.z) * NOUT + ((fa * NB + fb) * NC + fc) * ND + fd);
+}
 
 template <int S, class T, int H, int MODE>
 __global__ void __launch_bounds__(256, 4) slice_rows_kernel(const T *__restrict__ in, long long rows, int kvalid,
@@ -349,10 +401,16 @@ __global__ void __launch_bounds__(256, 4) slice_rows_kernel(const T *__restrict_
     const T *x = in + r * ld;
     long long jb = 0;
     int vrow = 0;
+    int lrow = 0;
+    int2 uvrow = make_int2(0, 0);
     if (MODE == ROW_PAIRS) {
       const long long pidx = r / rs.n;
       const int2 uv = rs.pairs[pidx];
       x = in + ((r - pidx * rs.n) + rs.n * (uv.x + rs.n * (long long)uv.y)) * ld;
+    } else if (MODE == ROW_STORE) {
+      const long long pidx = r / rs.n;
+      uvrow = rs.pairs[pidx];
+      lrow = (int)(r - pidx * rs.n);
     } else if (MODE == ROW_SYMM) {
       jb = r / rs.n;
       vrow = (int)(r - jb * rs.n);
@@ -369,6 +427,12 @@ __global__ void __launch_bounds__(256, 4) slice_rows_kernel(const T *__restrict_
           for (int j = 0; j < 8; ++j) {
             const int u = 8 * c + j, lo = min(u, vrow), hi = max(u, vrow);
             v[h][j] = u < kvalid ? __ldg(x + lo + (long long)hi * (hi + 1) / 2) : (T)0;
+          }
+        } else if (MODE == ROW_STORE) {
+#pragma unroll
+          for (int j = 0; j < 8; ++j) {
+            const int d = 8 * c + j;
+            v[h][j] = d < kvalid ? (T)store_value(rs.sv, d, lrow, uvrow.x, uvrow.y, (int)rs.n) : (T)0;
           }
         } else {
           load_chunk(x, 8 * c, kvalid, vec != 0, v[h]);
@@ -471,12 +535,13 @@ static int slice_gemm(mq_ctx *c, Sliced A, long long M, int batch, long long a_b
 
 template <int S, int MODE = ROW_PLAIN, class T>
 static int slice_rows(mq_ctx *c, const T *in, long long rows, int kvalid, long long ld, int Kp, Sliced o,
-                      RowSrc rs = RowSrc{nullptr, 1, 0}) {
+                      RowSrc rs = RowSrc{nullptr, 1, 0, StoreView{}}) {
   if (Kp % 8 || Kp > 512) return set_err(c, MQ_EINVAL, "slice_rows: Kp must be a multiple of 8 up to 512");
   const int tb = 256;
   const long long blocks = std::max<long long>(1, std::min<long long>((rows + 7) / 8, 1 << 20));
   const int per16 = 16 / (int)sizeof(T);
-  const int vec = MODE != ROW_SYMM && ((uintptr_t)in % 16 == 0) && (ld % per16 == 0) && (kvalid % per16 == 0);
+  const int vec = MODE != ROW_SYMM && MODE != ROW_STORE && ((uintptr_t)in % 16 == 0) && (ld % per16 == 0) &&
+                  (kvalid % per16 == 0);
   if (Kp <= 256)
     slice_rows_kernel<S, T, 1, MODE><<<(unsigned)blocks, tb, 0, c->stream>>>(in, rows, kvalid, ld, Kp, o.plane,
                                                                              o.base, o.e, vec, rs);
@@ -503,6 +568,35 @@ static int pair_table(mq_ctx *c, int n, const int2 **out) {
   MQ_CUDA(c, cudaGetLastError());
   *out = d;
   return MQ_OK;
+}
+
+// The quartet store as the ROW_STORE slicing reads it.
+static StoreView store_view(mq_ctx *c) {
+  const QStore &qs = c->qs;
+  StoreView v{};
+  v.X = qs.X;
+  v.pinfo = qs.pinfo;
+  v.ao_shell = qs.ao_shell;
+  v.ao0 = qs.shell_ao0;
+  for (int k = 0; k < 6; ++k) {
+    v.off[k] = qs.combo[k].off;
+    v.len[k] = qs.combo[k].len;
+    v.base[k] = qs.combo[k].base;
+  }
+  v.nsh = c->nshell;
+  return v;
+}
+
+// A operand of the first step -- XX(d, l, u, v), rows (l, u <= v), K = d --
+// cut into S planes: from the n^4 array, or looked up in the quartet store
+template <int S>
+static int slice_xx(mq_ctx *c, long long n, int Kp, Sliced A, const int2 *pairs) {
+  const long long np = n * (n + 1) / 2;
+  if (!c->xx_valid && c->qs.valid)
+    return slice_rows<S, ROW_STORE, double>(c, nullptr, n * np, (int)n, n, Kp, A,
+                                            RowSrc{pairs, n, np, store_view(c)});
+  MQ_TRY(ensure_xx_full(c));
+  return slice_rows<S, ROW_PAIRS>(c, c->d_XX, n * np, (int)n, n, Kp, A, RowSrc{pairs, n, np, StoreView{}});
 }
 
 template <int S>
@@ -545,11 +639,12 @@ static int ao2mo_slices(mq_ctx *c, const double *Ci, int no1, const double *Ca, 
   const long long np = n * (n + 1) / 2, rXp = n * np;
   const int2 *pairs = nullptr;
   MQ_TRY(pair_table(c, (int)n, &pairs));
-  const RowSrc rs{pairs, n, np};
+  const RowSrc rs{pairs, n, np, StoreView{}};
   // 1: XX(d,l,u,v) at d + n*((l,u,v)): rows (l,p), K = d -> Y1[b][p][l]
   // (already sliced on the side stream when the SCF prefetched it)
   Sliced A{pa, rX * Kp, ea};
-  if (c->xx_sliced != S) MQ_TRY((slice_rows<S, ROW_PAIRS>(c, c->d_XX, rXp, (int)n, n, Kp, A, rs)));
+  if (c->xx_sliced != S) MQ_TRY(slice_xx<S>(c, n, Kp, A, pairs));
+  (void)rXp;
   c->xx_sliced = 0;  // step 2 overwrites the slices
   g.out_f64 = 0;
   g.out32 = y1;
@@ -626,16 +721,13 @@ static int preslice(mq_ctx *c) {
     MQ_CUDA(c, cudaEventCreateWithFlags(&c->ev_main, cudaEventDisableTiming));
     MQ_CUDA(c, cudaEventCreateWithFlags(&c->ev_side, cudaEventDisableTiming));
   }
-  const long long np = n * (n + 1) / 2;
   const int2 *pairs = nullptr;
   MQ_TRY(pair_table(c, (int)n, &pairs));  // on the main stream, before the event below
   MQ_CUDA(c, cudaEventRecord(c->ev_main, c->stream));
   MQ_CUDA(c, cudaStreamWaitEvent(c->side, c->ev_main, 0));
   cudaStream_t main = c->stream;
-  c->stream = c->side;  // the fill from the quartet store and slice_rows launch on c->stream
-  int rc = ensure_xx_full(c);
-  if (rc == MQ_OK)
-    rc = slice_rows<S, ROW_PAIRS>(c, c->d_XX, n * np, (int)n, n, Kp, Sliced{pa, rX * Kp, ea}, RowSrc{pairs, n, np});
+  c->stream = c->side;  // the slicing launches on c->stream
+  const int rc = slice_xx<S>(c, n, Kp, Sliced{pa, rX * Kp, ea}, pairs);
   c->stream = main;
   MQ_TRY(rc);
   MQ_CUDA(c, cudaEventRecord(c->ev_side, c->side));

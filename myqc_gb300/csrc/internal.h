@@ -125,6 +125,8 @@ struct QStore {
   int *ksh_off = nullptr;     // [nshell + 1] offsets into ksh
   int2 *ksh = nullptr;        // (pair, row offset of the shell in the pair's partial K rows)
   int *shell_ao0 = nullptr;   // [nshell] first AO of each shell
+  int *ao_shell = nullptr;    // [n] shell of each AO
+  int4 *pinfo = nullptr;      // [S1 * nshell + S2]: pair, class, rank, bit 0: stored as (S2, S1), bit 1: S1 = S2
   double quartets = 0;        // quartets stored
   double unique = 0;          // canonical unique integrals stored (the digestion's 6 FMAs each)
 };

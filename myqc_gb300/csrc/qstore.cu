@@ -622,6 +622,22 @@ int qstore_build(mq_ctx *c) {
   const size_t o_ko = blob.add(ksh_off.data(), ksh_off.size());
   const size_t o_k = blob.add(ksh.data(), ksh.size());
   const size_t o_ao = blob.add(ao0.data(), ao0.size());
+  // AO -> shell, and (S1, S2) -> the pair holding both, with its class, rank
+  // within the class and orientation (for lookups of single integrals)
+  std::vector<int> ao_shell(n, 0);
+  for (int sh = 0; sh < nsh; ++sh) {
+    const int a1 = sh + 1 < nsh ? ao0[sh + 1] : n;
+    for (int a = ao0[sh]; a < a1; ++a) ao_shell[a] = sh;
+  }
+  std::vector<int4> pinfo((size_t)nsh * nsh, make_int4(0, 0, 0, 0));
+  for (int cl = 0; cl < 3; ++cl)
+    for (int t = 0; t < qs.ncls[cl]; ++t) {
+      const int p = perm[co[cl] + t], A = c->hp_shA[p], B = c->hp_shB[p];
+      pinfo[(size_t)A * nsh + B] = make_int4(p, cl, t, A == B ? 2 : 0);
+      pinfo[(size_t)B * nsh + A] = make_int4(p, cl, t, A == B ? 2 : 1);
+    }
+  const size_t o_aos = blob.add(ao_shell.data(), ao_shell.size());
+  const size_t o_pi = blob.add(pinfo.data(), pinfo.size());
   char *d = (char *)buf(c, "qstore_tab", blob.bytes.size() + 256);
   if (!d) return MQ_ENOMEM;
   MQ_CUDA(c, cudaMemcpyAsync(d, blob.bytes.data(), blob.bytes.size(), cudaMemcpyHostToDevice, c->stream));
@@ -640,6 +656,8 @@ int qstore_build(mq_ctx *c) {
   qs.ksh_off = (int *)(d + o_ko);
   qs.ksh = (int2 *)(d + o_k);
   qs.shell_ao0 = (int *)(d + o_ao);
+  qs.ao_shell = (int *)(d + o_aos);
+  qs.pinfo = (int4 *)(d + o_pi);
   qs.X_elems = (size_t)base;
   qs.X = (double *)buf(c, "qstore_X", sizeof(double) * std::max<size_t>(qs.X_elems, 1));
   if (!qs.X) return MQ_ENOMEM;

@@ -458,9 +458,9 @@ int scf_device(mq_ctx *c, const double *S, const double *H, const mq_scf_opts *o
   bool early_done = false;
   c->stats.fock_inc_builds = 0;
   c->stats.eig_early = 0;
-  // with the quartet store the n^4 array the transform slices is filled from
-  // the store: both run on the side stream from here on, memory-bound work
-  // beside the FP64-bound iterations
+  // the transform's first operand depends on the integrals alone: slice it on
+  // the side stream from here on, memory-bound work beside the FP64-bound
+  // iterations (purification steps launch singly while it runs)
   if (purify && c->ao2mo_prefetch && !o->direct && c->qs.valid && !c->xx_sliced) MQ_TRY(ao2mo_preslice_xx(c));
   for (; it < max_iter && !conv; ++it) {
     // G[D_k]

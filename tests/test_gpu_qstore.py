@@ -152,3 +152,22 @@ def test_partitions_sum_to_the_full_fock(qctx, basis_text, direct):
         qctx.set_partition(0, 1)
     assert all(np.max(np.abs(p)) > 0 for p in parts)
     assert np.max(np.abs(sum(parts) - G)) < 1e-12 * max(1.0, np.max(np.abs(G)))
+
+
+def test_transform_slices_from_the_store(qctx, basis_text):
+    """The split transform's first operand cut straight from the quartet store
+    equals the one cut from the n^4 array filled from it: the same MP2 energy,
+    bit for bit."""
+    from myqc_gb300 import PREC_SPLIT_BF16X3
+    sysm, basis = _system("water5", basis_text)
+    qctx.set_system(sysm, basis, None, MODE_TIGHT)
+    qctx.set_schwarz(1e-12)
+    qctx.set_eri_storage(STORE_QUARTETS)
+    S, H = qctx.int1e()
+    qctx.eri_store()
+    r = qctx.scf(S, H, sysm.nelcA, sysm.nelcB, conv=1e-10, conv_rms=True, diis=8, max_iter=100)
+    m_store = qctx.mp2_rhf(r.eig, sysm.nelcA, PREC_SPLIT_BF16X3, C=r.C)
+    n = qctx.n
+    qctx.fock(_density(n, 7), _density(n, 8))  # a UHF build fills the n^4 array from the store
+    m_full = qctx.mp2_rhf(r.eig, sysm.nelcA, PREC_SPLIT_BF16X3, C=r.C)
+    assert m_store["E_MP2"] == m_full["E_MP2"]
