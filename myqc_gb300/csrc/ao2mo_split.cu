@@ -345,6 +345,9 @@ struct StoreView {
   const int *len[6];
   long long base[6];
   int nsh;
+  const double *pbound;  // Schwarz bound of each pair
+  const double *qmax;    // per shell: the largest bound of a pair containing it
+  double thr;            // the store's threshold
 };
 struct RowSrc {
   const int2 *pairs;  // (u, v) of each pair p, u <= v
@@ -411,6 +414,10 @@ __global__ void __launch_bounds__(256, 4) slice_rows_kernel(const T *__restrict_
       const long long pidx = r / rs.n;
       uvrow = rs.pairs[pidx];
       lrow = (int)(r - pidx * rs.n);
+      // no quartet (D L|U V) of the row passes the screen: the row is zero
+      const int U = rs.sv.ao_shell[uvrow.x], V = rs.sv.ao_shell[uvrow.y], Ls = rs.sv.ao_shell[lrow];
+      const double quv = rs.sv.pbound[rs.sv.pinfo[U * rs.sv.nsh + V].x];
+      if (rs.sv.qmax[Ls] * quv < rs.sv.thr) lrow = -1;
     } else if (MODE == ROW_SYMM) {
       jb = r / rs.n;
       vrow = (int)(r - jb * rs.n);
@@ -432,7 +439,7 @@ __global__ void __launch_bounds__(256, 4) slice_rows_kernel(const T *__restrict_
 #pragma unroll
           for (int j = 0; j < 8; ++j) {
             const int d = 8 * c + j;
-            v[h][j] = d < kvalid ? (T)store_value(rs.sv, d, lrow, uvrow.x, uvrow.y, (int)rs.n) : (T)0;
+            v[h][j] = d < kvalid && lrow >= 0 ? (T)store_value(rs.sv, d, lrow, uvrow.x, uvrow.y, (int)rs.n) : (T)0;
           }
         } else {
           load_chunk(x, 8 * c, kvalid, vec != 0, v[h]);
@@ -584,6 +591,9 @@ static StoreView store_view(mq_ctx *c) {
     v.base[k] = qs.combo[k].base;
   }
   v.nsh = c->nshell;
+  v.pbound = c->pt.schwarz;
+  v.qmax = qs.shell_qmax;
+  v.thr = qs.thr;
   return v;
 }
 

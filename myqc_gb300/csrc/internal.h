@@ -126,6 +126,7 @@ struct QStore {
   int2 *ksh = nullptr;        // (pair, row offset of the shell in the pair's partial K rows)
   int *shell_ao0 = nullptr;   // [nshell] first AO of each shell
   int *ao_shell = nullptr;    // [n] shell of each AO
+  double *shell_qmax = nullptr;  // [nshell] the largest Schwarz bound of a pair containing the shell
   int4 *pinfo = nullptr;      // [S1 * nshell + S2]: pair, class, rank, bit 0: stored as (S2, S1), bit 1: S1 = S2
   double quartets = 0;        // quartets stored
   double unique = 0;          // canonical unique integrals stored (the digestion's 6 FMAs each)

@@ -636,6 +636,12 @@ int qstore_build(mq_ctx *c) {
       pinfo[(size_t)A * nsh + B] = make_int4(p, cl, t, A == B ? 2 : 0);
       pinfo[(size_t)B * nsh + A] = make_int4(p, cl, t, A == B ? 2 : 1);
     }
+  std::vector<double> qmax(nsh, 0.0);
+  for (int p = 0; p < np; ++p) {
+    qmax[c->hp_shA[p]] = std::max(qmax[c->hp_shA[p]], sch[p]);
+    qmax[c->hp_shB[p]] = std::max(qmax[c->hp_shB[p]], sch[p]);
+  }
+  const size_t o_qm = blob.add(qmax.data(), qmax.size());
   const size_t o_aos = blob.add(ao_shell.data(), ao_shell.size());
   const size_t o_pi = blob.add(pinfo.data(), pinfo.size());
   char *d = (char *)buf(c, "qstore_tab", blob.bytes.size() + 256);
@@ -657,6 +663,7 @@ int qstore_build(mq_ctx *c) {
   qs.ksh = (int2 *)(d + o_k);
   qs.shell_ao0 = (int *)(d + o_ao);
   qs.ao_shell = (int *)(d + o_aos);
+  qs.shell_qmax = (double *)(d + o_qm);
   qs.pinfo = (int4 *)(d + o_pi);
   qs.X_elems = (size_t)base;
   qs.X = (double *)buf(c, "qstore_X", sizeof(double) * std::max<size_t>(qs.X_elems, 1));
