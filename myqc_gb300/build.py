@@ -74,7 +74,7 @@ def build(force: bool = False, verbose: bool = False, extra=()) -> str:
     return LIB
 
 
-STAGES = ("int1e", "int2e", "scf", "ao2mo", "mp2", "int1p", "cphf", "props")
+STAGES = ("parse", "int1e", "int2e", "scf", "ao2mo", "mp2", "int1p", "cphf", "props")
 BINDIR = os.path.join(HERE, "bin")
 STAGE_BIN = os.path.join(BINDIR, "myqc-stage")
 

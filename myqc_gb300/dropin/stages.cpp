@@ -1,13 +1,14 @@
 // stages.cpp -- drop-in replacements of the reference's stage executables
-// int1e, int2e, scf, ao2mo and mp2 (and the property stages int1p, cphf and
+// parse, int1e, int2e, scf, ao2mo and mp2 (and the property stages int1p, cphf and
 // props), computing through libmyqc.
 //
-// One binary; the stage is the name it is invoked by (symlinks int1e, int2e,
+// One binary; the stage is the name it is invoked by (symlinks parse, int1e, int2e,
 // scf, ao2mo, mp2) or its first argument.  Like the reference's programs they
 // work in the current directory on the reference's files (formats of
-// src/myQC/env.f90, basis.f90, integrals/int1e.f90, int2e.f90, scf/scf.f90,
+// src/parser/parser.f90, src/myQC/env.f90, basis.f90, integrals/int1e.f90, int2e.f90, scf/scf.f90,
 // ao2mo/ao2mo.f90, mp2/mp2.f90):
-//   envdat, nucpos, fmem        written by the reference's parser
+//   ZMAT                        the input (parse)
+//   envdat, nucpos, fmem        text (parse)
 //   mybasis, Ftab               basis library and Boys table
 //   basinfo, setinfo            text, written by int1e / int2e
 //   Suv, Huv                    text (int1e)
@@ -325,6 +326,222 @@ std::vector<double> read_XX(int n) {
 }
 
 // ------------------------------------------------------------------ stages
+// ---- parse (src/parser/parser.f90): ZMAT -> nucpos, envdat, fmem
+//
+// CARTESIAN input only, as the reference: a line CARTESIAN, one line per atom
+// (symbol, x, y, z), END, one line skipped, then "KEY= value" option lines
+// (read_options, :700-735, and the get* functions, :160-430).  The geometry is
+// recentred on the centre of mass with integer masses, converted from
+// angstrom to bohr unless UNITS= Bohr (build, :435-547); the electron counts
+// follow from the charge and multiplicity.  Where the reference touches
+// `error` (atoms closer than 0.2 A, an impossible charge and multiplicity,
+// RHF for an open shell, contradicting options) the files are still written
+// and the stage then fails; where the reference only STOPs (an unknown
+// element, method, basis or reference, a multiplicity below 1) this stage
+// also writes `error`, so that a driver polling it stops.
+const double A2B = 1.8897161646320724;  // parser.f90:14
+
+std::vector<std::string> tokens(const std::string &line) {
+  std::istringstream ls(line);
+  std::vector<std::string> tok;
+  std::string w;
+  while (ls >> w) tok.push_back(w);
+  return tok;
+}
+
+// READ(chr,'(I8)'): the first 8 characters as an integer, blanks ignored
+long long read_i8(const std::string &tok, const char *key) {
+  std::string t;
+  for (char ch : tok.substr(0, 8))
+    if (ch != ' ') t.push_back(ch);
+  if (t.empty()) return 0;
+  char *end = nullptr;
+  const long long v = std::strtoll(t.c_str(), &end, 10);
+  if (!end || *end) fail(std::string("ZMAT: bad integer for ") + key + " " + tok);
+  return v;
+}
+
+double read_real(std::string t) {
+  for (char &ch : t)
+    if (ch == 'D' || ch == 'd') ch = 'E';
+  char *end = nullptr;
+  const double v = std::strtod(t.c_str(), &end);
+  if (!end || *end) fail("ZMAT: bad coordinate " + t);
+  return v;
+}
+
+int stage_parse() {
+  if (!exists("ZMAT")) fail("You need to create the input file : 'ZMAT'");
+  const std::string text = slurp("ZMAT");
+  std::fputs(text.c_str(), stdout);  // the reference echoes its input (cat ZMAT)
+  std::printf(" \n Input parameters\n");
+  std::vector<std::string> lines;
+  {
+    std::istringstream in(text);
+    std::string line;
+    while (std::getline(in, line)) {
+      if (!line.empty() && line.back() == '\r') line.pop_back();
+      lines.push_back(line);
+    }
+  }
+  const int fline = (int)lines.size();
+  const std::vector<std::string> head = lines.empty() ? std::vector<std::string>() : tokens(lines[0]);
+  const std::string sys = head.empty() ? std::string() : head[0].substr(0, 9);
+  if (sys == "INTERNAL") fail("Sorry, that input style not supported yet");
+  if (sys != "CARTESIAN") fail("Bad system type input. Exiting...");
+  // geometry (cartesian, :622-678)
+  std::vector<int> Z;
+  std::vector<double> X;  // nnuc x 3, row-major while parsing
+  int i = 1;
+  for (;; ++i) {
+    if (i >= fline) fail("You need to put 'END' marker in ZMAT");
+    const std::vector<std::string> tok = tokens(lines[i]);
+    if (!tok.empty() && tok[0] == "END") break;
+    if (tok.size() < 4) fail("ZMAT: bad atom line '" + lines[i] + "'");
+    const std::string id = tok[0].substr(0, 2);
+    int z = 0;
+    for (int k = 0; k < 10; ++k)
+      if (id == ELEM[k]) z = k + 1;
+    if (!z) fail("Sorry, that element is not implemented yet. Exiting ...");
+    Z.push_back(z);
+    for (int k = 1; k <= 3; ++k) X.push_back(read_real(tok[k]));
+  }
+  const int nnuc = (int)Z.size();
+  if (nnuc <= 0) fail("No atoms in system");
+  // options (defaults as :52; read_options skips the line after END)
+  long long opt[17] = {0, 0, 0, 0, 0, 1, 1000, 1, 7, 0, 1, 0, 1, 0, 0, 0, 0};
+  const int nline = nnuc + 2;
+  for (int l = nline + 1; l < fline; ++l) {
+    const std::vector<std::string> tok = tokens(lines[l]);
+    if (tok.size() < 2) continue;
+    const std::string &k = tok[0], &v = tok[1];
+    if (k == "CALC=") {
+      if (v == "SCF" || v == "HF") opt[1] = 0;
+      else if (v == "MP2") opt[1] = 1;
+      else if (v == "CIS") opt[1] = 2;
+      else fail("Sorry, that method has not been implimented. Exiting...");
+    } else if (k == "BASIS=") {
+      if (v == "STO-3G") opt[2] = 0;
+      else if (v == "tester1") opt[2] = 1;
+      else if (v == "tester2") opt[2] = 2;
+      else if (v == "tester3") opt[2] = 3;
+      else fail("Sorry, that basis has not been implimented. Exiting...");
+    } else if (k == "CHARGE=") {
+      opt[9] = read_i8(v, "CHARGE=");
+    } else if (k == "MULTI=") {
+      opt[10] = read_i8(v, "MULTI=");
+      if (opt[10] <= 0) fail("bad value for multiplicity, exiting.");
+    } else if (k == "REF=") {
+      if (v == "RHF") opt[3] = 0;
+      else if (v == "UHF") opt[3] = 1;
+      else if (v == "ROHF") fail("Sorry, this reference is not implimented yet. Exiting...");
+      else fail("Sorry, that reference has not been implimented. Exiting...");
+    } else if (k == "PAR=") {
+      opt[4] = v == "OMP" ? 2 : v == "MPI" ? 3 : 1;
+    } else if (k == "NODES=") {
+      std::printf(" Nodes : not implimented yet\n");
+      opt[5] = 1;
+    } else if (k == "MEMORY=") {
+      const long long m = read_i8(v, "MEMORY=");
+      if (m < 0) std::printf(" You specificed a memory less than zero.\n");
+      opt[6] = m < 0 ? 1000 : m;
+    } else if (k == "VERB=") {
+      opt[7] = v == "1" ? 1 : v == "2" ? 2 : v == "3" ? 3 : 0;
+    } else if (k == "SCF_Conv=") {
+      opt[8] = read_i8(v, "SCF_Conv=");
+    } else if (k == "UNITS=") {
+      opt[11] = v == "Bohr" ? 1 : 0;
+    } else if (k == "AO2MO=") {
+      if (v != "1") std::printf(" Sorry, only slow ao2mo supported\n");
+      opt[12] = 1;
+    } else if (k == "EXCITE=") {
+      opt[13] = (v == "CIS" || v == "1") ? 1 : 0;
+    } else if (k == "ROOT_ALG=") {
+      opt[14] = 0;
+    } else if (k == "E_NUM=") {
+      const long long m = read_i8(v, "E_NUM=");
+      opt[15] = m < 0 ? 1 : m;
+    } else if (k == "PROP=") {
+      opt[16] = (v == "FIRST" || v == "1") ? 1 : (v == "SECOND" || v == "2") ? 2 : 0;
+    } else {
+      std::printf(" parser could not understand options line %12d\n", l - nline - 1);
+    }
+  }
+  bool bad = false;
+  // checkgeom (:560-600): pairs closer than 0.2 A in the input units
+  for (int a = 0; a < nnuc; ++a)
+    for (int b = a + 1; b < nnuc; ++b) {
+      double r = 0.0;
+      for (int k = 0; k < 3; ++k) r += (X[3 * a + k] - X[3 * b + k]) * (X[3 * a + k] - X[3 * b + k]);
+      if (std::sqrt(r) < (opt[11] == 0 ? 0.2 : 0.2 * A2B)) {
+        std::printf(" These atoms are too close (r < 0.2 A) : %12d %12d\n", a, b);
+        bad = true;
+      }
+    }
+  // centre of mass with integer masses, then angstrom -> bohr
+  static const double MASS[10] = {1, 4, 7, 9, 11, 12, 14, 16, 19, 20};
+  double com[3] = {0, 0, 0}, tot = 0.0;
+  for (int a = 0; a < nnuc; ++a) {
+    for (int k = 0; k < 3; ++k) com[k] = com[k] + MASS[Z[a] - 1] * X[3 * a + k];
+    tot = tot + MASS[Z[a] - 1];
+  }
+  for (int k = 0; k < 3; ++k) com[k] = com[k] / tot;
+  for (int a = 0; a < nnuc; ++a)
+    for (int k = 0; k < 3; ++k) {
+      X[3 * a + k] = X[3 * a + k] - com[k];
+      if (opt[11] == 0) X[3 * a + k] = X[3 * a + k] * A2B;
+    }
+  // electrons
+  long long nelc = -opt[9];
+  for (int z : Z) nelc += z;
+  const long long unpr = opt[10] - 1;
+  long long nelcB = (nelc - unpr) / 2, nelcA = nelcB + unpr;
+  if (nelcA + nelcB != nelc) {
+    std::printf(" That charge and multiplicity is not allowed.\n");
+    bad = true;
+  }
+  if (nelc < 0 || nelcA < 0 || nelcB < 0) {
+    std::printf(" You have less than 0 electrons. :)\n");
+    bad = true;
+  }
+  if (nelcA != nelcB && opt[3] == 0) {
+    std::printf(" You cannot use RHF for open shell molecules!\n");
+    bad = true;
+  }
+  {
+    FILE *f = std::fopen("nucpos", "w");
+    if (!f) fail("cannot write nucpos");
+    for (int a = 0; a < nnuc; ++a)
+      std::fprintf(f, " %11d %25.17E %25.17E %25.17E\n", Z[a], X[3 * a], X[3 * a + 1], X[3 * a + 2]);
+    std::fclose(f);
+    f = std::fopen("envdat", "w");
+    if (!f) fail("cannot write envdat");
+    std::fprintf(f, " %11d\n %11lld %11lld\n %11d\n", nnuc, nelcA, nelcB, 17);
+    for (int k = 0; k < 17; ++k) std::fprintf(f, " %20lld", opt[k]);
+    std::fprintf(f, "\n \n #number of nuclei\n #number of electrons\n #length of options array\n options array\n");
+    std::fclose(f);
+    f = std::fopen("fmem", "w");
+    if (!f) fail("cannot write fmem");
+    std::fprintf(f, " %20lld\n", opt[6]);
+    std::fclose(f);
+  }
+  if (bad) fail("parser found an error in ZMAT");
+  // check_options (:767-800)
+  std::string why;
+  if (opt[13] != 0 && opt[1] != 0) why += " Sorry, only SCF CIS coded\n";
+  if (opt[13] != 0 && opt[3] != 1) why += " Sorry, only UHF CIS references are coded\n";
+  if (opt[16] != 0 && opt[1] != 0) why += " Sorry, only SCF properties are coded\n";
+  if (opt[16] != 0 && opt[3] != 0) why += " Sorry, only RHF reference properites are coded\n";
+  if (!why.empty()) {
+    std::fputs(why.c_str(), stdout);
+    fail("===========================================\n Bad options in ZMAT");
+  }
+  std::printf(" ===========================================\n");
+  std::printf(" nuclei %d, alpha electrons %lld, beta electrons %lld, %s, %s, SCF convergence 1e-%lld\n", nnuc, nelcA,
+              nelcB, opt[3] ? "UHF" : "RHF", opt[1] == 1 ? "MP2" : opt[1] == 2 ? "CIS" : "SCF", opt[8]);
+  return 0;
+}
+
 int stage_int1e() {
   std::printf("\n int1e called\n");
   Env e = read_env();
@@ -363,37 +580,95 @@ int stage_int2e() {
   return 0;
 }
 
-// MOLDEN file of the SCF orbitals ([Molden Format]: atoms in bohr, the STO-3G
-// contractions of each atom, then every orbital; occupation 1 when its energy
-// is negative, as the reference's writer does, scf.f90:1343-1466)
-void write_molden(const Env &e, const Basis &b, int n, const std::vector<double> &C, const std::vector<double> &eps,
-                  bool uhf) {
+// gfortran's list-directed REAL(8) item (1PG25.17E3): 17 significant
+// digits in F form, right-justified in 20 columns and followed by 5 blanks,
+// when the value rounded to 17 digits lies in [0.1, 1e17) (zero included, with
+// 16 decimals); otherwise E form with one leading digit, 16 decimals and a
+// three-digit exponent, right-justified in 25 columns
+std::string ld_real(double x) {
+  char buf[64];
+  if (x == 0.0) {
+    std::snprintf(buf, sizeof buf, "%20.16f     ", x);
+    return buf;
+  }
+  std::snprintf(buf, sizeof buf, "%.16e", x);
+  const int e10 = std::atoi(std::strchr(buf, 'e') + 1);
+  if (e10 >= -1 && e10 <= 16) {
+    std::snprintf(buf, sizeof buf, "%20.*f     ", 16 - e10, x);
+    return buf;
+  }
+  char m[64];
+  std::snprintf(m, sizeof m, "%.16E", x);  // d.dddE+XX: widen the exponent to three digits
+  char *ep = std::strchr(m, 'E');
+  const int ex = std::abs(std::atoi(ep + 1)) % 1000;
+  const char sign = ep[1] == '-' ? '-' : '+';
+  *ep = 0;
+  std::snprintf(buf, sizeof buf, "%.24sE%c%03d", m, sign, ex);
+  char out[64];
+  std::snprintf(out, sizeof out, "%25s", buf);
+  return out;
+}
+
+// MOLDEN file of the SCF orbitals in the reference writer's layout
+// (makeMOLDEN, src/scf/scf.f90:1343-1466): the atoms in bohr, then per atom
+// its mybasis sections as listed there (a shell letter, the primitive count,
+// "1.00", then exponent and coefficient of each primitive as list-directed
+// REAL(8) items), then every orbital with occupation 1 when its energy is
+// negative; beta orbitals follow for UHF
+void write_molden(const Env &e, int n, const std::vector<double> &C, const std::vector<double> &eps, bool uhf) {
+  std::vector<std::vector<std::string>> rows;
+  {
+    std::istringstream in(slurp("mybasis"));
+    std::string line;
+    while (std::getline(in, line)) {
+      std::istringstream ls(line);
+      std::vector<std::string> tok;
+      std::string w;
+      while (ls >> w) tok.push_back(w);
+      rows.push_back(tok);
+    }
+  }
+  auto first = [&](size_t r) { return rows[r].empty() ? std::string() : rows[r][0].substr(0, 8); };
+  auto real = [&](std::string t) {
+    for (char &ch : t)
+      if (ch == 'D' || ch == 'd') ch = 'E';
+    return std::stod(t);
+  };
   FILE *f = std::fopen("MOLDEN", "w");
   if (!f) fail("cannot write MOLDEN");
   std::fprintf(f, " [Molden Format]\n [ATOMS] AU\n");
   for (int a = 0; a < e.nnuc; ++a)
     std::fprintf(f, "%-2s    %3d    %3d    %15.8f    %15.8f    %15.8f\n", ELEM[e.Z[a] - 1], a + 1, e.Z[a], e.xyz[a],
                  e.xyz[a + e.nnuc], e.xyz[a + 2 * (size_t)e.nnuc]);
-  std::fprintf(f, " [GTO]\n");
-  const int OpS = b.basinfo[0], setl = b.setinfo[1], nset = b.setinfo[0];
+  std::fprintf(f, " [Molden Format]\n [GTO]\n");
+  static const char SHELL[] = "spdfgh";
+  size_t p = 0;
+  while (p < rows.size() && first(p) != "STO-3G") ++p;
   for (int a = 0; a < e.nnuc; ++a) {
-    std::fprintf(f, " %d 0\n", a + 1);
-    // one shell per AO group of the atom: s functions, then p triples
-    for (int o = 0; o < n; ++o) {
-      const int *bi = &b.basinfo[2 + 5 * (size_t)o];
-      if (bi[4] != a || bi[2] > 0) continue;  // one line per s function and per p triple (m = 0)
-      std::vector<std::pair<double, double>> prim;
-      for (int s = 0; s < nset; ++s) {
-        const int *si = &b.setinfo[1 + (size_t)s * setl];
-        for (int k = 0; k < si[1]; ++k)
-          if (si[4 + k] == o) prim.push_back({b.set[s], b.bas[(size_t)s * OpS + k]});
+    std::fprintf(f, " %11d %11d\n", a + 1, 0);
+    size_t q = p;
+    while (q < rows.size() && first(q) != ELEM[e.Z[a] - 1]) ++q;
+    if (q + 1 >= rows.size()) fail(std::string("mybasis: no ") + ELEM[e.Z[a] - 1]);
+    const int sec = std::stoi(rows[q + 1][0]);
+    q += 2;
+    for (int s = 0; s < sec; ++s) {
+      while (q < rows.size() && rows[q].size() < 5) ++q;
+      if (q >= rows.size()) fail("mybasis: truncated section");
+      const int func = std::stoi(rows[q][0]), coef = std::stoi(rows[q][1]), ang = std::stoi(rows[q][3]);
+      if (ang < 0 || ang > 5 || coef < 1) fail("mybasis: bad section header");
+      ++q;
+      std::fprintf(f, " %c %11d 1.00\n", SHELL[ang], func);
+      for (int k = 0; k < func; ++k, ++q) {
+        if (q >= rows.size() || (int)rows[q].size() < coef) fail("mybasis: truncated primitive line");
+        std::string line;
+        for (int c = 1; c < coef; ++c) line += " " + ld_real(real(rows[q][c]));
+        line += " " + ld_real(real(rows[q][0]));
+        std::fprintf(f, "%s\n", line.c_str());
       }
-      std::fprintf(f, " %c %zu 1.00\n", bi[1] == 0 ? 's' : 'p', prim.size());
-      for (auto &pr : prim) std::fprintf(f, " %18.10E %18.10E\n", pr.first, pr.second);
     }
     std::fprintf(f, "\n");
   }
-  std::fprintf(f, " [MO]\n");
+  std::fprintf(f, "\n [MO]\n");
   for (int s = 0; s < (uhf ? 2 : 1); ++s)
     for (int i = 0; i < n; ++i) {
       const double en = eps[(size_t)s * n + i];
@@ -459,7 +734,7 @@ int stage_scf() {
   }
   write_text("Cui", cm, n2);
   write_text("eig", em, (size_t)n);
-  write_molden(e, b, n, C, eps, uhf);
+  write_molden(e, n, C, eps, uhf);
   // the density files of the reference's loop (dens.f90 writes Da, scf.f90
   // keeps Dold): one unformatted record per spin; both hold the last
   // iteration's density here, converged to the SCF threshold
@@ -718,18 +993,19 @@ int main(int argc, char **argv) {
   std::string name = argv[0];
   const size_t slash = name.find_last_of('/');
   if (slash != std::string::npos) name = name.substr(slash + 1);
-  static const char *const stages[] = {"int1e", "int2e", "scf", "ao2mo", "mp2", "int1p", "cphf", "props"};
+  static const char *const stages[] = {"parse", "int1e", "int2e", "scf", "ao2mo", "mp2", "int1p", "cphf", "props"};
   bool known = false;
   for (const char *st : stages) known = known || name == st;
   if (!known) {
     if (argc < 2) {
-      std::fprintf(stderr, "usage: %s int1e|int2e|scf|ao2mo|mp2|int1p|cphf|props (or through a link of that name)\n",
+      std::fprintf(stderr, "usage: %s parse|int1e|int2e|scf|ao2mo|mp2|int1p|cphf|props (or through a link of that name)\n",
                    argv[0]);
       return 2;
     }
     name = argv[1];
   }
   if (exists("error")) return 0;  // a previous stage failed: stop, as the reference does
+  if (name == "parse") return stage_parse();
   if (name == "int1e") return stage_int1e();
   if (name == "int2e") return stage_int2e();
   if (name == "scf") return stage_scf();

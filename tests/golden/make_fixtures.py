@@ -6,7 +6,8 @@ Copies the reference's input data (``src/Ftab``, ``src/mybasis``, the example
 ZMAT files) and extracts its known answers into ``reference_pins.json``:
 
 * myQC's own MOLDEN orbital energies (examples/Be, examples/O/singlet,
-  examples/NO) -- the reference's parity pins;
+  examples/NO) -- the reference's parity pins -- and the three MOLDEN files
+  themselves (molden/), the layout the scf stage's MOLDEN writer follows;
 * the CFOUR energies shipped beside some examples (examples/*/cfour/out) --
   sanity pins only, since CFOUR uses true pi, exact Boys values and
   renormalised contractions.
@@ -60,7 +61,10 @@ def main(ref):
         shutil.copyfile(os.path.join(ref, "examples", ex, "ZMAT"),
                         os.path.join(HERE, "zmat", ex.replace("/", "_") + ".ZMAT"))
     pins = {"molden": {}, "cfour": {}}
+    os.makedirs(os.path.join(HERE, "molden"), exist_ok=True)
     for ex in ("Be", "O/singlet", "NO"):
+        shutil.copyfile(os.path.join(ref, "examples", ex, "MOLDEN"),
+                        os.path.join(HERE, "molden", ex.replace("/", "_") + ".MOLDEN"))
         a, b = molden_energies(os.path.join(ref, "examples", ex, "MOLDEN"))
         pins["molden"][ex.replace("/", "_")] = {"alpha": a, "beta": b}
     for ex in ("CO2", "HeH", "OH"):

@@ -1,8 +1,9 @@
-"""The drop-in stage executables (bin/int1e, int2e, scf, ao2mo, mp2) run in a
-scratch directory on the reference's inputs (envdat, nucpos, fmem, mybasis,
-Ftab), chained through the reference's files exactly as its driver chains its
-own programs, against the oracle: integrals in the files, the printed SCF and
-MP2 energies.  RHF (CO2) and UHF (O triplet)."""
+"""The drop-in stage executables (bin/parse, int1e, int2e, scf, ao2mo, mp2)
+run in a scratch directory on the reference's inputs (ZMAT or envdat, nucpos,
+fmem; mybasis, Ftab), chained through the reference's files exactly as its
+driver chains its own programs, against the oracle: integrals in the files,
+the printed SCF and MP2 energies (RHF CO2, UHF O triplet), and the MOLDEN
+file against the reference's own (Be, O singlet, NO)."""
 import os
 import re
 import shutil
@@ -12,7 +13,7 @@ import numpy as np
 import pytest
 
 import oracle as O
-from conftest import golden
+from conftest import golden, molden_header_values, molden_orbital_errors, read_molden
 from myqc_gb300 import formats
 from myqc_gb300.build import BINDIR
 
@@ -59,6 +60,47 @@ def test_stage_chain(tmp_path, ftab, basis_text, name):
     (tmp_path / "error").write_text("")
     r = subprocess.run([os.path.join(BINDIR, "scf")], cwd=str(tmp_path), capture_output=True, text=True)
     assert r.returncode == 0 and "STARTING SCF" not in r.stdout
+
+
+@pytest.mark.parametrize("name,tol_e,tol_p", [("Be", 2e-8, 1e-8), ("O_singlet", 2e-8, 1e-8), ("NO", 1.5e-7, 2e-6)])
+def test_molden_from_zmat(tmp_path, basis_text, name, tol_e, tol_p):
+    """parse -> int1e -> int2e -> scf from the example's ZMAT alone, and the
+    MOLDEN file the scf stage writes against the one the reference wrote for
+    the same input: the same header up to [MO] (atoms, the mybasis sections
+    in list-directed layout) -- the very text where the reference's file
+    comes from a gfortran that prints 17 digits (O singlet, NO), the same
+    values where it printed 15 (Be) -- then the orbitals -- energies, occupations and
+    degenerate-set projectors, up to a common rotation of the p functions
+    (none is fixed for an atom or a linear molecule).  The reference's
+    SCF_Conv default (1e-7 on the density) bounds the NO agreement."""
+    shutil.copy(golden("zmat", name + ".ZMAT"), tmp_path / "ZMAT")
+    shutil.copy(golden("mybasis"), tmp_path / "mybasis")
+    shutil.copy(golden("Ftab"), tmp_path / "Ftab")
+    out = "".join(_run(s, str(tmp_path)) for s in ("parse", "int1e", "int2e", "scf"))
+    assert "Total SCF energy" in out
+    head, mos = read_molden((tmp_path / "MOLDEN").read_text())
+    ref_head, ref_mos = read_molden(open(golden("molden", name + ".MOLDEN")).read())
+    assert molden_header_values(head) == molden_header_values(ref_head)
+    if name != "Be":
+        assert head == ref_head
+    sysm = formats.read_env(str(tmp_path))
+    basis = formats.parse_mybasis_text(basis_text, sysm.atoms)
+    de, occ_ok, dp = molden_orbital_errors(mos, ref_mos, basis.basinfo)
+    assert de < tol_e and occ_ok and dp < tol_p, (de, occ_ok, dp)
+
+
+def test_chain_from_zmat(tmp_path, ftab, basis_text):
+    """The whole chain from the ZMAT of the reference's CO2 example, the way
+    its driver runs it (parse first): the printed MP2 energy against the
+    oracle's run of the same input."""
+    zt = open(golden("zmat", "CO2.ZMAT")).read()
+    (tmp_path / "ZMAT").write_text(zt)
+    shutil.copy(golden("mybasis"), tmp_path / "mybasis")
+    shutil.copy(golden("Ftab"), tmp_path / "Ftab")
+    out = "".join(_run(s, str(tmp_path)) for s in ("parse", "int1e", "int2e", "scf", "ao2mo", "mp2"))
+    ref = O.run_job(zt, basis_text, ftab, 0)
+    assert abs(_number(r"Total SCF energy \(a\.u\)", out) - ref["scf"].energy) < 1e-8
+    assert abs(_number(r"E\(MBPT2\) =", out) - ref["mp2"]["E_MP2"]) < 1e-7
 
 
 def test_cis_blocks(tmp_path, ftab, basis_text):

@@ -1,6 +1,7 @@
 """The oracle against the reference's own known answers (no GPU).
 
-* myQC's MOLDEN orbital energies (examples/Be, O/singlet, NO) -- parity pins;
+* myQC's MOLDEN orbital energies and orbitals (examples/Be, O/singlet, NO)
+  -- parity pins;
 * Ftab, a known-answer table: decoded values equal the exact Boys function
   except for the four corrupted entries the reference ships;
 * CFOUR energies beside the examples -- loose sanity pins (true pi, exact
@@ -13,7 +14,7 @@ import numpy as np
 import pytest
 
 import oracle as O
-from conftest import golden
+from conftest import golden, molden_orbital_errors, molden_text_of, read_molden
 
 PINS = json.load(open(golden("reference_pins.json")))
 
@@ -32,6 +33,20 @@ def test_molden_orbital_energies(ftab, basis_text, name, tol):
         assert np.max(np.abs(eig[1] - p["beta"])) < tol
     else:
         assert np.max(np.abs(eig - p["alpha"])) < tol
+
+
+@pytest.mark.parametrize("name,tol_e,tol_p", [("Be", 1e-8, 1e-9), ("O_singlet", 1e-8, 1e-9), ("NO", 1e-7, 1e-6)])
+def test_molden_orbitals(ftab, basis_text, name, tol_e, tol_p):
+    """The oracle's orbitals against the reference's MOLDEN file: energies,
+    occupations and the projector onto every set of degenerate orbitals (up
+    to a common rotation of the p functions, which nothing fixes for an atom
+    or a linear molecule).  The NO run converges to 1e-7 like the
+    reference's, so its orbitals agree to that order."""
+    r = _run(name, ftab, basis_text)
+    _, ref = read_molden(open(golden("molden", name + ".MOLDEN")).read())
+    _, ours = read_molden(molden_text_of(r["mol"], r["scf"].eig, r["scf"].C, r["mol"].options[3] == 1))
+    de, occ_ok, dp = molden_orbital_errors(ours, ref, r["basis"].basinfo)
+    assert de < tol_e and occ_ok and dp < tol_p, (de, occ_ok, dp)
 
 
 def test_ftab_known_answers(ftab):
