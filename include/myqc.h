@@ -123,6 +123,18 @@ int mq_set_partition(mq_ctx *ctx, int part, int nparts);
 #define MQ_STORE_QUARTETS 1
 int mq_set_eri_storage(mq_ctx *ctx, int storage);
 
+/* The integral autotuner (no counterpart in the reference, whose set-quartet
+ * loop has no launch shape, src/integrals/int2e.f90:192-241): mode 1
+ * (default) times the candidate launch shapes of each integral launch of a
+ * new size class once -- launch order binned by surviving primitive quartets
+ * or not, 64/128/256 threads per CTA -- and keeps the fastest for the
+ * context's later passes; mode 0 uses the defaults (binned, 128). */
+int mq_set_eri_tuning(mq_ctx *ctx, int mode);
+
+/* The autotuner's choices so far as text, one line per launch signature (the
+ * candidates with their times, the chosen one marked '*'); truncated to len. */
+int mq_eri_tuning_report(const mq_ctx *ctx, char *buf, int len);
+
 /* Upload an existing XX (n^4 doubles, the int2e file payload) to the device,
  * e.g. when a drop-in scf reads the reference's XX file. */
 int mq_eri_upload(mq_ctx *ctx, const double *XX);

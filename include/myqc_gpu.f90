@@ -67,6 +67,12 @@ MODULE myqc_gpu
     INTEGER(c_int) FUNCTION mq_set_eri_storage(ctx, storage) BIND(C)
       IMPORT; TYPE(c_ptr), VALUE :: ctx; INTEGER(c_int), VALUE :: storage   ! MQ_STORE_FULL / MQ_STORE_QUARTETS
     END FUNCTION
+    INTEGER(c_int) FUNCTION mq_set_eri_tuning(ctx, mode) BIND(C)
+      IMPORT; TYPE(c_ptr), VALUE :: ctx; INTEGER(c_int), VALUE :: mode
+    END FUNCTION
+    INTEGER(c_int) FUNCTION mq_eri_tuning_report(ctx, buf, len) BIND(C)
+      IMPORT; TYPE(c_ptr), VALUE :: ctx; CHARACTER(KIND=c_char) :: buf(*); INTEGER(c_int), VALUE :: len
+    END FUNCTION
     INTEGER(c_int) FUNCTION mq_int1e(ctx, S, H) BIND(C)
       IMPORT; TYPE(c_ptr), VALUE :: ctx; REAL(c_double) :: S(*), H(*)
     END FUNCTION

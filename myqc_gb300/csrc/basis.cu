@@ -168,31 +168,43 @@ void pairs_host(const std::vector<HostShell> &shells, const std::vector<double> 
       h.aoB.push_back(B.ao0);
       h.mol.push_back(0);
       h.off.push_back((int)h.p.size());
+      // the surviving primitive pairs, K descending (stable: ties keep the
+      // (i, j) order): the pairs of a ket passing the screen against one bra
+      // primitive are then a prefix of the ket's list, and the integral
+      // kernels visit exactly the surviving primitive quartets
+      std::vector<std::pair<double, std::pair<int, int>>> live_pp;
       for (int i = 0; i < A.nprim; ++i)
         for (int j = 0; j < B.nprim; ++j) {
-          double a = A.alpha[i], b = B.alpha[j], pp = a + b;
-          double Kab = std::exp(-a * b * AB2 / pp);
+          const double a = A.alpha[i], b = B.alpha[j];
+          const double Kab = std::exp(-a * b * AB2 / (a + b));
           // a primitive pair whose EIJ is below 1e-14 fails the reference's
           // screen EIJ*EGH < 1e-14 (int2e.f90:257; int1e.f90:238) for any
           // partner, since EGH <= 1
-          if (Kab < 1.0e-14) continue;
-          double P[3], PA[3], PB[3];
-          for (int k = 0; k < 3; ++k) {
-            P[k] = (a * xa[k] + b * xb[k]) / pp;
-            PA[k] = P[k] - xa[k];
-            PB[k] = P[k] - xb[k];
-          }
-          h.p.push_back(pp);
-          h.inv2p.push_back(1.0 / (2.0 * pp));
-          h.beta.push_back(b);
-          h.Px.push_back(P[0]); h.Py.push_back(P[1]); h.Pz.push_back(P[2]);
-          h.PAx.push_back(PA[0]); h.PAy.push_back(PA[1]); h.PAz.push_back(PA[2]);
-          h.PBx.push_back(PB[0]); h.PBy.push_back(PB[1]); h.PBz.push_back(PB[2]);
-          h.K.push_back(Kab);
-          double ca[2] = {A.cs[i], A.cp[i]}, cb[2] = {B.cs[j], B.cp[j]};
-          for (int la = 0; la < 2; ++la)
-            for (int lb = 0; lb < 2; ++lb) h.c4.push_back(Kab * ca[la] * cb[lb]);
+          if (Kab >= 1.0e-14) live_pp.push_back({Kab, {i, j}});
         }
+      std::stable_sort(live_pp.begin(), live_pp.end(),
+                       [](const auto &x, const auto &y) { return x.first > y.first; });
+      for (const auto &lp : live_pp) {
+        const int i = lp.second.first, j = lp.second.second;
+        double a = A.alpha[i], b = B.alpha[j], pp = a + b;
+        double Kab = lp.first;
+        double P[3], PA[3], PB[3];
+        for (int k = 0; k < 3; ++k) {
+          P[k] = (a * xa[k] + b * xb[k]) / pp;
+          PA[k] = P[k] - xa[k];
+          PB[k] = P[k] - xb[k];
+        }
+        h.p.push_back(pp);
+        h.inv2p.push_back(1.0 / (2.0 * pp));
+        h.beta.push_back(b);
+        h.Px.push_back(P[0]); h.Py.push_back(P[1]); h.Pz.push_back(P[2]);
+        h.PAx.push_back(PA[0]); h.PAy.push_back(PA[1]); h.PAz.push_back(PA[2]);
+        h.PBx.push_back(PB[0]); h.PBy.push_back(PB[1]); h.PBz.push_back(PB[2]);
+        h.K.push_back(Kab);
+        double ca[2] = {A.cs[i], A.cp[i]}, cb[2] = {B.cs[j], B.cp[j]};
+        for (int la = 0; la < 2; ++la)
+          for (int lb = 0; lb < 2; ++lb) h.c4.push_back(Kab * ca[la] * cb[lb]);
+      }
       ++idx;
     }
   }

@@ -347,6 +347,20 @@ int mq_set_eri_storage(mq_ctx *c, int storage) {
   return MQ_OK;
 }
 
+int mq_set_eri_tuning(mq_ctx *c, int mode) {
+  if (!c || (mode != 0 && mode != 1)) return MQ_EINVAL;
+  c->eri_tune_mode = mode;
+  return MQ_OK;
+}
+
+int mq_eri_tuning_report(const mq_ctx *c, char *out, int len) {
+  if (!c || !out || len <= 0) return MQ_EINVAL;
+  const std::string r = eri_tune_report(c);
+  strncpy(out, r.c_str(), len - 1);
+  out[len - 1] = 0;
+  return MQ_OK;
+}
+
 int mq_eri_full(mq_ctx *c, double *XX) {
   if (!XX) return set_err(c, MQ_EINVAL, "null output");
   MQ_TRY(need_system(c));

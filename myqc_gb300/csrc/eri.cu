@@ -17,10 +17,11 @@ namespace mq {
 __global__ void quartet_screen_kernel(EriArgs g, long long *__restrict__ part, int *__restrict__ counts) {
   __shared__ int warp_cnt[32], warp_off[33];
   const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  long long qd = q;
   int P = 0, Q = 0, m = 0;
   EriArgs h = g;
   h.list = nullptr;
-  const bool keep = q < g.nq && decode(h, q, P, Q, m);
+  const bool keep = q < g.nq && decode(h, qd, P, Q, m);
   const unsigned bal = __ballot_sync(0xffffffffu, keep);
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   if (lane == 0) warp_cnt[w] = __popc(bal);

@@ -272,45 +272,69 @@ __device__ __forceinline__ void quartet(const EriArgs &g, int P, int Q, size_t n
   const bool parity = g.mode == MQ_MODE_REFERENCE;
   const RT pref0 = parity ? RT(2.0 * 17.493419544621675) : RT(2.0 * 17.493418327624862);  // 2 pi^2.5
   unsigned nprim = 0;
-  for (int ip = p0; ip < p1; ++ip) {
-    PrimPair<RT> ab;
-    load_pp(t, ip, ab);
-    const RT p = ab.p, i2p = ab.i2p, Kab = ab.K;
-    const RT Px = ab.Px, Py = ab.Py, Pz = ab.Pz;
-    RT ex[2][2][3], ey[2][2][3], ez[2][2][3];
-    pair_E(ab.PAx, ab.PBx, i2p, RT(1), ex);
-    pair_E(ab.PAy, ab.PBy, i2p, RT(1), ey);
-    pair_E(ab.PAz, ab.PBz, i2p, RT(1), ez);
-    RT cab[4];
-#pragma unroll
-    for (int k = 0; k < 4; ++k) cab[k] = ab.c[k];
-    // bra products E^{ab}_{tuv} * c_a c_b K_ab (kept per (a, b) unless ONFLY)
-    RT eb[ONFLY ? 1 : A1 - A0][ONFLY ? 1 : B1 - B0][3][3][3];
-    if (!ONFLY) {
-#pragma unroll
-      for (int a = A0; a < A1; ++a)
-#pragma unroll
-        for (int b = B0; b < B1; ++b)
-#pragma unroll
-          for (int x = 0; x <= fl(a, 0) + fl(b, 0); ++x)
-#pragma unroll
-            for (int y = 0; y <= fl(a, 1) + fl(b, 1); ++y)
-#pragma unroll
-              for (int z = 0; z <= fl(a, 2) + fl(b, 2); ++z)
-                eb[ONFLY ? 0 : a - A0][ONFLY ? 0 : b - B0][x][y][z] = ex[fl(a, 0)][fl(b, 0)][x] *
-                                                                     ey[fl(a, 1)][fl(b, 1)][y] *
-                                                                     ez[fl(a, 2)][fl(b, 2)][z] *
-                                                                     cab[2 * fang(a) + fang(b)];
-    }
-    for (int iq = q0; iq < q1; ++iq) {
-      PrimPair<RT> cd;
+  // The surviving primitive quartets only, in one flat loop.  The primitive
+  // pairs of a shell pair are ordered by K descending, so the ket primitives
+  // that pass the reference's screen Kab*Kcd >= 1e-14 (int2e.f90:257) against
+  // one bra primitive are a prefix of the ket list, and the bra primitives
+  // with any partner a prefix of the bra list: the loop moves to the next bra
+  // primitive at the first failing ket, and stops at the first bra primitive
+  // without a partner.  A warp's trip count is the largest survivor count of
+  // its lanes (which the binned launch order makes nearly equal).  The
+  // Schwarz bounds take every primitive quartet: they must bound the exact
+  // (ab|ab), and the screen can remove every primitive quartet of (ab|ab) for
+  // a distant pair while (ab|cd) with a compact partner survives it.
+  const RT screen = EPI == EPI_SCHWARZ ? RT(0) : RT(1.0e-14);
+  RT p = RT(0), i2p = RT(0), Kab = RT(0), Px = RT(0), Py = RT(0), Pz = RT(0);
+  RT ex[2][2][3], ey[2][2][3], ez[2][2][3];
+  RT cab[4];
+  // bra products E^{ab}_{tuv} * c_a c_b K_ab (kept per (a, b) unless ONFLY)
+  RT eb[ONFLY ? 1 : A1 - A0][ONFLY ? 1 : B1 - B0][3][3][3];
+  int ip = p0 - 1, iq = q1;
+  for (;;) {
+    PrimPair<RT> cd;
+    bool next_bra = iq >= q1;
+    if (!next_bra) {
       load_pp(t, iq, cd);
-      const RT Kcd = cd.K;
-      // int2e.f90:257; not for the Schwarz bounds, which must bound the exact
-      // (ab|ab): the screen removes every primitive quartet of (ab|ab) for a
-      // distant pair while (ab|cd) with a compact partner survives it
-      if (EPI != EPI_SCHWARZ && Kab * Kcd < RT(1.0e-14)) continue;
-      ++nprim;
+      next_bra = Kab * cd.K < screen;
+    }
+    if (next_bra) {
+      if (++ip >= p1 || q0 >= q1) break;
+      PrimPair<RT> ab;
+      load_pp(t, ip, ab);
+      load_pp(t, q0, cd);
+      if (ab.K * cd.K < screen) break;  // nor any later bra primitive
+      p = ab.p;
+      i2p = ab.i2p;
+      Kab = ab.K;
+      Px = ab.Px;
+      Py = ab.Py;
+      Pz = ab.Pz;
+      pair_E(ab.PAx, ab.PBx, i2p, RT(1), ex);
+      pair_E(ab.PAy, ab.PBy, i2p, RT(1), ey);
+      pair_E(ab.PAz, ab.PBz, i2p, RT(1), ez);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) cab[k] = ab.c[k];
+      if (!ONFLY) {
+#pragma unroll
+        for (int a = A0; a < A1; ++a)
+#pragma unroll
+          for (int b = B0; b < B1; ++b)
+#pragma unroll
+            for (int x = 0; x <= fl(a, 0) + fl(b, 0); ++x)
+#pragma unroll
+              for (int y = 0; y <= fl(a, 1) + fl(b, 1); ++y)
+#pragma unroll
+                for (int z = 0; z <= fl(a, 2) + fl(b, 2); ++z)
+                  eb[ONFLY ? 0 : a - A0][ONFLY ? 0 : b - B0][x][y][z] = ex[fl(a, 0)][fl(b, 0)][x] *
+                                                                       ey[fl(a, 1)][fl(b, 1)][y] *
+                                                                       ez[fl(a, 2)][fl(b, 2)][z] *
+                                                                       cab[2 * fang(a) + fang(b)];
+      }
+      iq = q0;
+    }
+    ++iq;
+    ++nprim;
+    {
       const RT q = cd.p, i2q = cd.i2p;
       const RT X = Px - cd.Px, Y = Py - cd.Py, Z = Pz - cd.Pz;
       const RT s = p + q;
@@ -377,7 +401,6 @@ __device__ __forceinline__ void quartet(const EriArgs &g, int P, int Q, size_t n
         }
     }
   }
-
   // ---------------- epilogues ----------------
   const int A = t.shA[P], B = t.shB[P], C = t.shA[Q], D = t.shB[Q];
   const int i0 = t.aoA[P], j0 = t.aoB[P], k0 = t.aoA[Q], l0 = t.aoB[Q];
@@ -468,10 +491,17 @@ __device__ __forceinline__ void quartet(const EriArgs &g, int P, int Q, size_t n
         }
 }
 
-// decode (P, Q) of quartet index q in the launch, and the molecule m (0 for
-// one system); returns false past the end
-__device__ __forceinline__ bool decode(const EriArgs &g, long long q, int &P, int &Q, int &m) {
+// decode (P, Q) of the launch's q-th quartet, and the molecule m (0 for one
+// system); returns false past the end.  With a list (Schwarz-compacted or
+// binned launch order) q is first replaced by its list entry, the quartet's
+// index in the launch's own numbering (the quartet store's block index).
+__device__ __forceinline__ bool decode(const EriArgs &g, long long &q, int &P, int &Q, int &m) {
   if (q >= g.nq) return false;
+  const bool listed = g.list != nullptr;
+  if (listed) {
+    if (q >= *g.list_n) return false;
+    q = g.list[q];
+  }
   if (g.st_off) {  // largest r with st_off[r] <= q
     int lo = 0, hi = g.st_n - 1;
     while (lo < hi) {
@@ -483,11 +513,6 @@ __device__ __forceinline__ bool decode(const EriArgs &g, long long q, int &P, in
     P = g.permP[lo];
     Q = g.permQ[(int)(q - g.st_off[lo])];
     return true;
-  }
-  const bool listed = g.list != nullptr;
-  if (listed) {
-    if (q >= *g.list_n) return false;
-    q = g.list[q];
   }
   m = 0;
   int pOff = g.pOff, qOff = g.qOff, nQ = g.nQ;
@@ -534,21 +559,38 @@ __host__ __device__ constexpr int ridx(int L, int t, int u, int v) {
 }
 __host__ __device__ constexpr int nherm(int L) { return (L + 1) * (L + 2) * (L + 3) / 6; }
 
+// The next surviving primitive quartet after (ip, iq) of a quartet whose
+// primitive pairs are ordered by K descending (see quartet()): the next ket
+// while it passes the screen against the bra, else the first ket of the next
+// bra.  Returns false when none is left (ip is then p1).
+__device__ __forceinline__ bool next_survivor(const PairTable &t, int p1, int q0, int q1, int &ip, int &iq,
+                                              double &Kab) {
+  if (++iq < q1 && Kab * t.K[iq] >= 1.0e-14) return true;
+  if (++ip >= p1) return false;
+  Kab = t.K[ip];
+  iq = q0;
+  if (Kab * t.K[q0] >= 1.0e-14) return true;
+  ip = p1;
+  return false;
+}
+
 // Quartet-store pass of the split classes ((sp sp|sp s): 4 warps, one ket
 // function c each; (sp sp|sp sp): 16 warps, one ket pair (c, d) each), with
 // the per-primitive-quartet work shared.  The CTA's warps serve the same 32
 // quartets (lane = quartet), so every one of them needs the same Boys values
-// and Hermite integrals R_tuv of each primitive quartet.  Each round, warp w
-// forms them for primitive quartet (bra primitive i, ket primitive j0 + w) of
-// its lane's quartet -- the prefactor, screening, Boys and R recursion done
-// once instead of once per warp -- and leaves R in shared memory; after a
-// barrier every warp contracts all the round's primitives into its own
-// outputs (ket and bra Hermite expansions, as quartet() does).  Trip counts
-// are the warp's maxima, equal in all warps of the CTA, so the barriers are
-// reached by every thread.
+// and Hermite integrals R_tuv of each primitive quartet.  A lane's surviving
+// primitive quartets are numbered k = 0 .. S-1 (bra outer, ket inner, the
+// survivors of the K-ordered lists as quartet() visits them); in round r warp
+// w forms the prefactor, Boys values and R recursion of survivor
+// r * NSPLIT + w of its lane's quartet -- once instead of once per warp --
+// and leaves R and the survivor's (bra, ket) primitive pair in shared memory;
+// after a barrier every warp contracts all the round's survivors into its own
+// outputs.  The round count is the warp's largest S (every warp of the CTA
+// computes the same S per lane), so the barriers are reached by every thread,
+// and a round has idle producers only at the end of a lane's list.
 template <int LA, int LB, int LC, int LD, int NSPLIT, int C0, int C1, int D0, int D1>
 __device__ __forceinline__ void quartet_store_shared(const EriArgs &g, bool valid, int P, int Q, double *XXout,
-                                                     double *smR, unsigned char *smF) {
+                                                     double *smR, int2 *smI) {
   constexpr int LAB = LA + LB, LT = LA + LB + LC + LD, NR = nherm(LT);
   constexpr int QREF = 3 * LT;
   constexpr int NA = nfun(LA), NB = nfun(LB), NC = nfun(LC), ND = nfun(LD);
@@ -563,110 +605,128 @@ __device__ __forceinline__ void quartet_store_shared(const EriArgs &g, bool vali
       for (int c = 0; c < C1 - C0; ++c)
 #pragma unroll
         for (int d = 0; d < D1 - D0; ++d) acc[a][b][c][d] = 0.0;
-  const int p0 = valid ? t.pp_off[P] : 0, np_l = valid ? t.pp_off[P + 1] - p0 : 0;
-  const int q0 = valid ? t.pp_off[Q] : 0, nq_l = valid ? t.pp_off[Q + 1] - q0 : 0;
-  const int pmax = __reduce_max_sync(0xffffffffu, np_l), qmax = __reduce_max_sync(0xffffffffu, nq_l);
+  const int p0 = valid ? t.pp_off[P] : 0, p1 = valid ? t.pp_off[P + 1] : 0;
+  const int q0 = valid ? t.pp_off[Q] : 0, q1 = valid ? t.pp_off[Q + 1] : 0;
+  // S: the survivors of this lane's quartet (the prefix lengths of the bra
+  // primitives, each no longer than the previous)
+  int S = 0;
+  {
+    int m = q1 - q0;
+    for (int i = p0; i < p1 && m > 0; ++i) {
+      const double Ki = t.K[i];
+      while (m > 0 && Ki * t.K[q0 + m - 1] < 1.0e-14) --m;
+      S += m;
+    }
+  }
+  const int rounds = (__reduce_max_sync(0xffffffffu, S) + NSPLIT - 1) / NSPLIT;
+  // this warp's producer position: survivor w, then NSPLIT further each round
+  int ip = p0, iq = q0 - 1;
+  double Kab = valid && p0 < p1 ? t.K[p0] : 0.0;
+  bool live = S > 0;
+  for (int k = 0; k <= w && live; ++k) live = next_survivor(t, p1, q0, q1, ip, iq, Kab);
   const bool parity = g.mode == MQ_MODE_REFERENCE;
   const double pref0 = parity ? 2.0 * 17.493419544621675 : 2.0 * 17.493418327624862;  // 2 pi^2.5
   unsigned nprim = 0;
-  for (int pi = 0; pi < pmax; ++pi) {
-    const bool pok = pi < np_l;
-    PrimPair<double> ab{};
-    if (pok) load_pp(t, p0 + pi, ab);
-    double ex[2][2][3], ey[2][2][3], ez[2][2][3];
-    pair_E(ab.PAx, ab.PBx, ab.i2p, 1.0, ex);
-    pair_E(ab.PAy, ab.PBy, ab.i2p, 1.0, ey);
-    pair_E(ab.PAz, ab.PBz, ab.i2p, 1.0, ez);
-    for (int jq = 0; jq < qmax; jq += NSPLIT) {
-      // producer: primitive quartet (pi, jq + w) of this lane's quartet
-      {
-        const int qj = jq + w;
-        unsigned char ok = 0;
-        if (pok && qj < nq_l) {
-          PrimPair<double> cd;
-          load_pp(t, q0 + qj, cd);
-          if (ab.K * cd.K >= 1.0e-14) {  // int2e.f90:257
-            ok = 1;
-            ++nprim;
-            const double q = cd.p, X = ab.Px - cd.Px, Y = ab.Py - cd.Py, Z = ab.Pz - cd.Pz;
-            const double sum = ab.p + q, rs = rsqrt(sum);
-            const double ipq = 4.0 * ab.i2p * cd.i2p;
-            const double alpha = (ab.p * q) * (rs * rs);
-            const double T = alpha * (X * X + Y * Y + Z * Z);
-            const double pref = pref0 * rs * ipq;
-            double F[LT + 1];
-            boys<QREF, LT>(g.mode, T, g.boys, F);
+  int cur_ip = -1;  // the bra primitive whose expansion the consumer holds
+  double ex[2][2][3], ey[2][2][3], ez[2][2][3], cab[4];
+  for (int r = 0; r < rounds; ++r) {
+    // producer: survivor r * NSPLIT + w of this lane's quartet
+    {
+      int2 id = make_int2(-1, -1);
+      if (live) {
+        PrimPair<double> ab, cd;
+        load_pp(t, ip, ab);
+        load_pp(t, iq, cd);
+        id = make_int2(ip, iq);
+        ++nprim;
+        const double q = cd.p, X = ab.Px - cd.Px, Y = ab.Py - cd.Py, Z = ab.Pz - cd.Pz;
+        const double sum = ab.p + q, rs = rsqrt(sum);
+        const double ipq = 4.0 * ab.i2p * cd.i2p;
+        const double alpha = (ab.p * q) * (rs * rs);
+        const double T = alpha * (X * X + Y * Y + Z * Z);
+        const double pref = pref0 * rs * ipq;
+        double F[LT + 1];
+        boys<QREF, LT>(g.mode, T, g.boys, F);
 #pragma unroll
-            for (int j = 0; j <= LT; ++j) F[j] *= pref;
-            double R[LT + 1][LT + 1][LT + 1];
-            hermite_R<LT>(F, -2.0 * alpha, X, Y, Z, R);
-            double *dst = smR + (size_t)(w * 32 + lane) * NR;
+        for (int j = 0; j <= LT; ++j) F[j] *= pref;
+        double R[LT + 1][LT + 1][LT + 1];
+        hermite_R<LT>(F, -2.0 * alpha, X, Y, Z, R);
+        double *dst = smR + (size_t)(w * 32 + lane) * NR;
 #pragma unroll
-            for (int x = 0; x <= LT; ++x)
+        for (int x = 0; x <= LT; ++x)
 #pragma unroll
-              for (int y = 0; y <= LT; ++y)
+          for (int y = 0; y <= LT; ++y)
 #pragma unroll
-                for (int z = 0; z <= LT; ++z)
-                  if (x + y + z <= LT) dst[ridx(LT, x, y, z)] = R[x][y][z];
-          }
-        }
-        smF[w * 32 + lane] = ok;
+            for (int z = 0; z <= LT; ++z)
+              if (x + y + z <= LT) dst[ridx(LT, x, y, z)] = R[x][y][z];
+        for (int k = 0; k < NSPLIT && live; ++k) live = next_survivor(t, p1, q0, q1, ip, iq, Kab);
       }
-      __syncthreads();
-      // consumers: every primitive of the round into this warp's outputs
-      for (int j = 0; j < NSPLIT; ++j) {
-        const int qj = jq + j;
-        if (!(pok && qj < nq_l) || !smF[j * 32 + lane]) continue;
-        const double *Rs = smR + (size_t)(j * 32 + lane) * NR;
-        PrimPair<double> cd;
-        load_pp(t, q0 + qj, cd);
-        double fx[2][2][3], fy[2][2][3], fz[2][2][3];
-        pair_E(cd.PAx, cd.PBx, cd.i2p, -1.0, fx);
-        pair_E(cd.PAy, cd.PBy, cd.i2p, -1.0, fy);
-        pair_E(cd.PAz, cd.PBz, cd.i2p, -1.0, fz);
-#pragma unroll
-        for (int c = C0; c < C1; ++c)
-#pragma unroll
-          for (int d = D0; d < D1; ++d) {
-            const double cf = cd.c[2 * fang(c) + fang(d)];
-            double W[LAB + 1][LAB + 1][LAB + 1];
-#pragma unroll
-            for (int x = 0; x <= LAB; ++x)
-#pragma unroll
-              for (int y = 0; y <= LAB; ++y)
-#pragma unroll
-                for (int z = 0; z <= LAB; ++z) {
-                  if (x + y + z > LAB) continue;
-                  double wv = 0.0;
-#pragma unroll
-                  for (int xx = 0; xx <= fl(c, 0) + fl(d, 0); ++xx)
-#pragma unroll
-                    for (int yy = 0; yy <= fl(c, 1) + fl(d, 1); ++yy)
-#pragma unroll
-                      for (int zz = 0; zz <= fl(c, 2) + fl(d, 2); ++zz)
-                        wv += (fx[fl(c, 0)][fl(d, 0)][xx] * fy[fl(c, 1)][fl(d, 1)][yy] * fz[fl(c, 2)][fl(d, 2)][zz]) *
-                              Rs[ridx(LT, x + xx, y + yy, z + zz)];
-                  W[x][y][z] = wv * cf;
-                }
-#pragma unroll
-            for (int a = 0; a < NA; ++a)
-#pragma unroll
-              for (int b = 0; b < NB; ++b) {
-                double v = 0.0;
-#pragma unroll
-                for (int x = 0; x <= fl(a, 0) + fl(b, 0); ++x)
-#pragma unroll
-                  for (int y = 0; y <= fl(a, 1) + fl(b, 1); ++y)
-#pragma unroll
-                    for (int z = 0; z <= fl(a, 2) + fl(b, 2); ++z)
-                      v += ex[fl(a, 0)][fl(b, 0)][x] * ey[fl(a, 1)][fl(b, 1)][y] * ez[fl(a, 2)][fl(b, 2)][z] *
-                           W[x][y][z];
-                acc[a][b][c - C0][d - D0] += v * ab.c[2 * fang(a) + fang(b)];
-              }
-          }
-      }
-      __syncthreads();
+      smI[w * 32 + lane] = id;
     }
+    __syncthreads();
+    // consumers: every survivor of the round into this warp's outputs
+    for (int j = 0; j < NSPLIT; ++j) {
+      const int2 id = smI[j * 32 + lane];
+      if (id.x < 0) continue;
+      if (id.x != cur_ip) {
+        PrimPair<double> ab;
+        load_pp(t, id.x, ab);
+        pair_E(ab.PAx, ab.PBx, ab.i2p, 1.0, ex);
+        pair_E(ab.PAy, ab.PBy, ab.i2p, 1.0, ey);
+        pair_E(ab.PAz, ab.PBz, ab.i2p, 1.0, ez);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) cab[k] = ab.c[k];
+        cur_ip = id.x;
+      }
+      const double *Rs = smR + (size_t)(j * 32 + lane) * NR;
+      PrimPair<double> cd;
+      load_pp(t, id.y, cd);
+      double fx[2][2][3], fy[2][2][3], fz[2][2][3];
+      pair_E(cd.PAx, cd.PBx, cd.i2p, -1.0, fx);
+      pair_E(cd.PAy, cd.PBy, cd.i2p, -1.0, fy);
+      pair_E(cd.PAz, cd.PBz, cd.i2p, -1.0, fz);
+#pragma unroll
+      for (int c = C0; c < C1; ++c)
+#pragma unroll
+        for (int d = D0; d < D1; ++d) {
+          const double cf = cd.c[2 * fang(c) + fang(d)];
+          double W[LAB + 1][LAB + 1][LAB + 1];
+#pragma unroll
+          for (int x = 0; x <= LAB; ++x)
+#pragma unroll
+            for (int y = 0; y <= LAB; ++y)
+#pragma unroll
+              for (int z = 0; z <= LAB; ++z) {
+                if (x + y + z > LAB) continue;
+                double wv = 0.0;
+#pragma unroll
+                for (int xx = 0; xx <= fl(c, 0) + fl(d, 0); ++xx)
+#pragma unroll
+                  for (int yy = 0; yy <= fl(c, 1) + fl(d, 1); ++yy)
+#pragma unroll
+                    for (int zz = 0; zz <= fl(c, 2) + fl(d, 2); ++zz)
+                      wv += (fx[fl(c, 0)][fl(d, 0)][xx] * fy[fl(c, 1)][fl(d, 1)][yy] * fz[fl(c, 2)][fl(d, 2)][zz]) *
+                            Rs[ridx(LT, x + xx, y + yy, z + zz)];
+                W[x][y][z] = wv * cf;
+              }
+#pragma unroll
+          for (int a = 0; a < NA; ++a)
+#pragma unroll
+            for (int b = 0; b < NB; ++b) {
+              double v = 0.0;
+#pragma unroll
+              for (int x = 0; x <= fl(a, 0) + fl(b, 0); ++x)
+#pragma unroll
+                for (int y = 0; y <= fl(a, 1) + fl(b, 1); ++y)
+#pragma unroll
+                  for (int z = 0; z <= fl(a, 2) + fl(b, 2); ++z)
+                    v += ex[fl(a, 0)][fl(b, 0)][x] * ey[fl(a, 1)][fl(b, 1)][y] * ez[fl(a, 2)][fl(b, 2)][z] *
+                         W[x][y][z];
+              acc[a][b][c - C0][d - D0] += v * cab[2 * fang(a) + fang(b)];
+            }
+        }
+    }
+    __syncthreads();
   }
   if (g.counters) {  // quartets by warp 0, the primitive quartets each warp formed
     const unsigned np_w = __reduce_add_sync(0xffffffffu, nprim);
@@ -693,31 +753,31 @@ __global__ void __launch_bounds__(512) eri_store_shared_kernel(EriArgs g) {
   constexpr int NOUT = nfun(LA) * nfun(LB) * nfun(LC) * nfun(LD);
   constexpr int NSPLIT = NOUT <= 64 ? 4 : 16;
   constexpr int NR = nherm(LA + LB + LC + LD);
-  extern __shared__ double sm_shared[];  // R of the round's primitives [NSPLIT][32][NR], then their flags
+  extern __shared__ double sm_shared[];  // R of the round's survivors [NSPLIT][32][NR], then their (bra, ket) pairs
   double *smR = sm_shared;
-  unsigned char *smF = reinterpret_cast<unsigned char *>(sm_shared + NSPLIT * 32 * NR);
+  int2 *smI = reinterpret_cast<int2 *>(sm_shared + NSPLIT * 32 * NR);
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const long long q = (long long)blockIdx.x * 32 + lane;
+  long long q = (long long)blockIdx.x * 32 + lane;
   int P = 0, Q = 0, m = 0;
   const bool valid = decode(g, q, P, Q, m);
   double *out = valid ? g.store + q * NOUT : nullptr;
   if constexpr (NSPLIT == 4) {
     switch (w) {
-      case 0: quartet_store_shared<LA, LB, LC, LD, 4, 0, 1, 0, 1>(g, valid, P, Q, out, smR, smF); break;
-      case 1: quartet_store_shared<LA, LB, LC, LD, 4, 1, 2, 0, 1>(g, valid, P, Q, out, smR, smF); break;
-      case 2: quartet_store_shared<LA, LB, LC, LD, 4, 2, 3, 0, 1>(g, valid, P, Q, out, smR, smF); break;
-      default: quartet_store_shared<LA, LB, LC, LD, 4, 3, 4, 0, 1>(g, valid, P, Q, out, smR, smF); break;
+      case 0: quartet_store_shared<LA, LB, LC, LD, 4, 0, 1, 0, 1>(g, valid, P, Q, out, smR, smI); break;
+      case 1: quartet_store_shared<LA, LB, LC, LD, 4, 1, 2, 0, 1>(g, valid, P, Q, out, smR, smI); break;
+      case 2: quartet_store_shared<LA, LB, LC, LD, 4, 2, 3, 0, 1>(g, valid, P, Q, out, smR, smI); break;
+      default: quartet_store_shared<LA, LB, LC, LD, 4, 3, 4, 0, 1>(g, valid, P, Q, out, smR, smI); break;
     }
   } else {
 #define MQ_SH16(s)                                                                                             \
   case s:                                                                                                      \
     quartet_store_shared<LA, LB, LC, LD, 16, (s) / 4, (s) / 4 + 1, (s) % 4, (s) % 4 + 1>(g, valid, P, Q, out, smR, \
-                                                                                       smF);                   \
+                                                                                       smI);                   \
     break;
     switch (w) {
       MQ_SH16(0) MQ_SH16(1) MQ_SH16(2) MQ_SH16(3) MQ_SH16(4) MQ_SH16(5) MQ_SH16(6) MQ_SH16(7) MQ_SH16(8)
       MQ_SH16(9) MQ_SH16(10) MQ_SH16(11) MQ_SH16(12) MQ_SH16(13) MQ_SH16(14)
-      default: quartet_store_shared<LA, LB, LC, LD, 16, 3, 4, 3, 4>(g, valid, P, Q, out, smR, smF); break;
+      default: quartet_store_shared<LA, LB, LC, LD, 16, 3, 4, 3, 4>(g, valid, P, Q, out, smR, smI); break;
     }
 #undef MQ_SH16
   }
@@ -733,14 +793,14 @@ __device__ __forceinline__ void schwarz_diag(const EriArgs &g, int P, size_t n, 
 }
 
 template <int LA, int LB, int LC, int LD, int EPI, class RT = double>
-__global__ void __launch_bounds__(128) eri_kernel(EriArgs g) {
+__global__ void __launch_bounds__(256) eri_kernel(EriArgs g) {
   constexpr int NA = nfun(LA), NB = nfun(LB);
   constexpr int NOUT = NA * NB * nfun(LC) * nfun(LD);
   if constexpr (EPI == EPI_SCHWARZ) {  // diagonal classes only (LC = LA, LD = LB)
     constexpr int NDIAG = NA * NB;
     const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int split = (int)(warp % NDIAG);
-    const long long q = (warp / NDIAG) * 32 + (threadIdx.x & 31);
+    long long q = (warp / NDIAG) * 32 + (threadIdx.x & 31);
     int P, Q, m;
     if (!decode(g, q, P, Q, m)) return;
     const size_t n = (size_t)g.n;
@@ -759,7 +819,7 @@ __global__ void __launch_bounds__(128) eri_kernel(EriArgs g) {
   const long long warp = gtid >> 5;
   const int lane = threadIdx.x & 31;
   const int split = (int)(warp % NSPLIT);
-  const long long q = (warp / NSPLIT) * 32 + lane;
+  long long q = (warp / NSPLIT) * 32 + lane;
   int P, Q, m;
   if (!decode(g, q, P, Q, m)) return;
   size_t n = (size_t)g.n;
@@ -796,13 +856,19 @@ static inline int nsplit_of(int cP, int cQ) {
   return nout <= 16 ? 1 : (nout <= 64 ? 4 : 16);
 }
 
+// The launch order of an integral launch sorted by surviving primitive
+// quartets (eri_store.cu): h.list / h.list_n are set.
+int bin_quartets(mq_ctx *c, EriArgs &h, int slot);
+
+// One class combination's integral launch; `block` is the CTA size of the
+// thread-per-quartet kernel (64, 128 or 256; the autotuner's choice)
 template <int EPI, class RT = double>
-static int launch_class(mq_ctx *c, EriArgs g, int cP, int cQ) {
+static int launch_class(mq_ctx *c, EriArgs g, int cP, int cQ, int block = 128) {
   // Schwarz: one warp slot per diagonal function pair (ab|ab) of the class
   const int nsplit = EPI == EPI_SCHWARZ ? (cP == 0 ? 1 : cP == 1 ? 4 : 16) : nsplit_of(cP, cQ);
   const long long warps = (g.nq + 31) / 32 * nsplit;
   const long long threads = warps * 32;
-  const int block = 128;
+  if (block != 64 && block != 128 && block != 256) return set_err(c, MQ_EINVAL, "integral launch: bad CTA size");
   const long long grid = (threads + block - 1) / block;
   if (grid == 0) return MQ_OK;
   if (grid > 2147483647LL) return set_err(c, MQ_EINVAL, "integral launch too large");
@@ -812,12 +878,12 @@ static int launch_class(mq_ctx *c, EriArgs g, int cP, int cQ) {
       const long long ctas = (g.nq + 31) / 32;
       if (ctas > 2147483647LL) return set_err(c, MQ_EINVAL, "integral launch too large");
       if (cP == 2 && cQ == 1) {
-        const size_t sm = sizeof(double) * 4 * 32 * nherm(3) + 4 * 32;
+        const size_t sm = sizeof(double) * 4 * 32 * nherm(3) + sizeof(int2) * 4 * 32;
         MQ_CUDA(c, cudaFuncSetAttribute(eri_store_shared_kernel<1, 1, 1, 0>,
                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
         eri_store_shared_kernel<1, 1, 1, 0><<<(unsigned)ctas, 128, sm, c->stream>>>(g);
       } else {
-        const size_t sm = sizeof(double) * 16 * 32 * nherm(4) + 16 * 32;
+        const size_t sm = sizeof(double) * 16 * 32 * nherm(4) + sizeof(int2) * 16 * 32;
         MQ_CUDA(c, cudaFuncSetAttribute(eri_store_shared_kernel<1, 1, 1, 1>,
                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
         eri_store_shared_kernel<1, 1, 1, 1><<<(unsigned)ctas, 512, sm, c->stream>>>(g);

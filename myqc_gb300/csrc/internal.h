@@ -184,6 +184,17 @@ struct StageTimer {
 
 }  // namespace mq
 
+namespace mq {
+// The integral autotuner's choice for one launch signature (eri_store.cu):
+// launch order binned by surviving primitive quartets or not, CTA size, and
+// the time the candidate took when it was measured
+struct EriTune {
+  int binned = 1;
+  int block = 128;
+  float ms = 0.f;
+};
+}  // namespace mq
+
 struct mq_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;  // the context's stream (highest priority)
@@ -249,6 +260,12 @@ struct mq_ctx {
   // the quartet-store rows whose bra pair index is part mod nparts
   int part = 0, nparts = 1;
   mq::QStore qs;
+  // integral autotuner (eri_store.cu): 1 tune launches of a new signature on
+  // first use, 0 the defaults; choices per (epilogue, class combination,
+  // size class) and the measured candidates, in the order tuned
+  int eri_tune_mode = 1;
+  std::map<unsigned long long, mq::EriTune> eri_tune;
+  std::vector<std::pair<unsigned long long, std::vector<mq::EriTune>>> eri_tune_log;
   std::vector<int> hp_shA, hp_shB, hp_aoA, hp_aoB;  // host copy of the pair table's shells and AO offsets
   int hp_class_off[4] = {0, 0, 0, 0};
   unsigned long long *d_eri_counters = nullptr;  // its quartet counters (device)  // the digestion kernel alone, collected at the caller's sync points
@@ -348,6 +365,7 @@ void tight_boys_device_table(std::vector<double> &tab);  // the table, its grid,
 int eri_full_device(mq_ctx *c, double *d_XX);
 // integral blocks of every combination of the quartet store (tables built)
 int eri_store_quartets(mq_ctx *c);
+std::string eri_tune_report(const mq_ctx *c);  // the autotuner's choices and timings, one line per signature
 // qstore.cu: rank the pairs, build the staircase and digestion tables, compute
 // the integral blocks; RHF G from the store; the n^4 array filled from it
 int qstore_build(mq_ctx *c);

@@ -193,6 +193,17 @@ class Context:
         screened shell quartet once; needs a Schwarz threshold > 0)."""
         self._check(self.L.mq_set_eri_storage(self.h, int(storage)))
 
+    def set_eri_tuning(self, mode: int):
+        """1 (default): the integral autotuner times the candidate launch shapes
+        of each new launch signature once and keeps the fastest; 0: defaults."""
+        self._check(self.L.mq_set_eri_tuning(self.h, int(mode)))
+
+    def eri_tuning_report(self) -> str:
+        """The autotuner's choices and candidate timings, one line per signature."""
+        buf = ctypes.create_string_buffer(1 << 16)
+        self._check(self.L.mq_eri_tuning_report(self.h, buf, 1 << 16))
+        return buf.value.decode()
+
     def set_partition(self, part: int, nparts: int):
         """Keep only this process's share (part of nparts) of the molecule's
         shell quartets in RHF Fock builds from the quartet store or direct;

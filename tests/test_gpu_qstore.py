@@ -171,3 +171,32 @@ def test_transform_slices_from_the_store(qctx, basis_text):
     qctx.fock(_density(n, 7), _density(n, 8))  # a UHF build fills the n^4 array from the store
     m_full = qctx.mp2_rhf(r.eig, sysm.nelcA, PREC_SPLIT_BF16X3, C=r.C)
     assert m_store["E_MP2"] == m_full["E_MP2"]
+
+
+def test_autotuned_integral_launches(qctx, ftab, basis_text):
+    """The integral autotuner on (H2O)16 (launches large enough to be tuned):
+    every candidate launch shape writes the same integrals, so the store --
+    and the Fock matrix digested from it -- is bit-identical whether the pass
+    ran with the defaults, while tuning, or with the tuned choices; the
+    report lists each tuned signature with its chosen candidate.  The survivor
+    counts (primitive quartets) match between the passes."""
+    sysm, basis = _system("water16", basis_text)
+    qctx.set_system(sysm, basis, ftab, MODE_REFERENCE)
+    qctx.set_schwarz(1e-12)
+    qctx.set_eri_storage(STORE_QUARTETS)
+    D = _density(qctx.n, 7)
+    qctx.set_eri_tuning(0)
+    qctx.eri_store()
+    G0 = qctx.fock(D)
+    prims0 = qctx.stat("prim_quartets")
+    qctx.set_eri_tuning(1)
+    qctx.eri_store()  # tunes: each candidate runs once
+    G1 = qctx.fock(D)
+    rep = qctx.eri_tuning_report()
+    qctx.eri_store()  # the tuned choices
+    G2 = qctx.fock(D)
+    assert np.array_equal(G0, G1) and np.array_equal(G0, G2)
+    assert qctx.stat("prim_quartets") == prims0
+    lines = [ln for ln in rep.splitlines() if ln.strip()]
+    assert lines and all("*" in ln for ln in lines), rep
+    assert any("binned" in ln and "plain" in ln for ln in lines), rep
