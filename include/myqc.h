@@ -166,6 +166,16 @@ int mq_set_fock_precision(mq_ctx *ctx, int precision);
  * tau = 0 (default): full builds only.  MQ_EINVAL outside [0, 1e-2]. */
 int mq_set_fock_incremental(mq_ctx *ctx, double tau);
 
+/* Screened FP64 increments in mq_scf from the quartet store (RHF; no
+ * reference counterpart: the reference rebuilds G from all of XX every
+ * iteration, src/I2G/RHFI2G.f90:80-90).  tau > 0: after the SCF's first build,
+ * each build is G_k = G_(k-1) + G[D_k - D_(k-1)] in FP64, digesting only the
+ * shell quartets whose Schwarz bounds satisfy Q_P Q_Q max|D_k - D_(k-1)| >=
+ * tau -- the integral screen's own criterion applied to the density change,
+ * so late iterations, whose density moves little, digest a small part of the
+ * store.  tau = 0 (default): full builds.  MQ_EINVAL outside [0, 1e-6]. */
+int mq_set_fock_screened_increments(mq_ctx *ctx, double tau);
+
 /* Overlap for the split-precision transform; no reference counterpart.
  * planes = 2 or 3 (MQ_PREC_SPLIT_BF16 / MQ_PREC_SPLIT_BF16X3): an mq_scf that
  * ends with an eigensolve of the purified Fock matrix (opts.purify) cuts the

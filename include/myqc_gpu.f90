@@ -67,6 +67,9 @@ MODULE myqc_gpu
     INTEGER(c_int) FUNCTION mq_set_eri_storage(ctx, storage) BIND(C)
       IMPORT; TYPE(c_ptr), VALUE :: ctx; INTEGER(c_int), VALUE :: storage   ! MQ_STORE_FULL / MQ_STORE_QUARTETS
     END FUNCTION
+    INTEGER(c_int) FUNCTION mq_set_fock_screened_increments(ctx, tau) BIND(C)
+      IMPORT; TYPE(c_ptr), VALUE :: ctx; REAL(c_double), VALUE :: tau
+    END FUNCTION
     INTEGER(c_int) FUNCTION mq_set_eri_tuning(ctx, mode) BIND(C)
       IMPORT; TYPE(c_ptr), VALUE :: ctx; INTEGER(c_int), VALUE :: mode
     END FUNCTION

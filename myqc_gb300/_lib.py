@@ -74,6 +74,7 @@ def lib(path: str | None = None):
     L.mq_set_eri_mixed.argtypes = [vp, c_double]
     L.mq_set_eri_storage.argtypes = [vp, c_int]
     L.mq_set_eri_tuning.argtypes = [vp, c_int]
+    L.mq_set_fock_screened_increments.argtypes = [vp, ctypes.c_double]
     L.mq_eri_tuning_report.argtypes = [vp, ctypes.c_char_p, c_int]
     L.mq_set_partition.argtypes = [vp, c_int, c_int]
     L.mq_probe_fp64.argtypes = [vp, ctypes.POINTER(ctypes.c_double)]

@@ -647,6 +647,13 @@ int mq_set_fock_incremental(mq_ctx *c, double tau) {
   return MQ_OK;
 }
 
+int mq_set_fock_screened_increments(mq_ctx *c, double tau) {
+  if (!c) return MQ_EINVAL;
+  if (!(tau >= 0.0) || tau > 1e-6) return set_err(c, MQ_EINVAL, "screened-increment threshold must be in [0, 1e-6]");
+  c->fock_inc_screen = tau;
+  return MQ_OK;
+}
+
 int mq_batch_clear(mq_ctx *c) {
   if (!c) return MQ_EINVAL;
   return batch_clear(c);
@@ -756,6 +763,9 @@ int mq_stat(const mq_ctx *c, const char *key, double *value) {
   else if (!strcmp(key, "eig_jacobi_sweeps")) *value = s.eig_jacobi_sweeps;
   else if (!strcmp(key, "fock_precision")) *value = c->fock_df32;
   else if (!strcmp(key, "fock_inc_builds")) *value = s.fock_inc_builds;
+  else if (!strcmp(key, "fock_screened_builds")) *value = s.fock_screened_builds;
+  else if (!strcmp(key, "fock_full_builds")) *value = s.fock_full_builds;
+  else if (!strcmp(key, "fock_full")) *value = s.ms_fock_full;
   else if (!strcmp(key, "eig_early")) *value = s.eig_early;
   else if (!strcmp(key, "fock_kernel")) *value = s.ms_fock_kernel;
   else if (!strcmp(key, "fock_kernel_launches")) *value = s.fock_kernel_launches;

@@ -145,6 +145,9 @@ struct Stats {
   double eig_f32_sweeps = 0, eig_f32_off = 0, ms_eig_f32 = 0, ms_eig_refine = 0, ms_eig_jacobi = 0;
   double eig_jacobi_sweeps = 0;
   double fock_inc_builds = 0;  // FP32 incremental builds of the last SCF
+  double fock_screened_builds = 0;  // screened FP64 increments from the quartet store, last SCF
+  double fock_full_builds = 0;      // stored full builds of the last SCF, and their time (ms)
+  double ms_fock_full = 0;
   double eig_early = 0;        // 1: the last SCF's final eigensolve started from its early eigensolve
 };
 
@@ -275,6 +278,10 @@ struct mq_ctx {
   // mq_scf with stored integrals: once max|D_k - D_{k-1}| < fock_inc_tau, G_k =
   // G_{k-1} + G[D_k - D_{k-1}] digested in FP32 (0: every build full; mq_set_fock_incremental)
   double fock_inc_tau = 0.0;
+  // mq_scf from the quartet store (RHF): after the first build, G_k = G_{k-1} +
+  // G[D_k - D_{k-1}] in FP64 over the quartets with Q_P Q_Q max|dD| >= this
+  // (0: full builds; mq_set_fock_screened_increments)
+  double fock_inc_screen = 0.0;
   size_t XX_elems = 0;
   double *d_iajb = nullptr;  // last (ia|jb) block
   size_t iajb_elems = 0;
@@ -369,7 +376,10 @@ std::string eri_tune_report(const mq_ctx *c);  // the autotuner's choices and ti
 // qstore.cu: rank the pairs, build the staircase and digestion tables, compute
 // the integral blocks; RHF G from the store; the n^4 array filled from it
 int qstore_build(mq_ctx *c);
-int qstore_fock_rhf(mq_ctx *c, const double *d_D, double *d_G);
+// G = d_Gprev + G[d_D] (d_Gprev null: G[d_D]); kscreen > 0 skips the shell
+// quartets with Schwarz bounds Q_P Q_Q < kscreen (screened increments)
+int qstore_fock_rhf(mq_ctx *c, const double *d_D, double *d_G, const double *d_Gprev = nullptr,
+                    double kscreen = 0.0);
 int qstore_expand(mq_ctx *c, double *d_XX);
 // direct RHF G (no integrals kept between builds): the store's integral blocks
 // recomputed, then digested like a stored build (atomic-free, deterministic)

@@ -94,6 +94,11 @@ struct QsArgs {
   double *Jrow;   // [pair][16]
   double *Jcol;   // [pair][16]
   double *Jh, *Kh;
+  // screened increments: the kets (and, in the column pass, the bras) of a
+  // quartet with sch[P] sch[Q] < kscreen are skipped (0: none); the store's
+  // ranks ascend as the bounds fall, so each walk stops at the first one
+  const double *sch;
+  double kscreen;
 };
 
 // canonical-element weight of (i,j,k,l) in a degenerate block (0: not
@@ -168,10 +173,12 @@ __device__ __forceinline__ void row_role(const QsArgs &g, int r, int P, int A, i
   const double *Xc = g.X + g.base[K] + (size_t)g.off[K][r] * NOUT;
   const size_t n = g.n;
   const double *D = g.D;
+  const double kq = g.kscreen > 0.0 ? g.kscreen / g.sch[P] : 0.0;  // smallest ket bound kept
 #pragma unroll 1
   for (int e = lo + k; e < hi; e += S) {
     const int4 q = g.lst[e];  // rank, pair, shells C | D << 16, AOs k0 | l0 << 16
     if (q.x >= lenr) break;   // ranks ascend: the rest lie beyond the staircase
+    if (kq > 0.0 && g.sch[q.y] < kq) break;  // and their bounds fall: the rest are screened out too
     const int Q = q.y, C = q.z & 0xffff, Dsh = q.z >> 16, k0 = q.w & 0xffff, l0 = q.w >> 16;
     const double *Xb = Xc + (size_t)q.x * NOUT;
     if ((A == B) || (C == Dsh) || (P == Q))
@@ -279,9 +286,11 @@ __device__ __forceinline__ void col_combo(const QsArgs &g, int s, int Q, int C, 
   const int r0 = CP == CQ ? s : 0, r1 = g.rcol[K][s];
   const size_t n = g.n;
   const double *D = g.D;
+  const double kp = g.kscreen > 0.0 ? g.kscreen / g.sch[Q] : 0.0;  // smallest bra bound kept
   for (int r = r0 + (int)threadIdx.x; r < r1; r += blockDim.x) {
     const int4 pi = g.rinfo[g.cls_off[CP] + r];  // pair, A | B << 16, i0 | j0 << 16
     const int P = pi.x, A = pi.y & 0xffff, B = pi.y >> 16, i0 = pi.z & 0xffff, j0 = pi.z >> 16;
+    if (kp > 0.0 && g.sch[P] < kp) break;  // bra ranks ascend as their bounds fall
     if (s >= g.len[K][r]) continue;  // a row another partition holds
     const double *Xb = g.X + g.base[K] + ((size_t)g.off[K][r] + s) * NOUT;
     const bool degen = (A == B) || (C == Dsh) || (P == Q);
@@ -374,13 +383,14 @@ __global__ void qs_jhat_kernel(QsArgs g) {
     }
 }
 
-// G = (Jh + Jh^T)/2 - f (Kh + Kh^T)/2
+// G = Gprev + (Jh + Jh^T)/2 - f (Kh + Kh^T)/2   (Gprev null: zero)
 __global__ void qs_combine_kernel(const double *__restrict__ Jh, const double *__restrict__ Kh, int n, double f,
-                                  double *__restrict__ G) {
+                                  const double *__restrict__ Gprev, double *__restrict__ G) {
   const size_t N = n, idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= N * N) return;
   const size_t t = (idx % N) * N + idx / N;
-  G[idx] = 0.5 * (Jh[idx] + Jh[t]) - f * 0.5 * (Kh[idx] + Kh[t]);
+  const double g = 0.5 * (Jh[idx] + Jh[t]) - f * 0.5 * (Kh[idx] + Kh[t]);
+  G[idx] = Gprev ? Gprev[idx] + g : g;
 }
 
 // The store's blocks written into the full n^4 array, each canonical element
@@ -726,7 +736,7 @@ static QsArgs qs_args(mq_ctx *c) {
   return g;
 }
 
-int qstore_fock_rhf(mq_ctx *c, const double *d_D, double *d_G) {
+int qstore_fock_rhf(mq_ctx *c, const double *d_D, double *d_G, const double *d_Gprev, double kscreen) {
   const QStore &qs = c->qs;
   if (!qs.valid) return set_err(c, MQ_ESTATE, "no quartet store");
   const int n = c->nao, np = c->pt.npairs;
@@ -737,6 +747,8 @@ int qstore_fock_rhf(mq_ctx *c, const double *d_D, double *d_G) {
   if (!w) return MQ_ENOMEM;
   QsArgs g = qs_args(c);
   g.D = d_D;
+  g.sch = c->pt.schwarz;
+  g.kscreen = kscreen;
   g.Kpart = w;
   g.Jrow = w + SH * np * 8 * N;
   g.Jcol = g.Jrow + SH * np * 16;
@@ -758,7 +770,7 @@ int qstore_fock_rhf(mq_ctx *c, const double *d_D, double *d_G) {
   if (qs.ncls[2]) qs_col_kernel<2><<<qs.ncls[2], QS_COL_THREADS, 0, c->stream>>>(g);
   qs_khat_kernel<<<dim3(c->nshell, (4 * n + QS_COL_THREADS - 1) / QS_COL_THREADS), QS_COL_THREADS, 0, c->stream>>>(g);
   qs_jhat_kernel<<<(np + 127) / 128, 128, 0, c->stream>>>(g);
-  qs_combine_kernel<<<(unsigned)((n2 + 255) / 256), 256, 0, c->stream>>>(g.Jh, g.Kh, n, 0.5, d_G);
+  qs_combine_kernel<<<(unsigned)((n2 + 255) / 256), 256, 0, c->stream>>>(g.Jh, g.Kh, n, 0.5, d_Gprev, d_G);
   c->stats.launches += 9;
   MQ_CUDA(c, cudaGetLastError());
   return sync_check(c, "qstore_fock");

@@ -26,6 +26,11 @@ namespace mq {
 
 static inline bool cuda_ok(cudaError_t e) { return e == cudaSuccess; }
 
+__global__ void sub_kernel(const double *a, const double *b, double *c, size_t n) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) c[i] = a[i] - b[i];
+}
+
 __global__ void add_kernel(const double *a, const double *b, double *c, size_t n) {
   size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) c[i] = a[i] + b[i];
@@ -436,7 +441,7 @@ int scf_device(mq_ctx *c, const double *S, const double *H, const mq_scf_opts *o
   }
 
   const double enuc = nuclear_repulsion(c);
-  StageTimer t_fock, t_diag, t_all;
+  StageTimer t_fock, t_diag, t_all, t_full;  // t_full: the full builds of a screened-increment SCF
   c->t_fock_kernel.collect();
   c->t_fock_kernel.total = 0;
   c->stats.fock_kernel_launches = 0;
@@ -453,6 +458,18 @@ int scf_device(mq_ctx *c, const double *S, const double *H, const mq_scf_opts *o
   // digested in FP32; its error scales with the increment, so the converged
   // energy stays within ~1e-9 Eh of the full builds'
   const bool inc = !o->direct && c->fock_inc_tau > 0.0;
+  // screened FP64 increments from the quartet store (RHF): after the first
+  // build, G_k = G_{k-1} + G[D_k - D_{k-1}] over the shell quartets with
+  // Q_P Q_Q max|D_k - D_{k-1}| >= fock_inc_screen -- the Schwarz screen's
+  // criterion applied to the density change, in FP64 throughout
+  const bool inc_store = !o->direct && !uhf && c->qs.valid && !c->fock_df32 && c->fock_inc_screen > 0.0;
+  double *dInc = nullptr;
+  if (inc_store) {
+    dInc = (double *)buf(c, "scf_dinc", sizeof(double) * n2);
+    if (!dInc) return MQ_ENOMEM;
+  }
+  c->stats.fock_screened_builds = 0;
+  c->stats.fock_full_builds = 0;
   bool have_prev_g = false;
   double last_maxdiff = INFINITY, prev_rms = INFINITY;
   bool early_done = false;
@@ -474,14 +491,27 @@ int scf_device(mq_ctx *c, const double *S, const double *H, const mq_scf_opts *o
       double *J = dT1, *Ka = dT2, *Kb = uhf ? dT3 : nullptr;
       MQ_TRY(fock_direct_device(c, dD, uhf ? dD + n2 : nullptr, J, Ka, Kb));
       MQ_TRY(direct_combine(c, J, Ka, Kb, dG, uhf ? dG + n2 : nullptr));
+    } else if (inc_store && have_prev_g) {
+      c->t_fock_kernel.collect();
+      c->t_fock_kernel.start(c->stream);
+      sub_kernel<<<blocks(n2), 256, 0, c->stream>>>(dD, dDp, dInc, n2);
+      const double kscreen = last_maxdiff > 0.0 ? c->fock_inc_screen / last_maxdiff : INFINITY;
+      MQ_TRY(qstore_fock_rhf(c, dInc, dG, dGp, kscreen));
+      c->t_fock_kernel.stop(c->stream);
+      c->stats.fock_kernel_launches += 1;
+      c->stats.fock_screened_builds += 1;
+      c->stats.launches += 1;
     } else if (inc && have_prev_g && last_maxdiff < c->fock_inc_tau) {
       MQ_TRY(fock_stored_increment(c, dD, uhf ? dD + n2 : nullptr, dDp, uhf ? dDp + n2 : nullptr, dGp,
                                    uhf ? dGp + n2 : nullptr, dG, uhf ? dG + n2 : nullptr));
       c->stats.fock_inc_builds += 1;
     } else {
+      t_full.start(c->stream);
       MQ_TRY(fock_stored_device(c, dD, uhf ? dD + n2 : nullptr, dG, uhf ? dG + n2 : nullptr));
+      t_full.stop(c->stream);
+      c->stats.fock_full_builds += 1;
     }
-    if (inc) {
+    if (inc || inc_store) {
       MQ_CUDA(c, cudaMemcpyAsync(dGp, dG, n2 * ns * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
       MQ_CUDA(c, cudaMemcpyAsync(dDp, dD, n2 * ns * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
       have_prev_g = true;
@@ -547,6 +577,7 @@ int scf_device(mq_ctx *c, const double *S, const double *H, const mq_scf_opts *o
     MQ_CUDA(c, cudaMemcpyAsync(hs, dScal, 10 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     MQ_CUDA(c, cudaStreamSynchronize(c->stream));
     t_fock.collect();
+    t_full.collect();
     t_diag.collect();
     c->t_fock_kernel.collect();
     E = hs[0] + (uhf ? hs[2] : 0.0) + enuc;
@@ -587,6 +618,7 @@ int scf_device(mq_ctx *c, const double *S, const double *H, const mq_scf_opts *o
   t_all.collect();
   c->stats.ms_scf = t_all.total;
   c->stats.ms_fock = t_fock.total;
+  c->stats.ms_fock_full = t_full.total;
   c->stats.ms_fock_kernel = c->t_fock_kernel.total;
   c->stats.ms_diag = t_diag.total;
   c->stats.fock_calls = it;

@@ -193,6 +193,12 @@ class Context:
         screened shell quartet once; needs a Schwarz threshold > 0)."""
         self._check(self.L.mq_set_eri_storage(self.h, int(storage)))
 
+    def set_fock_screened_increments(self, tau: float):
+        """tau > 0: after the first build of an RHF SCF from the quartet store,
+        each build adds G[D_k - D_(k-1)] in FP64 over the shell quartets with
+        Q_P Q_Q max|dD| >= tau; 0 (default): full builds."""
+        self._check(self.L.mq_set_fock_screened_increments(self.h, float(tau)))
+
     def set_eri_tuning(self, mode: int):
         """1 (default): the integral autotuner times the candidate launch shapes
         of each new launch signature once and keeps the fastest; 0: defaults."""

@@ -200,3 +200,33 @@ def test_autotuned_integral_launches(qctx, ftab, basis_text):
     lines = [ln for ln in rep.splitlines() if ln.strip()]
     assert lines and all("*" in ln for ln in lines), rep
     assert any("binned" in ln and "plain" in ln for ln in lines), rep
+
+
+@pytest.mark.parametrize("name", ["water8", "water16"])
+def test_screened_increments(qctx, basis_text, name):
+    """Screened FP64 increments (after the first build, G_k = G_(k-1) +
+    G[D_k - D_(k-1)] over the quartets with Q_P Q_Q max|dD| >= 1e-12) against
+    full builds from the same store: the SCF energy to 1e-10 Eh, the MP2 energy
+    to 1e-10 Eh, the same iteration count within one; every build after the
+    first is an increment."""
+    sysm, basis = _system(name, basis_text)
+    qctx.set_system(sysm, basis, None, MODE_TIGHT)
+    qctx.set_schwarz(1e-12)
+    qctx.set_eri_storage(STORE_QUARTETS)
+    S, H = qctx.int1e()
+    qctx.eri_store()
+    out = {}
+    try:
+        for tau in (0.0, 1e-12):
+            qctx.set_fock_screened_increments(tau)
+            r = qctx.scf(S, H, sysm.nelcA, sysm.nelcB, conv=1e-10, conv_rms=True, diis=8, max_iter=100)
+            m = qctx.mp2_rhf(r.eig, sysm.nelcA, PREC_FP64, C=r.C)
+            out[tau] = (r.energy, m["E_MP2"], r.iterations, qctx.stat("fock_screened_builds"),
+                        qctx.stat("fock_full_builds"))
+    finally:
+        qctx.set_fock_screened_increments(0.0)
+    full, inc = out[0.0], out[1e-12]
+    assert abs(full[0] - inc[0]) < 1e-10, (full, inc)
+    assert abs(full[1] - inc[1]) < 1e-10, (full, inc)
+    assert abs(full[2] - inc[2]) <= 1
+    assert full[3] == 0 and inc[4] == 1 and inc[3] == inc[2] - 1
