@@ -119,7 +119,8 @@ def load_workload(seed: int):
 
 MODEL = os.path.join(ROOT, "myqc_gb300", "data", "guess_mlp.npz")
 SCHWARZ = 1e-12  # contracted quartets with a Schwarz bound below this are skipped (fast arms)
-AO2MO_PREFETCH = 3  # XX cut into 3 BF16 planes beside the SCF's final eigensolve (fast arms)
+AO2MO_PREFETCH = 3  # the transform's first operand cut into 3 BF16 planes on the side stream (fast arms)
+PREFETCH = [AO2MO_PREFETCH]  # --ao2mo-prefetch 0: slice it in the transform itself, after the SCF
 # The FP32-pipe options of the library, measured only in the labelled secondary
 # arm "fp32_options" (never the headline): quartets with a Schwarz bound below
 # ERI_F32_TAU in FP32, the double-float Fock digestion (and purification), and
@@ -176,7 +177,7 @@ def solve(ctx, sysm, basis, arm: str, set_system: bool):
     ctx.set_fock_precision(FOCK_DF32 if f32 else FOCK_FP64)
     ctx.set_fock_incremental(FOCK_INC_TAU if f32 else 0.0)
     ctx.set_fock_screened_increments(FOCK_INC_SCREEN if arm == "fast" else 0.0)
-    ctx.set_ao2mo_prefetch(AO2MO_PREFETCH if fast else 0)
+    ctx.set_ao2mo_prefetch(PREFETCH[0] if fast else 0)
     if set_system:
         ctx.set_system(sysm, basis, None, MODE_TIGHT)
     ctx.set_schwarz(SCHWARZ if fast else 0.0)  # recomputes the bounds of the current system
@@ -232,7 +233,8 @@ def run_ours(args):
     L0 = stat(ctx, "launches")
     acc = {k: 0.0 for k in ("fock", "fock_calls", "fock_kernel", "fock_kernel_launches", "eri", "eri_kernel",
                             "quartets", "quartets_f32", "prim_quartets", "diag", "ao2mo", "mp2", "fock_inc_builds",
-                            "store_unique", "store_bytes", "fock_full", "fock_full_builds", "fock_screened_builds")}
+                            "store_unique", "store_bytes", "fock_full", "fock_full_builds", "fock_screened_builds",
+                            "purify_persistent", "purify_stepwise", "purify_steps", "ao2mo_first")}
     iters = []
     barrier()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -330,7 +332,10 @@ def run_ours(args):
         "rooflines": rooflines,
         "clocks": clk.summary(),
         "breakdown_ms_per_solve": {"eri": per["eri"], "scf_fock": per["fock"], "scf_diag": per["diag"],
-                                   "ao2mo": per["ao2mo"], "mp2_pair_sums": per["mp2"]},
+                                   "ao2mo": per["ao2mo"], "ao2mo_first_quarter": per["ao2mo_first"],
+                                   "mp2_pair_sums": per["mp2"]},
+        "purification_per_solve": {"one_launch": per["purify_persistent"], "stepwise": per["purify_stepwise"],
+                                   "steps": per["purify_steps"]},
         "scf_iterations": {"fast": float(np.mean(iters)), "plain": res_p.iterations,
                            "fast_used_learned_guess": bool(getattr(res, "learned_guess", False))},
         "plain_fp64": {"ms_per_solve": ms_plain, "solves_per_s": 1000.0 / ms_plain,
@@ -741,6 +746,8 @@ def parse_args(argv=None):
     ap.add_argument("--no-secondary", dest="secondary", action="store_false",
                     help="skip the batched and direct-Fock measurements after the headline")
     ap.add_argument("--batch-count", type=int, default=4096)
+    ap.add_argument("--ao2mo-prefetch", type=int, default=AO2MO_PREFETCH, choices=[0, 3],
+                    help="3: slice the transform's first operand beside the SCF iterations; 0: after them")
     ap.add_argument("--eri-tuning", type=int, default=1, choices=[0, 1],
                     help="0: the integral launches with their default shapes (no autotuner runs; for profiler captures)")
     ap.add_argument("--nmol", type=int, default=NMOL, help="water molecules in the cluster")
@@ -761,6 +768,7 @@ def main():
     NMOL, BOX = args.nmol, args.box
     ERI_F32_TAU = args.eri_f32_tau
     FOCK_INC_TAU = args.fock_inc_tau
+    PREFETCH[0] = args.ao2mo_prefetch
     if args.impl == "reference":
         run_reference(args)
     else:

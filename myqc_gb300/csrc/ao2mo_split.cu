@@ -19,7 +19,9 @@
 //
 // The four steps use the integral symmetry (uv|ld) = (dl|uv) = (vu|ld) so that
 // XX itself is the first step's K-major A and each epilogue writes the next
-// step's A with coalesced stores:
+// step's A with coalesced stores (with the quartet store instead of XX, the
+// first step is a sparse FP32 product on the CUDA cores, store_first_quarter
+// below: its operand is mostly screened-out zeros):
 //   1  Y1[b][(l,p)]     = sum_d XX(d,l,u,v) Cb(d,b)       A1 rows (l,p),   K = d
 //   2  Y2[j,b][p]       = sum_l Y1[b][(l,p)] Cj(l,j)       A2 rows p,       K = l
 //   3  Y3[a,j,b][v]     = sum_u Y2[j,b][(u,v)] Ca(u,a)     A3 rows v,       K = u
@@ -332,11 +334,11 @@ __device__ __forceinline__ void load_chunk(const T *__restrict__ x, int k0, int 
 //              l + n (u + n v) of XX (rows of n values), l = r mod n;
 //   ROW_SYMM   row (v, jb) of the pair-packed Y2: element u is
 //              in[jb * npairs + pidx(min(u, v), max(u, v))], pidx(u, v) = u + v (v + 1) / 2.
-//   ROW_STORE  as ROW_PAIRS, each value (d l|u v) looked up in the quartet store
-//              (no n^4 array): the canonical element of its shell quartet, zero
-//              when the quartet was screened out -- the value the full array
-//              filled from the store holds.
-enum { ROW_PLAIN = 0, ROW_PAIRS = 1, ROW_SYMM = 2, ROW_STORE = 3 };
+// (the first step's operand from the quartet store: slice_store_kernel below)
+//   ROW_TRANS  row (b, p) of the [p][l][b] array the store's first quarter
+//              writes: element l at in[(p n + l) nb + b]; the rows are visited
+//              with b fastest, so the warps reading one p share its sectors
+enum { ROW_PLAIN = 0, ROW_PAIRS = 1, ROW_SYMM = 2, ROW_TRANS = 3 };
 struct StoreView {
   const double *X;
   const int4 *pinfo;  // [S1 * nsh + S2]: pair, class, rank, bit 0: stored as (S2, S1), bit 1: S1 = S2
@@ -347,50 +349,71 @@ struct StoreView {
   int nsh;
   const double *pbound;  // Schwarz bound of each pair
   const double *qmax;    // per shell: the largest bound of a pair containing it
+  const int *partners;   // per shell S: the shells D by the bound of the pair (D, S), descending
   double thr;            // the store's threshold
 };
 struct RowSrc {
   const int2 *pairs;  // (u, v) of each pair p, u <= v
   long long n, npairs;
-  StoreView sv;  // ROW_STORE
+  long long nb;  // ROW_TRANS: the columns b of the [p][l][b] source
 };
 
 __host__ __device__ constexpr int sv_nfa(int cls) { return cls >= 1 ? 4 : 1; }
 __host__ __device__ constexpr int sv_nfb(int cls) { return cls == 2 ? 4 : 1; }
 
-// (d l|u v) from the quartet store
-__device__ __forceinline__ double store_value(const StoreView &sv, int d, int l, int u, int v, int n) {
-  const int D = sv.ao_shell[d], Ls = sv.ao_shell[l], U = sv.ao_shell[u], V = sv.ao_shell[v];
-  const int4 e1 = sv.pinfo[D * sv.nsh + Ls], e2 = sv.pinfo[U * sv.nsh + V];
-  // stored orientation: first-shell AO i, second-shell AO j, function indices
-  int i1 = (e1.w & 1) ? l : d, j1 = (e1.w & 1) ? d : l, i2 = (e2.w & 1) ? v : u, j2 = (e2.w & 1) ? u : v;
-  if ((e1.w & 2) && i1 < j1) {  // A = B: the canonical element has i >= j
-    const int t = i1;
-    i1 = j1;
-    j1 = t;
+// The S planes and the exponent of one row whose values a warp holds in
+// registers: lane owns the 8-element chunks lane + 32 h (h < H) of the row.
+template <int S, class T, int H>
+__device__ __forceinline__ void slice_row_regs(T (&v)[H][8], long long r, int nchunk, int Kp, long long plane,
+                                               bf16 *__restrict__ out, int *__restrict__ e) {
+  const int lane = threadIdx.x & 31;
+  int emax = 0;
+#pragma unroll
+  for (int h = 0; h < H; ++h)
+    if (lane + 32 * h < nchunk)
+#pragma unroll
+      for (int j = 0; j < 8; ++j) emax = max(emax, exp_field(v[h][j]));
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o));
+  // |x| < 2^erow with erow = unbiased exponent of the largest element + 1
+  const int erow = emax == 0 ? -200 : emax - (sizeof(T) == 8 ? 1022 : 126);
+  if (lane == 0) e[r] = erow;
+#pragma unroll
+  for (int h = 0; h < H; ++h) {
+    const int c = lane + 32 * h;
+    if (c >= nchunk) continue;
+    unsigned packed[S][4];
+#pragma unroll
+    for (int j = 0; j < 8; j += 2) {
+      float dig[2][S];
+#pragma unroll
+      for (int t = 0; t < 2; ++t) {
+        long long mant;
+        int ex;
+        decompose(v[h][j + t], mant, ex);
+        // q = round(mant * 2^(ex + 8S - 1 - erow)); the shift is negative for every nonzero x
+        const int sh = -(ex + 8 * S - 1 - erow);
+        int q = 0;
+        if (mant != 0 && sh < 62) q = (int)(sh > 0 ? ((mant + (1ll << (sh - 1))) >> sh) : (mant << -sh));
+#pragma unroll
+        for (int d = S - 1; d > 0; --d) {
+          const int hi = (q + 128) >> 8;  // balanced digit: q = hi*256 + lo, lo in [-128, 127]
+          dig[t][d] = (float)(q - hi * 256);
+          q = hi;
+        }
+        dig[t][0] = (float)q;
+      }
+#pragma unroll
+      for (int d = 0; d < S; ++d) {
+        const __nv_bfloat162 b2 = __floats2bfloat162_rn(dig[0][d], dig[1][d]);
+        packed[d][j >> 1] = *reinterpret_cast<const unsigned *>(&b2);
+      }
+    }
+#pragma unroll
+    for (int d = 0; d < S; ++d)
+      *reinterpret_cast<uint4 *>(out + d * plane + r * Kp + 8 * c) =
+          make_uint4(packed[d][0], packed[d][1], packed[d][2], packed[d][3]);
   }
-  if ((e2.w & 2) && i2 < j2) {
-    const int t = i2;
-    i2 = j2;
-    j2 = t;
-  }
-  const bool first_bra = e1.y > e2.y || (e1.y == e2.y && e1.z >= e2.z);
-  const int4 eb = first_bra ? e1 : e2, ek = first_bra ? e2 : e1;
-  int ia = first_bra ? i1 : i2, ja = first_bra ? j1 : j2, ka = first_bra ? i2 : i1, la = first_bra ? j2 : j1;
-  const int K = eb.y * (eb.y + 1) / 2 + ek.y;
-  if (ek.z >= sv.len[K][eb.z]) return 0.0;  // screened out
-  if (eb.x == ek.x && (long long)ia * n + ja < (long long)ka * n + la) {  // P = Q: ij >= kl
-    int t = ia;
-    ia = ka;
-    ka = t;
-    t = ja;
-    ja = la;
-    la = t;
-  }
-  const int NB = sv_nfb(eb.y), NC = sv_nfa(ek.y), ND = sv_nfb(ek.y), NOUT = sv_nfa(eb.y) * NB * NC * ND;
-  const int fa = ia - sv.ao0[sv.ao_shell[ia]], fb = ja - sv.ao0[sv.ao_shell[ja]];
-  const int fc = ka - sv.ao0[sv.ao_shell[ka]], fd = la - sv.ao0[sv.ao_shell[la]];
-  return __ldg(sv.X + sv.base[K] + (sv.off[K][eb.z] + ek.z) * NOUT + ((fa * NB + fb) * NC + fc) * ND + fd);
 }
 
 template <int S, class T, int H, int MODE>
@@ -400,31 +423,25 @@ __global__ void __launch_bounds__(256, 4) slice_rows_kernel(const T *__restrict_
   const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
   const int lane = threadIdx.x & 31;
   const int nchunk = Kp >> 3;
-  for (long long r = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); r < rows; r += warps) {
+  for (long long ri = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); ri < rows; ri += warps) {
+    long long r = ri;
     const T *x = in + r * ld;
     long long jb = 0;
     int vrow = 0;
-    int lrow = 0;
-    int2 uvrow = make_int2(0, 0);
-    if (MODE == ROW_PAIRS) {
+    if (MODE == ROW_TRANS) {
+      const long long p = ri / rs.nb, b = ri - p * rs.nb;
+      r = b * rs.npairs + p;
+      x = in + p * rs.n * rs.nb + b;
+    } else if (MODE == ROW_PAIRS) {
       const long long pidx = r / rs.n;
       const int2 uv = rs.pairs[pidx];
       x = in + ((r - pidx * rs.n) + rs.n * (uv.x + rs.n * (long long)uv.y)) * ld;
-    } else if (MODE == ROW_STORE) {
-      const long long pidx = r / rs.n;
-      uvrow = rs.pairs[pidx];
-      lrow = (int)(r - pidx * rs.n);
-      // no quartet (D L|U V) of the row passes the screen: the row is zero
-      const int U = rs.sv.ao_shell[uvrow.x], V = rs.sv.ao_shell[uvrow.y], Ls = rs.sv.ao_shell[lrow];
-      const double quv = rs.sv.pbound[rs.sv.pinfo[U * rs.sv.nsh + V].x];
-      if (rs.sv.qmax[Ls] * quv < rs.sv.thr) lrow = -1;
     } else if (MODE == ROW_SYMM) {
       jb = r / rs.n;
       vrow = (int)(r - jb * rs.n);
       x = in + jb * rs.npairs;
     }
     T v[H][8];
-    int emax = 0;
 #pragma unroll
     for (int h = 0; h < H; ++h) {
       const int c = lane + 32 * h;
@@ -435,61 +452,311 @@ __global__ void __launch_bounds__(256, 4) slice_rows_kernel(const T *__restrict_
             const int u = 8 * c + j, lo = min(u, vrow), hi = max(u, vrow);
             v[h][j] = u < kvalid ? __ldg(x + lo + (long long)hi * (hi + 1) / 2) : (T)0;
           }
-        } else if (MODE == ROW_STORE) {
+        } else if (MODE == ROW_TRANS) {
 #pragma unroll
-          for (int j = 0; j < 8; ++j) {
-            const int d = 8 * c + j;
-            v[h][j] = d < kvalid && lrow >= 0 ? (T)store_value(rs.sv, d, lrow, uvrow.x, uvrow.y, (int)rs.n) : (T)0;
-          }
+          for (int j = 0; j < 8; ++j) v[h][j] = 8 * c + j < kvalid ? __ldg(x + (8 * c + j) * rs.nb) : (T)0;
         } else {
           load_chunk(x, 8 * c, kvalid, vec != 0, v[h]);
         }
-#pragma unroll
-        for (int j = 0; j < 8; ++j) emax = max(emax, exp_field(v[h][j]));
       }
     }
+    slice_row_regs<S, T, H>(v, r, nchunk, Kp, plane, out, e);
+  }
+}
+
+// ---- Stored blocks of a row group (L; U <= V) of the first step: the rows
+// (l, p = (u <= v)) with l in shell L and (u, v) the AO pairs u <= v of the
+// shells U, V, element (d l|u v) at column d.  Every row of a group reads the
+// same blocks -- (D L|U V) for the shells D whose pair (D, L) passes the
+// screen with (U, V), a prefix of L's partner list (ordered by the bound of
+// (D, L)), cut by the same bound product test as the store's staircase.
+struct LiveBlock {
+  long long off;  // the block in the store
+  int a0;         // first AO of D
+  int flags;      // bit0: (D, L) stored as (L, D); bit1: D = L; bit2: (D, L) is the bra; bit3: (D, L) = (U, V);
+                  // bits 4, 5, 6: 4 functions in the block's second, third, fourth shell; bits 8-11: AOs of D
+};
+
+// the store offset of the element (d l|u v) of a listed block; (i2, f2) and
+// (j2, g2): the AOs of (u, v) and their function indices, in the stored
+// orientation of (U, V)
+__device__ __forceinline__ long long live_offset(const LiveBlock &b, int d, int fd, int l, int fl, int i2, int f2,
+                                                 int j2, int g2, int n) {
+  int i1 = d, fi1 = fd, j1 = l, fj1 = fl;
+  if (b.flags & 1) {
+    i1 = l, fi1 = fl, j1 = d, fj1 = fd;
+  }
+  if ((b.flags & 2) && i1 < j1) {  // A = B: the canonical element has i >= j
+    const int t = i1, ft = fi1;
+    i1 = j1, fi1 = fj1, j1 = t, fj1 = ft;
+  }
+  const bool bra1 = b.flags & 4;
+  int ia = bra1 ? i1 : i2, fa = bra1 ? fi1 : f2, ja = bra1 ? j1 : j2, fb = bra1 ? fj1 : g2;
+  int ka = bra1 ? i2 : i1, fc = bra1 ? f2 : fi1, la = bra1 ? j2 : j1, fdd = bra1 ? g2 : fj1;
+  if ((b.flags & 8) && (long long)ia * n + ja < (long long)ka * n + la) {  // P = Q: ij >= kl
+    int t = fa;
+    fa = fc, fc = t;
+    t = fb;
+    fb = fdd, fdd = t;
+  }
+  const int NB = (b.flags & 16) ? 4 : 1, NC = (b.flags & 32) ? 4 : 1, ND = (b.flags & 64) ? 4 : 1;
+  return b.off + ((fa * NB + fb) * NC + fc) * ND + fdd;
+}
+
+// ---- The first quarter transform straight from the quartet store.
+// Y1[p][l][b] = sum_d (d l|u v) C(d, b) for the AO pairs p = (u <= v): b
+// fastest, so that each row's columns are one coalesced store (the second
+// step's slicing reads it transposed, ROW_TRANS).
+// Over (l, p) x d the operand (d l|u v) is mostly zeros -- shell quartets that
+// fail the Schwarz screen -- so instead of cutting it into BF16 planes for a
+// dense tensor-core product, each warp takes one row group (L; U <= V), lists
+// the stored blocks (D L|U V) and their AOs d once, and works through the
+// group's rows (u, v, l) in passes of up to FQ_ROWS: it gathers the stored
+// elements (d l|u v) of the pass into shared memory (FP32, each by one lane)
+// and forms the products with C in FP32 on the CUDA cores -- lane k owns the
+// columns b = k + 32 j, and each gathered element is one shared-memory
+// broadcast for KB multiply-adds per lane.  Every lane is busy whatever the
+// row count, and only stored elements are visited.
+constexpr int FQ_ROWS = 8;
+constexpr int FQ_KCHUNK = 64;  // listed AOs gathered at a time
+constexpr int FQ_LCH = 16;      // shells L per group
+constexpr int FQ_GATHER = 2;    // gathered elements in flight per lane
+
+// row f of a group: AO pair (u, v) number f / nl of the shells U <= V (u <= v),
+// l = l0 + f % nl
+__device__ __forceinline__ void fq_row(int f, int nl, int u0, int nu, int v0, int nv, bool same, int &u, int &v,
+                                       int &l) {
+  const int pi = f / nl;
+  l = f - pi * nl;
+  if (!same) {
+    u = u0 + pi / nv;
+    v = v0 + pi % nv;
+  } else {  // pairs u <= v within one shell, v outer
+    int vv = 0;
+    while ((vv + 1) * (vv + 2) / 2 <= pi) ++vv;
+    u = u0 + (pi - vv * (vv + 1) / 2);
+    v = v0 + vv;
+  }
+}
+
+// rows f0 .. f0 + nr - 1 of the group (nr <= R; the others of the pass are zeros, not written).
+// Not inlined: the three pass widths would otherwise triple the kernel's code,
+// and its instruction fetches were a leading stall.
+template <int KB, int R>
+__device__ __noinline__ void fq_pass(const StoreView &sv, int n, int Kp, const float *Cf, int nvb,
+                                        float *__restrict__ Y1, long long np, const int *dl, const LiveBlock *tab,
+                                        int nd, float *Vs, int f0, int nr, int nl, int l0, int u0, int nu, int v0,
+                                        int nv, bool same, int4 e2) {
+  const int lane = threadIdx.x & 31;
+  float acc[R][KB];
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o));
-    // |x| < 2^erow with erow = unbiased exponent of the largest element + 1
-    const int erow = emax == 0 ? -200 : emax - (sizeof(T) == 8 ? 1022 : 126);
-    if (lane == 0) e[r] = erow;
+  for (int rr = 0; rr < R; ++rr)
 #pragma unroll
-    for (int h = 0; h < H; ++h) {
-      const int c = lane + 32 * h;
-      if (c >= nchunk) continue;
-      unsigned packed[S][4];
+    for (int j = 0; j < KB; ++j) acc[rr][j] = 0.f;
+  // the listed AOs in chunks of FQ_KCHUNK: gather the chunk's elements, then
+  // its products
+  for (int kc = 0; kc < nd; kc += FQ_KCHUNK) {
+    const int kn = min(FQ_KCHUNK, nd - kc);
+    // gather: element (k, rr) by lane (k * R + rr) mod 32; FQ_GATHER
+    // elements per lane at a time -- their offsets first, then every load in
+    // flight together, then the shared-memory stores
+    for (int base = 0; base < kn * R; base += 32 * FQ_GATHER) {
+      long long off[FQ_GATHER];
 #pragma unroll
-      for (int j = 0; j < 8; j += 2) {
-        float dig[2][S];
-#pragma unroll
-        for (int t = 0; t < 2; ++t) {
-          long long mant;
-          int ex;
-          decompose(v[h][j + t], mant, ex);
-          // q = round(mant * 2^(ex + 8S - 1 - erow)); the shift is negative for every nonzero x
-          const int sh = -(ex + 8 * S - 1 - erow);
-          int q = 0;
-          if (mant != 0 && sh < 62) q = (int)(sh > 0 ? ((mant + (1ll << (sh - 1))) >> sh) : (mant << -sh));
-#pragma unroll
-          for (int d = S - 1; d > 0; --d) {
-            const int hi = (q + 128) >> 8;  // balanced digit: q = hi*256 + lo, lo in [-128, 127]
-            dig[t][d] = (float)(q - hi * 256);
-            q = hi;
-          }
-          dig[t][0] = (float)q;
+      for (int t = 0; t < FQ_GATHER; ++t) {
+        off[t] = -1;
+        const int idx = base + lane + 32 * t;
+        if (idx >= kn * R) continue;
+        const int k = idx / R, rr = idx - k * R;
+        if (rr >= nr) continue;
+        int u, v, l;
+        fq_row(f0 + rr, nl, u0, nu, v0, nv, same, u, v, l);
+        int i2 = u, f2 = u - u0, j2 = v, g2 = v - v0;
+        if (e2.w & 1) {
+          i2 = v, f2 = v - v0, j2 = u, g2 = u - u0;
         }
+        if ((e2.w & 2) && i2 < j2) {
+          const int tt = i2, ft = f2;
+          i2 = j2, f2 = g2, j2 = tt, g2 = ft;
+        }
+        const int e = dl[kc + k], d = e & 0xffff;
+        const LiveBlock b = tab[e >> 16];
+        off[t] = live_offset(b, d, d - b.a0, l0 + l, l, i2, f2, j2, g2, n);
+      }
+      double x[FQ_GATHER];
 #pragma unroll
-        for (int d = 0; d < S; ++d) {
-          const __nv_bfloat162 b2 = __floats2bfloat162_rn(dig[0][d], dig[1][d]);
-          packed[d][j >> 1] = *reinterpret_cast<const unsigned *>(&b2);
+      for (int t = 0; t < FQ_GATHER; ++t) x[t] = off[t] >= 0 ? __ldg(sv.X + off[t]) : 0.0;
+#pragma unroll
+      for (int t = 0; t < FQ_GATHER; ++t) {
+        const int idx = base + lane + 32 * t;
+        if (idx < kn * R) {
+          const int k = idx / R, rr = idx - k * R;
+          Vs[k * FQ_ROWS + rr] = (float)x[t];
         }
       }
+    }
+    __syncwarp();
+#pragma unroll 2
+    for (int k = 0; k < kn; ++k) {
+      const float *crow = Cf + (size_t)(dl[kc + k] & 0xffff) * nvb;
+      float cv[KB];
 #pragma unroll
-      for (int d = 0; d < S; ++d)
-        *reinterpret_cast<uint4 *>(out + d * plane + r * Kp + 8 * c) =
-            make_uint4(packed[d][0], packed[d][1], packed[d][2], packed[d][3]);
+      for (int j = 0; j < KB; ++j) cv[j] = lane + 32 * j < nvb ? crow[lane + 32 * j] : 0.f;
+      const float *x = Vs + k * FQ_ROWS;
+      if constexpr (R >= 4) {
+#pragma unroll
+        for (int r4 = 0; r4 < R; r4 += 4) {
+          const float4 x4 = *reinterpret_cast<const float4 *>(x + r4);
+#pragma unroll
+          for (int j = 0; j < KB; ++j) {
+            acc[r4][j] = fmaf(cv[j], x4.x, acc[r4][j]);
+            acc[r4 + 1][j] = fmaf(cv[j], x4.y, acc[r4 + 1][j]);
+            acc[r4 + 2][j] = fmaf(cv[j], x4.z, acc[r4 + 2][j]);
+            acc[r4 + 3][j] = fmaf(cv[j], x4.w, acc[r4 + 3][j]);
+          }
+        }
+      } else {
+#pragma unroll
+        for (int rr = 0; rr < R; ++rr)
+#pragma unroll
+          for (int j = 0; j < KB; ++j) acc[rr][j] = fmaf(cv[j], x[rr], acc[rr][j]);
+      }
+    }
+    __syncwarp();  // Vs is read before the next chunk's gather
+  }
+#pragma unroll
+  for (int rr = 0; rr < R; ++rr) {
+    if (rr >= nr) break;
+    int u, v, l;
+    fq_row(f0 + rr, nl, u0, nu, v0, nv, same, u, v, l);
+    const long long p = (long long)u + (long long)v * (v + 1) / 2;
+#pragma unroll
+    for (int j = 0; j < KB; ++j) {
+      const int bb = lane + 32 * j;
+      if (bb < nvb) Y1[((size_t)p * n + l0 + l) * nvb + bb] = acc[rr][j];
     }
   }
+}
+
+template <int KB>
+__global__ void __launch_bounds__(256, 2) store_first_quarter_kernel(const StoreView sv, int n, int Kp,
+                                                                   const float *Cf, int nvb, int cs_floats,
+                                                                   float *__restrict__ Y1, long long np,
+                                                                   long long ngroups) {
+  extern __shared__ __align__(16) unsigned char fq_sm_raw[];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int nsh = sv.nsh;
+  // C in shared memory when it fits (cs_floats > 0), then per warp: gathered
+  // elements [FQ_KCHUNK][FQ_ROWS] floats, listed blocks [nsh], listed AOs [n]
+  float *Cs = reinterpret_cast<float *>(fq_sm_raw);
+  if (cs_floats > 0) {
+    for (int i = threadIdx.x; i < cs_floats; i += blockDim.x) Cs[i] = __ldg(Cf + i);
+    __syncthreads();
+    Cf = Cs;
+  }
+  // (the per-warp regions start on a 16-byte boundary: Vs is read as float4)
+  unsigned char *fq_sm = fq_sm_raw + (size_t)((cs_floats + 3) & ~3) * sizeof(float);
+  constexpr int VSZ = FQ_KCHUNK * FQ_ROWS;
+  float *Vs = reinterpret_cast<float *>(fq_sm) + (size_t)w * VSZ;
+  LiveBlock *tab = reinterpret_cast<LiveBlock *>(reinterpret_cast<float *>(fq_sm) + (size_t)nw * VSZ) +
+                   (size_t)w * nsh;
+  int *dl = reinterpret_cast<int *>(reinterpret_cast<LiveBlock *>(reinterpret_cast<float *>(fq_sm) +
+                                                                  (size_t)nw * VSZ) +
+                                    (size_t)nw * nsh) +
+            (size_t)w * n;
+  const long long warps = (long long)gridDim.x * nw;
+  // group g: shell pair q = U + V (V + 1) / 2 (U <= V) and the chunk of FQ_LCH
+  // consecutive shells L; the warp's rows then cover whole runs of l for each
+  // (u, v), so the sectors of Y1 it writes are completed while in L2
+  const int nch = (nsh + FQ_LCH - 1) / FQ_LCH;
+  for (long long g = (long long)blockIdx.x * nw + w; g < ngroups; g += warps) {
+    const long long q = g / nch;
+    const int Lc = (int)(g - q * nch);
+    int V1 = (int)((sqrt(8.0 * (double)q + 1.0) - 1.0) * 0.5);
+    while ((long long)V1 * (V1 + 1) / 2 > q) --V1;
+    while ((long long)(V1 + 1) * (V1 + 2) / 2 <= q) ++V1;
+    const int U = (int)(q - (long long)V1 * (V1 + 1) / 2), Vs1 = V1;
+    const int u0 = sv.ao0[U], u1 = U + 1 < nsh ? sv.ao0[U + 1] : n, nu = u1 - u0;
+    const int v0 = sv.ao0[Vs1], v1 = Vs1 + 1 < nsh ? sv.ao0[Vs1 + 1] : n, nv = v1 - v0;
+    const bool same = U == Vs1;
+    const int4 e2 = sv.pinfo[U * nsh + Vs1];
+    const double quv = sv.pbound[e2.x];
+    for (int L = Lc * FQ_LCH; L < min(nsh, (Lc + 1) * FQ_LCH); ++L) {
+    const int l0 = sv.ao0[L], l1 = L + 1 < nsh ? sv.ao0[L + 1] : n, nl = l1 - l0;
+    // the stored blocks of the group, then their AOs d
+    int cnt = 0;
+    if (sv.qmax[L] * quv >= sv.thr) {
+      const int *ptn = sv.partners + (size_t)L * nsh;
+      for (int base = 0; base < nsh; base += 32) {
+        const int k = base + lane;
+        bool ok = false, live = false;
+        LiveBlock b{};
+        if (k < nsh) {
+          const int D = ptn[k];
+          const int4 e1 = sv.pinfo[D * nsh + L];
+          ok = sv.pbound[e1.x] * quv >= sv.thr;
+          if (ok) {
+            const bool first_bra = e1.y > e2.y || (e1.y == e2.y && e1.z >= e2.z);
+            const int4 eb = first_bra ? e1 : e2, ek = first_bra ? e2 : e1;
+            const int K = eb.y * (eb.y + 1) / 2 + ek.y;
+            live = ek.z < sv.len[K][eb.z];
+            const int NB = sv_nfb(eb.y), NC = sv_nfa(ek.y), ND = sv_nfb(ek.y), NOUT = sv_nfa(eb.y) * NB * NC * ND;
+            const int a0 = sv.ao0[D], a1 = D + 1 < nsh ? sv.ao0[D + 1] : n;
+            b.off = sv.base[K] + (sv.off[K][eb.z] + ek.z) * NOUT;
+            b.a0 = a0;
+            b.flags = (e1.w & 3) | (first_bra ? 4 : 0) | (eb.x == ek.x ? 8 : 0) | (NB == 4 ? 16 : 0) |
+                      (NC == 4 ? 32 : 0) | (ND == 4 ? 64 : 0) | ((a1 - a0) << 8);
+          }
+        }
+        const unsigned lv = __ballot_sync(0xffffffffu, live);
+        if (live) tab[cnt + __popc(lv & ((1u << lane) - 1))] = b;
+        cnt += __popc(lv);
+        if (!__all_sync(0xffffffffu, ok)) break;
+      }
+    }
+    __syncwarp();
+    int nd = 0;  // listed AOs: dl[k] = d | (block << 16)
+    for (int base = 0; base < cnt; base += 32) {
+      const int t = base + lane;
+      const int na = t < cnt ? (tab[t].flags >> 8) : 0;
+      int incl = na;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+      }
+      const int pos = nd + incl - na;
+      for (int i = 0; i < na; ++i) dl[pos + i] = (tab[t].a0 + i) | (t << 16);
+      nd += __shfl_sync(0xffffffffu, incl, 31);
+    }
+    __syncwarp();
+    const int rows = (same ? nu * (nu + 1) / 2 : nu * nv) * nl;
+    for (int f0 = 0; f0 < rows;) {
+      const int left = rows - f0;
+      if (left >= 5 && KB <= 2) {
+        const int nr = min(left, 8);
+        fq_pass<KB, 8>(sv, n, Kp, Cf, nvb, Y1, np, dl, tab, nd, Vs, f0, nr, nl, l0, u0, nu, v0, nv, same, e2);
+        f0 += nr;
+      } else if (left >= 2) {
+        const int nr = min(left, 4);
+        fq_pass<KB, 4>(sv, n, Kp, Cf, nvb, Y1, np, dl, tab, nd, Vs, f0, nr, nl, l0, u0, nu, v0, nv, same, e2);
+        f0 += nr;
+      } else {
+        fq_pass<KB, 1>(sv, n, Kp, Cf, nvb, Y1, np, dl, tab, nd, Vs, f0, 1, nl, l0, u0, nu, v0, nv, same, e2);
+        f0 += 1;
+      }
+    }
+    __syncwarp();  // the tables are read before the next shell L's
+    }
+  }
+}
+
+// C(d, b) as FP32, b fastest
+__global__ void coef_f32_kernel(const double *__restrict__ C, int n, int nvb, float *__restrict__ Cf) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n * nvb) return;
+  const int d = i / nvb, b = i % nvb;
+  Cf[i] = (float)C[d + (size_t)n * b];
 }
 
 // ------------------------------------------------------------------ host side
@@ -542,12 +809,12 @@ static int slice_gemm(mq_ctx *c, Sliced A, long long M, int batch, long long a_b
 
 template <int S, int MODE = ROW_PLAIN, class T>
 static int slice_rows(mq_ctx *c, const T *in, long long rows, int kvalid, long long ld, int Kp, Sliced o,
-                      RowSrc rs = RowSrc{nullptr, 1, 0, StoreView{}}) {
+                      RowSrc rs = RowSrc{nullptr, 1, 0, 1}) {
   if (Kp % 8 || Kp > 512) return set_err(c, MQ_EINVAL, "slice_rows: Kp must be a multiple of 8 up to 512");
   const int tb = 256;
   const long long blocks = std::max<long long>(1, std::min<long long>((rows + 7) / 8, 1 << 20));
   const int per16 = 16 / (int)sizeof(T);
-  const int vec = MODE != ROW_SYMM && MODE != ROW_STORE && ((uintptr_t)in % 16 == 0) && (ld % per16 == 0) &&
+  const int vec = MODE != ROW_SYMM && MODE != ROW_TRANS && ((uintptr_t)in % 16 == 0) && (ld % per16 == 0) &&
                   (kvalid % per16 == 0);
   if (Kp <= 256)
     slice_rows_kernel<S, T, 1, MODE><<<(unsigned)blocks, tb, 0, c->stream>>>(in, rows, kvalid, ld, Kp, o.plane,
@@ -577,7 +844,7 @@ static int pair_table(mq_ctx *c, int n, const int2 **out) {
   return MQ_OK;
 }
 
-// The quartet store as the ROW_STORE slicing reads it.
+// The quartet store as the first step's slicing reads it.
 static StoreView store_view(mq_ctx *c) {
   const QStore &qs = c->qs;
   StoreView v{};
@@ -593,20 +860,47 @@ static StoreView store_view(mq_ctx *c) {
   v.nsh = c->nshell;
   v.pbound = c->pt.schwarz;
   v.qmax = qs.shell_qmax;
+  v.partners = qs.partners;
   v.thr = qs.thr;
   return v;
 }
 
 // A operand of the first step -- XX(d, l, u, v), rows (l, u <= v), K = d --
-// cut into S planes: from the n^4 array, or looked up in the quartet store
+// cut into S planes from the n^4 array
 template <int S>
 static int slice_xx(mq_ctx *c, long long n, int Kp, Sliced A, const int2 *pairs) {
   const long long np = n * (n + 1) / 2;
-  if (!c->xx_valid && c->qs.valid)
-    return slice_rows<S, ROW_STORE, double>(c, nullptr, n * np, (int)n, n, Kp, A,
-                                            RowSrc{pairs, n, np, store_view(c)});
+  if (c->nparts > 1) return set_err(c, MQ_EINVAL, "the transform needs every integral: reset the partition first");
   MQ_TRY(ensure_xx_full(c));
-  return slice_rows<S, ROW_PAIRS>(c, c->d_XX, n * np, (int)n, n, Kp, A, RowSrc{pairs, n, np, StoreView{}});
+  return slice_rows<S, ROW_PAIRS>(c, c->d_XX, n * np, (int)n, n, Kp, A, RowSrc{pairs, n, np, 1});
+}
+
+// Y1[p][l][b] from the quartet store and C(:, b), b < nvb
+static int store_first_quarter(mq_ctx *c, long long n, int Kp, const double *Cb, int nvb, float *y1, long long np) {
+  const int nsh = c->nshell, nw = 256 / 32;
+  float *Cf = (float *)buf(c, "fq_coef", sizeof(float) * (size_t)n * std::max(nvb, 1));
+  if (!Cf) return MQ_ENOMEM;
+  coef_f32_kernel<<<(unsigned)((n * nvb + 255) / 256), 256, 0, c->stream>>>(Cb, (int)n, nvb, Cf);
+  const long long groups = (long long)nsh * (nsh + 1) / 2 * ((nsh + FQ_LCH - 1) / FQ_LCH);
+  size_t sm = (size_t)nw * ((size_t)FQ_KCHUNK * FQ_ROWS * sizeof(float) + (size_t)n * sizeof(int) +
+                            (size_t)nsh * sizeof(LiveBlock));
+  // C in shared memory when the CTA still fits twice per SM
+  const int cs_floats = sm + (size_t)n * nvb * sizeof(float) <= 110 * 1024 ? (int)(n * nvb) : 0;
+  sm += (size_t)((cs_floats + 3) & ~3) * sizeof(float);
+  if (sm > 200 * 1024) return set_err(c, MQ_EINVAL, "split transform: too many shells for the store transform");
+  if (n > 0xffff || nsh > 0xffff) return set_err(c, MQ_EINVAL, "split transform: too many AOs for the store transform");
+  auto kern = nvb <= 32 ? store_first_quarter_kernel<1>
+                        : (nvb <= 64 ? store_first_quarter_kernel<2>
+                                     : (nvb <= 128 ? store_first_quarter_kernel<4> : store_first_quarter_kernel<8>));
+  // (with KB >= 4, passes of at most 4 rows keep the accumulators in registers)
+  MQ_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+  const long long blocks = std::max<long long>(1, std::min<long long>((groups + nw - 1) / nw, (long long)sms * 16));
+  kern<<<(unsigned)blocks, 256, sm, c->stream>>>(store_view(c), (int)n, Kp, Cf, nvb, cs_floats, y1, np, groups);
+  c->stats.launches += 2;
+  MQ_CUDA(c, cudaGetLastError());
+  return sync_check(c, "store_first_quarter");
 }
 
 template <int S>
@@ -620,7 +914,12 @@ static int ao2mo_slices(mq_ctx *c, const double *Ci, int no1, const double *Ca, 
   MQ_TRY(join_side(c));  // a prefetch of the XX slices, before any buffer is touched
   const long long n2 = n * n, n3 = n2 * n;
   // A operand rows per step, and the FP32 intermediates [rows][Kp]
-  const long long rX = n3, r1 = (long long)nv2 * n2, r2 = (long long)no2 * nv2 * n, r3 = (long long)nv1 * no2 * nv2;
+  // the first step reads the quartet store directly when there is no n^4 array
+  const bool from_store = !c->xx_valid && c->qs.valid;
+  if (from_store && c->nparts > 1)
+    return set_err(c, MQ_EINVAL, "the transform needs every integral: reset the partition first");
+  const long long rX = from_store ? 0 : n3, r1 = (long long)nv2 * n2, r2 = (long long)no2 * nv2 * n,
+                  r3 = (long long)nv1 * no2 * nv2;
   const long long rB = (long long)no1 + nv1 + no2 + nv2;
   const long long rmax = std::max(std::max(rX, r1), std::max(r2, r3));
   bf16 *pa = (bf16 *)buf(c, "slice_a", S * rmax * Kp * sizeof(bf16));
@@ -649,25 +948,39 @@ static int ao2mo_slices(mq_ctx *c, const double *Ci, int no1, const double *Ca, 
   const long long np = n * (n + 1) / 2, rXp = n * np;
   const int2 *pairs = nullptr;
   MQ_TRY(pair_table(c, (int)n, &pairs));
-  const RowSrc rs{pairs, n, np, StoreView{}};
-  // 1: XX(d,l,u,v) at d + n*((l,u,v)): rows (l,p), K = d -> Y1[b][p][l]
-  // (already sliced on the side stream when the SCF prefetched it)
+  const RowSrc rs{pairs, n, np, 1};
+  // 1: XX(d,l,u,v) at d + n*((l,u,v)): rows (l,p), K = d -> Y1[b][p][l]:
+  // from the quartet store on the CUDA cores (FP32), else from the n^4 array
+  // by the tensor cores (its slices already cut on the side stream when the
+  // SCF prefetched them)
   Sliced A{pa, rX * Kp, ea};
-  if (c->xx_sliced != S) MQ_TRY(slice_xx<S>(c, n, Kp, A, pairs));
-  (void)rXp;
-  c->xx_sliced = 0;  // step 2 overwrites the slices
-  g.out_f64 = 0;
-  g.out32 = y1;
-  g.mdiv = n;
-  g.s_m0 = 1;
-  g.s_m1 = Kp;
-  g.s_n = np * Kp;
-  g.s_b = 0;
-  MQ_TRY(slice_gemm<S>(c, A, rXp, 1, 0, Bb, nv2, Kp, g));
+  c->stats.ms_ao2mo_first = 0;
+  if (from_store) {
+    StageTimer t1;
+    t1.start(c->stream);
+    MQ_TRY(store_first_quarter(c, n, Kp, Cb, nv2, y1, np));
+    t1.stop(c->stream);
+    t1.collect_sync();
+    c->stats.ms_ao2mo_first = t1.total;
+  } else {
+    if (c->xx_sliced != S) MQ_TRY(slice_xx<S>(c, n, Kp, A, pairs));
+    c->xx_sliced = 0;  // step 2 overwrites the slices
+    g.out_f64 = 0;
+    g.out32 = y1;
+    g.mdiv = n;
+    g.s_m0 = 1;
+    g.s_m1 = Kp;
+    g.s_n = np * Kp;
+    g.s_b = 0;
+    MQ_TRY(slice_gemm<S>(c, A, rXp, 1, 0, Bb, nv2, Kp, g));
+  }
   // 2: batch b; rows p, K = l -> Y2[j,b][p] (packed pairs)
   const long long r1p = (long long)nv2 * np;
   A = Sliced{pa, r1p * Kp, ea};
-  MQ_TRY(slice_rows<S>(c, y1, r1p, (int)n, Kp, Kp, A));
+  if (from_store)  // Y1 as [p][l][b]
+    MQ_TRY((slice_rows<S, ROW_TRANS>(c, y1, r1p, (int)n, 0, Kp, A, RowSrc{nullptr, n, np, nv2})));
+  else
+    MQ_TRY(slice_rows<S>(c, y1, r1p, (int)n, Kp, Kp, A));
   g.out32 = y2;
   g.mdiv = 1ll << 62;
   g.s_m0 = 1;
@@ -719,7 +1032,10 @@ template <int S>
 static int preslice(mq_ctx *c) {
   const long long n = c->nao;
   const int Kp = (int)((n + 7) / 8 * 8);
-  if (Kp > SLICE_KMAX || (!c->xx_valid && !c->qs.valid)) return MQ_OK;  // the transform would reject it anyway
+  // nothing to cut ahead without the n^4 array: the first step then reads the
+  // quartet store itself, after the SCF (and a transform of more than 340
+  // functions is rejected anyway)
+  if (Kp > SLICE_KMAX || !c->xx_valid) return MQ_OK;
   const long long rX = n * n * n;
   bf16 *pa = (bf16 *)buf(c, "slice_a", S * rX * Kp * sizeof(bf16));
   int *ea = (int *)buf(c, "slice_ea", rX * sizeof(int));

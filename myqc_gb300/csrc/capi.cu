@@ -96,6 +96,7 @@ int ensure_xx_alloc(mq_ctx *c) {
 int ensure_xx_full(mq_ctx *c) {
   if (c->xx_valid) return MQ_OK;
   if (!c->qs.valid) return set_err(c, MQ_ESTATE, "no integrals on the device (call mq_eri_store or mq_eri_upload)");
+  if (c->nparts > 1) return set_err(c, MQ_EINVAL, "the full integral array needs every quartet: reset the partition first");
   MQ_TRY(ensure_xx_alloc(c));
   MQ_TRY(qstore_expand(c, c->d_XX));
   c->xx_valid = 1;
@@ -745,12 +746,15 @@ int mq_stat(const mq_ctx *c, const char *key, double *value) {
   else if (!strcmp(key, "fock")) *value = s.ms_fock;
   else if (!strcmp(key, "diag")) *value = s.ms_diag;
   else if (!strcmp(key, "ao2mo")) *value = s.ms_ao2mo;
+  else if (!strcmp(key, "ao2mo_first")) *value = s.ms_ao2mo_first;
   else if (!strcmp(key, "mp2")) *value = s.ms_mp2;
   else if (!strcmp(key, "scf")) *value = s.ms_scf;
   else if (!strcmp(key, "fock_calls")) *value = s.fock_calls;
   else if (!strcmp(key, "scf_iters")) *value = s.scf_iters;
   else if (!strcmp(key, "diag_calls")) *value = s.diag_calls;
   else if (!strcmp(key, "purify_steps")) *value = s.purify_steps;
+  else if (!strcmp(key, "purify_persistent")) *value = s.purify_persistent;
+  else if (!strcmp(key, "purify_stepwise")) *value = s.purify_stepwise;
   else if (!strcmp(key, "fock_jc")) *value = s.fock_jc;
   else if (!strcmp(key, "graph_launches")) *value = s.graph_launches;
   else if (!strcmp(key, "eig_cluster")) *value = s.eig_cluster;

@@ -128,13 +128,16 @@ struct QStore {
   int *ao_shell = nullptr;    // [n] shell of each AO
   double *shell_qmax = nullptr;  // [nshell] the largest Schwarz bound of a pair containing the shell
   int4 *pinfo = nullptr;      // [S1 * nshell + S2]: pair, class, rank, bit 0: stored as (S2, S1), bit 1: S1 = S2
+  int *partners = nullptr;    // [S * nshell + k]: the shells D by the bound of the pair (D, S), descending
   double quartets = 0;        // quartets stored
   double unique = 0;          // canonical unique integrals stored (the digestion's 6 FMAs each)
 };
 
 struct Stats {
   double ms_eri = 0, ms_fock = 0, ms_diag = 0, ms_ao2mo = 0, ms_mp2 = 0, ms_scf = 0;
+  double ms_ao2mo_first = 0;  // the transform's first quarter (from the quartet store), last transform
   double fock_calls = 0, diag_calls = 0, scf_iters = 0, purify_steps = 0, fock_jc = 0, tune_fock_ms = 0;
+  double purify_persistent = 0, purify_stepwise = 0;  // purifications of the last SCF by form
   double launches = 0, lib_launches = 0, quartets = 0, prim_quartets = 0;
   double ms_fock_kernel = 0, fock_kernel_launches = 0;  // the digestion kernel alone, last SCF or mq_fock
   double graph_launches = 0;  // CUDA-graph replays of the last batch SCF

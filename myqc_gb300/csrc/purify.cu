@@ -370,7 +370,11 @@ int purify_projector(mq_ctx *c, int n, int nocc, const double *d_Fp, double *d_P
   // operands on the side stream); otherwise one product and one update
   // launch per step
   if (c->side_pending && cudaEventQuery(c->ev_side) == cudaSuccess) MQ_TRY(join_side(c));  // it has finished
-  if (n <= PUR_PERSIST_MAX && !c->side_pending) return purify_persistent(c, n, nocc, d_P, d_W, d_err, steps);
+  if (n <= PUR_PERSIST_MAX && !c->side_pending) {
+    c->stats.purify_persistent += 1;
+    return purify_persistent(c, n, nocc, d_P, d_W, d_err, steps);
+  }
+  c->stats.purify_stepwise += 1;
   std::vector<double> e(MAX_STEPS);
   int k = 0, settled_at = -1;
   while (k < MAX_STEPS) {

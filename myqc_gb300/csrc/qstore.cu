@@ -651,6 +651,18 @@ int qstore_build(mq_ctx *c) {
     qmax[c->hp_shA[p]] = std::max(qmax[c->hp_shA[p]], sch[p]);
     qmax[c->hp_shB[p]] = std::max(qmax[c->hp_shB[p]], sch[p]);
   }
+  // per shell S: every shell D ordered by the bound of the pair (D, S),
+  // descending -- the shells D of the live quartets (D S|U V) of any pair
+  // (U, V) are a prefix of S's list
+  std::vector<int> ptn((size_t)nsh * nsh);
+  for (int S2 = 0; S2 < nsh; ++S2) {
+    int *row = ptn.data() + (size_t)S2 * nsh;
+    for (int D1 = 0; D1 < nsh; ++D1) row[D1] = D1;
+    std::stable_sort(row, row + nsh, [&](int a, int b) {
+      return sch[pinfo[(size_t)a * nsh + S2].x] > sch[pinfo[(size_t)b * nsh + S2].x];
+    });
+  }
+  const size_t o_ptn = blob.add(ptn.data(), ptn.size());
   const size_t o_qm = blob.add(qmax.data(), qmax.size());
   const size_t o_aos = blob.add(ao_shell.data(), ao_shell.size());
   const size_t o_pi = blob.add(pinfo.data(), pinfo.size());
@@ -675,6 +687,7 @@ int qstore_build(mq_ctx *c) {
   qs.ao_shell = (int *)(d + o_aos);
   qs.shell_qmax = (double *)(d + o_qm);
   qs.pinfo = (int4 *)(d + o_pi);
+  qs.partners = (int *)(d + o_ptn);
   qs.X_elems = (size_t)base;
   qs.X = (double *)buf(c, "qstore_X", sizeof(double) * std::max<size_t>(qs.X_elems, 1));
   if (!qs.X) return MQ_ENOMEM;

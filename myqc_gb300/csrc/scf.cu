@@ -421,6 +421,7 @@ int scf_device(mq_ctx *c, const double *S, const double *H, const mq_scf_opts *o
   // initial density
   c->stats.diag_calls = 0;
   c->stats.purify_steps = 0;
+  c->stats.purify_persistent = c->stats.purify_stepwise = 0;
   if (o->guess == 2 && o->D_in) {
     MQ_CUDA(c, cudaMemcpyAsync(dD, o->D_in, n2 * ns * sizeof(double), cudaMemcpyHostToDevice, c->stream));
   } else if (purify && !(o->guess == 1 && o->C_in)) {  // core Hamiltonian, purified

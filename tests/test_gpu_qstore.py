@@ -154,23 +154,36 @@ def test_partitions_sum_to_the_full_fock(qctx, basis_text, direct):
     assert np.max(np.abs(sum(parts) - G)) < 1e-12 * max(1.0, np.max(np.abs(G)))
 
 
-def test_transform_slices_from_the_store(qctx, basis_text):
-    """The split transform's first operand cut straight from the quartet store
-    equals the one cut from the n^4 array filled from it: the same MP2 energy,
-    bit for bit."""
+@pytest.mark.parametrize("name", ["water5", "water16"])
+def test_transform_from_the_store(qctx, basis_text, name):
+    """The split transform with no n^4 array: its first quarter read straight
+    from the quartet store (sparse, FP32 on the CUDA cores), the rest split
+    BF16 x3 on the tensor cores, against the FP64 transform of the n^4 array
+    filled from the same store: (ia|jb) within 1e-4 of the largest element and
+    E(MBPT2) within 1 uEh (the split transform's own bounds); and against the
+    split transform of the filled array within 1e-5 relative."""
     from myqc_gb300 import PREC_SPLIT_BF16X3
-    sysm, basis = _system("water5", basis_text)
+    sysm, basis = _system(name, basis_text)
     qctx.set_system(sysm, basis, None, MODE_TIGHT)
     qctx.set_schwarz(1e-12)
     qctx.set_eri_storage(STORE_QUARTETS)
     S, H = qctx.int1e()
     qctx.eri_store()
     r = qctx.scf(S, H, sysm.nelcA, sysm.nelcB, conv=1e-10, conv_rms=True, diis=8, max_iter=100)
-    m_store = qctx.mp2_rhf(r.eig, sysm.nelcA, PREC_SPLIT_BF16X3, C=r.C)
+    no = sysm.nelcA
+    C = r.C
+    blocks = (C[:, :no], C[:, no:], C[:, :no], C[:, no:])
+    got = qctx.ao2mo_iajb(*blocks, PREC_SPLIT_BF16X3)
+    m_store = qctx.mp2_rhf(r.eig, no, PREC_SPLIT_BF16X3, C=C)
     n = qctx.n
     qctx.fock(_density(n, 7), _density(n, 8))  # a UHF build fills the n^4 array from the store
-    m_full = qctx.mp2_rhf(r.eig, sysm.nelcA, PREC_SPLIT_BF16X3, C=r.C)
-    assert m_store["E_MP2"] == m_full["E_MP2"]
+    ref = qctx.ao2mo_iajb(*blocks, PREC_FP64)
+    split_full = qctx.ao2mo_iajb(*blocks, PREC_SPLIT_BF16X3)
+    m64 = qctx.mp2_rhf(r.eig, no, PREC_FP64, C=C)
+    big = np.max(np.abs(ref))
+    assert np.max(np.abs(got - ref)) < 1e-4 * big
+    assert np.max(np.abs(got - split_full)) < 1e-5 * big
+    assert abs(m_store["E_MP2"] - m64["E_MP2"]) < 1e-6, (m_store, m64)
 
 
 def test_autotuned_integral_launches(qctx, ftab, basis_text):
