@@ -505,19 +505,23 @@ def dominant_roofline(r):
 def measure_batched(ctx, count: int):
     """The batching workload, measured once after the headline: `count` closed-shell
     molecules drawn from the standard set (coordinates perturbed by N(0, 0.05 A)),
-    solved together by mq_batch_scf (CUDA-graph iterations, DIIS(8), RMS dD < 1e-10).
-    Not part of the headline metric."""
-    from myqc_gb300 import FOCK_FP64, formats, molecules
+    set up by atoms (basis built in the library) and solved together by
+    mq_batch_scf (autotuned integral launches, CUDA-graph iterations, DIIS(8),
+    RMS dD < 1e-10); the second of two identical passes is timed.  Not part of
+    the headline metric."""
+    from myqc_gb300 import FOCK_FP64, molecules
     ctx.set_fock_precision(FOCK_FP64)
     btext = open(os.path.join(ROOT, "myqc_gb300", "data", "sto3g.mybasis")).read()
     kinds, systems = molecules.batch_workload(count, 0)
-    t0 = time.perf_counter()
-    ctx.batch_clear()
-    for sysm in systems:
-        ctx.batch_add(sysm, formats.parse_mybasis_text(btext, sysm.atoms))
-    t1 = time.perf_counter()
-    r = ctx.batch_scf(conv=1e-10, conv_rms=True, diis=8, max_iter=100, graph=True)
-    t2 = time.perf_counter()
+    ctx.basis_library(btext)  # buildBasis in the library: no host-language parse per molecule
+    for timed in (False, True):  # an untimed pass first: the integral autotuner runs there
+        t0 = time.perf_counter()
+        ctx.batch_clear()
+        for sysm in systems:
+            ctx.batch_add_atoms(sysm)
+        t1 = time.perf_counter()
+        r = ctx.batch_scf(conv=1e-10, conv_rms=True, diis=8, max_iter=100, graph=True)
+        t2 = time.perf_counter()
     ctx.batch_clear()
     return {"molecules": count, "kinds": "H2 HF H2O NH3 CH4 CO CO2 C2H2 HCN (H2O)2..8", "basis_sizes": "2..56",
             "solves_per_s": count / (t2 - t1), "wall_s": t2 - t1, "host_setup_s": t1 - t0,

@@ -321,6 +321,24 @@ typedef struct mq_batch_opts {
                           a block whose first element is NaN takes the core guess */
 } mq_batch_opts;
 
+/* The basis library (the text of a mybasis file) kept by the context for the
+ * calls below; its STO-3G section is used, as the reference's buildBasis
+ * reads it (src/myQC/basis.f90:81). */
+int mq_basis_library(mq_ctx *ctx, const char *text);
+
+/* buildBasis (src/myQC/basis.f90:23-226) in the library: the flat bas, set,
+ * basinfo and setinfo arrays of the atoms Z[nnuc] from the library above.
+ * sizes[4]: on entry the capacities of the four arrays, on return the sizes
+ * needed; the arrays are written only when all four fit (null arrays: sizes
+ * only). */
+int mq_basis_build(mq_ctx *ctx, int nnuc, const int *Z, double *bas, double *set, int *basinfo, int *setinfo,
+                   int sizes[4]);
+
+/* mq_batch_add with the molecule's basis built by the library (mq_basis_library
+ * first): nuclei Z and coordinates xyz (bohr, nnuc x 3 row-major as
+ * mq_batch_add takes them), nocc doubly occupied orbitals. */
+int mq_batch_add_atoms(mq_ctx *ctx, int nnuc, const int *Z, const double *xyz, int nocc);
+
 /* Empty the context's batch. */
 int mq_batch_clear(mq_ctx *ctx);
 

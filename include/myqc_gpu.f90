@@ -70,6 +70,17 @@ MODULE myqc_gpu
     INTEGER(c_int) FUNCTION mq_set_fock_screened_increments(ctx, tau) BIND(C)
       IMPORT; TYPE(c_ptr), VALUE :: ctx; REAL(c_double), VALUE :: tau
     END FUNCTION
+    INTEGER(c_int) FUNCTION mq_basis_library(ctx, text) BIND(C)
+      IMPORT; TYPE(c_ptr), VALUE :: ctx; CHARACTER(KIND=c_char) :: text(*)   ! NUL-terminated mybasis text
+    END FUNCTION
+    INTEGER(c_int) FUNCTION mq_basis_build(ctx, nnuc, Z, bas, set, basinfo, setinfo, sizes) BIND(C)
+      IMPORT; TYPE(c_ptr), VALUE :: ctx; INTEGER(c_int), VALUE :: nnuc; INTEGER(c_int) :: Z(*)
+      REAL(c_double) :: bas(*), set(*); INTEGER(c_int) :: basinfo(*), setinfo(*), sizes(4)
+    END FUNCTION
+    INTEGER(c_int) FUNCTION mq_batch_add_atoms(ctx, nnuc, Z, xyz, nocc) BIND(C)
+      IMPORT; TYPE(c_ptr), VALUE :: ctx; INTEGER(c_int), VALUE :: nnuc, nocc; INTEGER(c_int) :: Z(*)
+      REAL(c_double) :: xyz(*)
+    END FUNCTION
     INTEGER(c_int) FUNCTION mq_set_eri_tuning(ctx, mode) BIND(C)
       IMPORT; TYPE(c_ptr), VALUE :: ctx; INTEGER(c_int), VALUE :: mode
     END FUNCTION

@@ -271,7 +271,7 @@ int eri_batch_device(mq_ctx *c, const PairTable &t, const MolDesc *d_mols, int n
       h.tri = cP == cQ;
       h.nq = total[k];
       h.mq_off = d_mq_off[k];
-      MQ_TRY(launch_class<EPI_XX>(c, h, cP, cQ));
+      MQ_TRY(eri_batch_launch(c, h, cP, cQ));
     }
   return MQ_OK;
 }

@@ -86,6 +86,11 @@ struct EriArgs {
   int st_n;
   const int *permP, *permQ;
   double *store;
+  // persistent launch (queue non-null): the grid is sized to the resident
+  // CTAs and each warp takes work units from *queue (zeroed first) while
+  // they last; units = warp slots of the launch (quartets / 32 x split)
+  unsigned long long *queue;
+  long long units;
 };
 
 __host__ __device__ constexpr int fl(int f, int axis) { return f == axis + 1 ? 1 : 0; }  // f: 0 s, 1 px, 2 py, 3 pz
@@ -792,6 +797,9 @@ __device__ __forceinline__ void schwarz_diag(const EriArgs &g, int P, size_t n, 
     quartet<LA, LB, LA, LB, a, a + 1, b, b + 1, a, a + 1, b, b + 1, EPI_SCHWARZ, double>(g, P, P, n, XX);
 }
 
+template <int LA, int LB, int LC, int LD, int EPI, class RT>
+__device__ __forceinline__ void eri_unit(const EriArgs &g, long long warp, int lane);
+
 template <int LA, int LB, int LC, int LD, int EPI, class RT = double>
 __global__ void __launch_bounds__(256) eri_kernel(EriArgs g) {
   constexpr int NA = nfun(LA), NB = nfun(LB);
@@ -815,9 +823,27 @@ __global__ void __launch_bounds__(256) eri_kernel(EriArgs g) {
     return;
   }
   constexpr int NSPLIT = NOUT <= 16 ? 1 : (NOUT <= 64 ? 4 : 16);
-  const long long gtid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const long long warp = gtid >> 5;
   const int lane = threadIdx.x & 31;
+  if (g.queue) {  // persistent: each warp takes work units from the launch's queue until it is empty
+    for (;;) {
+      unsigned long long unit = 0;
+      if (lane == 0) unit = atomicAdd(g.queue, 1ull);
+      unit = __shfl_sync(0xffffffffu, unit, 0);
+      if (unit >= (unsigned long long)g.units) break;
+      eri_unit<LA, LB, LC, LD, EPI, RT>(g, (long long)unit, lane);
+    }
+    return;
+  }
+  eri_unit<LA, LB, LC, LD, EPI, RT>(g, ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane);
+}
+
+// One work unit of an integral launch: warp unit w serves split w % NSPLIT of
+// the 32 consecutive quartets (w / NSPLIT) * 32 .. + 31 of the launch order.
+template <int LA, int LB, int LC, int LD, int EPI, class RT>
+__device__ __forceinline__ void eri_unit(const EriArgs &g, long long warp, int lane) {
+  constexpr int NA = nfun(LA), NB = nfun(LB);
+  constexpr int NOUT = NA * NB * nfun(LC) * nfun(LD);
+  constexpr int NSPLIT = NOUT <= 16 ? 1 : (NOUT <= 64 ? 4 : 16);
   const int split = (int)(warp % NSPLIT);
   long long q = (warp / NSPLIT) * 32 + lane;
   int P, Q, m;
@@ -859,18 +885,33 @@ static inline int nsplit_of(int cP, int cQ) {
 // The launch order of an integral launch sorted by surviving primitive
 // quartets (eri_store.cu): h.list / h.list_n are set.
 int bin_quartets(mq_ctx *c, EriArgs &h, int slot);
+// the batch's integral launch of one class combination, in its autotuned shape (eri_store.cu)
+int eri_batch_launch(mq_ctx *c, const EriArgs &h, int cP, int cQ);
 
 // One class combination's integral launch; `block` is the CTA size of the
 // thread-per-quartet kernel (64, 128 or 256; the autotuner's choice)
 template <int EPI, class RT = double>
-static int launch_class(mq_ctx *c, EriArgs g, int cP, int cQ, int block = 128) {
+static int launch_class(mq_ctx *c, EriArgs g, int cP, int cQ, int block = 128, bool persistent = false) {
   // Schwarz: one warp slot per diagonal function pair (ab|ab) of the class
   const int nsplit = EPI == EPI_SCHWARZ ? (cP == 0 ? 1 : cP == 1 ? 4 : 16) : nsplit_of(cP, cQ);
   const long long warps = (g.nq + 31) / 32 * nsplit;
   const long long threads = warps * 32;
   if (block != 64 && block != 128 && block != 256) return set_err(c, MQ_EINVAL, "integral launch: bad CTA size");
-  const long long grid = (threads + block - 1) / block;
+  long long grid = (threads + block - 1) / block;
   if (grid == 0) return MQ_OK;
+  if (persistent && EPI != EPI_SCHWARZ) {
+    // a work queue: as many CTAs as can be resident (more only find it empty)
+    unsigned long long *queue = (unsigned long long *)buf(c, "eri_queue", 256);
+    if (!queue) return MQ_ENOMEM;
+    MQ_CUDA(c, cudaMemsetAsync(queue, 0, sizeof(unsigned long long), c->stream));
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+    grid = std::min<long long>(grid, (long long)sms * (2048 / block));
+    g.queue = queue;
+    g.units = warps;
+  } else {
+    g.queue = nullptr;
+  }
   if (grid > 2147483647LL) return set_err(c, MQ_EINVAL, "integral launch too large");
   dim3 gd((unsigned)grid);
   if constexpr (EPI == EPI_STORE && std::is_same<RT, double>::value) {

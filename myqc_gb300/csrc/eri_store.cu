@@ -128,43 +128,51 @@ static unsigned long long tune_key(int epi, int combo, long long nq) {
   return ((unsigned long long)epi << 40) | ((unsigned long long)combo << 32) | (unsigned long long)b;
 }
 
-// One class combination's launch with a candidate (binned, block); the
-// binning kernels count towards its time, since every pass repeats them.
-static int run_candidate(mq_ctx *c, const EriArgs &h0, int cP, int cQ, int combo, const EriTune &t) {
+// One class combination's launch with a candidate (binned, block,
+// persistent); the binning kernels count towards its time, since every pass
+// repeats them.  `slot` names the launch's binning buffers.
+template <int EPI>
+static int run_candidate(mq_ctx *c, const EriArgs &h0, int cP, int cQ, int slot, const EriTune &t) {
   EriArgs h = h0;
-  if (t.binned) MQ_TRY(bin_quartets(c, h, combo));
-  return launch_class<EPI_STORE>(c, h, cP, cQ, t.block);
+  if (t.binned) MQ_TRY(bin_quartets(c, h, slot));
+  return launch_class<EPI>(c, h, cP, cQ, t.block, t.persistent != 0);
 }
 
 // The choice for this launch: cached per (epilogue, combination, size class);
 // otherwise every candidate runs once (timed with events after one untimed
 // run of the default) and the fastest is kept.  Every candidate writes the
-// same integrals, so the store is complete whichever ran last.
-static int tuned_launch(mq_ctx *c, const EriArgs &h, int cP, int cQ, int combo) {
-  const bool split = nsplit_of(cP, cQ) > 1;
+// same integrals (each to its own place), so the output is complete whichever
+// ran last.
+template <int EPI>
+static int tuned_launch(mq_ctx *c, const EriArgs &h, int cP, int cQ, int combo, int slot) {
+  // the split classes of the quartet store run their CTA-shared kernel: its
+  // shape is fixed by the warp count, only the order is a choice
+  const bool fixed_shape = EPI == EPI_STORE && nsplit_of(cP, cQ) > 1;
   EriTune def;
-  if (c->eri_tune_mode == 0 || h.nq < TUNE_MIN_QUARTETS) return run_candidate(c, h, cP, cQ, combo, def);
-  const unsigned long long key = tune_key(EPI_STORE, combo, h.nq);
+  if (c->eri_tune_mode == 0 || h.nq < TUNE_MIN_QUARTETS) return run_candidate<EPI>(c, h, cP, cQ, slot, def);
+  const unsigned long long key = tune_key(EPI, combo, h.nq);
   auto it = c->eri_tune.find(key);
-  if (it != c->eri_tune.end()) return run_candidate(c, h, cP, cQ, combo, it->second);
+  if (it != c->eri_tune.end()) return run_candidate<EPI>(c, h, cP, cQ, slot, it->second);
   std::vector<EriTune> cand;
   for (int binned = 1; binned >= 0; --binned)
-    for (int block : {64, 128, 256}) {
-      if (split && block != 128) continue;  // the split classes' CTA is fixed by their warp count
-      EriTune t;
-      t.binned = binned;
-      t.block = block;
-      cand.push_back(t);
-    }
+    for (int persistent = 0; persistent <= (fixed_shape ? 0 : 1); ++persistent)
+      for (int block : {64, 128, 256}) {
+        if ((fixed_shape || nsplit_of(cP, cQ) > 1) && block != 128) continue;
+        EriTune t;
+        t.binned = binned;
+        t.block = block;
+        t.persistent = persistent;
+        cand.push_back(t);
+      }
   cudaEvent_t e0, e1;
   MQ_CUDA(c, cudaEventCreate(&e0));
   MQ_CUDA(c, cudaEventCreate(&e1));
-  int rc = run_candidate(c, h, cP, cQ, combo, def);  // untimed: first-touch of buffers and code
+  int rc = run_candidate<EPI>(c, h, cP, cQ, slot, def);  // untimed: first-touch of buffers and code
   EriTune best;
   best.ms = 1e30f;
   for (size_t k = 0; rc == MQ_OK && k < cand.size(); ++k) {
     cudaEventRecord(e0, c->stream);
-    rc = run_candidate(c, h, cP, cQ, combo, cand[k]);
+    rc = run_candidate<EPI>(c, h, cP, cQ, slot, cand[k]);
     cudaEventRecord(e1, c->stream);
     if (rc != MQ_OK) break;
     if (cudaEventSynchronize(e1) != cudaSuccess) {
@@ -181,8 +189,27 @@ static int tuned_launch(mq_ctx *c, const EriArgs &h, int cP, int cQ, int combo) 
   if (rc != MQ_OK) return rc;
   c->eri_tune[key] = best;
   c->eri_tune_log.push_back({key, cand});
-  // the last candidate wrote the store; the chosen one is what later passes run
   return MQ_OK;
+}
+
+// One tuned pass of a class combination: while its signature is untuned the
+// tuning runs (counters off) and then the chosen shape runs once more, so the
+// counters count one pass.
+template <int EPI>
+static int tuned_pass(mq_ctx *c, const EriArgs &h, int cP, int cQ, int combo, int slot) {
+  if (c->eri_tune_mode != 0 && h.nq >= TUNE_MIN_QUARTETS && !c->eri_tune.count(tune_key(EPI, combo, h.nq))) {
+    EriArgs ht = h;
+    ht.counters = nullptr;
+    MQ_TRY(tuned_launch<EPI>(c, ht, cP, cQ, combo, slot));
+  }
+  return tuned_launch<EPI>(c, h, cP, cQ, combo, slot);
+}
+
+// The batch's integral pass (eri.cu builds the launches): the autotuned
+// shape per class combination.
+int eri_batch_launch(mq_ctx *c, const EriArgs &h, int cP, int cQ) {
+  const int combo = cP * (cP + 1) / 2 + cQ;
+  return tuned_pass<EPI_XX>(c, h, cP, cQ, combo, 16 + combo);
 }
 
 // The quartet store's integral blocks: one launch per class combination over
@@ -194,7 +221,6 @@ int eri_store_quartets(mq_ctx *c) {
   MQ_CUDA(c, cudaMemsetAsync(cnt, 0, 4 * sizeof(unsigned long long), c->stream));
   EriArgs g = base_args(c);
   g.counters = cnt;
-  const bool tuning = c->eri_tune_mode != 0;
   for (int k = 0; k < 6; ++k) {
     const QCombo &cb = qs.combo[k];
     if (cb.total == 0) continue;
@@ -205,13 +231,7 @@ int eri_store_quartets(mq_ctx *c) {
     h.permP = qs.perm + qs.cls_off[cb.cP];
     h.permQ = qs.perm + qs.cls_off[cb.cQ];
     h.store = qs.X + cb.base;
-    // the counters count one pass: a tuning run zeroes them before the pass that is kept
-    if (tuning && h.nq >= TUNE_MIN_QUARTETS && !c->eri_tune.count(tune_key(EPI_STORE, k, h.nq))) {
-      EriArgs ht = h;
-      ht.counters = nullptr;
-      MQ_TRY(tuned_launch(c, ht, cb.cP, cb.cQ, k));
-    }
-    MQ_TRY(tuned_launch(c, h, cb.cP, cb.cQ, k));
+    MQ_TRY(tuned_pass<EPI_STORE>(c, h, cb.cP, cb.cQ, k, k));
   }
   c->d_eri_counters = cnt;
   return MQ_OK;
@@ -224,12 +244,16 @@ std::string eri_tune_report(const mq_ctx *c) {
   static const char *const CLS[6] = {"(ss|ss)", "(sps|ss)", "(sps|sps)", "(spsp|ss)", "(spsp|sps)", "(spsp|spsp)"};
   for (const auto &e : c->eri_tune_log) {
     const int combo = (int)((e.first >> 32) & 0xff), b = (int)(e.first & 0xffffffff);
+    const int epi = (int)(e.first >> 40);
     const EriTune &ch = c->eri_tune.at(e.first);
-    char line[512];
-    int len = std::snprintf(line, sizeof line, "store %s 2^%d quartets:", combo < 6 ? CLS[combo] : "?", b);
+    char line[1024];
+    int len = std::snprintf(line, sizeof line, "%s %s 2^%d quartets:", epi == EPI_STORE ? "store" : "batch",
+                            combo < 6 ? CLS[combo] : "?", b);
     for (const EriTune &t : e.second)
-      len += std::snprintf(line + len, sizeof line - len, " %s/%d %.3fms%s", t.binned ? "binned" : "plain", t.block,
-                           t.ms, (t.binned == ch.binned && t.block == ch.block) ? "*" : "");
+      len += std::snprintf(line + len, sizeof line - len, " %s/%s%d %.3fms%s", t.binned ? "binned" : "plain",
+                           t.persistent ? "queue/" : "", t.block, t.ms,
+                           (t.binned == ch.binned && t.block == ch.block && t.persistent == ch.persistent) ? "*"
+                                                                                                             : "");
     out += line;
     out += "\n";
   }

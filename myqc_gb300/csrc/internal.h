@@ -192,11 +192,13 @@ struct StageTimer {
 
 namespace mq {
 // The integral autotuner's choice for one launch signature (eri_store.cu):
-// launch order binned by surviving primitive quartets or not, CTA size, and
-// the time the candidate took when it was measured
+// launch order binned by surviving primitive quartets or not, CTA size,
+// persistent work queue or one warp per work unit, and the time the
+// candidate took when it was measured
 struct EriTune {
   int binned = 1;
   int block = 128;
+  int persistent = 0;  // warps take work units from a queue in a grid of resident CTAs
   float ms = 0.f;
 };
 }  // namespace mq
@@ -270,6 +272,10 @@ struct mq_ctx {
   // first use, 0 the defaults; choices per (epilogue, class combination,
   // size class) and the measured candidates, in the order tuned
   int eri_tune_mode = 1;
+  // the basis library text as tokenised lines, and the row of its STO-3G key
+  // (mq_basis_library; basis_lib.cu)
+  std::vector<std::vector<std::string>> basis_rows;
+  int basis_key = -1;
   std::map<unsigned long long, mq::EriTune> eri_tune;
   std::vector<std::pair<unsigned long long, std::vector<mq::EriTune>>> eri_tune_log;
   std::vector<int> hp_shA, hp_shB, hp_aoA, hp_aoB;  // host copy of the pair table's shells and AO offsets

@@ -90,6 +90,29 @@ class Context:
         self._check(self.L.mq_batch_add(self.h, len(Z), ptr(k[0]), ptr(k[1]), ptr(k[2]), ptr(k[3]), ptr(k[4]),
                                         ptr(k[5]), sysm.nelcA))
 
+    def basis_library(self, text: str):
+        """Keep the mybasis text in the library (its STO-3G section) for
+        basis_build and batch_add_atoms."""
+        self._check(self.L.mq_basis_library(self.h, text.encode()))
+
+    def basis_build(self, atoms) -> BasisArrays:
+        """buildBasis in the library: the bas / set / basinfo / setinfo arrays of the atoms."""
+        Z = np.ascontiguousarray(atoms, dtype=np.int32)
+        sizes = np.zeros(4, dtype=np.int32)
+        self._check(self.L.mq_basis_build(self.h, len(Z), ptr(Z), None, None, None, None, ptr(sizes)))
+        bas, st = np.zeros(int(sizes[0])), np.zeros(int(sizes[1]))
+        bi, si = np.zeros(int(sizes[2]), dtype=np.int32), np.zeros(int(sizes[3]), dtype=np.int32)
+        self._check(self.L.mq_basis_build(self.h, len(Z), ptr(Z), ptr(bas), ptr(st), ptr(bi), ptr(si), ptr(sizes)))
+        return BasisArrays(bas=bas, set=st, basinfo=bi, setinfo=si)
+
+    def batch_add_atoms(self, sysm: System):
+        """batch_add with the basis built by the library (basis_library first)."""
+        if sysm.nelcA != sysm.nelcB:
+            raise ValueError("batches hold closed-shell molecules")
+        Z = np.ascontiguousarray(sysm.atoms, dtype=np.int32)
+        xyz = f64(np.asarray(sysm.xyz).reshape(-1, 3))
+        self._check(self.L.mq_batch_add_atoms(self.h, len(Z), ptr(Z), ptr(xyz), sysm.nelcA))
+
     def batch_sizes(self) -> np.ndarray:
         nm = ctypes.c_int()
         self._check(self.L.mq_batch_info(self.h, ctypes.byref(nm), None))

@@ -70,3 +70,43 @@ def test_batch_graph_equals_eager_and_guess(ctx, basis_text):
     assert np.max(np.abs(g["energy"] - a["energy"])) < 1e-9
     assert (g["iterations"][1:] <= 2).all(), g["iterations"]
     assert g["iterations"][0] == a["iterations"][0]
+
+
+def test_basis_built_by_the_library(ctx, basis_text):
+    """buildBasis in the library (mq_basis_build) gives exactly the arrays of
+    the host restatement for every molecule kind of the batch workload."""
+    ctx.basis_library(basis_text)
+    kinds, systems = molecules.batch_workload(40, 11)
+    for k, s in zip(kinds, systems):
+        a = ctx.basis_build(s.atoms)
+        b = formats.parse_mybasis_text(basis_text, s.atoms)
+        assert np.array_equal(a.bas, b.bas) and np.array_equal(a.set, b.set), k
+        assert np.array_equal(a.basinfo, b.basinfo) and np.array_equal(a.setinfo, b.setinfo), k
+
+
+def test_batch_work_queue_and_tuning(ctx, basis_text):
+    """The batch of 600 molecules (large enough for the integral autotuner)
+    set up by atoms (basis built in the library) solves to energies
+    bit-identical to the same batch with the integral launches in their
+    default shapes: every candidate shape -- binned or not, persistent work
+    queue or one warp per work unit, CTA size -- writes the same integrals;
+    the report names the chosen shapes."""
+    kinds, systems = molecules.batch_workload(600, 5)
+    ctx.basis_library(basis_text)
+    out = []
+    try:
+        for mode in (0, 1, 1):  # defaults, tuning pass, tuned shapes
+            ctx.set_eri_tuning(mode)
+            ctx.batch_clear()
+            for s in systems:
+                ctx.batch_add_atoms(s)
+            out.append(ctx.batch_scf(conv=1e-10, conv_rms=True, diis=8, max_iter=100, graph=True))
+    finally:
+        ctx.set_eri_tuning(1)
+        ctx.batch_clear()
+    for o in out[1:]:
+        assert np.array_equal(o["energy"], out[0]["energy"])
+        assert np.array_equal(o["iterations"], out[0]["iterations"])
+    rep = [ln for ln in ctx.eri_tuning_report().splitlines() if ln.startswith("batch")]
+    assert rep and all("*" in ln for ln in rep), rep
+    assert any("queue/" in ln for ln in rep), rep
