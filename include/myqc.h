@@ -321,6 +321,21 @@ typedef struct mq_batch_opts {
                           a block whose first element is NaN takes the core guess */
 } mq_batch_opts;
 
+/* The learned initial density (no reference counterpart; the reference starts
+ * from the core Hamiltonian, src/scf/scf.f90:410-512).  mq_guess_model loads the
+ * network (nin = 64 descriptors, width, nout = 25 block entries; params as
+ * mq_mlp_set_params takes them) and its standardisation: mu_x, sd_x (64 each)
+ * and mu_y, sd_y (5 block types x 25).  mq_guess_predict forms, on the GPU, the
+ * pair descriptors of nmol molecules (nnuc[m] atoms each, concatenated: Z, and
+ * xyz in bohr as xyz(0:N-1, 0:2) column-major over all N atoms), runs the
+ * network and assembles each
+ * molecule's predicted density (n x n, concatenated in order) into D.  A
+ * batched SCF given these densities checks each one (electron count, idempotency)
+ * and keeps the core guess where a check fails. */
+int mq_guess_model(mq_ctx *ctx, int nin, int width, int nout, const float *params, const double *mu_x,
+                   const double *sd_x, const double *mu_y, const double *sd_y);
+int mq_guess_predict(mq_ctx *ctx, int nmol, const int *nnuc, const int *Z, const double *xyz, double *D);
+
 /* The basis library (the text of a mybasis file) kept by the context for the
  * calls below; its STO-3G section is used, as the reference's buildBasis
  * reads it (src/myQC/basis.f90:81). */
@@ -335,8 +350,8 @@ int mq_basis_build(mq_ctx *ctx, int nnuc, const int *Z, double *bas, double *set
                    int sizes[4]);
 
 /* mq_batch_add with the molecule's basis built by the library (mq_basis_library
- * first): nuclei Z and coordinates xyz (bohr, nnuc x 3 row-major as
- * mq_batch_add takes them), nocc doubly occupied orbitals. */
+ * first): nuclei Z and coordinates xyz (bohr, xyz(0:nnuc-1, 0:2) column-major
+ * as mq_batch_add takes them), nocc doubly occupied orbitals. */
 int mq_batch_add_atoms(mq_ctx *ctx, int nnuc, const int *Z, const double *xyz, int nocc);
 
 /* Empty the context's batch. */

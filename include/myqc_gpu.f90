@@ -70,6 +70,14 @@ MODULE myqc_gpu
     INTEGER(c_int) FUNCTION mq_set_fock_screened_increments(ctx, tau) BIND(C)
       IMPORT; TYPE(c_ptr), VALUE :: ctx; REAL(c_double), VALUE :: tau
     END FUNCTION
+    INTEGER(c_int) FUNCTION mq_guess_model(ctx, nin, width, nout, params, mu_x, sd_x, mu_y, sd_y) BIND(C)
+      IMPORT; TYPE(c_ptr), VALUE :: ctx; INTEGER(c_int), VALUE :: nin, width, nout; REAL(c_float) :: params(*)
+      REAL(c_double) :: mu_x(*), sd_x(*), mu_y(*), sd_y(*)
+    END FUNCTION
+    INTEGER(c_int) FUNCTION mq_guess_predict(ctx, nmol, nnuc, Z, xyz, D) BIND(C)
+      IMPORT; TYPE(c_ptr), VALUE :: ctx; INTEGER(c_int), VALUE :: nmol; INTEGER(c_int) :: nnuc(*), Z(*)
+      REAL(c_double) :: xyz(*), D(*)
+    END FUNCTION
     INTEGER(c_int) FUNCTION mq_basis_library(ctx, text) BIND(C)
       IMPORT; TYPE(c_ptr), VALUE :: ctx; CHARACTER(KIND=c_char) :: text(*)   ! NUL-terminated mybasis text
     END FUNCTION

@@ -75,6 +75,8 @@ def lib(path: str | None = None):
     L.mq_set_eri_storage.argtypes = [vp, c_int]
     L.mq_set_eri_tuning.argtypes = [vp, c_int]
     L.mq_basis_library.argtypes = [vp, ctypes.c_char_p]
+    L.mq_guess_model.argtypes = [vp, c_int, c_int, c_int, vp, vp, vp, vp, vp]
+    L.mq_guess_predict.argtypes = [vp, c_int, vp, vp, vp, vp]
     L.mq_basis_build.argtypes = [vp, c_int, vp, vp, vp, vp, vp, vp]
     L.mq_batch_add_atoms.argtypes = [vp, c_int, vp, vp, c_int]
     L.mq_set_fock_screened_increments.argtypes = [vp, ctypes.c_double]

@@ -287,12 +287,50 @@ __global__ void __launch_bounds__(BT) batch_density_kernel(
 }
 
 // D <- the caller's guess for molecules whose block does not start with NaN
+// and that passes the guess checks (else the core guess stays): electron
+// count |tr(D S) - 2 nocc| < 0.5 and idempotency ||D S D / 2 - D||_F / ||D||_F
+// < 0.25 (the checks the learned guess must pass), in FP64, T = D S in
+// shared memory (n^2 doubles).  used[m] = 1 when the guess was taken.
 __global__ void batch_guess_kernel(const MolDesc *__restrict__ mols, const double *__restrict__ Dg,
-                                   double *__restrict__ D) {
+                                   const double *__restrict__ S, double *__restrict__ D, int *__restrict__ used) {
+  extern __shared__ double T[];
+  __shared__ double red[32];
   const MolDesc md = mols[blockIdx.x];
-  const size_t n2 = (size_t)md.n * md.n;
-  if (isnan(Dg[md.mat])) return;
-  for (size_t idx = threadIdx.x; idx < n2; idx += blockDim.x) D[md.mat + idx] = Dg[md.mat + idx];
+  const int n = md.n;
+  const size_t n2 = (size_t)n * n;
+  if (isnan(Dg[md.mat])) {
+    if (threadIdx.x == 0) used[blockIdx.x] = 0;
+    return;
+  }
+  const double *G = Dg + md.mat, *Sm = S + md.mat;
+  for (size_t idx = threadIdx.x; idx < n2; idx += blockDim.x) {  // T = G S (column-major)
+    const int i = (int)(idx % n), j = (int)(idx / n);
+    double v = 0.0;
+    for (int k = 0; k < n; ++k) v = fma(G[i + (size_t)n * k], Sm[k + (size_t)n * j], v);
+    T[idx] = v;
+  }
+  __syncthreads();
+  double tr = 0.0, e2 = 0.0, g2 = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) tr += T[i + (size_t)n * i];
+  for (size_t idx = threadIdx.x; idx < n2; idx += blockDim.x) {  // E = T G / 2 - G
+    const int i = (int)(idx % n), j = (int)(idx / n);
+    double v = 0.0;
+    for (int k = 0; k < n; ++k) v = fma(T[i + (size_t)n * k], G[k + (size_t)n * j], v);
+    const double e = 0.5 * v - G[idx];
+    e2 = fma(e, e, e2);
+    g2 = fma(G[idx], G[idx], g2);
+  }
+  tr = bsum(tr, red);
+  e2 = bsum(e2, red);
+  g2 = bsum(g2, red);
+  __shared__ int ok;
+  if (threadIdx.x == 0) {
+    ok = isfinite(tr) && fabs(tr - 2.0 * md.nocc) < 0.5 && sqrt(e2) < 0.25 * fmax(sqrt(g2), 1e-30);
+    used[blockIdx.x] = ok;
+  }
+  __syncthreads();
+  if (!ok) return;
+  for (size_t idx = threadIdx.x; idx < n2; idx += blockDim.x) D[md.mat + idx] = G[idx];
 }
 
 __global__ void batch_count_kernel(const int *__restrict__ active, int nmol, int *__restrict__ out) {
@@ -503,12 +541,20 @@ int batch_scf(mq_ctx *c, const mq_batch_opts *o, double *energy, int *iters, int
   batch_density_kernel<<<M, BT, smem, c->stream>>>(1, d_md, d_active, dX, dH, dD, dDn, d_eps, d_it, d_conv, d_Ek,
                                                    d_Ef, thr, o->conv_rms, max_iter, d_status);
   c->stats.launches += 2;
+  c->stats.guesses_taken = 0;
   if (o->D_in) {
     double *dg = (double *)buf(c, "batch_guess", mat * sizeof(double));
-    if (!dg) return MQ_ENOMEM;
+    int *d_used = (int *)buf(c, "batch_guess_used", (size_t)M * sizeof(int));
+    if (!dg || !d_used) return MQ_ENOMEM;
     MQ_CUDA(c, cudaMemcpyAsync(dg, o->D_in, mat * sizeof(double), cudaMemcpyHostToDevice, c->stream));
-    batch_guess_kernel<<<M, BT, 0, c->stream>>>(d_md, dg, dD);
+    const size_t sm_g = (size_t)nmax * nmax * sizeof(double);
+    MQ_CUDA(c, cudaFuncSetAttribute(batch_guess_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_g));
+    batch_guess_kernel<<<M, BT, sm_g, c->stream>>>(d_md, dg, dS, dD, d_used);
     c->stats.launches += 1;
+    std::vector<int> used(M);
+    MQ_CUDA(c, cudaMemcpyAsync(used.data(), d_used, (size_t)M * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    MQ_CUDA(c, cudaStreamSynchronize(c->stream));
+    for (int v : used) c->stats.guesses_taken += v;
   }
   MQ_CUDA(c, cudaGetLastError());
   // ---- one SCF iteration for all active molecules

@@ -755,6 +755,7 @@ int mq_stat(const mq_ctx *c, const char *key, double *value) {
   else if (!strcmp(key, "purify_steps")) *value = s.purify_steps;
   else if (!strcmp(key, "purify_persistent")) *value = s.purify_persistent;
   else if (!strcmp(key, "purify_stepwise")) *value = s.purify_stepwise;
+  else if (!strcmp(key, "guesses_taken")) *value = s.guesses_taken;
   else if (!strcmp(key, "fock_jc")) *value = s.fock_jc;
   else if (!strcmp(key, "graph_launches")) *value = s.graph_launches;
   else if (!strcmp(key, "eig_cluster")) *value = s.eig_cluster;

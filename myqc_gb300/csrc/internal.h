@@ -138,6 +138,7 @@ struct Stats {
   double ms_ao2mo_first = 0;  // the transform's first quarter (from the quartet store), last transform
   double fock_calls = 0, diag_calls = 0, scf_iters = 0, purify_steps = 0, fock_jc = 0, tune_fock_ms = 0;
   double purify_persistent = 0, purify_stepwise = 0;  // purifications of the last SCF by form
+  double guesses_taken = 0;  // batch: caller guesses that passed the checks (last batched SCF)
   double launches = 0, lib_launches = 0, quartets = 0, prim_quartets = 0;
   double ms_fock_kernel = 0, fock_kernel_launches = 0;  // the digestion kernel alone, last SCF or mq_fock
   double graph_launches = 0;  // CUDA-graph replays of the last batch SCF
@@ -276,6 +277,8 @@ struct mq_ctx {
   // (mq_basis_library; basis_lib.cu)
   std::vector<std::vector<std::string>> basis_rows;
   int basis_key = -1;
+  // the learned guess's feature and output standardisation (mq_guess_model; guess.cu)
+  std::vector<double> guess_mu_x, guess_sd_x, guess_mu_y, guess_sd_y;
   std::map<unsigned long long, mq::EriTune> eri_tune;
   std::vector<std::pair<unsigned long long, std::vector<mq::EriTune>>> eri_tune_log;
   std::vector<int> hp_shA, hp_shB, hp_aoA, hp_aoB;  // host copy of the pair table's shells and AO offsets
@@ -381,6 +384,9 @@ void tight_boys_device_table(std::vector<double> &tab);  // the table, its grid,
 int eri_full_device(mq_ctx *c, double *d_XX);
 // integral blocks of every combination of the quartet store (tables built)
 int eri_store_quartets(mq_ctx *c);
+// mlp.cu: the network's forward pass on device features (the learned guess)
+int mlp_forward_device(mq_ctx *c, int rows, const float *dX, float **dY);
+int mlp_dims(mq_ctx *c, int dims[4]);
 std::string eri_tune_report(const mq_ctx *c);  // the autotuner's choices and timings, one line per signature
 // qstore.cu: rank the pairs, build the staircase and digestion tables, compute
 // the integral blocks; RHF G from the store; the n^4 array filled from it

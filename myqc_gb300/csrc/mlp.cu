@@ -452,6 +452,13 @@ int mlp_init(mq_ctx *c, int nin, int width, int nout) {
   return mark_params(c);  // the zeroed parameters
 }
 
+int mlp_dims(mq_ctx *c, int dims[4]) {
+  Mlp *m = mlp_of(c);
+  if (!m) return set_err(c, MQ_ESTATE, "no MLP (mq_mlp_init)");
+  for (int k = 0; k < 4; ++k) dims[k] = m->d[k];
+  return MQ_OK;
+}
+
 int mlp_param_count(mq_ctx *c) {
   Mlp *m = mlp_of(c);
   if (!m) return 0;
@@ -687,6 +694,26 @@ static int forward_on_stream(mq_ctx *c, Mlp *m, int rows, const float *X, float 
   MQ_TRY(forward(c, m, a));
   MQ_CUDA(c, cudaMemcpyAsync(Y, a.out, (size_t)rows * m->d[3] * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
   MQ_CUDA(c, cudaStreamSynchronize(c->stream));
+  return MQ_OK;
+}
+
+// The forward pass of rows feature vectors already on the device (FP32, rows x
+// nin), on the context's stream; *dY points at the rows x nout outputs (FP32,
+// valid until the next network call).
+int mlp_forward_device(mq_ctx *c, int rows, const float *dX, float **dY) {
+  Mlp *m = mlp_of(c);
+  if (!m) return set_err(c, MQ_ESTATE, "no MLP (mq_mlp_init)");
+  if (rows <= 0) return set_err(c, MQ_EINVAL, "network forward: no rows");
+  if (!c->ev_params) MQ_TRY(mark_params(c));
+  MQ_CUDA(c, cudaStreamWaitEvent(c->stream, c->ev_params, 0));
+  Acts a;
+  MQ_TRY(acts_alloc(c, m, rows, a));
+  const long long n = (long long)rows * m->kp[0];
+  to_bf16_kernel<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(dX, rows, m->d[0], m->d[0], a.x, m->kp[0]);
+  c->stats.launches += 1;
+  MQ_CUDA(c, cudaGetLastError());
+  MQ_TRY(forward(c, m, a));
+  *dY = a.out;
   return MQ_OK;
 }
 

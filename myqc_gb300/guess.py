@@ -229,9 +229,12 @@ def pair_data(atoms, xyz_angstrom):
 
 
 class LearnedGuess:
-    """Trained network + normalisation, evaluated through a Context's MLP
-    kernels.  The file holds params (FP32), dims, mu_x/sd_x (feature
-    standardisation) and mu_y/sd_y (per block type and output entry)."""
+    """Trained network + normalisation, evaluated in the library
+    (mq_guess_predict: descriptors, forward pass and assembly on the GPU).
+    The file holds params (FP32), dims, mu_x/sd_x (feature standardisation)
+    and mu_y/sd_y (per block type and output entry).  `predict` is the host
+    restatement of the same steps (the training set's descriptors are formed
+    by it), kept for the tests that compare the two."""
 
     def __init__(self, ctx, path: str):
         z = np.load(path)
@@ -239,8 +242,7 @@ class LearnedGuess:
         self.dims = tuple(int(v) for v in z["dims"])
         self.mu_x, self.sd_x = z["mu_x"], z["sd_x"]
         self.mu_y, self.sd_y = z["mu_y"], z["sd_y"]
-        ctx.mlp_init(self.dims[0], self.dims[1], self.dims[3])
-        ctx.mlp_set_params(z["params"])
+        ctx.guess_model(self.dims, z["params"], self.mu_x, self.sd_x, self.mu_y, self.sd_y)
 
     def predict(self, atoms, xyz_angstrom) -> np.ndarray:
         pairs, feat, Q, t, mask = pair_data(atoms, xyz_angstrom)
@@ -249,11 +251,14 @@ class LearnedGuess:
         Y = (Yn * self.sd_y[t] + self.mu_y[t]) * mask
         return assemble(atoms, Y, pairs, Q)
 
+    def predict_many(self, systems) -> list:
+        """Predicted densities of many systems, on the GPU in one pass."""
+        return self.ctx.guess_predict(systems)
+
     def guess(self, sysm, S: np.ndarray):
         """Predicted closed-shell density, or None when it fails the
         electron-count or idempotency check (the caller then uses the core
         guess)."""
-        atoms, xyz = system_geometry(sysm)
-        D = self.predict(atoms, xyz)
+        D = self.ctx.guess_predict([sysm])[0]
         ok, _, _ = check_density(D, S, sysm.nelcA + sysm.nelcB)
         return D if ok else None

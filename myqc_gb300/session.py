@@ -90,6 +90,29 @@ class Context:
         self._check(self.L.mq_batch_add(self.h, len(Z), ptr(k[0]), ptr(k[1]), ptr(k[2]), ptr(k[3]), ptr(k[4]),
                                         ptr(k[5]), sysm.nelcA))
 
+    def guess_model(self, dims, params, mu_x, sd_x, mu_y, sd_y):
+        """Load the learned guess's network (dims nin, width, width, nout) and its
+        feature / output standardisation."""
+        P = np.ascontiguousarray(params, dtype=np.float32)
+        arrs = [f64(np.asarray(a).ravel()) for a in (mu_x, sd_x, mu_y, sd_y)]
+        self._check(self.L.mq_guess_model(self.h, int(dims[0]), int(dims[1]), int(dims[3]), ptr(P),
+                                          *[ptr(a) for a in arrs]))
+        self.mlp_dims = (int(dims[0]), int(dims[1]), int(dims[2]), int(dims[3]))
+
+    def guess_predict(self, systems) -> list:
+        """Predicted densities of the systems (one GPU pass for all of them)."""
+        nnuc = np.array([len(s.atoms) for s in systems], dtype=np.int32)
+        Z = np.ascontiguousarray(np.concatenate([np.asarray(s.atoms) for s in systems]), dtype=np.int32)
+        xyz = f64(np.concatenate([np.asarray(s.xyz, dtype=float).reshape(-1, 3) for s in systems]))
+        sizes = [int(sum(1 if z <= 2 else 5 for z in s.atoms)) for s in systems]
+        D = np.zeros(sum(n * n for n in sizes))
+        self._check(self.L.mq_guess_predict(self.h, len(systems), ptr(nnuc), ptr(Z), ptr(xyz), ptr(D)))
+        out, o = [], 0
+        for n in sizes:
+            out.append(D[o: o + n * n].reshape(n, n, order="F"))
+            o += n * n
+        return out
+
     def basis_library(self, text: str):
         """Keep the mybasis text in the library (its STO-3G section) for
         basis_build and batch_add_atoms."""
