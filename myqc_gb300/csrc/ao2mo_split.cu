@@ -334,7 +334,6 @@ __device__ __forceinline__ void load_chunk(const T *__restrict__ x, int k0, int 
 //              l + n (u + n v) of XX (rows of n values), l = r mod n;
 //   ROW_SYMM   row (v, jb) of the pair-packed Y2: element u is
 //              in[jb * npairs + pidx(min(u, v), max(u, v))], pidx(u, v) = u + v (v + 1) / 2.
-// (the first step's operand from the quartet store: slice_store_kernel below)
 //   ROW_TRANS  row (b, p) of the [p][l][b] array the store's first quarter
 //              writes: element l at in[(p n + l) nb + b]; the rows are visited
 //              with b fastest, so the warps reading one p share its sectors
