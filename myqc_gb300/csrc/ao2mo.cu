@@ -114,14 +114,31 @@ __global__ void mp2_partial_f32_kernel(const double *__restrict__ Om, int no1, i
     const float eija = (float)(eo1[i] + eo2[j] - ev1[a]);
     const bool ssp = same_spin && i < j;
     float fo = 0.f, fs = 0.f;
-    for (int b = 0; b < nv2; ++b) {
-      const float2 x = split_f64(__ldcs(Om + idx + sb * b));
-      const float inv = __frcp_rn(eija - evf[b]);
-      fo = fmaf(fmaf(2.f * x.x, x.y, x.x * x.x), inv, fo);
-      if (ssp && a < b) {
-        const float2 xp = split_f64(Om[i + (size_t)no1 * (b + (size_t)nv1 * j) + sb * a]);
-        const float yh = x.x - xp.x, yl = x.y - xp.y;
-        fs = fmaf(fmaf(2.f * yh, yl, yh * yh), inv, fs);
+    // b in runs of MP2_RUN: the run's integrals (and their exchange partners)
+    // are loaded before any is used, so a thread has up to 2 MP2_RUN loads in
+    // flight; the sums still take b in ascending order
+    constexpr int MP2_RUN = 8;
+    const double *xpb = Om + i + (size_t)no1 * nv1 * j + sb * a;  // (ib|ja) at xpb[no1 b]
+    for (int b0 = 0; b0 < nv2; b0 += MP2_RUN) {
+      double xv[MP2_RUN], xpv[MP2_RUN];
+#pragma unroll
+      for (int u = 0; u < MP2_RUN; ++u) {
+        const int b = b0 + u;
+        xv[u] = b < nv2 ? __ldcs(Om + idx + sb * b) : 0.0;
+        xpv[u] = (b < nv2 && ssp && a < b) ? xpb[(size_t)no1 * b] : 0.0;
+      }
+#pragma unroll
+      for (int u = 0; u < MP2_RUN; ++u) {
+        const int b = b0 + u;
+        if (b >= nv2) break;
+        const float2 x = split_f64(xv[u]);
+        const float inv = __frcp_rn(eija - evf[b]);
+        fo = fmaf(fmaf(2.f * x.x, x.y, x.x * x.x), inv, fo);
+        if (ssp && a < b) {
+          const float2 xp = split_f64(xpv[u]);
+          const float yh = x.x - xp.x, yl = x.y - xp.y;
+          fs = fmaf(fmaf(2.f * yh, yl, yh * yh), inv, fs);
+        }
       }
     }
     os = fo;
