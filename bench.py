@@ -47,7 +47,7 @@ def env_rank():
 
 class ClockSampler:
     """nvidia-smi samples of SM clock and throttle reasons.  The sampler starts
-    before the warm-up (its start-up, which touches the driver, stays out of the
+    before the warm-up (its start-up, which queries the GPU driver, stays out of the
     timed region); `window` marks the timed region and `summary` keeps the
     samples taken inside it."""
 

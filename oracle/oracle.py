@@ -520,7 +520,7 @@ def mp2_uhf(eA, eB, OAA, OBB, OAB):
 
 
 def mp2(mol: Molecule, res: SCFResult, XX: np.ndarray):
-    """ao2mo + mp2 as the driver runs them after scf (myQC.f90:73,84)."""
+    """ao2mo + mp2 as the reference's myQC program runs them after scf (myQC.f90:73,84)."""
     if mol.options[3] == 0:
         no = mol.nelcA
         C = res.C
