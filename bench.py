@@ -321,8 +321,9 @@ def run_ours(args):
                           "fallback), densities by FP64 TC2 purification, one FP64 Jacobi eigensolve at the end",
                    "guess_model": os.path.relpath(MODEL, ROOT) if learned_guess(ctx) is not None else None,
                    "mp2_precision": "split hi+mid+lo bf16 (tcgen05), fp32 accumulate" if prec else "fp64",
-                   "l2": f"inputs larger than L2: the quartet store ({ctx.stat('store_bytes') / 1e9:.2f} GB) is "
-                         "rebuilt every step and the transform streams its sliced operand from HBM",
+                   "l2": f"inputs larger than L2: the quartet store ({per['store_bytes'] / 1e9:.2f} GB, the "
+                         "fast solves' own) is rebuilt every step and the transform streams its intermediates "
+                         "from HBM",
                    "eri_tuning": [ln for ln in ctx.eri_tuning_report().splitlines() if ln.strip()],
                    "parallelism": f"replicas x{world}"},
         "e2e": {"value": world * 1000.0 / ms_e2e, "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
