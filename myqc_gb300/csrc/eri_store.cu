@@ -2,8 +2,8 @@
 // tables): one launch per class combination over the staircase of surviving
 // quartets; the split classes share their per-primitive work across warps.
 // Also the launch-order binning of the integral launches and the autotuner
-// that picks, per class combination and size, whether to bin and the CTA
-// size.
+// that picks, per class combination and size, whether to bin, whether the
+// warps take their quartets from a persistent work queue, and the CTA size.
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
